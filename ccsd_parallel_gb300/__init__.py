@@ -1,0 +1,178 @@
+"""GB300-native CCSD amplitude engine (sm_103a CUDA behind a C ABI).
+
+Python host binding over ``include/ccsd_gb300.h``.  The class
+``CCSD_Memory_optimized`` mirrors the reference class of the same name
+(``ccsd_memory_optimized.h:15-47``): construct it with the inputs of the
+iterative part (MO Fock matrix, MO integrals, occupied count) and call
+``CCSD(toler, print_stuff)``, which returns E_HF + E_corr exactly like the
+reference method; the converged amplitudes and the correlation energy stay on
+the object (``t1``, ``t2``, ``E_new``).
+
+Every compute call goes through the CUDA library; when it is missing or no GPU
+is present the call raises (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (CCSD_INTS_AO_DENSE, CCSD_INTS_DF, CCSD_INTS_MO_DENSE, CCSD_PREC_FP64,
+                   CCSD_PREC_SPLIT2, CCSD_PREC_SPLIT3, CCSD_PREC_SPLIT4, CCSDError)
+
+PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD_PREC_SPLIT3,
+              "split4": CCSD_PREC_SPLIT4}
+
+__all__ = ["Solver", "solve", "make_synthetic", "flops_per_update", "CCSD_Memory_optimized",
+           "CCSDError", "PRECISIONS"]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def make_synthetic(nocc: int, nvir: int, naux: int, seed: int):
+    """Seeded synthetic system from the library's generator: (fock, B[naux,n,n])."""
+    n = nocc + nvir
+    fock = np.empty((n, n))
+    df = np.empty((naux, n, n)) if naux > 0 else None
+    _abi.check(_abi.lib().ccsd_make_synthetic(nocc, nvir, naux, seed, _ptr(fock), _ptr(df)))
+    return fock, df
+
+
+def flops_per_update(nocc: int, nvir: int) -> float:
+    return float(_abi.lib().ccsd_flops_per_update(nocc, nvir))
+
+
+def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
+             fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, stream=None):
+    o = _abi.Options()
+    _abi.check(_abi.lib().ccsd_default_options(C.byref(o)))
+    o.energy_tol = energy_tol
+    o.residual_tol = residual_tol
+    o.max_iter = max_iter
+    o.fixed_iterations = fixed_iterations
+    o.diis_size = diis_size
+    o.diis_start = diis_start
+    o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    o.verbose = int(bool(verbose))
+    o.stream = stream
+    return o
+
+
+class Solver:
+    """One device-resident system (integrals uploaded/transformed once)."""
+
+    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, **opts):
+        fock = _f64(fock)
+        n = fock.shape[0]
+        self.nocc, self.nvir = nocc, n - nocc
+        p = _abi.Problem()
+        p.nocc, p.nvir = nocc, n - nocc
+        self._keep = [fock]
+        p.fock = _ptr(fock)
+        if df is not None:
+            df = _f64(df)
+            p.integral_kind, p.naux, p.df = CCSD_INTS_DF, df.shape[0], _ptr(df)
+            self._keep.append(df)
+        elif ao_eri is not None:
+            ao_eri, mo_coeff = _f64(ao_eri), _f64(mo_coeff)
+            p.integral_kind, p.nao = CCSD_INTS_AO_DENSE, ao_eri.shape[0]
+            p.eri, p.mo_coeff = _ptr(ao_eri), _ptr(mo_coeff)
+            self._keep += [ao_eri, mo_coeff]
+        elif eri is not None:
+            eri = _f64(eri)
+            p.integral_kind, p.eri = CCSD_INTS_MO_DENSE, _ptr(eri)
+            self._keep.append(eri)
+        else:
+            raise ValueError("one of eri / df / ao_eri is required")
+        self._opts = _options(**opts)
+        h = C.c_void_p()
+        _abi.check(_abi.lib().ccsd_create(C.byref(p), C.byref(self._opts), C.byref(h)))
+        self._h = h
+        self._keep = None  # inputs were copied to the device
+
+    def set_options(self, **opts):
+        self._opts = _options(**opts)
+        _abi.check(_abi.lib().ccsd_set_options(self._h, C.byref(self._opts)))
+
+    def solve(self, amplitudes: bool = True, history: int = 1001) -> dict:
+        o, v = self.nocc, self.nvir
+        r = _abi.Result()
+        t1 = np.empty((o, v)) if amplitudes else None
+        t2 = np.empty((o, o, v, v)) if amplitudes else None
+        eh = np.zeros(history)
+        ms = np.zeros(history)
+        r.t1, r.t2 = _ptr(t1), _ptr(t2)
+        r.energy_history, r.update_ms, r.history_capacity = _ptr(eh), _ptr(ms), history
+        _abi.check(_abi.lib().ccsd_solve(self._h, C.byref(r)))
+        return dict(e_corr=r.e_corr, iterations=r.iterations, converged=bool(r.converged),
+                    residual_norm=r.residual_norm, energies=eh[:r.history_len].copy(),
+                    update_ms=ms[:r.iterations].copy(), flops_per_update=r.flops_per_update,
+                    t1=t1, t2=t2)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.lib().ccsd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, amplitudes=True, **opts):
+    with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, **opts) as s:
+        return s.solve(amplitudes=amplitudes)
+
+
+class CCSD_Memory_optimized:
+    """Drop-in for the iterative part of the reference class.
+
+    reference (ccsd_memory_optimized.h)        here
+    ------------------------------------------------------------------
+    CCSD_Memory_optimized(n_N, Z, R, basis,     CCSD_Memory_optimized(fock, nocc, eri=|df=|ao_eri=,
+      n_Elec, rank, size, HartFock*, frozen)      mo_coeff=, E_HF=) -- the integrals that
+                                                  Prepear_AOs would build are passed in
+    double CCSD(double toler, bool print)      CCSD(toler, print_stuff) -> E_HF + E_corr
+    E_new, T_1, t2                             E_new, t1 (o x v), t2 (o,o,v,v)
+    n_Electrons, unocc_orb (spin orbitals)     n_Electrons = 2 nocc, unocc_orb = 2 nvir
+
+    Like the reference, CCSD() runs plain Jacobi updates from the MP2 guess
+    until |E_new - E_old| < toler or 999 updates (iter reaching 1000).
+    """
+
+    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, E_HF=0.0,
+                 precision="fp64"):
+        self._solver = Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff,
+                              precision=precision)
+        self.n_Electrons = 2 * nocc
+        self.unocc_orb = 2 * (np.asarray(fock).shape[0] - nocc)
+        self.E_HF = E_HF
+        self.E_new = 0.0
+        self.t1 = self.t2 = None
+        self.iter = 1
+
+    def CCSD(self, toler: float, print_stuff: bool = False) -> float:
+        self._solver.set_options(precision=self._solver._opts.precision, energy_tol=toler,
+                                 max_iter=999, verbose=print_stuff)
+        r = self._solver.solve()
+        self.E_new, self.t1, self.t2 = r["e_corr"], r["t1"], r["t2"]
+        self.iter = r["iterations"] + 1  # the reference counter starts at 1
+        self.energies = r["energies"]
+        if print_stuff:
+            print(f"CCSD correction [au] = {self.E_new:.15e}")
+        return self.E_new + self.E_HF

@@ -1,0 +1,108 @@
+"""ctypes binding of ``include/ccsd_gb300.h`` (the C ABI of the CUDA library).
+
+The library is the in-tree ``_lib/libccsd_gb300.so``.  Loading it needs no GPU;
+every compute entry point fails with ``CCSD_ERR_NO_DEVICE`` when no device is
+present (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libccsd_gb300.so"
+
+CCSD_OK = 0
+CCSD_ERR_INVALID_ARG = -1
+CCSD_ERR_CUDA = -2
+CCSD_ERR_OUT_OF_MEMORY = -3
+CCSD_ERR_DIVERGED = -4
+CCSD_ERR_NO_DEVICE = -5
+CCSD_ERR_TIMEOUT = -6
+CCSD_ERR_UNSUPPORTED = -7
+CCSD_ERR_NOT_CONVERGED = -8
+
+CCSD_INTS_MO_DENSE = 0
+CCSD_INTS_DF = 1
+CCSD_INTS_AO_DENSE = 2
+
+CCSD_PREC_FP64 = 0
+CCSD_PREC_SPLIT2 = 2
+CCSD_PREC_SPLIT3 = 3
+CCSD_PREC_SPLIT4 = 4
+
+_dp = C.POINTER(C.c_double)
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("nocc", C.c_int32), ("nvir", C.c_int32), ("integral_kind", C.c_int32),
+        ("naux", C.c_int32), ("nao", C.c_int32), ("device_inputs", C.c_int32),
+        ("fock", _dp), ("eri", _dp), ("df", _dp), ("mo_coeff", _dp),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
+        ("fixed_iterations", C.c_int32), ("diis_size", C.c_int32), ("diis_start", C.c_int32),
+        ("precision", C.c_int32), ("verbose", C.c_int32), ("stream", C.c_void_p),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("e_corr", C.c_double), ("residual_norm", C.c_double), ("iterations", C.c_int32),
+        ("converged", C.c_int32), ("t1", _dp), ("t2", _dp), ("energy_history", _dp),
+        ("update_ms", _dp), ("history_capacity", C.c_int32), ("history_len", C.c_int32),
+        ("flops_per_update", C.c_double),
+    ]
+
+
+# Every function the header declares, with its ctypes signature.
+SIGNATURES = {
+    "ccsd_default_options": (C.c_int, [C.POINTER(Options)]),
+    "ccsd_create": (C.c_int, [C.POINTER(Problem), C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    "ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(Result)]),
+    "ccsd_set_options": (C.c_int, [C.c_void_p, C.POINTER(Options)]),
+    "ccsd_destroy": (C.c_int, [C.c_void_p]),
+    "ccsd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
+    "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the library once; raise loudly when it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"CUDA library {LIB_PATH} is missing: run __graft_entry__.build() "
+                "(this package has no CPU fallback)")
+        h = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = h
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    lib().ccsd_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+class CCSDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ccsd error {code}: {msg}")
+        self.code = code
+
+
+def check(rc: int):
+    if rc != CCSD_OK:
+        raise CCSDError(rc, last_error())
+    return rc

@@ -1,0 +1,102 @@
+// Internal declarations shared by the host engine (C++) and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace ccsd {
+
+// Status carried through the engine as an exception internally; converted to
+// a C status code at the ABI boundary (abi.cpp).
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define CCSD_CUDA(call)                                                                    \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            throw ::ccsd::Error(e_ == cudaErrorMemoryAllocation ? -3 : -2,                 \
+                                std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                                    __FILE__ + ":" + std::to_string(__LINE__) + ")");      \
+        }                                                                                  \
+    } while (0)
+
+// One logical matrix dimension made of up to three tensor sub-indices,
+// outermost first: idx -> (i0, i1, i2) with i2 = idx % e2,
+// i1 = (idx / e2) % e1, i0 = idx / (e1 * e2); offset = i0*s0 + i1*s1 + i2*s2.
+// An unused level keeps the extent UINT32_MAX, so a 1-level dim is i2 = idx
+// and a 2-level dim is (i1, i2).  This lets a GEMM read a 4-index tensor in
+// any grouping without a copy.
+struct Dim {
+    uint32_t e1 = 0xFFFFFFFFu, e2 = 0xFFFFFFFFu;
+    int64_t s0 = 0, s1 = 0, s2 = 0;
+};
+
+__host__ __device__ inline int64_t dim_off(const Dim &d, uint32_t idx) {
+    uint32_t i2 = idx % d.e2;
+    uint32_t r = idx / d.e2;
+    uint32_t i1 = r % d.e1;
+    uint32_t i0 = r / d.e1;
+    return (int64_t)i0 * d.s0 + (int64_t)i1 * d.s1 + (int64_t)i2 * d.s2;
+}
+
+// Helpers to build dims.
+inline Dim ix1(int64_t s) { Dim d; d.s2 = s; return d; }
+inline Dim ix2(uint32_t e_inner, int64_t s_outer, int64_t s_inner) {
+    Dim d; d.e2 = e_inner; d.s1 = s_outer; d.s2 = s_inner; return d;
+}
+inline Dim ix3(uint32_t e_mid, uint32_t e_inner, int64_t s_outer, int64_t s_mid, int64_t s_inner) {
+    Dim d; d.e1 = e_mid; d.e2 = e_inner; d.s0 = s_outer; d.s1 = s_mid; d.s2 = s_inner; return d;
+}
+
+// A read-only matrix view rows x cols over a tensor.
+struct MatView {
+    const double *p = nullptr;
+    Dim row, col;
+};
+// A writable matrix view.
+struct OutView {
+    double *p = nullptr;
+    Dim row, col;
+};
+
+// ---- FP64 kernels (gemm_f64.cu, tensor_ops.cu) ------------------------------
+// C(m,n) = alpha * sum_k A(m,k) * B(n,k) + beta * C(m,n); A is M x K, B is N x K.
+// `ws` is scratch of `ws_elems` doubles used for split-K partial sums.
+void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+              const OutView &C, double *ws, size_t ws_elems, cudaStream_t st);
+// Elements needed in `ws` for this GEMM shape (0 when no split-K is used).
+size_t gemm_f64_ws_elems(int M, int N, int K);
+
+// Y(r,c) = alpha * X(r,c) + beta * Y(r,c) over an R x C grid (views may permute).
+void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
+                cudaStream_t st);
+
+// Elementwise/amplitude kernels (all closed-shell spatial, o = nocc, v = nvir).
+void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st);
+void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const double *ev, double *t2,
+                 cudaStream_t st);
+void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
+             cudaStream_t st);
+// t2_new = (R + Rp + Rp^T) / D2, returns into t2_new; also writes the per-block
+// partial sums of |t2_new - t2_old|^2 into `partials` (length >= grid).
+void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
+                 const double *ev, const double *t2_old, double *t2_new, double *partials,
+                 int nblocks, cudaStream_t st);
+void k_update_t1(int o, int v, const double *R1, const double *eo, const double *ev,
+                 const double *t1_old, double *t1_new, double *partials, cudaStream_t st);
+// E = sum_{ijab} L[i,j,a,b] * tau[i,j,a,b]; block partial sums into `partials`.
+void k_dot(size_t n, const double *x, const double *y, double *partials, int nblocks,
+           cudaStream_t st);
+// sum of `n` partials into out[0] (single block, deterministic order).
+void k_sum(int n, const double *partials, double *out, cudaStream_t st);
+void k_fill(size_t n, double val, double *p, cudaStream_t st);
+void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st);
+int reduce_blocks();
+
+}  // namespace ccsd

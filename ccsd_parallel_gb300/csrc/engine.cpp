@@ -1,0 +1,730 @@
+// CCSD amplitude engine (host side, C++).
+//
+// Replaces the iterative part of CCSD_Memory_optimized::CCSD
+// (ccsd_memory_optimized.cpp:473-557).  The reference iterates a spin-orbital
+// Jacobi map with T1 = 0 / MP2 T2 start and stops on |E_new - E_old| < toler
+// (:552); this engine iterates the same map written over spatial orbitals for
+// a closed-shell determinant (every iterate agrees with the spin-orbital one:
+// t(a alpha b beta, i alpha j beta) = t2[i][j][a][b]).  The residual uses
+// spin-adapted Stanton-Gauss intermediates; the particle-particle ladder
+// contracts the bare (ac|bd) with tau as the reference does (:2093) and adds
+// the T1 dressing through one o^3 v^3 contraction.
+//
+// Every contraction is expressed as C(m,n) = alpha sum_k A(m,k) B(n,k) +
+// beta C(m,n) over strided views of the stored tensors (no transposed copies)
+// and runs either on the FP64 kernel or on the split-precision tensor-core
+// engine, selected per call by the precision option.
+#include "engine.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace ccsd {
+
+// ---------------------------------------------------------------------------
+DBuf::DBuf(size_t count) { alloc(count); }
+DBuf::~DBuf() {
+    if (p) cudaFree(p);
+}
+DBuf &DBuf::operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+        if (p) cudaFree(p);
+        p = o.p;
+        n = o.n;
+        o.p = nullptr;
+        o.n = 0;
+    }
+    return *this;
+}
+void DBuf::alloc(size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = count;
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        throw Error(CCSD_ERR_OUT_OF_MEMORY,
+                    "cudaMalloc of " + std::to_string(count * sizeof(double)) +
+                        " bytes failed: " + cudaGetErrorString(e));
+    }
+}
+void DBuf::zero(cudaStream_t st) {
+    if (n) CCSD_CUDA(cudaMemsetAsync(p, 0, n * sizeof(double), st));
+}
+
+namespace {
+inline MatView mv(const double *p, Dim r, Dim c) {
+    MatView m;
+    m.p = p;
+    m.row = r;
+    m.col = c;
+    return m;
+}
+inline OutView ovw(double *p, Dim r, Dim c) {
+    OutView m;
+    m.p = p;
+    m.row = r;
+    m.col = c;
+    return m;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
+    }
+    if (prob.nocc <= 0 || prob.nvir <= 0)
+        throw Error(CCSD_ERR_INVALID_ARG, "nocc and nvir must be positive");
+    if (!prob.fock) throw Error(CCSD_ERR_INVALID_ARG, "fock is NULL");
+    o_ = prob.nocc;
+    v_ = prob.nvir;
+    n_ = o_ + v_;
+    const double ov2 = (double)o_ * o_ * v_ * v_;
+    if (ov2 > 2.0e9 || (double)v_ * v_ >= 2.0e9)
+        throw Error(CCSD_ERR_UNSUPPORTED, "shape too large for 32-bit tile indices");
+    set_options(opts);
+    build_integrals(prob);
+    build_derived();
+
+    const size_t o = o_, v = v_;
+    const size_t nT2 = o * o * v * v, nT1 = o * v;
+    t1_.alloc(nT1);
+    t2_.alloc(nT2);
+    t1n_.alloc(nT1);
+    t2n_.alloc(nT2);
+    tau_.alloc(nT2);
+    th1_.alloc(nT2);
+    th2_.alloc(nT2);
+    R1_.alloc(nT1);
+    R_.alloc(nT2);
+    Rp_.alloc(nT2);
+    Foo_.alloc(o * o);
+    Fvv_.alloc(v * v);
+    Fov_.alloc(o * v);
+    Loo_.alloc(o * o);
+    Lvv_.alloc(v * v);
+    tmpo_.alloc(o * o);
+    tmpo2_.alloc(o * o);
+    Woooo_.alloc(o * o * o * o);
+    Wvoov_.alloc(nT2);
+    Wvovo_.alloc(nT2);
+    Wa_.alloc(nT2);
+    Z_.alloc(o * o * o * v);
+    tmpB_.alloc(o * o * o * v);
+    Vk_.alloc(o * o * o * v);
+    ws_.alloc(4u << 20);
+    partials_.alloc(reduce_blocks() + 8);
+    scalars_.alloc(8);
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+}
+
+Engine::~Engine() {
+    if (st_) cudaStreamSynchronize(st_);
+    split_.reset();
+    if (own_stream_ && st_) cudaStreamDestroy(st_);
+}
+
+void Engine::set_options(const ccsd_options &opts) {
+    if (opts.precision != CCSD_PREC_FP64 && opts.precision != CCSD_PREC_SPLIT2 &&
+        opts.precision != CCSD_PREC_SPLIT3 && opts.precision != CCSD_PREC_SPLIT4)
+        throw Error(CCSD_ERR_INVALID_ARG, "unknown precision mode");
+    if (opts.diis_size < 0 || opts.diis_size > 16)
+        throw Error(CCSD_ERR_INVALID_ARG, "diis_size must be in [0, 16]");
+    if (opts.max_iter < 0 || opts.fixed_iterations < 0)
+        throw Error(CCSD_ERR_INVALID_ARG, "iteration counts must be >= 0");
+    if (opts.stream) {
+        if (own_stream_ && st_) cudaStreamDestroy(st_);
+        st_ = (cudaStream_t)opts.stream;
+        own_stream_ = false;
+    } else if (!st_) {
+        CCSD_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        own_stream_ = true;
+    }
+    opt_ = opts;
+    if (opt_.precision != CCSD_PREC_FP64) {
+        if (!split_ || split_->nslices() != opt_.precision) split_.reset(new SplitEngine(opt_.precision, st_));
+        split_->set_stream(st_);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Integral set-up (the reference's Prepear_AOs + Fill_FS, ccsd_memory_optimized.cpp:71-74)
+void Engine::build_integrals(const ccsd_problem &prob) {
+    const int n = n_, o = o_, v = v_;
+    // Fock: diagonal -> orbital energies; off-diagonal blocks enter the
+    // intermediates (the reference only supports a diagonal matrix, Fill_FS :3560).
+    DBuf fock(n * (size_t)n);
+    CCSD_CUDA(cudaMemcpyAsync(fock.p, prob.fock, sizeof(double) * n * n,
+                              prob.device_inputs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              st_));
+    eo_.alloc(o);
+    ev_.alloc(v);
+    k_copy_diag(n, fock.p, 0, o, eo_.p, st_);
+    k_copy_diag(n, fock.p, o, v, ev_.p, st_);
+    f_oo_off_.alloc((size_t)o * o);
+    f_vv_off_.alloc((size_t)v * v);
+    f_ov_.alloc((size_t)o * v);
+    axpby_view(o, o, 1.0, mv(fock.p, ix1(n), ix1(1)), 0.0, ovw(f_oo_off_.p, ix1(o), ix1(1)), st_);
+    axpby_view(v, v, 1.0, mv(fock.p + (size_t)o * n + o, ix1(n), ix1(1)), 0.0,
+               ovw(f_vv_off_.p, ix1(v), ix1(1)), st_);
+    axpby_view(o, v, 1.0, mv(fock.p + o, ix1(n), ix1(1)), 0.0, ovw(f_ov_.p, ix1(v), ix1(1)), st_);
+    // remove the diagonal (it sits in the denominators): X(r,r) -= diag
+    {
+        std::vector<double> hf((size_t)n * n);
+        if (prob.device_inputs)
+            CCSD_CUDA(cudaMemcpy(hf.data(), prob.fock, sizeof(double) * n * n, cudaMemcpyDeviceToHost));
+        else
+            std::memcpy(hf.data(), prob.fock, sizeof(double) * n * n);
+        std::vector<double> oo((size_t)o * o), vv((size_t)v * v);
+        for (int i = 0; i < o; ++i)
+            for (int j = 0; j < o; ++j) oo[i * o + j] = i == j ? 0.0 : hf[(size_t)i * n + j];
+        for (int a = 0; a < v; ++a)
+            for (int b = 0; b < v; ++b) vv[a * v + b] = a == b ? 0.0 : hf[(size_t)(o + a) * n + o + b];
+        CCSD_CUDA(cudaMemcpyAsync(f_oo_off_.p, oo.data(), sizeof(double) * o * o, cudaMemcpyHostToDevice, st_));
+        CCSD_CUDA(cudaMemcpyAsync(f_vv_off_.p, vv.data(), sizeof(double) * v * v, cudaMemcpyHostToDevice, st_));
+        CCSD_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    const cudaMemcpyKind kind = prob.device_inputs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (prob.integral_kind == CCSD_INTS_MO_DENSE) {
+        if (!prob.eri) throw Error(CCSD_ERR_INVALID_ARG, "eri is NULL");
+        DBuf eri((size_t)n * n * n * n);
+        CCSD_CUDA(cudaMemcpyAsync(eri.p, prob.eri, sizeof(double) * eri.n, kind, st_));
+        build_from_mo_dense(eri.p);
+        CCSD_CUDA(cudaStreamSynchronize(st_));
+    } else if (prob.integral_kind == CCSD_INTS_DF) {
+        if (!prob.df || prob.naux <= 0) throw Error(CCSD_ERR_INVALID_ARG, "df factors missing");
+        DBuf b((size_t)prob.naux * n * n);
+        CCSD_CUDA(cudaMemcpyAsync(b.p, prob.df, sizeof(double) * b.n, kind, st_));
+        build_from_df(b.p, prob.naux);
+        CCSD_CUDA(cudaStreamSynchronize(st_));
+    } else if (prob.integral_kind == CCSD_INTS_AO_DENSE) {
+        if (!prob.eri || !prob.mo_coeff || prob.nao < n)
+            throw Error(CCSD_ERR_INVALID_ARG, "AO integrals / mo_coeff missing or nao < n");
+        const size_t nao = prob.nao;
+        DBuf ao(nao * nao * nao * nao), c(nao * n);
+        CCSD_CUDA(cudaMemcpyAsync(ao.p, prob.eri, sizeof(double) * ao.n, kind, st_));
+        CCSD_CUDA(cudaMemcpyAsync(c.p, prob.mo_coeff, sizeof(double) * c.n, kind, st_));
+        DBuf mo;
+        ao_to_mo(ao.p, c.p, (int)nao, mo);
+        build_from_mo_dense(mo.p);
+        CCSD_CUDA(cudaStreamSynchronize(st_));
+    } else {
+        throw Error(CCSD_ERR_INVALID_ARG, "unknown integral_kind");
+    }
+}
+
+// Y[p'][q'][r'][s'] = eri[p0+p'][q0+q'][r0+r'][s0+s'] for every block.
+void Engine::build_from_mo_dense(const double *eri) {
+    const int64_t n = n_, o = o_, v = v_;
+    auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
+                   int64_t er, int64_t s0, int64_t es) {
+        dst.alloc((size_t)(ep * eq * er * es));
+        const double *base = eri + ((p0 * n + q0) * n + r0) * n + s0;
+        axpby_view((int)(ep * eq), (int)(er * es), 1.0,
+                   mv(base, ix2((uint32_t)eq, n * n * n, n * n), ix2((uint32_t)es, n, 1)), 0.0,
+                   ovw(dst.p, ix1(er * es), ix1(1)), st_);
+    };
+    blk(ovov_, 0, o, o, v, 0, o, o, v);
+    blk(oovv_, 0, o, 0, o, o, v, o, v);
+    blk(ovoo_, 0, o, o, v, 0, o, 0, o);
+    blk(oooo_, 0, o, 0, o, 0, o, 0, o);
+    blk(ovvv_, 0, o, o, v, o, v, o, v);
+    // Wv[a][b][c][d] = (ac|bd) = eri[o+a][o+c][o+b][o+d]
+    wv_.alloc((size_t)(v * v * v * v));
+    const double *base = eri + ((o * n + o) * n + o) * n + o;
+    axpby_view((int)(v * v), (int)(v * v), 1.0,
+               mv(base, ix2((uint32_t)v, n * n * n, n), ix2((uint32_t)v, n * n, 1)), 0.0,
+               ovw(wv_.p, ix1(v * v), ix1(1)), st_);
+}
+
+// (pq|rs) = sum_Q B[Q][p][q] B[Q][r][s] as contractions over Q.
+void Engine::build_from_df(const double *B, int naux) {
+    const int64_t n = n_, o = o_, v = v_, nn = n * n;
+    auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
+                   int64_t er, int64_t s0, int64_t es) {
+        dst.alloc((size_t)(ep * eq * er * es));
+        gemm((int)(ep * eq), (int)(er * es), naux, 1.0,
+             mv(B + p0 * n + q0, ix2((uint32_t)eq, n, 1), ix1(nn)),
+             mv(B + r0 * n + s0, ix2((uint32_t)es, n, 1), ix1(nn)), 0.0,
+             ovw(dst.p, ix1(er * es), ix1(1)));
+    };
+    blk(ovov_, 0, o, o, v, 0, o, o, v);
+    blk(oovv_, 0, o, 0, o, o, v, o, v);
+    blk(ovoo_, 0, o, o, v, 0, o, 0, o);
+    blk(oooo_, 0, o, 0, o, 0, o, 0, o);
+    blk(ovvv_, 0, o, o, v, o, v, o, v);
+    // Wv[a][b][c][d] = (ac|bd): M = (a,c), N = (b,d), K = Q
+    wv_.alloc((size_t)(v * v * v * v));
+    const double *bvv = B + o * n + o;
+    gemm((int)(v * v), (int)(v * v), naux, 1.0, mv(bvv, ix2((uint32_t)v, n, 1), ix1(nn)),
+         mv(bvv, ix2((uint32_t)v, n, 1), ix1(nn)), 0.0,
+         ovw(wv_.p, ix2((uint32_t)v, v * v * v, v), ix2((uint32_t)v, v * v, 1)));
+}
+
+// Four quarter transforms (mu nu|la si) -> (pq|rs) with C[mu][p]
+// (the reference's Prepear_AOs quarter matvecs, ccsd_memory_optimized.cpp:2990-3037).
+void Engine::ao_to_mo(const double *ao, const double *c, int nao_i, DBuf &mo) {
+    const int64_t N = nao_i, n = n_;
+    DBuf x1((size_t)(n * N * N * N)), x2((size_t)(n * n * N * N)), x3((size_t)(n * n * n * N));
+    mo.alloc((size_t)(n * n * n * n));
+    // x1[p][nu][la][si] = sum_mu C[mu][p] ao[mu][nu la si]
+    gemm((int)n, (int)(N * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+         mv(ao, ix1(1), ix1(N * N * N)), 0.0, ovw(x1.p, ix1(N * N * N), ix1(1)));
+    // x2[p][q][la si] = sum_nu C[nu][q] x1[p][nu][la si]; M = q, N = (p, lasi)
+    gemm((int)n, (int)(n * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+         mv(x1.p, ix2((uint32_t)(N * N), N * N * N, 1), ix1(N * N)), 0.0,
+         ovw(x2.p, ix1(N * N), ix2((uint32_t)(N * N), n * N * N, 1)));
+    // x3[pq][r][si] = sum_la C[la][r] x2[pq][la][si]; M = r, N = (pq, si)
+    gemm((int)n, (int)(n * n * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+         mv(x2.p, ix2((uint32_t)N, N * N, 1), ix1(N)), 0.0,
+         ovw(x3.p, ix1(N), ix2((uint32_t)N, n * N, 1)));
+    // mo[pqr][s] = sum_si C[si][s] x3[pqr][si]; M = s, N = pqr
+    gemm((int)n, (int)(n * n * n), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+         mv(x3.p, ix1(N), ix1(1)), 0.0, ovw(mo.p, ix1(1), ix1(n)));
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+}
+
+// L-combinations of the integrals, built once.
+void Engine::build_derived() {
+    const int64_t o = o_, v = v_;
+    const size_t nT2 = (size_t)(o * o * v * v);
+    // Lovov[k][c][l][d] = 2 (kc|ld) - (kd|lc)
+    Lovov_.alloc(nT2);
+    axpby_view((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(o * v), ix1(1)), 0.0,
+               ovw(Lovov_.p, ix1(o * v), ix1(1)), st_);
+    axpby_view((int)(o * v), (int)(o * v), -1.0,
+               mv(ovov_.p, ix2((uint32_t)v, v * o * v, 1), ix2((uint32_t)v, v, o * v)), 1.0,
+               ovw(Lovov_.p, ix1(o * v), ix1(1)), st_);
+    // Lovoo[l][c][k][i] = 2 (lc|ki) - (kc|li)
+    Lovoo_.alloc((size_t)(o * v * o * o));
+    axpby_view((int)(o * v), (int)(o * o), 2.0, mv(ovoo_.p, ix1(o * o), ix1(1)), 0.0,
+               ovw(Lovoo_.p, ix1(o * o), ix1(1)), st_);
+    // (kc|li) at [l][c][k][i]: row (l,c) -> l: o (in ovoo[k][c][l][i], l stride o), c: o*o
+    axpby_view((int)(o * v), (int)(o * o), -1.0,
+               mv(ovoo_.p, ix2((uint32_t)v, o, o * o), ix2((uint32_t)o, v * o * o, 1)), 1.0,
+               ovw(Lovoo_.p, ix1(o * o), ix1(1)), st_);
+    // Lovvv[k][d][a][c] = 2 (kd|ac) - (kc|ad)
+    const size_t nov3 = (size_t)(o * v * v * v);
+    Lovvv_.alloc(nov3);
+    axpby_view((int)(o * v), (int)(v * v), 2.0, mv(ovvv_.p, ix1(v * v), ix1(1)), 0.0,
+               ovw(Lovvv_.p, ix1(v * v), ix1(1)), st_);
+    // (kc|ad) = ovvv[k][c][a][d] placed at [k][d][a][c]: row (k,d): k v^3, d: 1; col (a,c): a v, c v^2
+    axpby_view((int)(o * v), (int)(v * v), -1.0,
+               mv(ovvv_.p, ix2((uint32_t)v, v * v * v, 1), ix2((uint32_t)v, v, v * v)), 1.0,
+               ovw(Lovvv_.p, ix1(v * v), ix1(1)), st_);
+    // LT1[i][a][k][c] = 2 (kc|ia) - (ki|ac)
+    LT1_.alloc(nT2);
+    axpby_view((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(1), ix1(o * v)), 0.0,
+               ovw(LT1_.p, ix1(o * v), ix1(1)), st_);
+    // (ki|ac) = oovv[k][i][a][c]: row (i,a): i v^2, a v; col (k,c): k o v^2, c 1
+    axpby_view((int)(o * v), (int)(o * v), -1.0,
+               mv(oovv_.p, ix2((uint32_t)v, v * v, v), ix2((uint32_t)v, o * v * v, 1)), 1.0,
+               ovw(LT1_.p, ix1(o * v), ix1(1)), st_);
+    // Lijab[i][j][a][b] = 2 (ia|jb) - (ib|ja)
+    Lijab_.alloc(nT2);
+    axpby_view((int)(o * o), (int)(v * v), 2.0,
+               mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
+               ovw(Lijab_.p, ix1(v * v), ix1(1)), st_);
+    axpby_view((int)(o * o), (int)(v * v), -1.0,
+               mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
+               ovw(Lijab_.p, ix1(v * v), ix1(1)), st_);
+}
+
+// ---------------------------------------------------------------------------
+bool Engine::use_split(int M, int N, int K) const {
+    if (opt_.precision == CCSD_PREC_FP64 || !split_) return false;
+    return M >= 16 && N >= 16 && K >= 16 && (double)M * N * K >= 1.0e7;
+}
+
+void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B,
+                  double beta, const OutView &C, int cache_a, int cache_b) {
+    if (use_split(M, N, K)) {
+        split_->gemm(M, N, K, alpha, A, B, beta, C, cache_a, cache_b);
+    } else {
+        gemm_f64(M, N, K, alpha, A, B, beta, C, ws_.p, ws_.n, st_);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual numerators (diagonal Fock moved to the denominators).
+//   R1[i][a]      T1 numerator
+//   R[i][j][a][b] terms already symmetric under (ij,ab) -> (ji,ba)
+//   Rp            terms to be symmetrised: R2 = R + Rp + Rp^T
+void Engine::residual() {
+    const int64_t o = o_, v = v_, ov = o * v, v2 = v * v, ov2 = o * v2, o2 = o * o;
+    const int io = (int)o, iv = (int)v;
+    cudaStream_t st = st_;
+    const double *t1 = t1_.p, *t2 = t2_.p, *tau = tau_.p;
+
+    k_tau(io, iv, t1, t2, tau_.p, st);
+    k_theta(io, iv, t1, t2, th1_.p, th2_.p, st);
+
+    // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d]
+    CCSD_CUDA(cudaMemcpyAsync(Foo_.p, f_oo_off_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
+    gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
+         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, 0);
+    // Fvv[a][c] = f_vv' - sum_{kld} Lovov[k,c,l,d] tau[k,l,a,d]
+    CCSD_CUDA(cudaMemcpyAsync(Fvv_.p, f_vv_off_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
+    gemm(iv, iv, (int)(o * o * v), -1.0, mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)),
+         mv(Lovov_.p, ix1(o * v), ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1)), 1.0,
+         ovw(Fvv_.p, ix1(v), ix1(1)), 0, 2);
+    // Fov[k][c] = f_ov + sum_ld Lovov[k,c,l,d] t1[l,d]
+    CCSD_CUDA(cudaMemcpyAsync(Fov_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
+    gemm((int)ov, 1, (int)ov, 1.0, mv(Lovov_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
+         ovw(Fov_.p, ix1(1), ix1(0)));
+    // Loo[k][i] = Foo + sum_c f_kc t1[i,c] + sum_lc Lovoo[l,c,k,i] t1[l,c]
+    CCSD_CUDA(cudaMemcpyAsync(Loo_.p, Foo_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
+    gemm(io, io, iv, 1.0, mv(f_ov_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
+         ovw(Loo_.p, ix1(o), ix1(1)));
+    gemm((int)o2, 1, (int)ov, 1.0, mv(Lovoo_.p, ix1(1), ix1(o2)), mv(t1, ix1(0), ix1(1)), 1.0,
+         ovw(Loo_.p, ix1(1), ix1(0)));
+    // Lvv[a][c] = Fvv - sum_k t1[k,a] f_kc + sum_kd Lovvv[k,d,a,c] t1[k,d]
+    CCSD_CUDA(cudaMemcpyAsync(Lvv_.p, Fvv_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
+    gemm(iv, iv, io, -1.0, mv(t1, ix1(1), ix1(v)), mv(f_ov_.p, ix1(1), ix1(v)), 1.0,
+         ovw(Lvv_.p, ix1(v), ix1(1)));
+    gemm((int)v2, 1, (int)ov, 1.0, mv(Lovvv_.p, ix1(1), ix1(v2)), mv(t1, ix1(0), ix1(1)), 1.0,
+         ovw(Lvv_.p, ix1(1), ix1(0)));
+
+    // ---- T1 numerator ----------------------------------------------------
+    CCSD_CUDA(cudaMemcpyAsync(R1_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
+    // -2 sum_kc f_kc t1[k,a] t1[i,c]: tmpo[i][k] = sum_c t1[i,c] f_kc
+    gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(f_ov_.p, ix1(v), ix1(1)), 0.0,
+         ovw(tmpo_.p, ix1(o), ix1(1)));
+    gemm(io, iv, io, -2.0, mv(tmpo_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)));
+    // + sum_c Fvv'[a,c] t1[i,c]
+    gemm(io, iv, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(Fvv_.p, ix1(v), ix1(1)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)));
+    // - sum_k Foo'[k,i] t1[k,a]
+    gemm(io, iv, io, -1.0, mv(Foo_.p, ix1(1), ix1(o)), mv(t1, ix1(1), ix1(v)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)));
+    // + sum_kc Fov[k,c] (2 t2[k,i,c,a] - t2[i,k,c,a])
+    gemm((int)ov, 1, (int)ov, 2.0, mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)),
+         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)));
+    gemm((int)ov, 1, (int)ov, -1.0, mv(t2, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)),
+         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)));
+    // + sum_kc Fov[k,c] t1[i,c] t1[k,a]
+    gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(Fov_.p, ix1(v), ix1(1)), 0.0,
+         ovw(tmpo2_.p, ix1(o), ix1(1)));
+    gemm(io, iv, io, 1.0, mv(tmpo2_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)));
+    // + sum_kc LT1[i,a,k,c] t1[k,c]
+    gemm((int)ov, 1, (int)ov, 1.0, mv(LT1_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
+         ovw(R1_.p, ix1(1), ix1(0)));
+    // + sum_kcd Lovvv[k,d,a,c] tau[i,k,c,d]
+    gemm(io, iv, (int)(o * v2), 1.0, mv(tau, ix1(ov2), ix1(1)),
+         mv(Lovvv_.p, ix1(v), ix3((uint32_t)v, (uint32_t)v, v * v2, 1, v2)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 3);
+    // - sum_klc Lovoo[l,c,k,i] tau[k,l,a,c]
+    gemm(io, iv, (int)(o2 * v), -1.0,
+         mv(Lovoo_.p, ix1(1), ix3((uint32_t)o, (uint32_t)v, o, v * o2, o2)),
+         mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)), 1.0,
+         ovw(R1_.p, ix1(v), ix1(1)), 4, 0);
+
+    // ---- Woooo[k][l][i][j] ------------------------------------------------
+    axpby_view((int)o2, (int)o2, 1.0, mv(oooo_.p, ix2((uint32_t)o, o * o2, o), ix2((uint32_t)o, o2, 1)),
+               0.0, ovw(Woooo_.p, ix1(o2), ix1(1)), st);
+    // + sum_c (lc|ki) t1[j,c]: M = (k,l,i), N = j, K = c
+    gemm((int)(o * o2), io, iv, 1.0,
+         mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, o, v * o2, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
+         1.0, ovw(Woooo_.p, ix1(o), ix1(1)));
+    // + sum_c (kc|lj) t1[i,c]: M = (k,l,j), N = i
+    gemm((int)(o * o2), io, iv, 1.0,
+         mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, v * o2, o, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
+         1.0, ovw(Woooo_.p, ix3((uint32_t)o, (uint32_t)o, o * o2, o2, 1), ix1(o)));
+    // + sum_cd (kc|ld) tau[i,j,c,d]: M = (k,l), N = (i,j), K = (c,d)
+    gemm((int)o2, (int)o2, (int)v2, 1.0,
+         mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
+         mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, 0);
+
+    // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
+    CCSD_CUDA(cudaMemcpyAsync(Wvoov_.p, ovov_.p, sizeof(double) * ov * ov, cudaMemcpyDeviceToDevice, st));
+    // + sum_d (kc|ad) t1[i,d]: M = (k,c,a), N = i, K = d
+    gemm((int)(ov * v), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
+         ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0);
+    // - sum_l (kc|li) t1[l,a]: M = (k,c,i), N = a, K = l
+    gemm((int)(ov * o), iv, io, -1.0,
+         mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, v * o2, o2, 1), ix1(o)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)));
+    // + sum_ld th1[i,a,l,d] (ld|kc)
+    gemm((int)ov, (int)ov, (int)ov, 1.0, mv(th1_.p, ix1(ov), ix1(1)), mv(ovov_.p, ix1(ov), ix1(1)),
+         1.0, ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 7);
+    // - 1/2 sum_ld (lc|kd) t2[i,l,a,d]
+    gemm((int)ov, (int)ov, (int)ov, -0.5, mv(t2, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)),
+         mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
+         ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 8);
+
+    // ---- Wvovo_s[i][a][k][c] = W_akci ------------------------------------
+    axpby_view((int)ov, (int)ov, 1.0, mv(oovv_.p, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)),
+               0.0, ovw(Wvovo_.p, ix1(ov), ix1(1)), st);
+    // + sum_d (kd|ac) t1[i,d]: M = (k,a,c), N = i, K = d
+    gemm((int)(ov * v), io, iv, 1.0,
+         mv(ovvv_.p, ix3((uint32_t)v, (uint32_t)v, v * v2, v, 1), ix1(v2)), mv(t1, ix1(v), ix1(1)),
+         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)v, v, ov, 1), ix1(v * ov)), 9, 0);
+    // - sum_l (lc|ki) t1[l,a]: M = (k,c,i), N = a, K = l
+    gemm((int)(ov * o), iv, io, -1.0,
+         mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, o, o2, 1), ix1(v * o2)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)));
+    // - sum_ld th2[i,a,l,d] (lc|kd)
+    gemm((int)ov, (int)ov, (int)ov, -1.0, mv(th2_.p, ix1(ov), ix1(1)),
+         mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
+         ovw(Wvovo_.p, ix1(ov), ix1(1)), 0, 8);
+    // Wa = 2 Wvoov - Wvovo
+    axpby_view((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
+    axpby_view((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
+
+    // ---- R (symmetric terms) ---------------------------------------------
+    // (ia|jb)
+    axpby_view((int)o2, (int)v2, 1.0,
+               mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
+               ovw(R_.p, ix1(v2), ix1(1)), st);
+    // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b]
+    gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
+         1.0, ovw(R_.p, ix1(v2), ix1(1)));
+    // + sum_cd (ac|bd) tau[i,j,c,d]: the v^4 particle-particle ladder, M = (a,b), N = (i,j)
+    gemm((int)v2, (int)o2, (int)v2, 1.0, mv(wv_.p, ix1(v2), ix1(1)), mv(tau, ix1(v2), ix1(1)), 1.0,
+         ovw(R_.p, ix1(1), ix1(v2)), 10, 0);
+
+    // ---- Rp (terms under P(ij,ab)) -----------------------------------------
+    // + sum_c (ia|bc) t1[j,c]: M = (i,a,b), N = j, K = c
+    gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
+         ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0);
+    // - sum_k t1[k,a] sum_c (ki|bc) t1[j,c]: Vk[k][i][b][j] = sum_c oovv[k,i,b,c] t1[j,c]
+    gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
+         ovw(Vk_.p, ix1(o), ix1(1)));
+    gemm((int)(o * v * o), iv, io, -1.0,
+         mv(Vk_.p, ix3((uint32_t)v, (uint32_t)o, v * o, o, 1), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)o, ov2, 1, v2), ix1(v)));
+    // - sum_k tmpB[k,i,a,j] t1[k,b], tmpB = (ia|jk) + sum_c (kc|ia) t1[j,c]
+    axpby_view((int)(o * ov), io, 1.0,
+               mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), 0.0,
+               ovw(tmpB_.p, ix1(o), ix1(1)), st);
+    gemm((int)(o * ov), io, iv, 1.0,
+         mv(ovov_.p, ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1), ix1(o * v)), mv(t1, ix1(v), ix1(1)),
+         1.0, ovw(tmpB_.p, ix1(o), ix1(1)));
+    gemm((int)(o2 * v), iv, io, -1.0,
+         mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Rp_.p, ix1(v), ix1(1)));
+    // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d]
+    gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
+         mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
+         ovw(Z_.p, ix1(ov), ix1(1)), 0, 12);
+    gemm((int)(o2 * v), iv, io, -1.0, mv(Z_.p, ix2((uint32_t)v, ov, 1), ix1(v)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Rp_.p, ix1(v), ix1(1)));
+    // + sum_c Lvv'[a,c] t2[i,j,c,b]: M = a, N = (i,j,b), K = c
+    gemm(iv, (int)(o2 * v), iv, 1.0, mv(Lvv_.p, ix1(v), ix1(1)),
+         mv(t2, ix2((uint32_t)v, v2, 1), ix1(v)), 1.0, ovw(Rp_.p, ix1(v), ix2((uint32_t)v, v2, 1)));
+    // - sum_k Loo'[k,i] t2[k,j,a,b]: M = i, N = (j,a,b), K = k
+    gemm(io, (int)ov2, io, -1.0, mv(Loo_.p, ix1(1), ix1(o)), mv(t2, ix1(1), ix1(ov2)), 1.0,
+         ovw(Rp_.p, ix1(ov2), ix1(1)));
+    // rings, M = (i,a), N = (j,b), K = (k,c)
+    // + sum_kc Wa[i,a,k,c] t2[k,j,c,b]
+    gemm((int)ov, (int)ov, (int)ov, 1.0, mv(Wa_.p, ix1(ov), ix1(1)),
+         mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)), 1.0,
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)));
+    // - sum_kc Wvoov[i,a,k,c] t2[k,j,b,c]
+    gemm((int)ov, (int)ov, (int)ov, -1.0, mv(Wvoov_.p, ix1(ov), ix1(1)),
+         mv(t2, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)), 1.0,
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)));
+    // - sum_kc Wvovo[i,b,k,c] t2[k,j,a,c]: M = (i,b), N = (j,a)
+    gemm((int)ov, (int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)),
+         mv(t2, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)), 1.0,
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)));
+}
+
+double Engine::reduce_sum(int nparts) {
+    k_sum(nparts, partials_.p, scalars_.p, st_);
+    double h = 0.0;
+    CCSD_CUDA(cudaMemcpyAsync(&h, scalars_.p, sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+    return h;
+}
+
+// E = sum_ijab [2(ia|jb) - (ib|ja)] tau_ij^ab  (ccsd_memory_optimized.cpp:592-648,
+// without the f_ia t_i^a term, :646)
+double Engine::energy_of(const double *t1, const double *t2) {
+    const size_t nT2 = (size_t)o_ * o_ * v_ * v_;
+    k_tau(o_, v_, t1, t2, tau_.p, st_);
+    k_dot(nT2, Lijab_.p, tau_.p, partials_.p, reduce_blocks(), st_);
+    return reduce_sum(reduce_blocks());
+}
+
+// Pulay DIIS on the amplitude vector (t1, t2) with errors T_new - T_old.
+// No counterpart in the reference CCSD; the reference's SCF DIIS
+// (hartree_fock_solver.cpp:1252-1311) builds B_ij = <e_i, e_j> and solves the
+// bordered system the same way.  A singular system keeps the plain step.
+void Engine::diis_step(int update_index) {
+    const int m = opt_.diis_size;
+    if (m <= 0) return;
+    const size_t nT1 = (size_t)o_ * v_, nT2 = nT1 * o_ * v_, len = nT1 + nT2;
+    if ((int)diis_t_.size() != m) {
+        diis_t_.clear();
+        diis_e_.clear();
+        for (int i = 0; i < m; ++i) {
+            diis_t_.emplace_back(len);
+            diis_e_.emplace_back(len);
+        }
+        diis_b_.assign((size_t)m * m, 0.0);
+        diis_count_ = 0;
+        diis_next_ = 0;
+    }
+    const int slot = diis_next_;
+    DBuf &T = diis_t_[slot], &E = diis_e_[slot];
+    CCSD_CUDA(cudaMemcpyAsync(T.p, t1n_.p, nT1 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+    CCSD_CUDA(cudaMemcpyAsync(T.p + nT1, t2n_.p, nT2 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+    CCSD_CUDA(cudaMemcpyAsync(E.p, t1n_.p, nT1 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+    CCSD_CUDA(cudaMemcpyAsync(E.p + nT1, t2n_.p, nT2 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+    axpby_view(1, (int)nT1, -1.0, mv(t1_.p, ix1(0), ix1(1)), 1.0, ovw(E.p, ix1(0), ix1(1)), st_);
+    axpby_view(1, (int)nT2, -1.0, mv(t2_.p, ix1(0), ix1(1)), 1.0, ovw(E.p + nT1, ix1(0), ix1(1)), st_);
+    diis_next_ = (diis_next_ + 1) % m;
+    diis_count_ = std::min(diis_count_ + 1, m);
+    for (int j = 0; j < m; ++j) {
+        if (j != slot && j >= diis_count_ && diis_count_ < m) continue;
+        if (j >= (int)diis_e_.size()) continue;
+        if (diis_count_ < m && j >= diis_count_) continue;
+        k_dot(len, E.p, diis_e_[j].p, partials_.p, reduce_blocks(), st_);
+        double d = reduce_sum(reduce_blocks());
+        diis_b_[(size_t)slot * m + j] = d;
+        diis_b_[(size_t)j * m + slot] = d;
+    }
+    if (diis_count_ < 2 || update_index < opt_.diis_start) return;
+    // bordered system [B -1; -1 0] [c; lam] = [0; -1], scaled for conditioning
+    const int k = diis_count_;
+    std::vector<int> idx;
+    for (int j = 0; j < m && (int)idx.size() < k; ++j) idx.push_back(j);
+    const int nn = k + 1;
+    std::vector<double> A((size_t)nn * nn, 0.0), rhs(nn, 0.0);
+    double scale = 0.0;
+    for (int a = 0; a < k; ++a) scale = std::max(scale, std::fabs(diis_b_[(size_t)idx[a] * m + idx[a]]));
+    if (!(scale > 0.0) || !std::isfinite(scale)) return;
+    for (int a = 0; a < k; ++a) {
+        for (int b = 0; b < k; ++b) A[(size_t)a * nn + b] = diis_b_[(size_t)idx[a] * m + idx[b]] / scale;
+        A[(size_t)a * nn + k] = -1.0;
+        A[(size_t)k * nn + a] = -1.0;
+    }
+    rhs[k] = -1.0;
+    // Gaussian elimination with partial pivoting
+    for (int c = 0; c < nn; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < nn; ++r)
+            if (std::fabs(A[(size_t)r * nn + c]) > std::fabs(A[(size_t)piv * nn + c])) piv = r;
+        if (std::fabs(A[(size_t)piv * nn + c]) < 1e-14) return;  // singular: keep the Jacobi step
+        if (piv != c) {
+            for (int q = 0; q < nn; ++q) std::swap(A[(size_t)c * nn + q], A[(size_t)piv * nn + q]);
+            std::swap(rhs[c], rhs[piv]);
+        }
+        for (int r = c + 1; r < nn; ++r) {
+            double f = A[(size_t)r * nn + c] / A[(size_t)c * nn + c];
+            for (int q = c; q < nn; ++q) A[(size_t)r * nn + q] -= f * A[(size_t)c * nn + q];
+            rhs[r] -= f * rhs[c];
+        }
+    }
+    std::vector<double> x(nn);
+    for (int r = nn - 1; r >= 0; --r) {
+        double s = rhs[r];
+        for (int q = r + 1; q < nn; ++q) s -= A[(size_t)r * nn + q] * x[q];
+        x[r] = s / A[(size_t)r * nn + r];
+    }
+    for (int a = 0; a < k; ++a)
+        if (!std::isfinite(x[a])) return;
+    // T_new = sum_a c_a T_a
+    k_fill(nT1, 0.0, t1n_.p, st_);
+    k_fill(nT2, 0.0, t2n_.p, st_);
+    for (int a = 0; a < k; ++a) {
+        const DBuf &Ta = diis_t_[idx[a]];
+        axpby_view(1, (int)nT1, x[a], mv(Ta.p, ix1(0), ix1(1)), 1.0, ovw(t1n_.p, ix1(0), ix1(1)), st_);
+        axpby_view(1, (int)nT2, x[a], mv(Ta.p + nT1, ix1(0), ix1(1)), 1.0, ovw(t2n_.p, ix1(0), ix1(1)),
+                   st_);
+    }
+}
+
+// ---------------------------------------------------------------------------
+void Engine::solve(ccsd_result *res) {
+    const int o = o_, v = v_;
+    const size_t nT1 = (size_t)o * v, nT2 = nT1 * o * v;
+    diis_t_.clear();
+    diis_e_.clear();
+    diis_count_ = diis_next_ = 0;
+    // T1 = 0, T2 = MP2 (ccsd_memory_optimized.cpp:473-490)
+    t1_.zero(st_);
+    k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
+    double e_new = energy_of(t1_.p, t2_.p);
+    int hist = 0;
+    if (res->energy_history && res->history_capacity > 0) res->energy_history[hist] = e_new;
+    hist = 1;
+
+    cudaEvent_t ev0, ev1;
+    CCSD_CUDA(cudaEventCreate(&ev0));
+    CCSD_CUDA(cudaEventCreate(&ev1));
+    int updates = 0;
+    bool converged = false;
+    const int cap = opt_.fixed_iterations > 0 ? opt_.fixed_iterations : std::max(opt_.max_iter, 1);
+    try {
+        while (true) {
+            const double e_old = e_new;
+            CCSD_CUDA(cudaEventRecord(ev0, st_));
+            residual();
+            k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
+            k_update_t1(o, v, R1_.p, eo_.p, ev_.p, t1_.p, t1n_.p, partials_.p + reduce_blocks(), st_);
+            const double rn2 = reduce_sum(reduce_blocks() + 1);
+            last_resid_ = std::sqrt(std::max(rn2, 0.0));
+            diis_step(updates);
+            std::swap(t1_, t1n_);
+            std::swap(t2_, t2n_);
+            e_new = energy_of(t1_.p, t2_.p);
+            CCSD_CUDA(cudaEventRecord(ev1, st_));
+            CCSD_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0.f;
+            CCSD_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            ++updates;
+            if (res->update_ms && updates - 1 < res->history_capacity) res->update_ms[updates - 1] = ms;
+            if (res->energy_history && hist < res->history_capacity) res->energy_history[hist] = e_new;
+            ++hist;
+            if (split_) {
+                int st = split_->error_status();
+                if (st) throw Error(CCSD_ERR_TIMEOUT, "split-precision kernel reported a bounded-wait timeout");
+            }
+            if (opt_.verbose)
+                std::printf("ccsd update %3d  E_corr = %.15e  dE = %.3e  |dT| = %.3e  %.3f ms\n", updates,
+                            e_new, e_new - e_old, last_resid_, ms);
+            if (!std::isfinite(e_new) || !std::isfinite(last_resid_))
+                throw Error(CCSD_ERR_DIVERGED, "amplitude iteration diverged (NaN/Inf)");
+            if (opt_.fixed_iterations > 0) {
+                if (updates >= opt_.fixed_iterations) break;
+                continue;
+            }
+            bool ok = std::fabs(e_new - e_old) < opt_.energy_tol;
+            if (opt_.residual_tol > 0.0) ok = ok && last_resid_ < opt_.residual_tol;
+            if (ok) {
+                converged = true;
+                break;
+            }
+            if (updates >= cap) break;
+        }
+    } catch (...) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        throw;
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    res->e_corr = e_new;
+    res->residual_norm = last_resid_;
+    res->iterations = updates;
+    res->converged = converged ? 1 : 0;
+    res->history_len = std::min(hist, std::max(res->history_capacity, 0));
+    res->flops_per_update = ccsd_flops_per_update(o, v);
+    if (res->t1) CCSD_CUDA(cudaMemcpyAsync(res->t1, t1_.p, nT1 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    if (res->t2) CCSD_CUDA(cudaMemcpyAsync(res->t2, t2_.p, nT2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+}
+
+}  // namespace ccsd

@@ -1,0 +1,87 @@
+// CCSD amplitude engine: device-resident integrals, amplitudes and
+// intermediates for one closed-shell system, and the iteration driver.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "../../include/ccsd_gb300.h"
+#include "common.h"
+#include "split_gemm.h"
+
+namespace ccsd {
+
+// Owning device buffer of doubles.
+struct DBuf {
+    double *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    explicit DBuf(size_t count);
+    ~DBuf();
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf &operator=(DBuf &&o) noexcept;
+    void alloc(size_t count);
+    void zero(cudaStream_t st);
+};
+
+class Engine {
+  public:
+    Engine(const ccsd_problem &prob, const ccsd_options &opts);
+    ~Engine();
+    void set_options(const ccsd_options &opts);
+    void solve(ccsd_result *res);
+
+    int nocc() const { return o_; }
+    int nvir() const { return v_; }
+
+  private:
+    // set-up
+    void build_integrals(const ccsd_problem &prob);
+    void build_from_mo_dense(const double *eri_dev);
+    void build_from_df(const double *b_dev, int naux);
+    void ao_to_mo(const double *ao_dev, const double *c_dev, int nao, DBuf &mo_out);
+    void build_derived();
+
+    // contractions: C(m,n) = alpha sum_k A(m,k) B(n,k) + beta C(m,n).
+    // `cache_a/b` != 0 marks an operand view over constant integrals whose
+    // split form is kept between updates.
+    void gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+              const OutView &C, int cache_a = 0, int cache_b = 0);
+    bool use_split(int M, int N, int K) const;
+
+    // one amplitude update: residual numerators from (t1_, t2_)
+    void residual();
+    double energy_of(const double *t1, const double *t2);  // uses tau_ as scratch
+    double reduce_sum(int nparts);
+    void diis_step(int update_index);
+
+    int o_ = 0, v_ = 0, n_ = 0;
+    ccsd_options opt_{};
+    cudaStream_t st_ = nullptr;
+    bool own_stream_ = false;
+
+    // fock-derived
+    DBuf eo_, ev_, f_oo_off_, f_vv_off_, f_ov_;
+    // integral blocks (chemist): ovov[i][a][j][b], oovv[i][j][a][b], ovoo[i][a][j][k],
+    // oooo[i][j][k][l], ovvv[i][a][b][c], Wv[a][b][c][d] = (ac|bd)
+    DBuf ovov_, oovv_, ovoo_, oooo_, ovvv_, wv_;
+    // derived: L-combinations
+    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_;
+    // amplitudes and intermediates
+    DBuf t1_, t2_, t1n_, t2n_, tau_, th1_, th2_;
+    DBuf R1_, R_, Rp_;
+    DBuf Foo_, Fvv_, Fov_, Loo_, Lvv_, tmpo_, tmpo2_;
+    DBuf Woooo_, Wvoov_, Wvovo_, Wa_, Z_, tmpB_, Vk_;
+    DBuf ws_, partials_, scalars_;
+    // DIIS storage: vectors (T) and errors (T_new - T_old), each o*v + o^2 v^2
+    std::vector<DBuf> diis_t_, diis_e_;
+    int diis_count_ = 0, diis_next_ = 0;
+    std::vector<double> diis_b_;  // (n x n) overlap matrix of stored errors
+
+    std::unique_ptr<SplitEngine> split_;
+    double last_resid_ = 0.0;
+};
+
+}  // namespace ccsd

@@ -1,0 +1,178 @@
+// FP64 contraction kernel of the plain-FP64 path.
+//
+// C(m,n) = alpha * sum_k A(m,k) B(n,k) + beta * C(m,n), with A, B and C read
+// and written through 3-level index views (common.h), so a 4-index CCSD
+// contraction runs without a transposed copy.  tcgen05 has no f64 kind, so
+// this path is DFMA on the CUDA cores: a 64x64 block tile, 16-deep K step,
+// 4x4 register micro-tile per thread.  Skinny shapes are split over K into a
+// scratch buffer and summed in a fixed order (deterministic results).
+#include "common.h"
+
+namespace ccsd {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+template <bool A_KC, bool B_KC>
+__global__ void __launch_bounds__(NT) gemm_f64_kernel(int M, int N, int K, int kchunk,
+                                                        double alpha, MatView A, MatView B,
+                                                        double beta, OutView C, double *ws) {
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(K, kbeg + kchunk);
+
+    // Load mapping. K-contiguous operand: thread reads k = tid%16 of rows
+    // tid/16 + 16q; otherwise m = tid%64 of k = tid/64 + 4q.
+    int64_t a_row[4], b_row[4];
+    bool a_ok[4], b_ok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        int ra = A_KC ? (tid / 16 + 16 * q) : (tid % 64);
+        int rb = B_KC ? (tid / 16 + 16 * q) : (tid % 64);
+        a_ok[q] = (m0 + ra) < M;
+        b_ok[q] = (n0 + rb) < N;
+        a_row[q] = a_ok[q] ? dim_off(A.row, m0 + ra) : 0;
+        b_row[q] = b_ok[q] ? dim_off(B.row, n0 + rb) : 0;
+    }
+
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int ka = A_KC ? (tid % 16) : (tid / 64 + 4 * q);
+            int ra = A_KC ? (tid / 16 + 16 * q) : (tid % 64);
+            int kk = k0 + ka;
+            double va = 0.0;
+            if (a_ok[q] && kk < kend) va = A.p[a_row[q] + dim_off(A.col, kk)];
+            As[ka][ra] = va;
+            int kb = B_KC ? (tid % 16) : (tid / 64 + 4 * q);
+            int rb = B_KC ? (tid / 16 + 16 * q) : (tid % 64);
+            int kk2 = k0 + kb;
+            double vb = 0.0;
+            if (b_ok[q] && kk2 < kend) vb = B.p[b_row[q] + dim_off(B.col, kk2)];
+            Bs[kb][rb] = vb;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+
+    if (gridDim.z == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            int m = m0 + ty + 16 * i;
+            if (m >= M) continue;
+            int64_t ro = dim_off(C.row, m);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int n = n0 + tx + 16 * j;
+                if (n >= N) continue;
+                double *c = C.p + ro + dim_off(C.col, n);
+                double v = alpha * acc[i][j];
+                if (beta != 0.0) v = fma(beta, *c, v);
+                *c = v;
+            }
+        }
+    } else {
+        double *w = ws + (size_t)blockIdx.z * M * N;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            int m = m0 + ty + 16 * i;
+            if (m >= M) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int n = n0 + tx + 16 * j;
+                if (n < N) w[(size_t)m * N + n] = acc[i][j];
+            }
+        }
+    }
+}
+
+__global__ void splitk_reduce_kernel(int M, int N, int splits, double alpha, const double *ws,
+                                     double beta, OutView C) {
+    size_t total = (size_t)M * N;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int z = 0; z < splits; ++z) s += ws[z * total + idx];
+        int m = (int)(idx / N), n = (int)(idx % N);
+        double *c = C.p + dim_off(C.row, m) + dim_off(C.col, n);
+        double v = alpha * s;
+        if (beta != 0.0) v = fma(beta, *c, v);
+        *c = v;
+    }
+}
+
+constexpr int kTargetBlocks = 2 * 152;
+
+int choose_splits(int M, int N, int K) {
+    long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    if (tiles >= kTargetBlocks) return 1;
+    long want = (kTargetBlocks + tiles - 1) / tiles;
+    long maxk = (K + 63) / 64;
+    long s = want < maxk ? want : maxk;
+    if (s > 64) s = 64;
+    return s < 1 ? 1 : (int)s;
+}
+
+}  // namespace
+
+size_t gemm_f64_ws_elems(int M, int N, int K) {
+    int s = choose_splits(M, N, K);
+    return s > 1 ? (size_t)s * M * N : 0;
+}
+
+void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+              const OutView &C, double *ws, size_t ws_elems, cudaStream_t st) {
+    if (M <= 0 || N <= 0) return;
+    if (K <= 0) {
+        axpby_view(M, N, 0.0, MatView{C.p, C.row, C.col}, beta, C, st);
+        return;
+    }
+    int splits = choose_splits(M, N, K);
+    while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
+    int kchunk = (K + splits - 1) / splits;
+    kchunk = (kchunk + BK - 1) / BK * BK;
+    splits = (K + kchunk - 1) / kchunk;
+    dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
+    bool akc = A.col.s2 == 1;
+    bool bkc = B.col.s2 == 1;
+    if (akc && bkc)
+        gemm_f64_kernel<true, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    else if (akc)
+        gemm_f64_kernel<true, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    else if (bkc)
+        gemm_f64_kernel<false, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    else
+        gemm_f64_kernel<false, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    CCSD_CUDA(cudaGetLastError());
+    if (splits > 1) {
+        size_t total = (size_t)M * N;
+        int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+        splitk_reduce_kernel<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
+        CCSD_CUDA(cudaGetLastError());
+    }
+}
+
+}  // namespace ccsd

@@ -1,0 +1,233 @@
+// Memory-bound kernels of the amplitude iteration: strided permute-add, tau,
+// the T2/T1 energy-denominator updates, the MP2 guess and the deterministic
+// reductions behind E_corr and the residual norm.  All FP64; their roofline
+// is HBM bandwidth.
+//
+// Index conventions (closed-shell spatial): t1[i][a], t2[i][j][a][b].
+#include "common.h"
+
+namespace ccsd {
+
+namespace {
+
+constexpr int kReduceBlocks = 4 * 152;
+constexpr int kReduceThreads = 256;
+
+inline int grid_for(size_t n, int threads = 256) {
+    size_t b = (n + threads - 1) / threads;
+    if (b > 8 * 152 * 4) b = 8 * 152 * 4;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+__global__ void axpby_view_kernel(int R, int C, double alpha, MatView X, double beta, OutView Y) {
+    size_t total = (size_t)R * C;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        uint32_t r = (uint32_t)(idx / C), c = (uint32_t)(idx % C);
+        double *y = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
+        double v = alpha == 0.0 ? 0.0 : alpha * X.p[dim_off(X.row, r) + dim_off(X.col, c)];
+        if (beta != 0.0) v = fma(beta, *y, v);
+        *y = v;
+    }
+}
+
+__global__ void tau_kernel(int o, int v, const double *t1, const double *t2, double *tau) {
+    size_t total = (size_t)o * o * v * v;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int b = idx % v;
+        size_t r = idx / v;
+        int a = r % v;
+        r /= v;
+        int j = r % o;
+        int i = (int)(r / o);
+        tau[idx] = t2[idx] + t1[i * v + a] * t1[j * v + b];
+    }
+}
+
+// th1[i,a,l,d] = t2[i,l,a,d] - t2[i,l,d,a]/2 - t1[i,d] t1[l,a]
+// th2[i,a,l,d] = t2[i,l,d,a]/2 + t1[i,d] t1[l,a]
+__global__ void theta_kernel(int o, int v, const double *t1, const double *t2, double *th1,
+                             double *th2) {
+    size_t total = (size_t)o * v * o * v;
+    size_t ov2 = (size_t)o * v * v, v2 = (size_t)v * v;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int d = idx % v;
+        size_t r = idx / v;
+        int l = r % o;
+        r /= o;
+        int a = r % v;
+        int i = (int)(r / v);
+        double tad = t2[i * ov2 + l * v2 + (size_t)a * v + d];
+        double tda = t2[i * ov2 + l * v2 + (size_t)d * v + a];
+        double tt = t1[i * v + d] * t1[l * v + a];
+        th1[idx] = tad - 0.5 * tda - tt;
+        th2[idx] = 0.5 * tda + tt;
+    }
+}
+
+__global__ void mp2_kernel(int o, int v, const double *ovov, const double *eo, const double *ev,
+                           double *t2) {
+    size_t total = (size_t)o * o * v * v;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int b = idx % v;
+        size_t r = idx / v;
+        int a = r % v;
+        r /= v;
+        int j = r % o;
+        int i = (int)(r / o);
+        double g = ovov[(((size_t)i * v + a) * o + j) * v + b];
+        t2[idx] = g / (eo[i] + eo[j] - ev[a] - ev[b]);
+    }
+}
+
+__device__ double block_sum(double x) {
+    __shared__ double sh[32];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = x;
+    __syncthreads();
+    double s = 0.0;
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        s = lane < nw ? sh[lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    }
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+__global__ void update_t2_kernel(int o, int v, const double *R, const double *Rp,
+                                 const double *eo, const double *ev, const double *t2_old,
+                                 double *t2_new, double *partials) {
+    size_t total = (size_t)o * o * v * v;
+    size_t v2 = (size_t)v * v, ov2 = (size_t)o * v2;
+    double acc = 0.0;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int b = idx % v;
+        size_t r = idx / v;
+        int a = r % v;
+        r /= v;
+        int j = r % o;
+        int i = (int)(r / o);
+        double num = R[idx] + Rp[idx] + Rp[j * ov2 + i * v2 + (size_t)b * v + a];
+        double t = num / (eo[i] + eo[j] - ev[a] - ev[b]);
+        double d = t - t2_old[idx];
+        acc = fma(d, d, acc);
+        t2_new[idx] = t;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void update_t1_kernel(int o, int v, const double *R1, const double *eo,
+                                 const double *ev, const double *t1_old, double *t1_new,
+                                 double *partials) {
+    double acc = 0.0;
+    for (int idx = threadIdx.x; idx < o * v; idx += blockDim.x) {
+        int i = idx / v, a = idx % v;
+        double t = R1[idx] / (eo[i] - ev[a]);
+        double d = t - t1_old[idx];
+        acc = fma(d, d, acc);
+        t1_new[idx] = t;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[0] = s;
+}
+
+__global__ void dot_kernel(size_t n, const double *x, const double *y, double *partials) {
+    double acc = 0.0;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x)
+        acc = fma(x[idx], y[idx], acc);
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void sum_kernel(int n, const double *partials, double *out) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partials[i];
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+__global__ void fill_kernel(size_t n, double val, double *p) {
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x)
+        p[idx] = val;
+}
+
+__global__ void copy_diag_kernel(int n, const double *fock, int off, int cnt, double *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < cnt) out[i] = fock[(size_t)(off + i) * n + off + i];
+}
+
+}  // namespace
+
+int reduce_blocks() { return kReduceBlocks; }
+
+void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
+                cudaStream_t st) {
+    if (R <= 0 || C <= 0) return;
+    axpby_view_kernel<<<grid_for((size_t)R * C), 256, 0, st>>>(R, C, alpha, X, beta, Y);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st) {
+    tau_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, tau);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
+             cudaStream_t st) {
+    theta_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const double *ev, double *t2,
+                 cudaStream_t st) {
+    mp2_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, ovov, eo, ev, t2);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
+                 const double *ev, const double *t2_old, double *t2_new, double *partials,
+                 int nblocks, cudaStream_t st) {
+    update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new,
+                                                         partials);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_update_t1(int o, int v, const double *R1, const double *eo, const double *ev,
+                 const double *t1_old, double *t1_new, double *partials, cudaStream_t st) {
+    update_t1_kernel<<<1, 1024, 0, st>>>(o, v, R1, eo, ev, t1_old, t1_new, partials);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_dot(size_t n, const double *x, const double *y, double *partials, int nblocks,
+           cudaStream_t st) {
+    dot_kernel<<<nblocks, kReduceThreads, 0, st>>>(n, x, y, partials);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_sum(int n, const double *partials, double *out, cudaStream_t st) {
+    sum_kernel<<<1, 1024, 0, st>>>(n, partials, out);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_fill(size_t n, double val, double *p, cudaStream_t st) {
+    if (n == 0) return;
+    fill_kernel<<<grid_for(n), 256, 0, st>>>(n, val, p);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st) {
+    copy_diag_kernel<<<(cnt + 255) / 256, 256, 0, st>>>(n, fock, off, cnt, out);
+    CCSD_CUDA(cudaGetLastError());
+}
+
+}  // namespace ccsd

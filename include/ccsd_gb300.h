@@ -1,0 +1,140 @@
+/*
+ * ccsd_gb300.h -- C ABI of the GB300 (sm_103a) CCSD amplitude engine.
+ *
+ * The engine is a drop-in for the iterative part of the reference class
+ * CCSD_Memory_optimized (otnorli/CCSD_PARALLEL):
+ *
+ *   reference                                         this ABI
+ *   ---------------------------------------------------------------------------
+ *   CCSD_Memory_optimized::CCSD(double toler, bool)   ccsd_create + ccsd_solve
+ *     (ccsd_memory_optimized.h:47, .cpp:16-567)
+ *   Prepear_AOs (AO->MO, .cpp:2698-3522)              integral_kind AO_DENSE /
+ *                                                     MO_DENSE / DF in ccsd_problem
+ *   Fill_FS (diagonal spin-orbital Fock, .cpp:3560)   ccsd_problem.fock (spatial)
+ *   MP2 guess + loop (.cpp:473-557)                   ccsd_solve
+ *   t2 / T_1 / E_new (class members)                  ccsd_result.t2 / t1 / e_corr
+ *   (no counterpart)                                  ccsd_lambda_grad, ccsd_solve_batched
+ *
+ * Conventions
+ *   - Spatial closed-shell quantities.  nocc / nvir are spatial counts
+ *     (reference: n_Electrons = 2*nocc, unocc_orb = 2*nvir).  Amplitudes are
+ *     returned as t1[i][a] (nocc x nvir) and t2[i][j][a][b]; the spin-orbital
+ *     amplitude of the reference is t(a alpha, b beta, i alpha, j beta) =
+ *     t2[i][j][a][b] and the same-spin block is t2[i][j][a][b] - t2[j][i][a][b].
+ *   - Integrals are real, chemist notation (pq|rs), 8-fold symmetric.
+ *   - Every function returns CCSD_OK (0) or a negative error code; the text of
+ *     the last error of the calling thread is available from ccsd_last_error.
+ *     No C++ exception crosses this boundary.
+ *   - The caller owns every host buffer.  A handle owns its device memory.
+ *     One handle must not be used by two threads at once.
+ *   - There is no CPU path: ccsd_create fails with CCSD_ERR_NO_DEVICE when no
+ *     CUDA device is present.
+ */
+#ifndef CCSD_GB300_H
+#define CCSD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define CCSD_OK 0
+#define CCSD_ERR_INVALID_ARG (-1)
+#define CCSD_ERR_CUDA (-2)
+#define CCSD_ERR_OUT_OF_MEMORY (-3)
+#define CCSD_ERR_DIVERGED (-4)      /* NaN/Inf in residual or energy        */
+#define CCSD_ERR_NO_DEVICE (-5)
+#define CCSD_ERR_TIMEOUT (-6)       /* a bounded device-side wait gave up   */
+#define CCSD_ERR_UNSUPPORTED (-7)
+#define CCSD_ERR_NOT_CONVERGED (-8) /* only from the C++ wrapper            */
+
+/* ---- integral input forms -------------------------------------------- */
+#define CCSD_INTS_MO_DENSE 0 /* eri = n^4 MO (pq|rs), row-major p,q,r,s         */
+#define CCSD_INTS_DF 1       /* df  = naux*n*n factors B[Q][p][q], (pq|rs) = sum_Q B B */
+#define CCSD_INTS_AO_DENSE 2 /* eri = nao^4 AO (mu nu|la si), mo_coeff = C[mu][p] */
+
+/* ---- contraction precision ------------------------------------------- */
+#define CCSD_PREC_FP64 0      /* every contraction in FP64 (DFMA)              */
+#define CCSD_PREC_SPLIT2 2    /* BF16 hi/lo slices, 3 tcgen05 products         */
+#define CCSD_PREC_SPLIT3 3    /* 3 BF16 slices, 6 tcgen05 products             */
+#define CCSD_PREC_SPLIT4 4    /* 4 BF16 slices, 10 tcgen05 products            */
+
+typedef struct ccsd_problem {
+    int32_t nocc;          /* spatial occupied orbitals (> 0)                  */
+    int32_t nvir;          /* spatial virtual orbitals (> 0)                   */
+    int32_t integral_kind; /* CCSD_INTS_*                                      */
+    int32_t naux;          /* DF: number of auxiliary functions                */
+    int32_t nao;           /* AO_DENSE: number of basis functions (>= n)       */
+    int32_t device_inputs; /* 0: pointers below are host memory; 1: device     */
+    const double *fock;    /* n x n MO Fock matrix, n = nocc + nvir            */
+    const double *eri;     /* MO_DENSE: n^4; AO_DENSE: nao^4                   */
+    const double *df;      /* DF: naux * n * n                                 */
+    const double *mo_coeff;/* AO_DENSE: nao x n, row-major C[mu][p]            */
+} ccsd_problem;
+
+typedef struct ccsd_options {
+    double energy_tol;         /* stop when |E_new - E_old| < energy_tol
+                                  (ccsd_memory_optimized.cpp:552)             */
+    double residual_tol;       /* also require ||T_new - T_old||_2 < this; 0 = off */
+    int32_t max_iter;          /* cap on amplitude updates (reference: 999)    */
+    int32_t fixed_iterations;  /* > 0: run exactly this many updates           */
+    int32_t diis_size;         /* 0 = plain Jacobi (reference); else vectors kept */
+    int32_t diis_start;        /* first update index that extrapolates         */
+    int32_t precision;         /* CCSD_PREC_*                                   */
+    int32_t verbose;           /* print one line per update to stdout          */
+    void *stream;              /* cudaStream_t, or NULL for a private stream   */
+} ccsd_options;
+
+typedef struct ccsd_result {
+    double e_corr;             /* correlation energy (E_new of the reference)  */
+    double residual_norm;      /* ||T_new - T_old||_2 of the last update       */
+    int32_t iterations;        /* amplitude updates performed                  */
+    int32_t converged;         /* 1 when the stopping rule was met             */
+    double *t1;                /* optional out: nocc*nvir host doubles         */
+    double *t2;                /* optional out: nocc^2*nvir^2 host doubles     */
+    double *energy_history;    /* optional out: E after 0..iterations updates  */
+    double *update_ms;         /* optional out: device ms of each update       */
+    int32_t history_capacity;  /* length of energy_history / update_ms         */
+    int32_t history_len;       /* entries written                              */
+    double flops_per_update;   /* algorithmic FLOP of one update (fixed count) */
+} ccsd_result;
+
+typedef struct ccsd_handle ccsd_handle;
+
+/* Defaults: energy_tol 1e-10, max_iter 999, FP64, no DIIS (reference rules). */
+int ccsd_default_options(ccsd_options *opts);
+
+/* Upload/transform the integrals and allocate the amplitude engine.
+ * Replaces the set-up half of CCSD_Memory_optimized::CCSD
+ * (ccsd_memory_optimized.cpp:49-466: AO->MO, Fill_FS, denominators). */
+int ccsd_create(const ccsd_problem *problem, const ccsd_options *opts, ccsd_handle **out);
+
+/* Run the amplitude iteration from the MP2 guess (T1 = 0) and fill `res`.
+ * Replaces ccsd_memory_optimized.cpp:473-566 (MP2 guess, loop, E_new). */
+int ccsd_solve(ccsd_handle *h, ccsd_result *res);
+
+/* Change options (precision, tolerances, DIIS, stream) between solves. */
+int ccsd_set_options(ccsd_handle *h, const ccsd_options *opts);
+
+int ccsd_destroy(ccsd_handle *h);
+
+/* Copy the calling thread's last error message; returns its length. */
+int ccsd_last_error(char *buf, size_t len);
+
+/* Algorithmic FLOP of one update: 2 o^2 v^4 + 4 o^4 v^2 + 8 o^3 v^3. */
+double ccsd_flops_per_update(int32_t nocc, int32_t nvir);
+
+/* Seeded synthetic closed-shell system (host only, no GPU needed): diagonal
+ * fock (n x n) with occupied U[-2,-0.3] / virtual U[0.1,3] energies, and
+ * DF factors B[Q][p][q] = 0.05 z / sqrt(naux), z ~ N(0,1), symmetric in p,q.
+ * Either output pointer may be NULL. */
+int ccsd_make_synthetic(int32_t nocc, int32_t nvir, int32_t naux, uint64_t seed,
+                        double *fock, double *df);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CCSD_GB300_H */

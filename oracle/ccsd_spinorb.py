@@ -1,0 +1,200 @@
+"""FP64 spin-orbital CCSD restatement of the reference (TEST INFRASTRUCTURE ONLY).
+
+Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
+``Method_Nr == -1`` ("CCSD1", ``initializer.cpp:98-103``):
+
+* antisymmetrised integrals <pq||rs> from spatial chemist (pq|rs), alpha/beta
+  interleaved (spin-orbital p -> spatial p//2, spin p%2)    ``ccsdt.cpp:1466-1478``
+* diagonal spin-orbital Fock fs(p,p) = eps(p//2)                ``ccsdt.cpp:1510-1516``
+* F1/F2/F3 (D1 = F_me, D2 = F_mi, D3 = F_ae)                   ``ccsdt.cpp:2529-2600``
+* W1 (W_mnij), W2, W3, W4 (W_mbej)                             ``ccsdt.cpp:2416-2526``
+* T1 residual (only spin-allowed (a+i) even)                   ``ccsdt.cpp:380-444``
+* T2 residual (a<b, i<j, (a+b+i+j) even, then the 4-fold
+  antisymmetric copies)                                        ``ccsdt.cpp:625-727``
+* tau = t2 + t1 t1 - t1 t1                                     ``ccsdt.cpp:2603-2620``
+* MP2 initial T2, T1 = 0                                       ``ccsdt.cpp:172-192``
+
+Driver semantics follow ``CCSD_Memory_optimized::CCSD``
+(``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
+the f_ia t_i^a term dropped (``:646``); ``iter`` starts at 1, each pass adds 1,
+the loop stops when |E_new - E_old| < toler or iter >= 1000 (``:552-556``).
+
+Arrays use the reference's index order: t1[a, i], t2[a, b, i, j],
+g[p, q, r, s] = <pq||rs>, with virtual indices offset by O (= n_Electrons).
+Only practical for a few dozen spin orbitals (dense N^4 integrals).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+ES = dict(optimize=True)
+
+
+def spin_orbital_integrals(eri: np.ndarray) -> np.ndarray:
+    """<pq||rs> over 2n interleaved spin orbitals from chemist (pq|rs)
+    (``ccsdt.cpp:1466-1478``: MOs(a,i)(b,j) = d(a,b)d(i,j)(ab|ij) - d(a,j)d(i,b)(aj|ib))."""
+    n = eri.shape[0]
+    N = 2 * n
+    sp = np.arange(N) // 2
+    spin = np.arange(N) % 2
+    same = (spin[:, None] == spin[None, :]).astype(np.float64)
+    # <pq|rs> = (pr|qs) delta(sp,sr) delta(sq,ss)
+    pr_qs = eri[np.ix_(sp, sp, sp, sp)]  # [p, r, q, s] = (pr|qs)
+    direct = pr_qs.transpose(0, 2, 1, 3) * same[:, None, :, None] * same[None, :, None, :]
+    return direct - direct.transpose(0, 1, 3, 2)
+
+
+def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
+    """fs(p,p) = eps(p/2) (``ccsdt.cpp:1510-1516``); off-diagonal spatial
+    elements are carried on same-spin pairs (the reference only ever fills
+    the diagonal)."""
+    n = fock.shape[0]
+    N = 2 * n
+    sp = np.arange(N) // 2
+    spin = np.arange(N) % 2
+    return fock[np.ix_(sp, sp)] * (spin[:, None] == spin[None, :])
+
+
+class SpinOrbitalCCSD:
+    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int):
+        """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial."""
+        self.fs = spin_orbital_fock(fock)
+        self.g = spin_orbital_integrals(eri)
+        self.O = 2 * nocc
+        self.N = self.fs.shape[0]
+        O, N = self.O, self.N
+        self.V = N - O
+        o, v = slice(0, O), slice(O, N)
+        g = self.g
+        self.goooo = g[o, o, o, o]
+        self.gooov = g[o, o, o, v]
+        self.goovo = g[o, o, v, o]
+        self.goovv = g[o, o, v, v]
+        self.govoo = g[o, v, o, o]
+        self.govov = g[o, v, o, v]
+        self.govvo = g[o, v, v, o]
+        self.govvv = g[o, v, v, v]
+        self.gvooo = g[v, o, o, o]
+        self.gvovo = g[v, o, v, o]
+        self.gvoov = g[v, o, o, v]
+        self.gvovv = g[v, o, v, v]
+        self.gvvoo = g[v, v, o, o]
+        self.gvvvo = g[v, v, v, o]
+        self.gvvvv = g[v, v, v, v]
+        self.f_vo = self.fs[v, o]
+        self.f_oo = self.fs[o, o]
+        self.f_vv = self.fs[v, v]
+        eo = np.diag(self.fs)[o]
+        ev = np.diag(self.fs)[v]
+        self.den = eo[None, :] - ev[:, None]  # den[a, i] = fs(i,i) - fs(a,a)
+        ai = (np.arange(O, N)[:, None] + np.arange(O)[None, :]) % 2 == 0
+        self.t1_mask = ai
+        a_idx = np.arange(O, N)
+        i_idx = np.arange(O)
+        par = (a_idx[:, None, None, None] + a_idx[None, :, None, None]
+               + i_idx[None, None, :, None] + i_idx[None, None, None, :]) % 2 == 0
+        upper = (a_idx[:, None, None, None] < a_idx[None, :, None, None]) & \
+                (i_idx[None, None, :, None] < i_idx[None, None, None, :])
+        self.t2_write = par & upper
+
+    # -- amplitudes ---------------------------------------------------------
+    def mp2_guess(self):
+        """t2(a,b)(i,j) = <ab||ij> / (den(a,i) + den(b,j)), t1 = 0."""
+        d2 = self.den[:, None, :, None] + self.den[None, :, None, :]
+        t2 = self.gvvoo / d2
+        t2 = np.where(self.full_mask(), t2, 0.0)
+        return np.zeros((self.V, self.O)), t2
+
+    def full_mask(self):
+        w = self.t2_write
+        return w | w.transpose(1, 0, 2, 3) | w.transpose(0, 1, 3, 2) | w.transpose(1, 0, 3, 2)
+
+    def tau(self, t1, t2):
+        return t2 + np.einsum("ai,bj->abij", t1, t1) - np.einsum("aj,bi->abij", t1, t1)
+
+    def energy(self, t1, t2):
+        """1/4 sum <ij||ab> tau_ij^ab; the f_ia t_i^a term is dropped as in
+        ``ccsd_memory_optimized.cpp:646``."""
+        return 0.25 * np.einsum("ijab,abij->", self.goovv, self.tau(t1, t2))
+
+    def update(self, t1, t2):
+        """One Jacobi pass: returns (t1_new, t2_new)."""
+        fs_vo, f_oo, f_vv = self.f_vo, self.f_oo, self.f_vv
+        O, V = self.O, self.V
+        tau = self.tau(t1, t2)
+        offd_oo = f_oo * (1.0 - np.eye(O))
+        offd_vv = f_vv * (1.0 - np.eye(V))
+        # F1 (D1[c,k])  ccsdt.cpp:2529-2546
+        D1 = fs_vo + np.einsum("klcd,dl->ck", self.goovv, t1, **ES)
+        # F2 (D2[k,i])  ccsdt.cpp:2549-2573
+        D2 = (offd_oo + np.einsum("ci,ck->ki", t1, D1, **ES)
+              + np.einsum("ickl,cl->ki", self.govoo, t1, **ES)
+              + 0.5 * np.einsum("klcd,cdil->ki", self.goovv, t2, **ES))
+        # F3 (D3[a,c])  ccsdt.cpp:2576-2600
+        D3 = (offd_vv - np.einsum("ak,ck->ac", t1, D1, **ES)
+              + np.einsum("akcd,dk->ac", self.gvovv, t1, **ES)
+              - 0.5 * np.einsum("klcd,adkl->ac", self.goovv, t2, **ES))
+        # W1[i,j,k,l]  ccsdt.cpp:2401-2424
+        W1 = (self.goooo - np.einsum("jckl,ci->ijkl", self.govoo, t1, **ES)
+              + np.einsum("ickl,cj->ijkl", self.govoo, t1, **ES)
+              + 0.5 * np.einsum("klcd,cdij->ijkl", self.goovv, tau, **ES))
+        # W2[a,k,i,j]  ccsdt.cpp:2427-2451
+        W2 = (np.einsum("ijak->akij", self.goovo)
+              + np.einsum("icak,cj->akij", self.govvo, t1, **ES)
+              - np.einsum("jcak,ci->akij", self.govvo, t1, **ES)
+              + 0.5 * np.einsum("akcd,cdij->akij", self.gvovv, tau, **ES))
+        # W3[c,i,k,l]  ccsdt.cpp:2454-2473
+        W3 = self.gvooo + np.einsum("cdkl,di->cikl", self.gvvoo, t1, **ES)
+        # W4[a,k,i,c]  ccsdt.cpp:2476-2504
+        W4 = (self.gvoov + np.einsum("kacd,di->akic", self.govvv, t1, **ES)
+              - np.einsum("al,cikl->akic", t1, W3, **ES)
+              + 0.5 * np.einsum("klcd,adil->akic", self.goovv, t2, **ES))
+        # T1  ccsdt.cpp:383-441 (Method_Nr < 0 branch)
+        R1 = (fs_vo - np.einsum("ak,ki->ai", t1, D2, **ES)
+              + offd_vv.sum(axis=1)[:, None]  # sum_c (1-delta_ac) fs(a,c), no t1 (as in the reference)
+              + np.einsum("cika,ck->ai", self.gvoov, t1, **ES)
+              + np.einsum("acik,ck->ai", t2, D1, **ES)
+              - 0.5 * np.einsum("cakl,cikl->ai", t2, W3, **ES)
+              + 0.5 * np.einsum("kacd,cdki->ai", self.govvv, tau, **ES))
+        t1_new = np.where(self.t1_mask, R1 / self.den, 0.0)
+        # T2  ccsdt.cpp:630-727 (Method_Nr < 0 branch)
+        ring = np.einsum("bcjk,akic->abij", t2, W4, **ES)
+        R2 = (np.einsum("ijab->abij", self.goovv)
+              + 0.5 * np.einsum("abkl,ijkl->abij", tau, W1, **ES)
+              - np.einsum("bk,akij->abij", t1, W2, **ES)
+              + np.einsum("ak,bkij->abij", t1, W2, **ES)
+              + np.einsum("abjk,ki->abij", t2, D2, **ES)
+              - np.einsum("abik,kj->abij", t2, D2, **ES)
+              + ring - ring.transpose(1, 0, 2, 3) - ring.transpose(0, 1, 3, 2)
+              + ring.transpose(1, 0, 3, 2)
+              - np.einsum("bcij,ac->abij", t2, D3, **ES)
+              + np.einsum("acij,bc->abij", t2, D3, **ES)
+              + np.einsum("abcj,ci->abij", self.gvvvo, t1, **ES)
+              - np.einsum("abci,cj->abij", self.gvvvo, t1, **ES)
+              + 0.5 * np.einsum("abcd,cdij->abij", self.gvvvv, tau, **ES))
+        d2 = self.den[:, None, :, None] + self.den[None, :, None, :]
+        val = np.where(self.t2_write, R2 / np.where(self.t2_write, d2, 1.0), 0.0)
+        # symmetric copies (ccsdt.cpp:720-723)
+        t2_new = val - val.transpose(1, 0, 2, 3) - val.transpose(0, 1, 3, 2) + val.transpose(1, 0, 3, 2)
+        return t1_new, t2_new
+
+    def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None):
+        """Reference driver loop. Returns dict with e_corr, energies (per
+        ``iter``), iter (reference counter), t1, t2."""
+        t1, t2 = self.mp2_guess()
+        e_new = self.energy(t1, t2)
+        energies = [e_new]
+        it = 1
+        passes = 0
+        while True:
+            e_old = e_new
+            t1, t2 = self.update(t1, t2)
+            e_new = self.energy(t1, t2)
+            it += 1
+            passes += 1
+            energies.append(e_new)
+            if abs(e_new - e_old) < toler or it >= itermax:
+                break
+            if max_passes is not None and passes >= max_passes:
+                break
+        return dict(e_corr=e_new, energies=np.array(energies), iter=it, t1=t1, t2=t2)

@@ -1,0 +1,94 @@
+"""CPU tests of the C ABI: the library loads without a GPU, exports every
+function include/ccsd_gb300.h declares, and its host-only helpers agree with
+the oracle.  No compute call runs here."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from ccsd_parallel_gb300 import _abi
+from oracle import synthetic as syn
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:int|double|void)\s*\*?\s*(ccsd_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _abi.lib()
+    names = _declared()
+    assert "ccsd_create" in names and "ccsd_solve" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # the ctypes table covers the same set
+    assert set(names) <= set(_abi.SIGNATURES)
+
+
+def test_struct_layouts_match_header_sizes():
+    assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8
+    assert C.sizeof(_abi.Options) == 2 * 8 + 6 * 4 + 8
+    assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
+
+
+def test_default_options_follow_reference_rules():
+    o = _abi.Options()
+    assert _abi.lib().ccsd_default_options(C.byref(o)) == 0
+    assert o.energy_tol == 1e-10 and o.max_iter == 999 and o.diis_size == 0
+    assert o.precision == _abi.CCSD_PREC_FP64
+
+
+def test_flop_count_formula():
+    f = _abi.lib().ccsd_flops_per_update(24, 300)
+    o, v = 24.0, 300.0
+    assert f == pytest.approx(2 * o**2 * v**4 + 4 * o**4 * v**2 + 8 * o**3 * v**3)
+    assert f == pytest.approx(1.24e13, rel=0.02)
+
+
+def test_library_generator_matches_oracle_generator():
+    o, v, q, seed = 3, 9, 7, 99
+    n = o + v
+    fock = np.zeros((n, n))
+    b = np.zeros((q, n, n))
+    rc = _abi.lib().ccsd_make_synthetic(o, v, q, seed, fock.ctypes.data_as(C.POINTER(C.c_double)),
+                                        b.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == 0
+    f_ref, b_ref = syn.make_system(o, v, q, seed)
+    np.testing.assert_allclose(fock, f_ref, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(b, b_ref, rtol=1e-14, atol=1e-17)
+    assert np.array_equal(b, b.transpose(0, 2, 1))
+
+
+def test_invalid_arguments_fail_without_compute():
+    lib = _abi.lib()
+    h = C.c_void_p()
+    assert lib.ccsd_create(None, None, C.byref(h)) == _abi.CCSD_ERR_INVALID_ARG
+    assert "NULL" in _abi.last_error()
+    assert lib.ccsd_solve(None, None) == _abi.CCSD_ERR_INVALID_ARG
+    assert lib.ccsd_make_synthetic(0, 5, 3, 1, None, None) == _abi.CCSD_ERR_INVALID_ARG
+    assert lib.ccsd_destroy(None) == 0
+
+
+def test_no_cpu_path_when_no_device():
+    """With no GPU visible, ccsd_create refuses (no silent CPU fallback)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    fock, b = syn.make_system(2, 4, 5, 1)
+    p = _abi.Problem()
+    p.nocc, p.nvir, p.integral_kind, p.naux = 2, 4, _abi.CCSD_INTS_DF, 5
+    fock = np.ascontiguousarray(fock)
+    b = np.ascontiguousarray(b)
+    p.fock = fock.ctypes.data_as(C.POINTER(C.c_double))
+    p.df = b.ctypes.data_as(C.POINTER(C.c_double))
+    h = C.c_void_p()
+    rc = _abi.lib().ccsd_create(C.byref(p), None, C.byref(h))
+    assert rc == _abi.CCSD_ERR_NO_DEVICE
+    assert "no CPU path" in _abi.last_error()

@@ -1,0 +1,113 @@
+"""GPU parity of the FP64 path against the oracle, through the C ABI.
+
+Bar: every per-update energy within 1e-10 Eh of the oracle, the same
+reference iteration counter at convergence, amplitudes within 1e-10."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ccsd_parallel_gb300 as cg
+from oracle import synthetic as syn
+from oracle.ccsd_rhf import RHFCCSD
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "synthetic_oracle.json").read_text())
+E_TOL = 1e-10
+
+
+def _system(c):
+    fock = np.diag(syn.orbital_energies(c["nocc"], c["nvir"], c["seed"]))
+    b = syn.df_factors(c["nocc"] + c["nvir"], c["naux"], c["seed"], sigma=c["sigma"])
+    return fock, b
+
+
+@pytest.mark.parametrize("key", sorted(GOLDEN))
+def test_fp64_matches_golden_every_update(key):
+    c = GOLDEN[key]
+    fock, b = _system(c)
+    r = cg.solve(fock, c["nocc"], df=b, energy_tol=c["tol"])
+    assert r["converged"]
+    assert r["iterations"] + 1 == c["iter"]  # reference counter starts at 1
+    np.testing.assert_allclose(r["energies"], c["energies"], rtol=0, atol=E_TOL)
+    assert abs(r["e_corr"] - c["e_corr"]) < E_TOL
+    assert abs(r["t1"].sum() - c["t1_sum"]) < 1e-10
+    assert abs((r["t2"] ** 2).sum() - c["t2_sq"]) < 1e-10 * max(1.0, c["t2_sq"])
+
+
+def test_library_generator_inputs_match_golden():
+    c = GOLDEN["syn_o10_v90_q300_s2024_sig0.05"]
+    fock, b = cg.make_synthetic(c["nocc"], c["nvir"], c["naux"], c["seed"])
+    r = cg.solve(fock, c["nocc"], df=b, energy_tol=c["tol"])
+    np.testing.assert_allclose(r["energies"], c["energies"], rtol=0, atol=E_TOL)
+
+
+def test_amplitudes_match_oracle():
+    fock, b = _system(dict(nocc=4, nvir=11, naux=30, seed=8, sigma=0.3))
+    ref = RHFCCSD(fock, 4, df=b).run(toler=1e-11, max_passes=9)
+    r = cg.solve(fock, 4, df=b, fixed_iterations=9)
+    np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r["t1"], ref["t1"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r["t2"], ref["t2"], rtol=0, atol=1e-12)
+    assert np.abs(r["t2"] - r["t2"].transpose(1, 0, 3, 2)).max() < 1e-15
+
+
+def test_integral_input_forms_agree():
+    o, v = 3, 9
+    fock, b = _system(dict(nocc=o, nvir=v, naux=25, seed=31, sigma=0.3))
+    eri = syn.eri_from_df(b)
+    r_df = cg.solve(fock, o, df=b, fixed_iterations=6)
+    r_mo = cg.solve(fock, o, eri=eri, fixed_iterations=6)
+    # AO form: eri = C^T ao C with a random orthogonal C
+    rng = np.random.default_rng(0)
+    cmat, _ = np.linalg.qr(rng.standard_normal((o + v, o + v)))
+    ao = np.einsum("pqrs,mp,nq,lr,ks->mnlk", eri, cmat, cmat, cmat, cmat, optimize=True)
+    r_ao = cg.solve(fock, o, ao_eri=ao, mo_coeff=cmat, fixed_iterations=6)
+    np.testing.assert_allclose(r_mo["energies"], r_df["energies"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(r_ao["energies"], r_df["energies"], rtol=0, atol=1e-12)
+
+
+def test_non_canonical_fock_matches_oracle():
+    o, v = 3, 8
+    fock, b = _system(dict(nocc=o, nvir=v, naux=20, seed=12, sigma=0.3))
+    rng = np.random.default_rng(5)
+    x = 0.01 * rng.standard_normal(fock.shape)
+    fock = fock + x + x.T
+    ref = RHFCCSD(fock, o, df=b).run(toler=1e-12, max_passes=8)
+    r = cg.solve(fock, o, df=b, fixed_iterations=8)
+    np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
+
+
+def test_diis_reaches_same_fixed_point_faster():
+    c = GOLDEN["syn_o6_v24_q60_s7_sig0.3"]
+    fock, b = _system(c)
+    r = cg.solve(fock, c["nocc"], df=b, energy_tol=1e-11, residual_tol=1e-8, diis_size=6, diis_start=2)
+    assert r["converged"]
+    assert abs(r["e_corr"] - c["e_corr"]) < 1e-9
+    assert r["iterations"] < c["iter"] - 1
+
+
+def test_reference_mirror_class():
+    c = GOLDEN["syn_o3_v7_q20_s5_sig0.3"]
+    fock, b = _system(c)
+    cc = cg.CCSD_Memory_optimized(fock, c["nocc"], df=b, E_HF=-1.5)
+    e = cc.CCSD(c["tol"], False)
+    assert abs(e - (-1.5 + c["e_corr"])) < E_TOL
+    assert cc.iter == c["iter"]
+    assert cc.n_Electrons == 2 * c["nocc"] and cc.unocc_orb == 2 * c["nvir"]
+
+
+def test_divergence_is_reported():
+    fock, b = _system(dict(nocc=3, nvir=7, naux=20, seed=5, sigma=0.8))
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve(fock, 3, df=b, max_iter=400)
+    assert ei.value.code == -4
+
+
+def test_bad_shape_is_rejected():
+    fock, b = _system(dict(nocc=2, nvir=4, naux=5, seed=1, sigma=0.05))
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve(fock, 0, df=b)
+    assert ei.value.code == -1
