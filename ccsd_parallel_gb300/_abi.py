@@ -68,6 +68,9 @@ SIGNATURES = {
     "ccsd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
     "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),
+    "ccsd_gemm": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
+                            C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,
+                            C.c_void_p]),
 }
 
 _lib = None

@@ -101,6 +101,50 @@ int ccsd_last_error(char *buf, size_t len) {
     return n;
 }
 
+int ccsd_gemm(int32_t precision, int32_t M, int32_t N, int32_t K, double alpha, const double *A, int64_t lda,
+              const double *B, int64_t ldb, double beta, double *C, int64_t ldc, void *stream) {
+    if (M < 0 || N < 0 || K < 0 || !A || !B || !C || lda < K || ldb < K || ldc < N)
+        return fail(CCSD_ERR_INVALID_ARG, "ccsd_gemm: bad shape, leading dimension or NULL pointer");
+    if (precision != CCSD_PREC_FP64 && precision != CCSD_PREC_SPLIT2 && precision != CCSD_PREC_SPLIT3 &&
+        precision != CCSD_PREC_SPLIT4)
+        return fail(CCSD_ERR_INVALID_ARG, "ccsd_gemm: unknown precision");
+    return guarded([&] {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw ccsd::Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
+        }
+        cudaStream_t st = (cudaStream_t)stream;
+        ccsd::MatView a, b;
+        a.p = A;
+        a.row.s2 = lda;
+        a.col.s2 = 1;
+        b.p = B;
+        b.row.s2 = ldb;
+        b.col.s2 = 1;
+        ccsd::OutView c;
+        c.p = C;
+        c.row.s2 = ldc;
+        c.col.s2 = 1;
+        if (M == 0 || N == 0) return;
+        if (precision == CCSD_PREC_FP64) {
+            size_t ws_n = ccsd::gemm_f64_ws_elems(M, N, K);
+            double *ws = nullptr;
+            if (ws_n) CCSD_CUDA(cudaMalloc(&ws, ws_n * sizeof(double)));
+            try {
+                ccsd::gemm_f64(M, N, K, alpha, a, b, beta, c, ws, ws_n, st);
+                CCSD_CUDA(cudaStreamSynchronize(st));
+            } catch (...) {
+                if (ws) cudaFree(ws);
+                throw;
+            }
+            if (ws) cudaFree(ws);
+        } else {
+            ccsd::split_gemm_oneshot(precision, M, N, K, alpha, a, b, beta, c, st);
+        }
+    });
+}
+
 double ccsd_flops_per_update(int32_t nocc, int32_t nvir) {
     const double o = nocc, v = nvir;
     return 2.0 * o * o * v * v * v * v + 4.0 * o * o * o * o * v * v + 8.0 * o * o * o * v * v * v;

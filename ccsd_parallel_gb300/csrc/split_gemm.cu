@@ -1,16 +1,504 @@
-// Split-precision tensor-core contraction engine (sm_103a tcgen05).
-// Placeholder until the kernel lands: requesting a split mode fails loudly.
+// Split-precision contraction engine on the sm_103a tensor cores (tcgen05).
+//
+// Operands (split_gemm.h): S BF16 planes per FP64 operand row, K-major,
+// per-row power-of-two scale.  Kernel: one 128 x BN output tile per CTA,
+// warp-specialised:
+//   warp 0      TMA producer: S planes of A (128 x 32) and of B (BN x 32) per
+//               pipeline stage, 64-byte swizzle, one mbarrier per stage
+//   warp 1      TMEM owner + single-thread tcgen05.mma issuer:
+//                 level 0 (P0 x P0)  -> TMEM acc0[buf] (double-buffered),
+//                                       restarted every 1024 K elements
+//                 levels 1..S-1      -> TMEM rest (one FP32 accumulator)
+//   warps 2..5  epilogue: drain acc0 after each 1024-K chunk into 32-bit
+//               integer registers (the chunk sums are integers < 2^24, exact
+//               in FP32), then C = alpha*sA*sB*2^-14*(I0 + rest) + beta*C.
+// Every mbarrier wait is bounded in wall time; a wait that gives up sets a
+// bit in the device error word, the other roles stop, in-flight TMA loads and
+// MMAs are awaited (bounded) and TMEM is freed before the CTA exits.
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "ptx.cuh"
 #include "split_gemm.h"
 
 namespace ccsd {
 
-SplitEngine::SplitEngine(int nslices, cudaStream_t st) : nslices_(nslices), st_(st) {
-    throw Error(-7, "split-precision engine not built yet");
+namespace {
+
+constexpr int BM = 128;                  // MMA M (one CTA, cta_group::1)
+constexpr int BK = 32;                   // K elements per stage (64 B rows)
+constexpr int CHUNK_KB = 1024 / BK;      // k-blocks per exact level-0 chunk
+constexpr int kThreads = 192;
+constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s wall-time bound per wait
+constexpr int kMaxKbPerSplit = 131072 / BK;  // int32 level-0 sum stays < 2^31
+
+__host__ __device__ constexpr int stage_bytes(int S, int BN) { return S * (BM + BN) * BK * 2; }
+__host__ __device__ constexpr int num_stages(int S, int BN) {
+    return (220 * 1024) / stage_bytes(S, BN) < 8 ? (220 * 1024) / stage_bytes(S, BN) : 8;
 }
-SplitEngine::~SplitEngine() {}
-void SplitEngine::gemm(int, int, int, double, const MatView &, const MatView &, double,
-                       const OutView &, int, int) {}
-int SplitEngine::error_status() { return 0; }
-size_t SplitEngine::cached_bytes() const { return 0; }
+__host__ __device__ constexpr int tmem_cols(int BN) {
+    return 3 * BN <= 128 ? 128 : (3 * BN <= 256 ? 256 : 512);
+}
+
+struct alignas(8) Bars {
+    uint64_t full[8];
+    uint64_t empty[8];
+    uint64_t acc_full[2];
+    uint64_t acc_empty[2];
+    uint64_t rest_full;
+    uint64_t drain;
+    uint32_t tmem_base;
+    int abort;
+    int never;  // stays 0: a wait that must not be cut short by another role
+};
+
+template <int S, int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      int M, int N, int rowsA_pad, int rowsB_pad, int nkb_total, int kb_per_split,
+                      const double *__restrict__ scaleA, const double *__restrict__ scaleB, double alpha,
+                      double beta, OutView C, double *ws, int *gerr) {
+    constexpr int NST = num_stages(S, BN);
+    constexpr int SB = stage_bytes(S, BN);
+    constexpr int A_TILE = BM * BK * 2;   // bytes per A plane tile
+    constexpr int B_TILE = BN * BK * 2;
+    constexpr uint32_t IDESC = ptx::idesc_bf16_f32(BM, BN);
+    constexpr int NCOLS = tmem_cols(BN);
+
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    Bars *bars = (Bars *)(smem + NST * SB);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kb0 = blockIdx.z * kb_per_split;
+    const int kb1 = min(nkb_total, kb0 + kb_per_split);
+    const int nkb = kb1 - kb0;
+    const int nch = (nkb + CHUNK_KB - 1) / CHUNK_KB;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            ptx::mbar_init(&bars->full[s], 1);
+            ptx::mbar_init(&bars->empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            ptx::mbar_init(&bars->acc_full[b], 1);
+            ptx::mbar_init(&bars->acc_empty[b], 4);
+        }
+        ptx::mbar_init(&bars->rest_full, 1);
+        ptx::mbar_init(&bars->drain, 1);
+        bars->abort = 0;
+        bars->never = 0;
+        ptx::fence_barrier_init();
+        ptx::prefetch_tmap(&tmA);
+        ptx::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(&bars->tmem_base, NCOLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = bars->tmem_base;
+    volatile int *abort = &bars->abort;
+
+    if (warp == 0) {
+        if (lane == 0 && nkb > 0) {
+            int issued = 0;
+            for (int l = 0; l < nkb; ++l) {
+                const int st = l % NST, round = l / NST;
+                if (!ptx::mbar_wait(&bars->empty[st], (round & 1) ^ 1, abort, gerr, 1, kWaitNs)) break;
+                ptx::mbar_arrive_expect_tx(&bars->full[st], SB);
+                unsigned char *sa = smem + st * SB;
+                unsigned char *sb = sa + S * A_TILE;
+                const int kx = (kb0 + l) * BK;
+#pragma unroll
+                for (int p = 0; p < S; ++p) {
+                    ptx::tma_load_2d(sa + p * A_TILE, &tmA, &bars->full[st], kx, p * rowsA_pad + m0);
+                    ptx::tma_load_2d(sb + p * B_TILE, &tmB, &bars->full[st], kx, p * rowsB_pad + n0);
+                }
+                issued = l + 1;
+            }
+            if (*abort) {  // let every TMA load this thread issued land before the CTA exits
+                for (int l = max(0, issued - NST); l < issued; ++l)
+                    ptx::mbar_wait(&bars->full[l % NST], (l / NST) & 1, &bars->never, gerr, 2, kWaitNs);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && nkb > 0) {
+            bool first_rest = true;
+            for (int l = 0; l < nkb; ++l) {
+                const int st = l % NST, round = l / NST;
+                const int c = l / CHUNK_KB, b = c & 1;
+                const bool chunk_start = (l % CHUNK_KB) == 0;
+                if (chunk_start) {
+                    if (!ptx::mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort, gerr, 4, kWaitNs)) break;
+                    ptx::tc_fence_after();
+                }
+                if (!ptx::mbar_wait(&bars->full[st], round & 1, abort, gerr, 8, kWaitNs)) break;
+                ptx::tc_fence_after();
+                const uint32_t sa = ptx::smem_u32(smem + st * SB);
+                const uint32_t sb = sa + S * A_TILE;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    uint64_t ad[S], bd[S];
+#pragma unroll
+                    for (int p = 0; p < S; ++p) {
+                        ad[p] = ptx::sdesc_k_sw64(sa + p * A_TILE + kk * 32);
+                        bd[p] = ptx::sdesc_k_sw64(sb + p * B_TILE + kk * 32);
+                    }
+                    ptx::mma_bf16(tmem + b * BN, ad[0], bd[0], IDESC, (chunk_start && kk == 0) ? 0u : 1u);
+#pragma unroll
+                    for (int lev = 1; lev < S; ++lev)
+#pragma unroll
+                        for (int p = 0; p <= lev; ++p) {
+                            ptx::mma_bf16(tmem + 2 * BN, ad[p], bd[lev - p], IDESC, first_rest ? 0u : 1u);
+                            first_rest = false;
+                        }
+                }
+                ptx::mma_commit(&bars->empty[st]);
+                if ((l % CHUNK_KB) == CHUNK_KB - 1 || l == nkb - 1) ptx::mma_commit(&bars->acc_full[b]);
+            }
+            ptx::mma_commit(&bars->rest_full);
+            ptx::mma_commit(&bars->drain);
+            ptx::mbar_wait(&bars->drain, 0, &bars->never, gerr, 16, kWaitNs);
+        }
+    } else {
+        // epilogue warps 2..5; TMEM lane quarter = warp % 4
+        const int q = warp & 3;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        int32_t iacc[BN];
+#pragma unroll
+        for (int j = 0; j < BN; ++j) iacc[j] = 0;
+        bool ok = nkb > 0;
+        for (int c = 0; c < nch && ok; ++c) {
+            const int b = c & 1;
+            const bool got = ptx::mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort, gerr, 32, kWaitNs);
+            if (!__all_sync(0xffffffffu, got)) {  // keep the warp converged for tcgen05.ld
+                ok = false;
+                break;
+            }
+            ptx::tc_fence_after();
+#pragma unroll
+            for (int g = 0; g < BN / 32; ++g) {
+                uint32_t r[32];
+                ptx::tmem_ld32(tmem + lane_off + b * BN + g * 32, r);
+                ptx::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) iacc[g * 32 + j] += __float2int_rn(__uint_as_float(r[j]));
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&bars->acc_empty[b]);
+        }
+        if (ok) ok = __all_sync(0xffffffffu, ptx::mbar_wait(&bars->rest_full, 0, abort, gerr, 64, kWaitNs));
+        if (ok || nkb == 0) {
+            ptx::tc_fence_after();
+            const int m = m0 + q * 32 + lane;
+            const bool mval = m < M;
+            const double sa = mval ? scaleA[m] * 0x1.0p-14 : 0.0;
+            const int64_t crow = mval ? dim_off(C.row, (uint32_t)m) : 0;
+            const bool direct = gridDim.z == 1;
+            double *wsz = ws + (size_t)blockIdx.z * M * N;
+#pragma unroll
+            for (int g = 0; g < BN / 32; ++g) {
+                uint32_t r[32];
+                if (nkb > 0) {
+                    ptx::tmem_ld32(tmem + lane_off + 2 * BN + g * 32, r);
+                    ptx::tmem_ld_wait();
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) r[j] = 0u;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int n = n0 + g * 32 + j;
+                    if (!mval || n >= N) continue;
+                    const double val =
+                        sa * scaleB[n] * ((double)iacc[g * 32 + j] + (double)__uint_as_float(r[j]));
+                    if (direct) {
+                        double *cp = C.p + crow + dim_off(C.col, (uint32_t)n);
+                        double out = alpha * val;
+                        if (beta != 0.0) out = fma(beta, *cp, out);
+                        *cp = out;
+                    } else {
+                        wsz[(size_t)m * N + n] = val;
+                    }
+                }
+            }
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, NCOLS);
+    }
+}
+
+// ---- FP64 -> S BF16 planes, one warp per row ---------------------------------
+template <int S>
+__global__ void split_rows_kernel(int rows, int rows_pad, int K, int kpad, MatView v,
+                                  __nv_bfloat16 *planes, double *scale) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const size_t plane = (size_t)rows_pad * kpad;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows_pad; r += nwarps) {
+        __nv_bfloat16 *dst = planes + (size_t)r * kpad;
+        if (r >= rows) {
+            for (int k = lane; k < kpad; k += 32)
+#pragma unroll
+                for (int p = 0; p < S; ++p) dst[p * plane + k] = __float2bfloat16_rn(0.f);
+            if (lane == 0) scale[r] = 1.0;
+            continue;
+        }
+        const int64_t ro = dim_off(v.row, (uint32_t)r);
+        double mx = 0.0;
+        for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(v.p[ro + dim_off(v.col, (uint32_t)k)]));
+        for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        int ex = 0;
+        if (mx > 0.0) frexp(mx, &ex);
+        if (lane == 0) scale[r] = ldexp(1.0, ex);
+        for (int k = lane; k < kpad; k += 32) {
+            double x = k < K ? v.p[ro + dim_off(v.col, (uint32_t)k)] : 0.0;
+            double y = ldexp(x, 7 - ex);  // |y| <= 128
+#pragma unroll
+            for (int p = 0; p < S; ++p) {
+                const double h = rint(y);
+                dst[p * plane + k] = __float2bfloat16_rn((float)ldexp(h, -8 * p));
+                y = (y - h) * 256.0;
+            }
+        }
+    }
+}
+
+__global__ void splitk_reduce(int M, int N, int splits, double alpha, const double *ws, double beta,
+                              OutView C) {
+    const size_t total = (size_t)M * N;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int z = 0; z < splits; ++z) s += ws[z * total + idx];
+        const int m = (int)(idx / N), n = (int)(idx % N);
+        double *cp = C.p + dim_off(C.row, (uint32_t)m) + dim_off(C.col, (uint32_t)n);
+        double out = alpha * s;
+        if (beta != 0.0) out = fma(beta, *cp, out);
+        *cp = out;
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        CCSD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p) throw Error(-2, "cuTensorMapEncodeTiled unavailable");
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+void encode(CUtensorMap *map, const SplitOperand &op, int box_rows) {
+    cuuint64_t gdim[2] = {(cuuint64_t)op.kpad, (cuuint64_t)op.nslices * op.rows_pad};
+    cuuint64_t gstride[1] = {(cuuint64_t)op.kpad * 2};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = get_encode()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, op.planes, gdim, gstride, box, estride,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+template <int S, int BN>
+void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+              const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+    constexpr int NST = num_stages(S, BN);
+    constexpr size_t smem = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        attr = true;
+    }
+    alignas(64) CUtensorMap ta, tb;
+    encode(&ta, A, BM);
+    encode(&tb, B, BN);
+    const int nkb = A.kpad / BK;
+    const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+    const long tiles = (long)tiles_m * tiles_n;
+    // split K for parallelism (few tiles) and to keep the int32 level-0 sums bounded
+    int splits = 1;
+    if (tiles < 148) splits = (int)std::min<long>((148 + tiles - 1) / tiles, std::max(1, nkb / 8));
+    splits = std::max(splits, (nkb + kMaxKbPerSplit - 1) / kMaxKbPerSplit);
+    while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
+    if ((nkb + splits - 1) / splits > kMaxKbPerSplit)
+        throw Error(-7, "split GEMM: K too long for the available split-K workspace");
+    int kbps = (nkb + splits - 1) / splits;
+    splits = (nkb + kbps - 1) / kbps;
+    dim3 grid(tiles_m, tiles_n, splits);
+    split_gemm_kernel<S, BN><<<grid, kThreads, smem, st>>>(ta, tb, M, N, A.rows_pad, B.rows_pad, nkb, kbps,
+                                                           A.scale, B.scale, alpha, beta, C, ws, d_err);
+    CCSD_CUDA(cudaGetLastError());
+    if (splits > 1) {
+        const size_t total = (size_t)M * N;
+        const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+        splitk_reduce<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
+        CCSD_CUDA(cudaGetLastError());
+    }
+}
+
+template <int S>
+void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+              const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+    if (N > 64)
+        launch_t<S, 128>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+    else if (N > 32)
+        launch_t<S, 64>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+    else
+        launch_t<S, 32>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st) {
+    const int threads = 256;
+    const long warps_needed = op.rows_pad;
+    const int blocks = (int)std::min<long>((warps_needed * 32 + threads - 1) / threads, 152 * 16);
+    __nv_bfloat16 *pl = (__nv_bfloat16 *)op.planes;
+    switch (op.nslices) {
+        case 2: split_rows_kernel<2><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
+        case 3: split_rows_kernel<3><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
+        case 4: split_rows_kernel<4><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
+        default: throw Error(-1, "nslices must be 2, 3 or 4");
+    }
+    CCSD_CUDA(cudaGetLastError());
+}
+
+void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+    if (A.kpad != B.kpad || A.nslices != B.nslices) throw Error(-1, "split operands disagree");
+    switch (A.nslices) {
+        case 2: launch_s<2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        case 3: launch_s<3>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        case 4: launch_s<4>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        default: throw Error(-1, "nslices must be 2, 3 or 4");
+    }
+}
+
+// One contraction on freshly split operands (the ccsd_gemm entry point).
+void split_gemm_oneshot(int nslices, int M, int N, int K, double alpha, const MatView &A, const MatView &B,
+                        double beta, const OutView &C, cudaStream_t st) {
+    SplitEngine eng(nslices, st);
+    eng.gemm(M, N, K, alpha, A, B, beta, C, 0, 0);
+    const int err = eng.error_status();
+    if (err) throw Error(-6, "split GEMM: a bounded device wait gave up (error word " + std::to_string(err) + ")");
+}
+
+// ---------------------------------------------------------------------------
+SplitEngine::SplitEngine(int nslices, cudaStream_t st) : nslices_(nslices), st_(st) {
+    if (nslices < 2 || nslices > 4) throw Error(-1, "nslices must be 2, 3 or 4");
+    int dev = 0, major = 0, minor = 0;
+    CCSD_CUDA(cudaGetDevice(&dev));
+    CCSD_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    CCSD_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3)
+        throw Error(-7, "split-precision engine needs an sm_103 GPU (tcgen05); found sm_" +
+                            std::to_string(major) + std::to_string(minor));
+    CCSD_CUDA(cudaMalloc(&d_err_, sizeof(int)));
+    CCSD_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), st_));
+    ws_elems_ = 8u << 20;
+    CCSD_CUDA(cudaMalloc(&ws_, ws_elems_ * sizeof(double)));
+}
+
+SplitEngine::~SplitEngine() {
+    for (auto &kv : cache_) free_op(*kv.second);
+    free_op(scratch_[0]);
+    free_op(scratch_[1]);
+    if (d_err_) cudaFree(d_err_);
+    if (ws_) cudaFree(ws_);
+}
+
+void SplitEngine::free_op(SplitOperand &op) {
+    if (op.planes) cudaFree(op.planes);
+    if (op.scale) cudaFree(op.scale);
+    op.planes = nullptr;
+    op.scale = nullptr;
+    op.bytes = 0;
+}
+
+void SplitEngine::ensure(SplitOperand &op, int rows, int K) {
+    const int rows_pad = (rows + BM - 1) / BM * BM;
+    const int kpad = (K + BK - 1) / BK * BK;
+    const size_t need = (size_t)nslices_ * rows_pad * kpad * 2;
+    if (!op.planes || need > op.bytes || (size_t)rows_pad > op.scale_cap) {
+        free_op(op);
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw Error(-3, "split planes: cudaMalloc of " + std::to_string(need) + " bytes failed");
+        }
+        op.planes = p;
+        op.bytes = need;
+        CCSD_CUDA(cudaMalloc(&op.scale, sizeof(double) * rows_pad));
+        op.scale_cap = rows_pad;
+    }
+    op.rows = rows;
+    op.rows_pad = rows_pad;
+    op.K = K;
+    op.kpad = kpad;
+    op.nslices = nslices_;
+}
+
+void SplitEngine::split_into(SplitOperand &op, int rows, int K, const MatView &v) {
+    ensure(op, rows, K);
+    split_operand_kernel_launch(op, rows, K, v, st_);
+}
+
+SplitOperand *SplitEngine::operand(int key, int rows, int K, const MatView &v, int slot) {
+    if (key == 0) {
+        split_into(scratch_[slot], rows, K, v);
+        return &scratch_[slot];
+    }
+    auto it = cache_.find(key);
+    if (it != cache_.end()) {
+        SplitOperand *op = it->second.get();
+        if (op->rows == rows && op->K == K) return op;
+        free_op(*op);
+        cache_.erase(it);
+    }
+    std::unique_ptr<SplitOperand> op(new SplitOperand());
+    split_into(*op, rows, K, v);
+    SplitOperand *raw = op.get();
+    cache_[key] = std::move(op);
+    return raw;
+}
+
+void SplitEngine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+                       const OutView &C, int cache_a, int cache_b) {
+    SplitOperand *a = operand(cache_a, M, K, A, 0);
+    SplitOperand *b = operand(cache_b, N, K, B, 1);
+    split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
+}
+
+int SplitEngine::error_status() {
+    int h = 0;
+    CCSD_CUDA(cudaMemcpyAsync(&h, d_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+    return h;
+}
+
+size_t SplitEngine::cached_bytes() const {
+    size_t s = 0;
+    for (auto &kv : cache_) s += kv.second->bytes;
+    return s;
+}
 
 }  // namespace ccsd

@@ -1,10 +1,10 @@
 // Split-precision contraction engine on the sm_103a tensor cores.
 //
-// An FP64 operand x (one row of A or B) is written as
+// An FP64 operand row x is written as
 //     x = s * 2^-7 * (P0 + P1 + ... + P_{S-1}),  s = 2^ceil(log2 max|row|),
 // where P0 = rint(x/s * 2^7) is an integer in [-128, 128] and every further
 // plane carries the next 8 bits of the remainder, pre-scaled by 2^-8 per
-// plane.  All planes are exact in BF16.  tcgen05.mma (kind::f16, BF16 in,
+// plane.  Every plane is exact in BF16.  tcgen05.mma (kind::f16, BF16 in,
 // FP32 accumulate in TMEM) forms the plane products with level p+q < S:
 //   * level 0 (P0 x P0) accumulates integers below 2^24 over K chunks of 1024
 //     -- exact in FP32 -- and is drained into 32-bit integer registers;
@@ -18,20 +18,18 @@
 #include <cstdint>
 #include <map>
 #include <memory>
-#include <vector>
 
 #include "common.h"
 
 namespace ccsd {
 
-// Split form of an M x K operand: S planes of [rows_pad][kpad] BF16 (K-major)
-// plus one FP64 scale per row.
+// Split form of a rows x K operand: S planes of [rows_pad][kpad] BF16
+// (K-major, plane p at row offset p * rows_pad) plus one FP64 scale per row.
 struct SplitOperand {
     void *planes = nullptr;  // __nv_bfloat16*
     double *scale = nullptr;
     int rows = 0, rows_pad = 0, K = 0, kpad = 0, nslices = 0;
-    size_t bytes = 0;
-    alignas(64) unsigned char tmap[128];  // CUtensorMap (2-D, over all planes)
+    size_t bytes = 0, scale_cap = 0;
 };
 
 class SplitEngine {
@@ -41,6 +39,8 @@ class SplitEngine {
     void set_stream(cudaStream_t st) { st_ = st; }
     int nslices() const { return nslices_; }
     // C(m,n) = alpha * sum_k A(m,k) B(n,k) + beta C(m,n) on the tensor cores.
+    // A nonzero cache key marks an operand view over constant data whose
+    // split form is kept (keyed) between calls.
     void gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
               const OutView &C, int cache_a, int cache_b);
     // Device error word (bounded waits that gave up); 0 when clean.
@@ -58,14 +58,18 @@ class SplitEngine {
     std::map<int, std::unique_ptr<SplitOperand>> cache_;
     SplitOperand scratch_[2];
     int *d_err_ = nullptr;
+    double *ws_ = nullptr;
+    size_t ws_elems_ = 0;
 };
 
-// Raw launch used by the engine and by the C-ABI test entry points.
-// A and B are split operands with the same kpad and nslices.
-void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha,
-                       double beta, const OutView &C, int *d_err, cudaStream_t st);
-void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v,
-                                 cudaStream_t st);
-bool encode_tmap(SplitOperand &op, int box_rows);
+// FP64 view -> split operand (S BF16 planes + row scales).
+void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st);
+// C = alpha * A B^T + beta C for split operands with equal kpad and nslices;
+// `ws` (ws_elems doubles) holds split-K partial sums; `d_err` the error word.
+void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st);
+// One contraction with temporary split operands and workspace.
+void split_gemm_oneshot(int nslices, int M, int N, int K, double alpha, const MatView &A, const MatView &B,
+                        double beta, const OutView &C, cudaStream_t st);
 
 }  // namespace ccsd

@@ -127,6 +127,18 @@ int ccsd_last_error(char *buf, size_t len);
 /* Algorithmic FLOP of one update: 2 o^2 v^4 + 4 o^4 v^2 + 8 o^3 v^3. */
 double ccsd_flops_per_update(int32_t nocc, int32_t nvir);
 
+/* One contraction on the engine's kernels, for row-major FP64 device matrices:
+ *   C[M][N] = alpha * A[M][K] * B[N][K]^T + beta * C     (leading dims lda/ldb/ldc)
+ * precision CCSD_PREC_FP64 runs the DFMA kernel, CCSD_PREC_SPLIT* the
+ * tcgen05 split-precision kernel.  It replaces the element-wise dot products
+ * accu(A % B) through which the reference forms every contraction (e.g. the
+ * particle-particle ladder, ccsd_memory_optimized.cpp:2093).  stream may be
+ * NULL (legacy default stream); the call returns after the work completes.
+ * Allocates its temporaries with cudaMalloc. */
+int ccsd_gemm(int32_t precision, int32_t M, int32_t N, int32_t K, double alpha, const double *A,
+              int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+              void *stream);
+
 /* Seeded synthetic closed-shell system (host only, no GPU needed): diagonal
  * fock (n x n) with occupied U[-2,-0.3] / virtual U[0.1,3] energies, and
  * DF factors B[Q][p][q] = 0.05 z / sqrt(naux), z ~ N(0,1), symmetric in p,q.

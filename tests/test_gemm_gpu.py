@@ -1,0 +1,95 @@
+"""GPU tests of the contraction kernels through ccsd_gemm (C ABI) against a
+plain PyTorch FP64 reference of the same product.
+
+Tolerances: the FP64 kernel must agree to 1e-13 relative to |A||B|^T; the
+split kernel with S BF16 planes represents each operand to 2^-(8S) of its row
+maximum and accumulates level 0 exactly, so its error is bounded by
+tol_S * (rowmax|A| * rowmax|B| * K) with tol_S = 2^-(8S-3)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from ccsd_parallel_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+PREC = {"fp64": 0, "split2": 2, "split3": 3, "split4": 4}
+
+
+def run_gemm(prec, A, B, Cin=None, alpha=1.0, beta=0.0):
+    M, K = A.shape
+    N = B.shape[0]
+    Cout = torch.zeros(M, N, dtype=torch.float64, device="cuda") if Cin is None else Cin.clone()
+    torch.cuda.synchronize()
+    rc = _abi.lib().ccsd_gemm(PREC[prec], M, N, K, alpha, C.c_void_p(A.data_ptr()), A.stride(0),
+                              C.c_void_p(B.data_ptr()), B.stride(0), beta, C.c_void_p(Cout.data_ptr()),
+                              Cout.stride(0), None)
+    _abi.check(rc)
+    return Cout
+
+
+def bound(A, B, S):
+    ra = A.abs().amax(dim=1, keepdim=True)
+    rb = B.abs().amax(dim=1, keepdim=True)
+    return (ra @ rb.T) * A.shape[1] * 2.0 ** (-(8 * S - 3))
+
+
+SHAPES = [(1, 1, 1), (5, 7, 3), (128, 128, 32), (200, 70, 1000), (130, 33, 2500), (300, 300, 5000),
+          (1000, 20, 64), (64, 513, 4097)]
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_fp64_kernel(M, N, K):
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 13 + K)
+    A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
+    C0 = torch.randn(M, N, dtype=torch.float64, device="cuda", generator=g)
+    out = run_gemm("fp64", A, B, C0, alpha=0.7, beta=-1.3)
+    ref = 0.7 * (A @ B.T) - 1.3 * C0
+    scale = 0.7 * (A.abs() @ B.abs().T) + 1.3 * C0.abs()
+    assert ((out - ref).abs() <= 1e-13 * scale + 1e-300).all()
+
+
+@pytest.mark.parametrize("prec,S", [("split2", 2), ("split3", 3), ("split4", 4)])
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_split_kernel(prec, S, M, N, K):
+    g = torch.Generator(device="cuda").manual_seed(M * 5 + N * 3 + K + S)
+    A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
+    out = run_gemm(prec, A, B)
+    ref = A @ B.T
+    err = (out - ref).abs()
+    assert (err <= bound(A, B, S)).all(), float((err / bound(A, B, S)).max())
+
+
+def test_split_alpha_beta_and_wide_dynamic_range():
+    g = torch.Generator(device="cuda").manual_seed(3)
+    M, N, K = 256, 96, 3000
+    A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    A *= torch.logspace(-6, 3, M, device="cuda", dtype=torch.float64)[:, None]
+    B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
+    A[7] = 0.0
+    C0 = torch.randn(M, N, dtype=torch.float64, device="cuda", generator=g)
+    out = run_gemm("split4", A, B, C0, alpha=-2.0, beta=0.5)
+    ref = -2.0 * (A @ B.T) + 0.5 * C0
+    assert ((out - ref).abs() <= 2.0 * bound(A, B, 4) + 1e-15 * C0.abs()).all()
+    assert torch.equal(out[7], 0.5 * C0[7])
+
+
+def test_split_level0_is_exact_for_integer_operands():
+    """Integer operands with a row maximum of 127 get the row scale 2^7 and sit
+    entirely in plane 0, so the result is the exact integer product (no FP32
+    rounding over long K).  (A row maximum of exactly 128 would get the scale
+    2^8 and spill the odd integers into plane 1.)"""
+    g = torch.Generator(device="cuda").manual_seed(11)
+    M, N, K = 160, 48, 20000
+    A = torch.randint(-127, 128, (M, K), generator=g, device="cuda").to(torch.float64)
+    A[:, 0] = 127.0
+    B = torch.randint(-127, 128, (N, K), generator=g, device="cuda").to(torch.float64)
+    B[:, 0] = -127.0
+    out = run_gemm("split2", A, B)
+    ref = A @ B.T
+    assert torch.equal(out, ref)
