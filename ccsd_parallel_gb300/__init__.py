@@ -50,7 +50,8 @@ def flops_per_update(nocc: int, nvir: int) -> float:
 
 
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
-             fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, stream=None):
+             fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, profile=False,
+             stream=None):
     o = _abi.Options()
     _abi.check(_abi.lib().ccsd_default_options(C.byref(o)))
     o.energy_tol = energy_tol
@@ -61,6 +62,7 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     o.diis_start = diis_start
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.verbose = int(bool(verbose))
+    o.profile = int(bool(profile))
     o.stream = stream
     return o
 
@@ -115,6 +117,16 @@ class Solver:
                     residual_norm=r.residual_norm, energies=eh[:r.history_len].copy(),
                     update_ms=ms[:r.iterations].copy(), flops_per_update=r.flops_per_update,
                     t1=t1, t2=t2)
+
+    def profile(self) -> dict:
+        """Per-contraction device times of the last solve (needs profile=True)."""
+        import json
+        n = _abi.lib().ccsd_profile_report(self._h, None, 0)
+        if n < 0:
+            _abi.check(n)
+        buf = C.create_string_buffer(n + 1)
+        _abi.lib().ccsd_profile_report(self._h, buf, n + 1)
+        return json.loads(buf.value.decode())
 
     def close(self):
         if getattr(self, "_h", None):

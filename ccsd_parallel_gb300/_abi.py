@@ -45,7 +45,8 @@ class Options(C.Structure):
     _fields_ = [
         ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
         ("fixed_iterations", C.c_int32), ("diis_size", C.c_int32), ("diis_start", C.c_int32),
-        ("precision", C.c_int32), ("verbose", C.c_int32), ("stream", C.c_void_p),
+        ("precision", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
+        ("stream", C.c_void_p),
     ]
 
 
@@ -66,6 +67,7 @@ SIGNATURES = {
     "ccsd_set_options": (C.c_int, [C.c_void_p, C.POINTER(Options)]),
     "ccsd_destroy": (C.c_int, [C.c_void_p]),
     "ccsd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "ccsd_profile_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
     "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),
     "ccsd_gemm": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,

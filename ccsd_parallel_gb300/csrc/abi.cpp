@@ -91,6 +91,19 @@ int ccsd_destroy(ccsd_handle *h) {
     return rc;
 }
 
+int ccsd_profile_report(ccsd_handle *h, char *buf, size_t len) {
+    if (!h || !h->engine) return fail(CCSD_ERR_INVALID_ARG, "handle is NULL");
+    std::string s;
+    int rc = guarded([&] { s = h->engine->profile_json(); });
+    if (rc != CCSD_OK) return rc;
+    if (buf && len > 0) {
+        size_t c = std::min(len - 1, s.size());
+        std::memcpy(buf, s.data(), c);
+        buf[c] = '\0';
+    }
+    return (int)s.size();
+}
+
 int ccsd_last_error(char *buf, size_t len) {
     const int n = (int)g_last_error.size();
     if (buf && len > 0) {

@@ -65,6 +65,16 @@ struct OutView {
     Dim row, col;
 };
 
+// Count of kernel launches issued by this library (host side, all threads).
+void note_launch(int n = 1);
+long launch_count();
+// After every <<<...>>> launch: check it and count it.
+#define CCSD_LAUNCH_CHECK()                 \
+    do {                                    \
+        CCSD_CUDA(cudaGetLastError());      \
+        ::ccsd::note_launch();              \
+    } while (0)
+
 // ---- FP64 kernels (gemm_f64.cu, tensor_ops.cu) ------------------------------
 // C(m,n) = alpha * sum_k A(m,k) * B(n,k) + beta * C(m,n); A is M x K, B is N x K.
 // `ws` is scratch of `ws_elems` doubles used for split-K partial sums.

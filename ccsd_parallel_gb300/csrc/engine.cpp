@@ -90,8 +90,11 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     if (ov2 > 2.0e9 || (double)v_ * v_ >= 2.0e9)
         throw Error(CCSD_ERR_UNSUPPORTED, "shape too large for 32-bit tile indices");
     set_options(opts);
+    if (opt_.precision != CCSD_PREC_FP64) build_split_.reset(new SplitEngine(CCSD_PREC_SPLIT4, st_));
     build_integrals(prob);
     build_derived();
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+    build_split_.reset();
 
     const size_t o = o_, v = v_;
     const size_t nT2 = o * o * v * v, nT1 = o * v;
@@ -127,6 +130,12 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
+    for (const ProfPending &p : prof_pending_) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+        cudaEventDestroy(p.c);
+    }
+    for (cudaEvent_t e : prof_pool_) cudaEventDestroy(e);
     split_.reset();
     if (own_stream_ && st_) cudaStreamDestroy(st_);
 }
@@ -340,17 +349,88 @@ void Engine::build_derived() {
 
 // ---------------------------------------------------------------------------
 bool Engine::use_split(int M, int N, int K) const {
-    if (opt_.precision == CCSD_PREC_FP64 || !split_) return false;
+    if (opt_.precision == CCSD_PREC_FP64 || (!split_ && !build_split_)) return false;
     return M >= 16 && N >= 16 && K >= 16 && (double)M * N * K >= 1.0e7;
 }
 
 void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B,
-                  double beta, const OutView &C, int cache_a, int cache_b) {
-    if (use_split(M, N, K)) {
-        split_->gemm(M, N, K, alpha, A, B, beta, C, cache_a, cache_b);
+                  double beta, const OutView &C, int cache_a, int cache_b, const char *site) {
+    const bool prof = opt_.profile && site;
+    const bool split = use_split(M, N, K);
+    if (split && SplitEngine::prefer_swap(M, N)) {
+        gemm(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, cache_b, cache_a, site);
+        return;
+    }
+    cudaEvent_t ea = nullptr, eb = nullptr, ec = nullptr;
+    if (prof) {
+        ea = prof_event();
+        eb = prof_event();
+        ec = prof_event();
+        CCSD_CUDA(cudaEventRecord(ea, st_));
+    }
+    if (split) {
+        SplitEngine *se = build_split_ ? build_split_.get() : split_.get();
+        SplitOperand *a = se->prepare(cache_a, M, K, A, 0);
+        SplitOperand *b = se->prepare(cache_b, N, K, B, 1);
+        if (prof) CCSD_CUDA(cudaEventRecord(eb, st_));
+        se->run(*a, *b, M, N, alpha, beta, C);
     } else {
+        if (prof) CCSD_CUDA(cudaEventRecord(eb, st_));
         gemm_f64(M, N, K, alpha, A, B, beta, C, ws_.p, ws_.n, st_);
     }
+    if (prof) {
+        CCSD_CUDA(cudaEventRecord(ec, st_));
+        prof_pending_.push_back(ProfPending{site, ea, eb, ec, 2.0 * M * (double)N * K, split});
+    }
+}
+
+cudaEvent_t Engine::prof_event() {
+    if (!prof_pool_.empty()) {
+        cudaEvent_t e = prof_pool_.back();
+        prof_pool_.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    CCSD_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+// Resolve the recorded events (the stream has been synchronised).
+void Engine::prof_flush() {
+    for (const ProfPending &p : prof_pending_) {
+        float split_ms = 0.f, ms = 0.f;
+        CCSD_CUDA(cudaEventElapsedTime(&split_ms, p.a, p.b));
+        CCSD_CUDA(cudaEventElapsedTime(&ms, p.b, p.c));
+        ProfSite &s = prof_[p.site];
+        s.calls += 1;
+        s.ms += ms;
+        s.split_ms += split_ms;
+        s.flops += p.flops;
+        s.split = p.split;
+        prof_pool_.push_back(p.a);
+        prof_pool_.push_back(p.b);
+        prof_pool_.push_back(p.c);
+    }
+    prof_pending_.clear();
+}
+
+std::string Engine::profile_json() const {
+    std::string s = "{\"updates\": " + std::to_string(prof_updates_) +
+                    ", \"update_ms_total\": " + std::to_string(prof_update_ms_) +
+                    ", \"launches\": " + std::to_string(prof_launches_) + ", \"sites\": [";
+    bool first = true;
+    char buf[512];
+    for (const auto &kv : prof_) {
+        std::snprintf(buf, sizeof buf,
+                      "%s{\"site\": \"%s\", \"calls\": %ld, \"ms\": %.6f, \"split_ms\": %.6f, \"flops\": %.6e, "
+                      "\"path\": \"%s\"}",
+                      first ? "" : ", ", kv.first.c_str(), kv.second.calls, kv.second.ms, kv.second.split_ms,
+                      kv.second.flops, kv.second.split ? "split" : "fp64");
+        s += buf;
+        first = false;
+    }
+    s += "]}";
+    return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -366,68 +446,71 @@ void Engine::residual() {
 
     k_tau(io, iv, t1, t2, tau_.p, st);
     k_theta(io, iv, t1, t2, th1_.p, th2_.p, st);
+    // the split forms of tau as (ij|cd) (key -1) and of the ring view of t2
+    // (key -2) are shared by several contractions of this update
+    if (split_ && opt_.precision != CCSD_PREC_FP64) split_->begin_update();
 
     // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d]
     CCSD_CUDA(cudaMemcpyAsync(Foo_.p, f_oo_off_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
     gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
-         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, 0);
+         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, 0, "Foo");
     // Fvv[a][c] = f_vv' - sum_{kld} Lovov[k,c,l,d] tau[k,l,a,d]
     CCSD_CUDA(cudaMemcpyAsync(Fvv_.p, f_vv_off_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
     gemm(iv, iv, (int)(o * o * v), -1.0, mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)),
          mv(Lovov_.p, ix1(o * v), ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1)), 1.0,
-         ovw(Fvv_.p, ix1(v), ix1(1)), 0, 2);
+         ovw(Fvv_.p, ix1(v), ix1(1)), 0, 2, "Fvv");
     // Fov[k][c] = f_ov + sum_ld Lovov[k,c,l,d] t1[l,d]
     CCSD_CUDA(cudaMemcpyAsync(Fov_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
     gemm((int)ov, 1, (int)ov, 1.0, mv(Lovov_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
-         ovw(Fov_.p, ix1(1), ix1(0)));
+         ovw(Fov_.p, ix1(1), ix1(0)), 0, 0, "Fov");
     // Loo[k][i] = Foo + sum_c f_kc t1[i,c] + sum_lc Lovoo[l,c,k,i] t1[l,c]
     CCSD_CUDA(cudaMemcpyAsync(Loo_.p, Foo_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
     gemm(io, io, iv, 1.0, mv(f_ov_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
-         ovw(Loo_.p, ix1(o), ix1(1)));
+         ovw(Loo_.p, ix1(o), ix1(1)), 0, 0, "Loo_f");
     gemm((int)o2, 1, (int)ov, 1.0, mv(Lovoo_.p, ix1(1), ix1(o2)), mv(t1, ix1(0), ix1(1)), 1.0,
-         ovw(Loo_.p, ix1(1), ix1(0)));
+         ovw(Loo_.p, ix1(1), ix1(0)), 0, 0, "Loo_t1");
     // Lvv[a][c] = Fvv - sum_k t1[k,a] f_kc + sum_kd Lovvv[k,d,a,c] t1[k,d]
     CCSD_CUDA(cudaMemcpyAsync(Lvv_.p, Fvv_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
     gemm(iv, iv, io, -1.0, mv(t1, ix1(1), ix1(v)), mv(f_ov_.p, ix1(1), ix1(v)), 1.0,
-         ovw(Lvv_.p, ix1(v), ix1(1)));
+         ovw(Lvv_.p, ix1(v), ix1(1)), 0, 0, "Lvv_f");
     gemm((int)v2, 1, (int)ov, 1.0, mv(Lovvv_.p, ix1(1), ix1(v2)), mv(t1, ix1(0), ix1(1)), 1.0,
-         ovw(Lvv_.p, ix1(1), ix1(0)));
+         ovw(Lvv_.p, ix1(1), ix1(0)), 0, 0, "Lvv_t1");
 
     // ---- T1 numerator ----------------------------------------------------
     CCSD_CUDA(cudaMemcpyAsync(R1_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
     // -2 sum_kc f_kc t1[k,a] t1[i,c]: tmpo[i][k] = sum_c t1[i,c] f_kc
     gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(f_ov_.p, ix1(v), ix1(1)), 0.0,
-         ovw(tmpo_.p, ix1(o), ix1(1)));
+         ovw(tmpo_.p, ix1(o), ix1(1)), 0, 0, "R1_ft1");
     gemm(io, iv, io, -2.0, mv(tmpo_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)));
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_ft1t1");
     // + sum_c Fvv'[a,c] t1[i,c]
     gemm(io, iv, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(Fvv_.p, ix1(v), ix1(1)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)));
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_Fvv");
     // - sum_k Foo'[k,i] t1[k,a]
     gemm(io, iv, io, -1.0, mv(Foo_.p, ix1(1), ix1(o)), mv(t1, ix1(1), ix1(v)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)));
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_Foo");
     // + sum_kc Fov[k,c] (2 t2[k,i,c,a] - t2[i,k,c,a])
     gemm((int)ov, 1, (int)ov, 2.0, mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)),
-         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)));
+         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2a");
     gemm((int)ov, 1, (int)ov, -1.0, mv(t2, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)),
-         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)));
+         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2b");
     // + sum_kc Fov[k,c] t1[i,c] t1[k,a]
     gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(Fov_.p, ix1(v), ix1(1)), 0.0,
-         ovw(tmpo2_.p, ix1(o), ix1(1)));
+         ovw(tmpo2_.p, ix1(o), ix1(1)), 0, 0, "R1_Fovt1");
     gemm(io, iv, io, 1.0, mv(tmpo2_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)));
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_Fovt1t1");
     // + sum_kc LT1[i,a,k,c] t1[k,c]
     gemm((int)ov, 1, (int)ov, 1.0, mv(LT1_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
-         ovw(R1_.p, ix1(1), ix1(0)));
+         ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_LT1");
     // + sum_kcd Lovvv[k,d,a,c] tau[i,k,c,d]
     gemm(io, iv, (int)(o * v2), 1.0, mv(tau, ix1(ov2), ix1(1)),
          mv(Lovvv_.p, ix1(v), ix3((uint32_t)v, (uint32_t)v, v * v2, 1, v2)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)), 0, 3);
+         ovw(R1_.p, ix1(v), ix1(1)), 0, 3, "R1_ovvv_tau");
     // - sum_klc Lovoo[l,c,k,i] tau[k,l,a,c]
     gemm(io, iv, (int)(o2 * v), -1.0,
          mv(Lovoo_.p, ix1(1), ix3((uint32_t)o, (uint32_t)v, o, v * o2, o2)),
          mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)), 4, 0);
+         ovw(R1_.p, ix1(v), ix1(1)), 4, 0, "R1_ovoo_tau");
 
     // ---- Woooo[k][l][i][j] ------------------------------------------------
     axpby_view((int)o2, (int)o2, 1.0, mv(oooo_.p, ix2((uint32_t)o, o * o2, o), ix2((uint32_t)o, o2, 1)),
@@ -435,32 +518,32 @@ void Engine::residual() {
     // + sum_c (lc|ki) t1[j,c]: M = (k,l,i), N = j, K = c
     gemm((int)(o * o2), io, iv, 1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, o, v * o2, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
-         1.0, ovw(Woooo_.p, ix1(o), ix1(1)));
+         1.0, ovw(Woooo_.p, ix1(o), ix1(1)), 0, 0, "Woooo_t1a");
     // + sum_c (kc|lj) t1[i,c]: M = (k,l,j), N = i
     gemm((int)(o * o2), io, iv, 1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, v * o2, o, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
-         1.0, ovw(Woooo_.p, ix3((uint32_t)o, (uint32_t)o, o * o2, o2, 1), ix1(o)));
+         1.0, ovw(Woooo_.p, ix3((uint32_t)o, (uint32_t)o, o * o2, o2, 1), ix1(o)), 0, 0, "Woooo_t1b");
     // + sum_cd (kc|ld) tau[i,j,c,d]: M = (k,l), N = (i,j), K = (c,d)
     gemm((int)o2, (int)o2, (int)v2, 1.0,
          mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
-         mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, 0);
+         mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
 
     // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
     CCSD_CUDA(cudaMemcpyAsync(Wvoov_.p, ovov_.p, sizeof(double) * ov * ov, cudaMemcpyDeviceToDevice, st));
     // + sum_d (kc|ad) t1[i,d]: M = (k,c,a), N = i, K = d
     gemm((int)(ov * v), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
-         ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0);
+         ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0, "Wvoov_t1v");
     // - sum_l (kc|li) t1[l,a]: M = (k,c,i), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, v * o2, o2, 1), ix1(o)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)));
+         1.0, ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)), 0, 0, "Wvoov_t1o");
     // + sum_ld th1[i,a,l,d] (ld|kc)
     gemm((int)ov, (int)ov, (int)ov, 1.0, mv(th1_.p, ix1(ov), ix1(1)), mv(ovov_.p, ix1(ov), ix1(1)),
-         1.0, ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 7);
+         1.0, ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 7, "Wvoov_th1");
     // - 1/2 sum_ld (lc|kd) t2[i,l,a,d]
     gemm((int)ov, (int)ov, (int)ov, -0.5, mv(t2, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)),
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
-         ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 8);
+         ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 8, "Wvoov_t2");
 
     // ---- Wvovo_s[i][a][k][c] = W_akci ------------------------------------
     axpby_view((int)ov, (int)ov, 1.0, mv(oovv_.p, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)),
@@ -468,15 +551,15 @@ void Engine::residual() {
     // + sum_d (kd|ac) t1[i,d]: M = (k,a,c), N = i, K = d
     gemm((int)(ov * v), io, iv, 1.0,
          mv(ovvv_.p, ix3((uint32_t)v, (uint32_t)v, v * v2, v, 1), ix1(v2)), mv(t1, ix1(v), ix1(1)),
-         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)v, v, ov, 1), ix1(v * ov)), 9, 0);
+         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)v, v, ov, 1), ix1(v * ov)), 9, 0, "Wvovo_t1v");
     // - sum_l (lc|ki) t1[l,a]: M = (k,c,i), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, o, o2, 1), ix1(v * o2)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)));
+         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)), 0, 0, "Wvovo_t1o");
     // - sum_ld th2[i,a,l,d] (lc|kd)
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(th2_.p, ix1(ov), ix1(1)),
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
-         ovw(Wvovo_.p, ix1(ov), ix1(1)), 0, 8);
+         ovw(Wvovo_.p, ix1(ov), ix1(1)), 0, 8, "Wvovo_th2");
     // Wa = 2 Wvoov - Wvovo
     axpby_view((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
     axpby_view((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
@@ -488,56 +571,56 @@ void Engine::residual() {
                ovw(R_.p, ix1(v2), ix1(1)), st);
     // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b]
     gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
-         1.0, ovw(R_.p, ix1(v2), ix1(1)));
+         1.0, ovw(R_.p, ix1(v2), ix1(1)), 0, 0, "hh_ladder");
     // + sum_cd (ac|bd) tau[i,j,c,d]: the v^4 particle-particle ladder, M = (a,b), N = (i,j)
     gemm((int)v2, (int)o2, (int)v2, 1.0, mv(wv_.p, ix1(v2), ix1(1)), mv(tau, ix1(v2), ix1(1)), 1.0,
-         ovw(R_.p, ix1(1), ix1(v2)), 10, 0);
+         ovw(R_.p, ix1(1), ix1(v2)), 10, -1, "pp_ladder");
 
     // ---- Rp (terms under P(ij,ab)) -----------------------------------------
     // + sum_c (ia|bc) t1[j,c]: M = (i,a,b), N = j, K = c
     gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
-         ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0);
+         ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
     // - sum_k t1[k,a] sum_c (ki|bc) t1[j,c]: Vk[k][i][b][j] = sum_c oovv[k,i,b,c] t1[j,c]
     gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
-         ovw(Vk_.p, ix1(o), ix1(1)));
+         ovw(Vk_.p, ix1(o), ix1(1)), 0, 0, "Rp_oovv_t1");
     gemm((int)(o * v * o), iv, io, -1.0,
          mv(Vk_.p, ix3((uint32_t)v, (uint32_t)o, v * o, o, 1), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)o, ov2, 1, v2), ix1(v)));
+         1.0, ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)o, ov2, 1, v2), ix1(v)), 0, 0, "Rp_oovv_t1t1");
     // - sum_k tmpB[k,i,a,j] t1[k,b], tmpB = (ia|jk) + sum_c (kc|ia) t1[j,c]
     axpby_view((int)(o * ov), io, 1.0,
                mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), 0.0,
                ovw(tmpB_.p, ix1(o), ix1(1)), st);
     gemm((int)(o * ov), io, iv, 1.0,
          mv(ovov_.p, ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1), ix1(o * v)), mv(t1, ix1(v), ix1(1)),
-         1.0, ovw(tmpB_.p, ix1(o), ix1(1)));
+         1.0, ovw(tmpB_.p, ix1(o), ix1(1)), 0, 0, "Rp_ovov_t1");
     gemm((int)(o2 * v), iv, io, -1.0,
          mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix1(v), ix1(1)));
+         1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
     // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d]
     gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
          mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
-         ovw(Z_.p, ix1(ov), ix1(1)), 0, 12);
+         ovw(Z_.p, ix1(ov), ix1(1)), -1, 12, "Rp_Z");
     gemm((int)(o2 * v), iv, io, -1.0, mv(Z_.p, ix2((uint32_t)v, ov, 1), ix1(v)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix1(v), ix1(1)));
+         1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_Z_t1");
     // + sum_c Lvv'[a,c] t2[i,j,c,b]: M = a, N = (i,j,b), K = c
     gemm(iv, (int)(o2 * v), iv, 1.0, mv(Lvv_.p, ix1(v), ix1(1)),
-         mv(t2, ix2((uint32_t)v, v2, 1), ix1(v)), 1.0, ovw(Rp_.p, ix1(v), ix2((uint32_t)v, v2, 1)));
+         mv(t2, ix2((uint32_t)v, v2, 1), ix1(v)), 1.0, ovw(Rp_.p, ix1(v), ix2((uint32_t)v, v2, 1)), 0, 0, "Rp_Lvv");
     // - sum_k Loo'[k,i] t2[k,j,a,b]: M = i, N = (j,a,b), K = k
     gemm(io, (int)ov2, io, -1.0, mv(Loo_.p, ix1(1), ix1(o)), mv(t2, ix1(1), ix1(ov2)), 1.0,
-         ovw(Rp_.p, ix1(ov2), ix1(1)));
+         ovw(Rp_.p, ix1(ov2), ix1(1)), 0, 0, "Rp_Loo");
     // rings, M = (i,a), N = (j,b), K = (k,c)
     // + sum_kc Wa[i,a,k,c] t2[k,j,c,b]
     gemm((int)ov, (int)ov, (int)ov, 1.0, mv(Wa_.p, ix1(ov), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)), 1.0,
-         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)));
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)), 0, 0, "ring1");
     // - sum_kc Wvoov[i,a,k,c] t2[k,j,b,c]
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(Wvoov_.p, ix1(ov), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)), 1.0,
-         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)));
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)), 0, -2, "ring2");
     // - sum_kc Wvovo[i,b,k,c] t2[k,j,a,c]: M = (i,b), N = (j,a)
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)), 1.0,
-         ovw(Rp_.p, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)));
+         ovw(Rp_.p, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)), 0, -2, "ring3");
 }
 
 double Engine::reduce_sum(int nparts) {
@@ -653,6 +736,11 @@ void Engine::solve(ccsd_result *res) {
     diis_t_.clear();
     diis_e_.clear();
     diis_count_ = diis_next_ = 0;
+    prof_.clear();
+    prof_pending_.clear();
+    prof_update_ms_ = 0.0;
+    prof_updates_ = 0;
+    prof_launches_ = 0;
     // T1 = 0, T2 = MP2 (ccsd_memory_optimized.cpp:473-490)
     t1_.zero(st_);
     k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
@@ -670,6 +758,7 @@ void Engine::solve(ccsd_result *res) {
     try {
         while (true) {
             const double e_old = e_new;
+            const long launches0 = launch_count();
             CCSD_CUDA(cudaEventRecord(ev0, st_));
             residual();
             k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
@@ -684,6 +773,12 @@ void Engine::solve(ccsd_result *res) {
             CCSD_CUDA(cudaEventSynchronize(ev1));
             float ms = 0.f;
             CCSD_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            if (opt_.profile) {
+                prof_flush();
+                prof_update_ms_ += ms;
+                prof_updates_ += 1;
+                prof_launches_ += launch_count() - launches0;
+            }
             ++updates;
             if (res->update_ms && updates - 1 < res->history_capacity) res->update_ms[updates - 1] = ms;
             if (res->energy_history && hist < res->history_capacity) res->energy_history[hist] = e_new;

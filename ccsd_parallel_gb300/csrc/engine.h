@@ -2,7 +2,9 @@
 // intermediates for one closed-shell system, and the iteration driver.
 #pragma once
 
+#include <map>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "../../include/ccsd_gb300.h"
@@ -48,8 +50,33 @@ class Engine {
     // `cache_a/b` != 0 marks an operand view over constant integrals whose
     // split form is kept between updates.
     void gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
-              const OutView &C, int cache_a = 0, int cache_b = 0);
+              const OutView &C, int cache_a = 0, int cache_b = 0, const char *site = nullptr);
     bool use_split(int M, int N, int K) const;
+
+    // contraction profiling (options.profile)
+    struct ProfSite {
+        long calls = 0;
+        double ms = 0.0, split_ms = 0.0, flops = 0.0;
+        bool split = false;
+    };
+    struct ProfPending {
+        const char *site;
+        cudaEvent_t a, b, c;
+        double flops;
+        bool split;
+    };
+    cudaEvent_t prof_event();
+    void prof_flush();
+    std::map<std::string, ProfSite> prof_;
+    std::vector<ProfPending> prof_pending_;
+    std::vector<cudaEvent_t> prof_pool_;
+    double prof_update_ms_ = 0.0;
+    int prof_updates_ = 0;
+
+  public:
+    std::string profile_json() const;
+
+  private:
 
     // one amplitude update: residual numerators from (t1_, t2_)
     void residual();
@@ -81,6 +108,10 @@ class Engine {
     std::vector<double> diis_b_;  // (n x n) overlap matrix of stored errors
 
     std::unique_ptr<SplitEngine> split_;
+    // Split modes build the integral blocks from DF factors / AO integrals on
+    // a 4-plane engine (relative error ~1e-10), FP64 mode in FP64.
+    std::unique_ptr<SplitEngine> build_split_;
+    long prof_launches_ = 0;
     double last_resid_ = 0.0;
 };
 

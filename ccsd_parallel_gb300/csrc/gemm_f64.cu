@@ -124,6 +124,51 @@ __global__ void splitk_reduce_kernel(int M, int N, int splits, double alpha, con
     }
 }
 
+// Matrix-vector form (N == 1): y(m) = alpha sum_k A(m,k) x(k) + beta y(m).
+// Memory-bound, so the reads follow the contiguous index of A:
+//  ROWC: A(m,k) contiguous in m -> a block covers 32 rows x 8 k-slices, every
+//        warp load is 32 consecutive rows, the 8 slices meet in shared memory;
+//  else: one warp per row, lanes stride over k.
+template <bool ROWC>
+__global__ void __launch_bounds__(256) gemv_f64_kernel(int M, int K, double alpha, MatView A, MatView X,
+                                                       double beta, OutView Y) {
+    if (ROWC) {
+        __shared__ double part[8][33];
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+        const int m = blockIdx.x * 32 + tx;
+        double acc = 0.0;
+        if (m < M) {
+            const int64_t ro = dim_off(A.row, m);
+            for (int k = ty; k < K; k += 8) acc = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], acc);
+        }
+        part[ty][tx] = acc;
+        __syncthreads();
+        if (ty == 0 && m < M) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s += part[q][tx];
+            double *y = Y.p + dim_off(Y.row, m) + dim_off(Y.col, 0);
+            double v = alpha * s;
+            if (beta != 0.0) v = fma(beta, *y, v);
+            *y = v;
+        }
+    } else {
+        const int lane = threadIdx.x & 31;
+        const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        if (m >= M) return;
+        const int64_t ro = dim_off(A.row, m);
+        double acc = 0.0;
+        for (int k = lane; k < K; k += 32) acc = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], acc);
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (lane == 0) {
+            double *y = Y.p + dim_off(Y.row, m) + dim_off(Y.col, 0);
+            double v = alpha * acc;
+            if (beta != 0.0) v = fma(beta, *y, v);
+            *y = v;
+        }
+    }
+}
+
 constexpr int kTargetBlocks = 2 * 152;
 
 int choose_splits(int M, int N, int K) {
@@ -139,6 +184,7 @@ int choose_splits(int M, int N, int K) {
 }  // namespace
 
 size_t gemm_f64_ws_elems(int M, int N, int K) {
+    if (M == 1 || N == 1) return 0;
     int s = choose_splits(M, N, K);
     return s > 1 ? (size_t)s * M * N : 0;
 }
@@ -148,6 +194,19 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
     if (M <= 0 || N <= 0) return;
     if (K <= 0) {
         axpby_view(M, N, 0.0, MatView{C.p, C.row, C.col}, beta, C, st);
+        return;
+    }
+    if (N == 1 || M == 1) {
+        // matrix-vector: put the long side in the rows of the view
+        const MatView &Am = N == 1 ? A : B;
+        const MatView &Xv = N == 1 ? B : A;
+        const OutView Y = N == 1 ? C : OutView{C.p, C.col, C.row};
+        const int R = N == 1 ? M : N;
+        if (Am.row.s2 == 1 && Am.col.s2 != 1)
+            gemv_f64_kernel<true><<<(R + 31) / 32, 256, 0, st>>>(R, K, alpha, Am, Xv, beta, Y);
+        else
+            gemv_f64_kernel<false><<<(R + 7) / 8, 256, 0, st>>>(R, K, alpha, Am, Xv, beta, Y);
+        CCSD_LAUNCH_CHECK();
         return;
     }
     int splits = choose_splits(M, N, K);
@@ -166,12 +225,12 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         gemm_f64_kernel<false, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
     else
         gemm_f64_kernel<false, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
     if (splits > 1) {
         size_t total = (size_t)M * N;
         int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
         splitk_reduce_kernel<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
-        CCSD_CUDA(cudaGetLastError());
+        CCSD_LAUNCH_CHECK();
     }
 }
 

@@ -34,6 +34,7 @@ constexpr int CHUNK_KB = 1024 / BK;      // k-blocks per exact level-0 chunk
 constexpr int kThreads = 192;
 constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s wall-time bound per wait
 constexpr int kMaxKbPerSplit = 131072 / BK;  // int32 level-0 sum stays < 2^31
+constexpr int kGroupM = 16;                  // row tiles per rasterisation group
 
 __host__ __device__ constexpr int stage_bytes(int S, int BN) { return S * (BM + BN) * BK * 2; }
 __host__ __device__ constexpr int num_stages(int S, int BN) {
@@ -58,9 +59,9 @@ struct alignas(8) Bars {
 template <int S, int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      int M, int N, int rowsA_pad, int rowsB_pad, int nkb_total, int kb_per_split,
-                      const double *__restrict__ scaleA, const double *__restrict__ scaleB, double alpha,
-                      double beta, OutView C, double *ws, int *gerr) {
+                      int M, int N, int tiles_m, int tiles_n, int rowsA_pad, int rowsB_pad, int nkb_total,
+                      int kb_per_split, const double *__restrict__ scaleA, const double *__restrict__ scaleB,
+                      double alpha, double beta, OutView C, double *ws, int *gerr) {
     constexpr int NST = num_stages(S, BN);
     constexpr int SB = stage_bytes(S, BN);
     constexpr int A_TILE = BM * BK * 2;   // bytes per A plane tile
@@ -73,7 +74,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     Bars *bars = (Bars *)(smem + NST * SB);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    // Grouped rasterisation: consecutive CTAs walk kGroupM row tiles across
+    // all column tiles, so the CTAs resident together share A and B tiles in L2.
+    int mt, nt;
+    {
+        const int t = blockIdx.x;
+        const int group = kGroupM * tiles_n;
+        const int g = t / group, first_m = g * kGroupM;
+        const int gm = min(tiles_m - first_m, kGroupM);
+        const int local = t - g * group;
+        mt = first_m + local % gm;
+        nt = local / gm;
+    }
+    const int m0 = mt * BM, n0 = nt * BN;
     const int kb0 = blockIdx.z * kb_per_split;
     const int kb1 = min(nkb_total, kb0 + kb_per_split);
     const int nkb = kb1 - kb0;
@@ -241,42 +254,121 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-// ---- FP64 -> S BF16 planes, one warp per row ---------------------------------
-template <int S>
-__global__ void split_rows_kernel(int rows, int rows_pad, int K, int kpad, MatView v,
-                                  __nv_bfloat16 *planes, double *scale) {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const size_t plane = (size_t)rows_pad * kpad;
-    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows_pad; r += nwarps) {
-        __nv_bfloat16 *dst = planes + (size_t)r * kpad;
-        if (r >= rows) {
-            for (int k = lane; k < kpad; k += 32)
-#pragma unroll
-                for (int p = 0; p < S; ++p) dst[p * plane + k] = __float2bfloat16_rn(0.f);
-            if (lane == 0) scale[r] = 1.0;
-            continue;
-        }
-        const int64_t ro = dim_off(v.row, (uint32_t)r);
-        double mx = 0.0;
-        for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(v.p[ro + dim_off(v.col, (uint32_t)k)]));
-        for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-        int ex = 0;
-        if (mx > 0.0) frexp(mx, &ex);
-        if (lane == 0) scale[r] = ldexp(1.0, ex);
-        for (int k = lane; k < kpad; k += 32) {
-            double x = k < K ? v.p[ro + dim_off(v.col, (uint32_t)k)] : 0.0;
-            double y = ldexp(x, 7 - ex);  // |y| <= 128
-#pragma unroll
-            for (int p = 0; p < S; ++p) {
-                const double h = rint(y);
-                dst[p * plane + k] = __float2bfloat16_rn((float)ldexp(h, -8 * p));
-                y = (y - h) * 256.0;
+// ---- FP64 -> S BF16 planes ---------------------------------------------------
+// All integer arithmetic (FP64 runs at 1/64 of the FP32 rate on this part):
+// pass 1 takes the row maxima of |x| as IEEE bit patterns (they order like the
+// values for non-negative doubles); pass 2 turns x into the fixed-point
+// integer Y = round(x * 2^(7 - ex + 8(S-1))), ex = exponent of the row
+// maximum (|Y| <= 2^(8S-1)), and peels balanced base-256 digits
+// d in [-128, 127] off Y from the bottom; the remaining top digit P0 lies in
+// [-128, 128].  Plane p stores d_p * 2^(-8p), exact in BF16.
+constexpr int kRowmaxKT = 32;  // 32-wide k tiles per row-max block
+
+template <bool ROWC>
+__global__ void rowmax_kernel(int rows, int K, int nkg, MatView v, unsigned long long *rmax) {
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    const int r0 = (int)(blockIdx.x / nkg) * 32;
+    const int kbeg = (int)(blockIdx.x % nkg) * 32 * kRowmaxKT;
+    const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
+    if (ROWC) {
+        // thread owns row r0 + tx; the 8 thread rows split the k range
+        __shared__ unsigned long long part[8][32];
+        const int r = r0 + tx;
+        unsigned long long m = 0;
+        if (r < rows) {
+            const int64_t ro = dim_off(v.row, (uint32_t)r);
+            const int kend = min(K, kbeg + 32 * kRowmaxKT);
+            for (int k = kbeg + ty; k < kend; k += 8) {
+                const unsigned long long b =
+                    (unsigned long long)__double_as_longlong(v.p[ro + dim_off(v.col, (uint32_t)k)]) & absmask;
+                m = b > m ? b : m;
             }
+        }
+        part[ty][tx] = m;
+        __syncthreads();
+        if (ty == 0 && r < rows) {
+#pragma unroll
+            for (int q = 1; q < 8; ++q) m = part[q][tx] > m ? part[q][tx] : m;
+            if (m) atomicMax(rmax + r, m);
+        }
+    } else {
+        // thread row ty owns rows r0 + ty + 8j; lanes run along k
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = r0 + ty + 8 * j;
+            unsigned long long m = 0;
+            if (r < rows) {
+                const int64_t ro = dim_off(v.row, (uint32_t)r);
+                const int kend = min(K, kbeg + 32 * kRowmaxKT);
+                for (int k = kbeg + tx; k < kend; k += 32) {
+                    const unsigned long long b =
+                        (unsigned long long)__double_as_longlong(v.p[ro + dim_off(v.col, (uint32_t)k)]) & absmask;
+                    m = b > m ? b : m;
+                }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
+                m = o > m ? o : m;
+            }
+            if (tx == 0 && r < rows && m) atomicMax(rmax + r, m);
         }
     }
 }
 
+template <bool ROWC>
+__device__ __forceinline__ void load_tile(double (&t)[32][33], int rows, int K, const MatView &v, int r0,
+                                          int k0) {
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int a = ty + 8 * j;
+        const int r = ROWC ? r0 + tx : r0 + a;
+        const int k = ROWC ? k0 + a : k0 + tx;
+        double x = 0.0;
+        if (r < rows && k < K) x = v.p[dim_off(v.row, (uint32_t)r) + dim_off(v.col, (uint32_t)k)];
+        if (ROWC)
+            t[tx][a] = x;
+        else
+            t[a][tx] = x;
+    }
+}
+
+template <int S, bool ROWC>
+__global__ void split_planes_kernel(int rows, int rows_pad, int K, int kpad, int nkt, MatView v,
+                                    const unsigned long long *rmax, __nv_bfloat16 *planes, double *scale) {
+    __shared__ double t[32][33];
+    const int k0 = (int)(blockIdx.x % nkt) * 32, r0 = (int)(blockIdx.x / nkt) * 32;
+    load_tile<ROWC>(t, rows, K, v, r0, k0);
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const size_t plane = (size_t)rows_pad * kpad;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int a = ty + 8 * j;
+        const int r = r0 + a, k = k0 + tx;
+        if (r >= rows_pad || k >= kpad) continue;
+        const int emax = r < rows ? (int)((rmax[r] >> 52) & 0x7FF) : 0;  // 0: zero (or denormal) row
+        if (k0 == 0 && tx == 0)
+            scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;  // 2^(emax-1022)
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(t[a][tx]);
+        const int e = (int)((bits >> 52) & 0x7FF);
+        long long Y = 0;
+        const int rs = emax - e + 54 - 8 * S;  // right shift that puts x on the 2^-(8(S-1)) grid
+        if (emax && e && rs < 63) {
+            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+            Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
+            if (bits >> 63) Y = -Y;
+        }
+        __nv_bfloat16 *dst = planes + (size_t)r * kpad + k;
+#pragma unroll
+        for (int p = S - 1; p >= 1; --p) {
+            const long long d = ((Y + 128) & 255) - 128;
+            Y = (Y - d) >> 8;
+            dst[p * plane] = __float2bfloat16_rn((float)d * exp2f(-8.0f * p));
+        }
+        dst[0] = __float2bfloat16_rn((float)Y);
+    }
+}
 __global__ void splitk_reduce(int M, int N, int splits, double alpha, const double *ws, double beta,
                               OutView C) {
     const size_t total = (size_t)M * N;
@@ -341,15 +433,16 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
         throw Error(-7, "split GEMM: K too long for the available split-K workspace");
     int kbps = (nkb + splits - 1) / splits;
     splits = (nkb + kbps - 1) / kbps;
-    dim3 grid(tiles_m, tiles_n, splits);
-    split_gemm_kernel<S, BN><<<grid, kThreads, smem, st>>>(ta, tb, M, N, A.rows_pad, B.rows_pad, nkb, kbps,
-                                                           A.scale, B.scale, alpha, beta, C, ws, d_err);
-    CCSD_CUDA(cudaGetLastError());
+    dim3 grid((unsigned)(tiles_m * tiles_n), 1, splits);
+    split_gemm_kernel<S, BN><<<grid, kThreads, smem, st>>>(ta, tb, M, N, tiles_m, tiles_n, A.rows_pad,
+                                                           B.rows_pad, nkb, kbps, A.scale, B.scale, alpha, beta,
+                                                           C, ws, d_err);
+    CCSD_LAUNCH_CHECK();
     if (splits > 1) {
         const size_t total = (size_t)M * N;
         const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
         splitk_reduce<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
-        CCSD_CUDA(cudaGetLastError());
+        CCSD_LAUNCH_CHECK();
     }
 }
 
@@ -368,17 +461,37 @@ void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double
 
 // ---------------------------------------------------------------------------
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st) {
-    const int threads = 256;
-    const long warps_needed = op.rows_pad;
-    const int blocks = (int)std::min<long>((warps_needed * 32 + threads - 1) / threads, 152 * 16);
+    const int nkt = op.kpad / 32, nrt = op.rows_pad / 32;
+    const long long blocks = (long long)nkt * nrt;
+    if (blocks >= (1ll << 31)) throw Error(-7, "split operand too large");
+    const dim3 thr(32, 8);
+    // read along rows when the row index is the contiguous one
+    const bool rowc = v.row.s2 == 1 && v.col.s2 != 1;
+    const long long nkg = (op.kpad + 32 * kRowmaxKT - 1) / (32 * kRowmaxKT);
+    CCSD_CUDA(cudaMemsetAsync(op.rmax, 0, sizeof(unsigned long long) * op.rows_pad, st));
     __nv_bfloat16 *pl = (__nv_bfloat16 *)op.planes;
+    if (rowc)
+        rowmax_kernel<true><<<(unsigned)(nrt * nkg), thr, 0, st>>>(rows, K, nkg, v, op.rmax);
+    else
+        rowmax_kernel<false><<<(unsigned)(nrt * nkg), thr, 0, st>>>(rows, K, nkg, v, op.rmax);
+    CCSD_LAUNCH_CHECK();
+#define CCSD_SPLIT_CASE(S_)                                                                                  \
+    case S_:                                                                                                  \
+        if (rowc)                                                                                             \
+            split_planes_kernel<S_, true><<<(unsigned)blocks, thr, 0, st>>>(rows, op.rows_pad, K, op.kpad, nkt, v, \
+                                                                            op.rmax, pl, op.scale);           \
+        else                                                                                                  \
+            split_planes_kernel<S_, false><<<(unsigned)blocks, thr, 0, st>>>(rows, op.rows_pad, K, op.kpad, nkt, \
+                                                                             v, op.rmax, pl, op.scale);      \
+        break;
     switch (op.nslices) {
-        case 2: split_rows_kernel<2><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
-        case 3: split_rows_kernel<3><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
-        case 4: split_rows_kernel<4><<<blocks, threads, 0, st>>>(rows, op.rows_pad, K, op.kpad, v, pl, op.scale); break;
+        CCSD_SPLIT_CASE(2)
+        CCSD_SPLIT_CASE(3)
+        CCSD_SPLIT_CASE(4)
         default: throw Error(-1, "nslices must be 2, 3 or 4");
     }
-    CCSD_CUDA(cudaGetLastError());
+#undef CCSD_SPLIT_CASE
+    CCSD_LAUNCH_CHECK();
 }
 
 void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
@@ -419,6 +532,7 @@ SplitEngine::SplitEngine(int nslices, cudaStream_t st) : nslices_(nslices), st_(
 
 SplitEngine::~SplitEngine() {
     for (auto &kv : cache_) free_op(*kv.second);
+    for (auto &kv : dyn_) free_op(*kv.second);
     free_op(scratch_[0]);
     free_op(scratch_[1]);
     if (d_err_) cudaFree(d_err_);
@@ -428,8 +542,10 @@ SplitEngine::~SplitEngine() {
 void SplitEngine::free_op(SplitOperand &op) {
     if (op.planes) cudaFree(op.planes);
     if (op.scale) cudaFree(op.scale);
+    if (op.rmax) cudaFree(op.rmax);
     op.planes = nullptr;
     op.scale = nullptr;
+    op.rmax = nullptr;
     op.bytes = 0;
 }
 
@@ -448,6 +564,7 @@ void SplitEngine::ensure(SplitOperand &op, int rows, int K) {
         op.planes = p;
         op.bytes = need;
         CCSD_CUDA(cudaMalloc(&op.scale, sizeof(double) * rows_pad));
+        CCSD_CUDA(cudaMalloc(&op.rmax, sizeof(unsigned long long) * rows_pad));
         op.scale_cap = rows_pad;
     }
     op.rows = rows;
@@ -467,6 +584,15 @@ SplitOperand *SplitEngine::operand(int key, int rows, int K, const MatView &v, i
         split_into(scratch_[slot], rows, K, v);
         return &scratch_[slot];
     }
+    if (key < 0) {
+        std::unique_ptr<SplitOperand> &op = dyn_[key];
+        if (!op) op.reset(new SplitOperand());
+        if (!dyn_valid_[key] || op->rows != rows || op->K != K) {
+            split_into(*op, rows, K, v);
+            dyn_valid_[key] = true;
+        }
+        return op.get();
+    }
     auto it = cache_.find(key);
     if (it != cache_.end()) {
         SplitOperand *op = it->second.get();
@@ -483,9 +609,18 @@ SplitOperand *SplitEngine::operand(int key, int rows, int K, const MatView &v, i
 
 void SplitEngine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
                        const OutView &C, int cache_a, int cache_b) {
+    if (prefer_swap(M, N)) {  // C^T = B A^T keeps the long side in the 128-row MMA tile
+        gemm(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, cache_b, cache_a);
+        return;
+    }
     SplitOperand *a = operand(cache_a, M, K, A, 0);
     SplitOperand *b = operand(cache_b, N, K, B, 1);
     split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
+}
+
+void SplitEngine::run(const SplitOperand &a, const SplitOperand &b, int M, int N, double alpha, double beta,
+                      const OutView &C) {
+    split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
 }
 
 int SplitEngine::error_status() {

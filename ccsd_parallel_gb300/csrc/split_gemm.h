@@ -28,6 +28,7 @@ namespace ccsd {
 struct SplitOperand {
     void *planes = nullptr;  // __nv_bfloat16*
     double *scale = nullptr;
+    unsigned long long *rmax = nullptr;  // row maxima (bit patterns) while splitting
     int rows = 0, rows_pad = 0, K = 0, kpad = 0, nslices = 0;
     size_t bytes = 0, scale_cap = 0;
 };
@@ -43,6 +44,21 @@ class SplitEngine {
     // split form is kept (keyed) between calls.
     void gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
               const OutView &C, int cache_a, int cache_b);
+    // The two halves of gemm(): split (or fetch from the cache) one operand,
+    // then run the tensor-core kernel on two prepared operands.
+    SplitOperand *prepare(int key, int rows, int K, const MatView &v, int slot) {
+        return operand(key, rows, K, v, slot);
+    }
+    void run(const SplitOperand &a, const SplitOperand &b, int M, int N, double alpha, double beta,
+             const OutView &C);
+    // The tensor-core tile is 128 rows by at most 128 columns: a product whose
+    // row count is short and column count long runs faster transposed.
+    static bool prefer_swap(int M, int N) { return M < 128 && N > M; }
+    // Negative cache keys name amplitude-derived operands that several
+    // contractions of one update share; begin_update() invalidates them.
+    void begin_update() {
+        for (auto &kv : dyn_valid_) kv.second = false;
+    }
     // Device error word (bounded waits that gave up); 0 when clean.
     int error_status();
     size_t cached_bytes() const;
@@ -56,6 +72,8 @@ class SplitEngine {
     int nslices_;
     cudaStream_t st_;
     std::map<int, std::unique_ptr<SplitOperand>> cache_;
+    std::map<int, std::unique_ptr<SplitOperand>> dyn_;
+    std::map<int, bool> dyn_valid_;
     SplitOperand scratch_[2];
     int *d_err_ = nullptr;
     double *ws_ = nullptr;

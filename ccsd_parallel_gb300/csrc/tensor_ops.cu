@@ -4,6 +4,8 @@
 // is HBM bandwidth.
 //
 // Index conventions (closed-shell spatial): t1[i][a], t2[i][j][a][b].
+#include <atomic>
+
 #include "common.h"
 
 namespace ccsd {
@@ -170,28 +172,34 @@ __global__ void copy_diag_kernel(int n, const double *fock, int off, int cnt, do
 
 int reduce_blocks() { return kReduceBlocks; }
 
+namespace {
+std::atomic<long> g_launches{0};
+}
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
                 cudaStream_t st) {
     if (R <= 0 || C <= 0) return;
     axpby_view_kernel<<<grid_for((size_t)R * C), 256, 0, st>>>(R, C, alpha, X, beta, Y);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st) {
     tau_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, tau);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
              cudaStream_t st) {
     theta_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const double *ev, double *t2,
                  cudaStream_t st) {
     mp2_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, ovov, eo, ev, t2);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
@@ -199,35 +207,35 @@ void k_update_t2(int o, int v, const double *R, const double *Rp, const double *
                  int nblocks, cudaStream_t st) {
     update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new,
                                                          partials);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_update_t1(int o, int v, const double *R1, const double *eo, const double *ev,
                  const double *t1_old, double *t1_new, double *partials, cudaStream_t st) {
     update_t1_kernel<<<1, 1024, 0, st>>>(o, v, R1, eo, ev, t1_old, t1_new, partials);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_dot(size_t n, const double *x, const double *y, double *partials, int nblocks,
            cudaStream_t st) {
     dot_kernel<<<nblocks, kReduceThreads, 0, st>>>(n, x, y, partials);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_sum(int n, const double *partials, double *out, cudaStream_t st) {
     sum_kernel<<<1, 1024, 0, st>>>(n, partials, out);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_fill(size_t n, double val, double *p, cudaStream_t st) {
     if (n == 0) return;
     fill_kernel<<<grid_for(n), 256, 0, st>>>(n, val, p);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st) {
     copy_diag_kernel<<<(cnt + 255) / 256, 256, 0, st>>>(n, fock, off, cnt, out);
-    CCSD_CUDA(cudaGetLastError());
+    CCSD_LAUNCH_CHECK();
 }
 
 }  // namespace ccsd

@@ -85,6 +85,7 @@ typedef struct ccsd_options {
     int32_t diis_start;        /* first update index that extrapolates         */
     int32_t precision;         /* CCSD_PREC_*                                   */
     int32_t verbose;           /* print one line per update to stdout          */
+    int32_t profile;           /* 1: time every contraction with CUDA events   */
     void *stream;              /* cudaStream_t, or NULL for a private stream   */
 } ccsd_options;
 
@@ -120,6 +121,14 @@ int ccsd_solve(ccsd_handle *h, ccsd_result *res);
 int ccsd_set_options(ccsd_handle *h, const ccsd_options *opts);
 
 int ccsd_destroy(ccsd_handle *h);
+
+/* JSON report of the last solve when options.profile was set: per
+ * contraction site the calls, device ms of the contraction kernel, device ms
+ * of the operand splitting (split modes), algorithmic FLOP and the path that
+ * ran.  Times come from CUDA events recorded on the engine's stream.  The
+ * reference only prints clock() CPU time per iteration
+ * (ccsd_memory_optimized.cpp:515,542-548).  Returns the report length. */
+int ccsd_profile_report(ccsd_handle *h, char *buf, size_t len);
 
 /* Copy the calling thread's last error message; returns its length. */
 int ccsd_last_error(char *buf, size_t len);

@@ -30,9 +30,15 @@ ES = dict(optimize=True)
 
 
 class Blocks:
-    """Spatial chemist-notation integral blocks for one closed-shell system."""
+    """Spatial chemist-notation integral blocks for one closed-shell system.
 
-    def __init__(self, eri=None, nocc=None, df=None):
+    With ``with_vvvv=False`` (DF input only) the v^4 block is not formed; the
+    particle-particle ladder is then available row by row through
+    ``RHFCCSD.ladder_rows`` (used to time a bounded sample of the largest
+    shapes on the CPU)."""
+
+    def __init__(self, eri=None, nocc=None, df=None, with_vvvv=True):
+        self.df = df
         if eri is not None:
             o = nocc
             n = eri.shape[0]
@@ -55,11 +61,11 @@ class Blocks:
             self.ovoo = e(bov, bo)
             self.oooo = e(bo, bo)
             self.ovvv = e(bov, bvv)
-            self.vvvv = e(bvv, bvv)
+            self.vvvv = e(bvv, bvv) if with_vvvv else None
 
 
 class RHFCCSD:
-    def __init__(self, fock: np.ndarray, nocc: int, eri=None, df=None):
+    def __init__(self, fock: np.ndarray, nocc: int, eri=None, df=None, with_vvvv=True):
         self.o = nocc
         self.n = fock.shape[0]
         self.v = self.n - nocc
@@ -71,7 +77,15 @@ class RHFCCSD:
         self.ev = np.diag(fock)[o:].copy()
         self.d1 = self.eo[:, None] - self.ev[None, :]
         self.d2 = self.d1[:, None, :, None] + self.d1[None, :, None, :]
-        self.B = Blocks(eri=eri, nocc=nocc, df=df)
+        self.B = Blocks(eri=eri, nocc=nocc, df=df, with_vvvv=with_vvvv)
+
+    def ladder_rows(self, tau, a0: int, a1: int):
+        """sum_cd (ac|bd) tau[i,j,c,d] for a in [a0, a1), building the needed
+        (ac|bd) rows from the DF factors; returns [i, j, a - a0, b]."""
+        o = self.o
+        bvv = self.B.df[:, o:, o:]
+        w = np.einsum("Qac,Qbd->acbd", bvv[:, a0:a1], bvv, optimize=True)
+        return np.einsum("acbd,ijcd->ijab", w, tau, optimize=True)
 
     def tau(self, t1, t2):
         return t2 + np.einsum("ia,jb->ijab", t1, t1)
@@ -151,7 +165,10 @@ class RHFCCSD:
         R2 += P(X - Y)
         R2 += np.einsum("klij,klab->ijab", Woooo, tau, **ES)
         # particle-particle ladder with bare (ac|bd), then the T1 dressing
-        R2 += np.einsum("acbd,ijcd->ijab", vvvv, tau, **ES)
+        if vvvv is not None:
+            R2 += np.einsum("acbd,ijcd->ijab", vvvv, tau, **ES)
+        elif not getattr(self, "skip_ladder", False):
+            R2 += self.ladder_rows(tau, 0, self.v)
         Z = np.einsum("kdac,ijcd->ijka", ovvv, tau, **ES)           # sum_cd (ac|kd) tau_ij^cd
         R2 -= P(np.einsum("ijka,kb->ijab", Z, t1, **ES))
         R2 += P(np.einsum("ac,ijcb->ijab", Lvv_p, t2, **ES))

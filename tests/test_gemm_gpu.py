@@ -38,7 +38,7 @@ def bound(A, B, S):
 
 
 SHAPES = [(1, 1, 1), (5, 7, 3), (128, 128, 32), (200, 70, 1000), (130, 33, 2500), (300, 300, 5000),
-          (1000, 20, 64), (64, 513, 4097)]
+          (1000, 20, 64), (64, 513, 4097), (5000, 1, 300), (1, 700, 9000), (40, 1000, 500)]
 
 
 @pytest.mark.parametrize("M,N,K", SHAPES)
