@@ -37,6 +37,11 @@ int guarded(F &&f) {
 }
 }  // namespace
 
+namespace ccsd {
+// Lets entry points defined in other files report through ccsd_last_error.
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace ccsd
+
 extern "C" {
 
 int ccsd_default_options(ccsd_options *opts) {

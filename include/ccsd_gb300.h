@@ -148,6 +148,29 @@ int ccsd_gemm(int32_t precision, int32_t M, int32_t N, int32_t K, double alpha, 
               int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
               void *stream);
 
+/* ccsd_gemm without any device allocation, for callers that may not call
+ * cudaMalloc/cudaFree: a process whose device memory belongs to another
+ * allocator with a fixed budget (a framework's caching allocator, a serving
+ * runtime that reserves all of HBM up front), or code in the middle of a
+ * pipelined stream that cannot take the device-wide synchronisation of
+ * cudaFree.  No counterpart in the reference.
+ *   - precision must be CCSD_PREC_SPLIT2/3/4 (the tensor-core kernel); the
+ *     result equals ccsd_gemm's within the split kernel's error bound.
+ *   - Scratch (BF16 planes, row scales, split-K partials, error word) lives in
+ *     one static device array of 64 MiB that every GPU loading the library
+ *     holds until exit.  Shapes whose scratch exceeds it are rejected with
+ *     CCSD_ERR_INVALID_ARG and a message giving the bytes needed; roughly
+ *     S * (M + N) * K * 2 bytes must stay below 64 MiB.
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the array: calls whose work overlaps on the GPU (other
+ *     streams or threads on the same device) race; serialise them.
+ *   - Returns after the work completes (it synchronises `stream`). */
+int ccsd_gemm_noalloc(int32_t precision, int32_t M, int32_t N, int32_t K, double alpha,
+                      const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                      double *C, int64_t ldc, void *stream);
+
 /* Seeded synthetic closed-shell system (host only, no GPU needed): diagonal
  * fock (n x n) with occupied U[-2,-0.3] / virtual U[0.1,3] energies, and
  * DF factors B[Q][p][q] = 0.05 z / sqrt(naux), z ~ N(0,1), symmetric in p,q.
