@@ -152,15 +152,16 @@ def peaks():
 
 
 def ladder_traffic(nocc, nvir):
-    """DRAM bytes per pp-ladder launch from the committed ncu summary, scaled
-    from the captured case to this one by the units (v^2 x o^2 tile work is
-    not the driver: traffic scales with the split (vv|vv) planes, v^4)."""
+    """DRAM bytes per pp-ladder launch from the committed ncu capture
+    (profiles/pp_ladder_traffic.json, a smaller nvir at the same nocc), scaled
+    to this nvir by the split (vv|vv) plane bytes, which grow as nvir^4."""
     p = ROOT / "profiles" / "pp_ladder_traffic.json"
     if not p.exists():
         return None, None
     d = json.loads(p.read_text())
-    scale = (nvir / d["nvir"]) ** 4 * (1.0 if d["nocc"] == nocc else (nocc / d["nocc"]) ** 0)
-    return d["dram_bytes_per_launch"] * scale, d
+    if d["nocc"] != nocc:
+        return None, d
+    return d["dram_bytes_per_launch"] * (nvir / d["nvir"]) ** 4, d
 
 
 def cpu_sample(fock, df, nocc, steps=1):

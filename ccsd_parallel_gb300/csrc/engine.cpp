@@ -16,6 +16,8 @@
 // engine, selected per call by the precision option.
 #include "engine.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -57,6 +59,16 @@ void DBuf::zero(cudaStream_t st) {
 }
 
 namespace {
+struct NvtxScope {
+    bool on;
+    explicit NvtxScope(const char *name) : on(name != nullptr) {
+        if (on) nvtxRangePushA(name);
+    }
+    ~NvtxScope() {
+        if (on) nvtxRangePop();
+    }
+};
+
 inline MatView mv(const double *p, Dim r, Dim c) {
     MatView m;
     m.p = p;
@@ -362,6 +374,7 @@ void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const Mat
         return;
     }
     cudaEvent_t ea = nullptr, eb = nullptr, ec = nullptr;
+    NvtxScope nvtx(prof ? site : nullptr);  // lets ncu --nvtx-include pick one contraction site
     if (prof) {
         ea = prof_event();
         eb = prof_event();
