@@ -97,7 +97,8 @@ class Solver:
         h = C.c_void_p()
         _abi.check(_abi.lib().ccsd_create(C.byref(p), C.byref(self._opts), C.byref(h)))
         self._h = h
-        self._keep = None  # inputs were copied to the device
+        self._problem = p  # re-read by lambda_grad (the arrays in _keep stay referenced)
+        self._n = n
 
     def set_options(self, **opts):
         self._opts = _options(**opts)
@@ -117,6 +118,29 @@ class Solver:
                     residual_norm=r.residual_norm, energies=eh[:r.history_len].copy(),
                     update_ms=ms[:r.iterations].copy(), flops_per_update=r.flops_per_update,
                     t1=t1, t2=t2)
+
+    def lambda_grad(self, tol: float = 1e-10, max_iter: int = 500, lambdas: bool = False) -> dict:
+        """Lambda equations at the last solve and dE_corr/d(inputs) (see ccsd_lambda_grad)."""
+        o, v, n = self.nocc, self.nvir, self._n
+        p = self._problem
+        g = _abi.Grad()
+        out = {"d_fock": np.zeros((n, n))}
+        if p.integral_kind == CCSD_INTS_DF:
+            out["d_df"] = np.zeros((p.naux, n, n))
+        elif p.integral_kind == CCSD_INTS_AO_DENSE:
+            out["d_eri"] = np.zeros((p.nao,) * 4)
+            out["d_mo_coeff"] = np.zeros((p.nao, n))
+        else:
+            out["d_eri"] = np.zeros((n,) * 4)
+        if lambdas:
+            out["lambda1"] = np.zeros((o, v))
+            out["lambda2"] = np.zeros((o, o, v, v))
+        for k, arr in out.items():
+            setattr(g, k, _ptr(arr))
+        g.tol, g.max_iter = tol, max_iter
+        _abi.check(_abi.lib().ccsd_lambda_grad(self._h, C.byref(p), C.byref(g)))
+        out.update(iterations=g.iterations, residual_norm=g.residual_norm, e_corr=g.e_corr)
+        return out
 
     def profile(self) -> dict:
         """Per-contraction device times of the last solve (needs profile=True)."""

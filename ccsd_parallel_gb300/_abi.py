@@ -59,11 +59,20 @@ class Result(C.Structure):
     ]
 
 
+class Grad(C.Structure):
+    _fields_ = [
+        ("d_fock", _dp), ("d_eri", _dp), ("d_df", _dp), ("d_mo_coeff", _dp), ("lambda1", _dp),
+        ("lambda2", _dp), ("tol", C.c_double), ("max_iter", C.c_int32), ("iterations", C.c_int32),
+        ("residual_norm", C.c_double), ("e_corr", C.c_double),
+    ]
+
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "ccsd_default_options": (C.c_int, [C.POINTER(Options)]),
     "ccsd_create": (C.c_int, [C.POINTER(Problem), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "ccsd_solve": (C.c_int, [C.c_void_p, C.POINTER(Result)]),
+    "ccsd_lambda_grad": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(Grad)]),
     "ccsd_set_options": (C.c_int, [C.c_void_p, C.POINTER(Options)]),
     "ccsd_destroy": (C.c_int, [C.c_void_p]),
     "ccsd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),

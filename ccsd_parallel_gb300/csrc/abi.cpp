@@ -84,6 +84,11 @@ int ccsd_solve(ccsd_handle *h, ccsd_result *res) {
     return guarded([&] { h->engine->solve(res); });
 }
 
+int ccsd_lambda_grad(ccsd_handle *h, const ccsd_problem *problem, ccsd_grad *grad) {
+    if (!h || !h->engine || !problem || !grad) return fail(CCSD_ERR_INVALID_ARG, "handle/problem/grad is NULL");
+    return guarded([&] { h->engine->lambda_grad(*problem, grad); });
+}
+
 int ccsd_set_options(ccsd_handle *h, const ccsd_options *opts) {
     if (!h || !h->engine || !opts) return fail(CCSD_ERR_INVALID_ARG, "handle/opts is NULL");
     return guarded([&] { h->engine->set_options(*opts); });

@@ -179,64 +179,76 @@ void Engine::set_options(const ccsd_options &opts) {
 // Integral set-up (the reference's Prepear_AOs + Fill_FS, ccsd_memory_optimized.cpp:71-74)
 void Engine::build_integrals(const ccsd_problem &prob) {
     const int n = n_, o = o_, v = v_;
-    // Fock: diagonal -> orbital energies; off-diagonal blocks enter the
-    // intermediates (the reference only supports a diagonal matrix, Fill_FS :3560).
-    DBuf fock(n * (size_t)n);
-    CCSD_CUDA(cudaMemcpyAsync(fock.p, prob.fock, sizeof(double) * n * n,
-                              prob.device_inputs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                              st_));
-    eo_.alloc(o);
-    ev_.alloc(v);
-    k_copy_diag(n, fock.p, 0, o, eo_.p, st_);
-    k_copy_diag(n, fock.p, o, v, ev_.p, st_);
-    f_oo_off_.alloc((size_t)o * o);
-    f_vv_off_.alloc((size_t)v * v);
-    f_ov_.alloc((size_t)o * v);
-    axpby_view(o, o, 1.0, mv(fock.p, ix1(n), ix1(1)), 0.0, ovw(f_oo_off_.p, ix1(o), ix1(1)), st_);
-    axpby_view(v, v, 1.0, mv(fock.p + (size_t)o * n + o, ix1(n), ix1(1)), 0.0,
-               ovw(f_vv_off_.p, ix1(v), ix1(1)), st_);
-    axpby_view(o, v, 1.0, mv(fock.p + o, ix1(n), ix1(1)), 0.0, ovw(f_ov_.p, ix1(v), ix1(1)), st_);
-    // remove the diagonal (it sits in the denominators): X(r,r) -= diag
+    // Fock, on the host: the diagonal goes to the denominators; the
+    // off-diagonal blocks enter the intermediates (the reference only supports
+    // a diagonal matrix, Fill_FS :3560).
     {
         std::vector<double> hf((size_t)n * n);
         if (prob.device_inputs)
             CCSD_CUDA(cudaMemcpy(hf.data(), prob.fock, sizeof(double) * n * n, cudaMemcpyDeviceToHost));
         else
             std::memcpy(hf.data(), prob.fock, sizeof(double) * n * n);
-        std::vector<double> oo((size_t)o * o), vv((size_t)v * v);
+        std::vector<double> eo(o), ev(v), oo((size_t)o * o), vv((size_t)v * v), ov((size_t)o * v);
+        for (int i = 0; i < o; ++i) eo[i] = hf[(size_t)i * n + i];
+        for (int a = 0; a < v; ++a) ev[a] = hf[(size_t)(o + a) * n + o + a];
         for (int i = 0; i < o; ++i)
             for (int j = 0; j < o; ++j) oo[i * o + j] = i == j ? 0.0 : hf[(size_t)i * n + j];
         for (int a = 0; a < v; ++a)
             for (int b = 0; b < v; ++b) vv[a * v + b] = a == b ? 0.0 : hf[(size_t)(o + a) * n + o + b];
+        for (int i = 0; i < o; ++i)
+            for (int a = 0; a < v; ++a) ov[i * v + a] = hf[(size_t)i * n + o + a];
+        eo_.ensure(o);
+        ev_.ensure(v);
+        f_oo_off_.ensure((size_t)o * o);
+        f_vv_off_.ensure((size_t)v * v);
+        f_ov_.ensure((size_t)o * v);
+        CCSD_CUDA(cudaMemcpyAsync(eo_.p, eo.data(), sizeof(double) * o, cudaMemcpyHostToDevice, st_));
+        CCSD_CUDA(cudaMemcpyAsync(ev_.p, ev.data(), sizeof(double) * v, cudaMemcpyHostToDevice, st_));
         CCSD_CUDA(cudaMemcpyAsync(f_oo_off_.p, oo.data(), sizeof(double) * o * o, cudaMemcpyHostToDevice, st_));
         CCSD_CUDA(cudaMemcpyAsync(f_vv_off_.p, vv.data(), sizeof(double) * v * v, cudaMemcpyHostToDevice, st_));
+        CCSD_CUDA(cudaMemcpyAsync(f_ov_.p, ov.data(), sizeof(double) * o * v, cudaMemcpyHostToDevice, st_));
         CCSD_CUDA(cudaStreamSynchronize(st_));
     }
 
+    // Input copies (and transform intermediates) stay alive while a build is
+    // recorded for the gradient; otherwise they are freed on return.
+    keep_.clear();
+    auto keep = [&](std::unique_ptr<DBuf> b) {
+        if (tape_) keep_.push_back(std::move(b));
+    };
     const cudaMemcpyKind kind = prob.device_inputs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (prob.integral_kind == CCSD_INTS_MO_DENSE) {
         if (!prob.eri) throw Error(CCSD_ERR_INVALID_ARG, "eri is NULL");
-        DBuf eri((size_t)n * n * n * n);
-        CCSD_CUDA(cudaMemcpyAsync(eri.p, prob.eri, sizeof(double) * eri.n, kind, st_));
-        build_from_mo_dense(eri.p);
+        std::unique_ptr<DBuf> eri(new DBuf((size_t)n * n * n * n));
+        CCSD_CUDA(cudaMemcpyAsync(eri->p, prob.eri, sizeof(double) * eri->n, kind, st_));
+        build_from_mo_dense(eri->p);
         CCSD_CUDA(cudaStreamSynchronize(st_));
+        input_eri_ = eri.get();
+        keep(std::move(eri));
     } else if (prob.integral_kind == CCSD_INTS_DF) {
         if (!prob.df || prob.naux <= 0) throw Error(CCSD_ERR_INVALID_ARG, "df factors missing");
-        DBuf b((size_t)prob.naux * n * n);
-        CCSD_CUDA(cudaMemcpyAsync(b.p, prob.df, sizeof(double) * b.n, kind, st_));
-        build_from_df(b.p, prob.naux);
+        std::unique_ptr<DBuf> b(new DBuf((size_t)prob.naux * n * n));
+        CCSD_CUDA(cudaMemcpyAsync(b->p, prob.df, sizeof(double) * b->n, kind, st_));
+        build_from_df(b->p, prob.naux);
         CCSD_CUDA(cudaStreamSynchronize(st_));
+        input_df_ = b.get();
+        keep(std::move(b));
     } else if (prob.integral_kind == CCSD_INTS_AO_DENSE) {
         if (!prob.eri || !prob.mo_coeff || prob.nao < n)
             throw Error(CCSD_ERR_INVALID_ARG, "AO integrals / mo_coeff missing or nao < n");
         const size_t nao = prob.nao;
-        DBuf ao(nao * nao * nao * nao), c(nao * n);
-        CCSD_CUDA(cudaMemcpyAsync(ao.p, prob.eri, sizeof(double) * ao.n, kind, st_));
-        CCSD_CUDA(cudaMemcpyAsync(c.p, prob.mo_coeff, sizeof(double) * c.n, kind, st_));
-        DBuf mo;
-        ao_to_mo(ao.p, c.p, (int)nao, mo);
-        build_from_mo_dense(mo.p);
+        std::unique_ptr<DBuf> ao(new DBuf(nao * nao * nao * nao)), c(new DBuf(nao * n));
+        CCSD_CUDA(cudaMemcpyAsync(ao->p, prob.eri, sizeof(double) * ao->n, kind, st_));
+        CCSD_CUDA(cudaMemcpyAsync(c->p, prob.mo_coeff, sizeof(double) * c->n, kind, st_));
+        std::unique_ptr<DBuf> mo(new DBuf());
+        ao_to_mo(ao->p, c->p, (int)nao, *mo);
+        build_from_mo_dense(mo->p);
         CCSD_CUDA(cudaStreamSynchronize(st_));
+        input_eri_ = ao.get();
+        input_c_ = c.get();
+        keep(std::move(ao));
+        keep(std::move(c));
+        keep(std::move(mo));
     } else {
         throw Error(CCSD_ERR_INVALID_ARG, "unknown integral_kind");
     }
@@ -247,11 +259,11 @@ void Engine::build_from_mo_dense(const double *eri) {
     const int64_t n = n_, o = o_, v = v_;
     auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
                    int64_t er, int64_t s0, int64_t es) {
-        dst.alloc((size_t)(ep * eq * er * es));
+        dst.ensure((size_t)(ep * eq * er * es));
         const double *base = eri + ((p0 * n + q0) * n + r0) * n + s0;
-        axpby_view((int)(ep * eq), (int)(er * es), 1.0,
-                   mv(base, ix2((uint32_t)eq, n * n * n, n * n), ix2((uint32_t)es, n, 1)), 0.0,
-                   ovw(dst.p, ix1(er * es), ix1(1)), st_);
+        axpby((int)(ep * eq), (int)(er * es), 1.0,
+              mv(base, ix2((uint32_t)eq, n * n * n, n * n), ix2((uint32_t)es, n, 1)), 0.0,
+              ovw(dst.p, ix1(er * es), ix1(1)));
     };
     blk(ovov_, 0, o, o, v, 0, o, o, v);
     blk(oovv_, 0, o, 0, o, o, v, o, v);
@@ -259,11 +271,11 @@ void Engine::build_from_mo_dense(const double *eri) {
     blk(oooo_, 0, o, 0, o, 0, o, 0, o);
     blk(ovvv_, 0, o, o, v, o, v, o, v);
     // Wv[a][b][c][d] = (ac|bd) = eri[o+a][o+c][o+b][o+d]
-    wv_.alloc((size_t)(v * v * v * v));
+    wv_.ensure((size_t)(v * v * v * v));
     const double *base = eri + ((o * n + o) * n + o) * n + o;
-    axpby_view((int)(v * v), (int)(v * v), 1.0,
-               mv(base, ix2((uint32_t)v, n * n * n, n), ix2((uint32_t)v, n * n, 1)), 0.0,
-               ovw(wv_.p, ix1(v * v), ix1(1)), st_);
+    axpby((int)(v * v), (int)(v * v), 1.0,
+          mv(base, ix2((uint32_t)v, n * n * n, n), ix2((uint32_t)v, n * n, 1)), 0.0,
+          ovw(wv_.p, ix1(v * v), ix1(1)));
 }
 
 // (pq|rs) = sum_Q B[Q][p][q] B[Q][r][s] as contractions over Q.
@@ -271,7 +283,7 @@ void Engine::build_from_df(const double *B, int naux) {
     const int64_t n = n_, o = o_, v = v_, nn = n * n;
     auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
                    int64_t er, int64_t s0, int64_t es) {
-        dst.alloc((size_t)(ep * eq * er * es));
+        dst.ensure((size_t)(ep * eq * er * es));
         gemm((int)(ep * eq), (int)(er * es), naux, 1.0,
              mv(B + p0 * n + q0, ix2((uint32_t)eq, n, 1), ix1(nn)),
              mv(B + r0 * n + s0, ix2((uint32_t)es, n, 1), ix1(nn)), 0.0,
@@ -283,7 +295,7 @@ void Engine::build_from_df(const double *B, int naux) {
     blk(oooo_, 0, o, 0, o, 0, o, 0, o);
     blk(ovvv_, 0, o, o, v, o, v, o, v);
     // Wv[a][b][c][d] = (ac|bd): M = (a,c), N = (b,d), K = Q
-    wv_.alloc((size_t)(v * v * v * v));
+    wv_.ensure((size_t)(v * v * v * v));
     const double *bvv = B + o * n + o;
     gemm((int)(v * v), (int)(v * v), naux, 1.0, mv(bvv, ix2((uint32_t)v, n, 1), ix1(nn)),
          mv(bvv, ix2((uint32_t)v, n, 1), ix1(nn)), 0.0,
@@ -294,23 +306,29 @@ void Engine::build_from_df(const double *B, int naux) {
 // (the reference's Prepear_AOs quarter matvecs, ccsd_memory_optimized.cpp:2990-3037).
 void Engine::ao_to_mo(const double *ao, const double *c, int nao_i, DBuf &mo) {
     const int64_t N = nao_i, n = n_;
-    DBuf x1((size_t)(n * N * N * N)), x2((size_t)(n * n * N * N)), x3((size_t)(n * n * n * N));
-    mo.alloc((size_t)(n * n * n * n));
+    std::unique_ptr<DBuf> x1(new DBuf((size_t)(n * N * N * N))), x2(new DBuf((size_t)(n * n * N * N))),
+        x3(new DBuf((size_t)(n * n * n * N)));
+    mo.ensure((size_t)(n * n * n * n));
     // x1[p][nu][la][si] = sum_mu C[mu][p] ao[mu][nu la si]
     gemm((int)n, (int)(N * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
-         mv(ao, ix1(1), ix1(N * N * N)), 0.0, ovw(x1.p, ix1(N * N * N), ix1(1)));
+         mv(ao, ix1(1), ix1(N * N * N)), 0.0, ovw(x1->p, ix1(N * N * N), ix1(1)));
     // x2[p][q][la si] = sum_nu C[nu][q] x1[p][nu][la si]; M = q, N = (p, lasi)
     gemm((int)n, (int)(n * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
-         mv(x1.p, ix2((uint32_t)(N * N), N * N * N, 1), ix1(N * N)), 0.0,
-         ovw(x2.p, ix1(N * N), ix2((uint32_t)(N * N), n * N * N, 1)));
+         mv(x1->p, ix2((uint32_t)(N * N), N * N * N, 1), ix1(N * N)), 0.0,
+         ovw(x2->p, ix1(N * N), ix2((uint32_t)(N * N), n * N * N, 1)));
     // x3[pq][r][si] = sum_la C[la][r] x2[pq][la][si]; M = r, N = (pq, si)
     gemm((int)n, (int)(n * n * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
-         mv(x2.p, ix2((uint32_t)N, N * N, 1), ix1(N)), 0.0,
-         ovw(x3.p, ix1(N), ix2((uint32_t)N, n * N, 1)));
+         mv(x2->p, ix2((uint32_t)N, N * N, 1), ix1(N)), 0.0,
+         ovw(x3->p, ix1(N), ix2((uint32_t)N, n * N, 1)));
     // mo[pqr][s] = sum_si C[si][s] x3[pqr][si]; M = s, N = pqr
     gemm((int)n, (int)(n * n * n), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
-         mv(x3.p, ix1(N), ix1(1)), 0.0, ovw(mo.p, ix1(1), ix1(n)));
+         mv(x3->p, ix1(N), ix1(1)), 0.0, ovw(mo.p, ix1(1), ix1(n)));
     CCSD_CUDA(cudaStreamSynchronize(st_));
+    if (tape_) {
+        keep_.push_back(std::move(x1));
+        keep_.push_back(std::move(x2));
+        keep_.push_back(std::move(x3));
+    }
 }
 
 // L-combinations of the integrals, built once.
@@ -318,45 +336,45 @@ void Engine::build_derived() {
     const int64_t o = o_, v = v_;
     const size_t nT2 = (size_t)(o * o * v * v);
     // Lovov[k][c][l][d] = 2 (kc|ld) - (kd|lc)
-    Lovov_.alloc(nT2);
-    axpby_view((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(o * v), ix1(1)), 0.0,
-               ovw(Lovov_.p, ix1(o * v), ix1(1)), st_);
-    axpby_view((int)(o * v), (int)(o * v), -1.0,
-               mv(ovov_.p, ix2((uint32_t)v, v * o * v, 1), ix2((uint32_t)v, v, o * v)), 1.0,
-               ovw(Lovov_.p, ix1(o * v), ix1(1)), st_);
+    Lovov_.ensure(nT2);
+    axpby((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(o * v), ix1(1)), 0.0,
+          ovw(Lovov_.p, ix1(o * v), ix1(1)));
+    axpby((int)(o * v), (int)(o * v), -1.0,
+          mv(ovov_.p, ix2((uint32_t)v, v * o * v, 1), ix2((uint32_t)v, v, o * v)), 1.0,
+          ovw(Lovov_.p, ix1(o * v), ix1(1)));
     // Lovoo[l][c][k][i] = 2 (lc|ki) - (kc|li)
-    Lovoo_.alloc((size_t)(o * v * o * o));
-    axpby_view((int)(o * v), (int)(o * o), 2.0, mv(ovoo_.p, ix1(o * o), ix1(1)), 0.0,
-               ovw(Lovoo_.p, ix1(o * o), ix1(1)), st_);
+    Lovoo_.ensure((size_t)(o * v * o * o));
+    axpby((int)(o * v), (int)(o * o), 2.0, mv(ovoo_.p, ix1(o * o), ix1(1)), 0.0,
+          ovw(Lovoo_.p, ix1(o * o), ix1(1)));
     // (kc|li) at [l][c][k][i]: row (l,c) -> l: o (in ovoo[k][c][l][i], l stride o), c: o*o
-    axpby_view((int)(o * v), (int)(o * o), -1.0,
-               mv(ovoo_.p, ix2((uint32_t)v, o, o * o), ix2((uint32_t)o, v * o * o, 1)), 1.0,
-               ovw(Lovoo_.p, ix1(o * o), ix1(1)), st_);
+    axpby((int)(o * v), (int)(o * o), -1.0,
+          mv(ovoo_.p, ix2((uint32_t)v, o, o * o), ix2((uint32_t)o, v * o * o, 1)), 1.0,
+          ovw(Lovoo_.p, ix1(o * o), ix1(1)));
     // Lovvv[k][d][a][c] = 2 (kd|ac) - (kc|ad)
     const size_t nov3 = (size_t)(o * v * v * v);
-    Lovvv_.alloc(nov3);
-    axpby_view((int)(o * v), (int)(v * v), 2.0, mv(ovvv_.p, ix1(v * v), ix1(1)), 0.0,
-               ovw(Lovvv_.p, ix1(v * v), ix1(1)), st_);
+    Lovvv_.ensure(nov3);
+    axpby((int)(o * v), (int)(v * v), 2.0, mv(ovvv_.p, ix1(v * v), ix1(1)), 0.0,
+          ovw(Lovvv_.p, ix1(v * v), ix1(1)));
     // (kc|ad) = ovvv[k][c][a][d] placed at [k][d][a][c]: row (k,d): k v^3, d: 1; col (a,c): a v, c v^2
-    axpby_view((int)(o * v), (int)(v * v), -1.0,
-               mv(ovvv_.p, ix2((uint32_t)v, v * v * v, 1), ix2((uint32_t)v, v, v * v)), 1.0,
-               ovw(Lovvv_.p, ix1(v * v), ix1(1)), st_);
+    axpby((int)(o * v), (int)(v * v), -1.0,
+          mv(ovvv_.p, ix2((uint32_t)v, v * v * v, 1), ix2((uint32_t)v, v, v * v)), 1.0,
+          ovw(Lovvv_.p, ix1(v * v), ix1(1)));
     // LT1[i][a][k][c] = 2 (kc|ia) - (ki|ac)
-    LT1_.alloc(nT2);
-    axpby_view((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(1), ix1(o * v)), 0.0,
-               ovw(LT1_.p, ix1(o * v), ix1(1)), st_);
+    LT1_.ensure(nT2);
+    axpby((int)(o * v), (int)(o * v), 2.0, mv(ovov_.p, ix1(1), ix1(o * v)), 0.0,
+          ovw(LT1_.p, ix1(o * v), ix1(1)));
     // (ki|ac) = oovv[k][i][a][c]: row (i,a): i v^2, a v; col (k,c): k o v^2, c 1
-    axpby_view((int)(o * v), (int)(o * v), -1.0,
-               mv(oovv_.p, ix2((uint32_t)v, v * v, v), ix2((uint32_t)v, o * v * v, 1)), 1.0,
-               ovw(LT1_.p, ix1(o * v), ix1(1)), st_);
+    axpby((int)(o * v), (int)(o * v), -1.0,
+          mv(oovv_.p, ix2((uint32_t)v, v * v, v), ix2((uint32_t)v, o * v * v, 1)), 1.0,
+          ovw(LT1_.p, ix1(o * v), ix1(1)));
     // Lijab[i][j][a][b] = 2 (ia|jb) - (ib|ja)
-    Lijab_.alloc(nT2);
-    axpby_view((int)(o * o), (int)(v * v), 2.0,
-               mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
-               ovw(Lijab_.p, ix1(v * v), ix1(1)), st_);
-    axpby_view((int)(o * o), (int)(v * v), -1.0,
-               mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
-               ovw(Lijab_.p, ix1(v * v), ix1(1)), st_);
+    Lijab_.ensure(nT2);
+    axpby((int)(o * o), (int)(v * v), 2.0,
+          mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
+          ovw(Lijab_.p, ix1(v * v), ix1(1)));
+    axpby((int)(o * o), (int)(v * v), -1.0,
+          mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
+          ovw(Lijab_.p, ix1(v * v), ix1(1)));
 }
 
 // ---------------------------------------------------------------------------
@@ -367,6 +385,24 @@ bool Engine::use_split(int M, int N, int K) const {
 
 void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B,
                   double beta, const OutView &C, int cache_a, int cache_b, const char *site) {
+    if (tape_) {  // record, then run the same call unrecorded
+        TapeOp op;
+        op.kind = TapeOp::Gemm;
+        op.M = M;
+        op.N = N;
+        op.K = K;
+        op.alpha = alpha;
+        op.beta = beta;
+        op.A = A;
+        op.B = B;
+        op.C = C;
+        tape_->push_back(op);
+        std::vector<TapeOp> *t = tape_;
+        tape_ = nullptr;
+        gemm(M, N, K, alpha, A, B, beta, C, cache_a, cache_b, site);
+        tape_ = t;
+        return;
+    }
     const bool prof = opt_.profile && site;
     const bool split = use_split(M, N, K);
     if (split && SplitEngine::prefer_swap(M, N)) {
@@ -457,40 +493,40 @@ void Engine::residual() {
     cudaStream_t st = st_;
     const double *t1 = t1_.p, *t2 = t2_.p, *tau = tau_.p;
 
-    k_tau(io, iv, t1, t2, tau_.p, st);
-    k_theta(io, iv, t1, t2, th1_.p, th2_.p, st);
+    tau_op(t1, t2, tau_.p);
+    theta_op(t1, t2, th1_.p, th2_.p);
     // the split forms of tau as (ij|cd) (key -1) and of the ring view of t2
     // (key -2) are shared by several contractions of this update
     if (split_ && opt_.precision != CCSD_PREC_FP64) split_->begin_update();
 
     // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d]
-    CCSD_CUDA(cudaMemcpyAsync(Foo_.p, f_oo_off_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
+    copy(Foo_.p, f_oo_off_.p, (size_t)(o2));
     gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
          mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, 0, "Foo");
     // Fvv[a][c] = f_vv' - sum_{kld} Lovov[k,c,l,d] tau[k,l,a,d]
-    CCSD_CUDA(cudaMemcpyAsync(Fvv_.p, f_vv_off_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
+    copy(Fvv_.p, f_vv_off_.p, (size_t)(v2));
     gemm(iv, iv, (int)(o * o * v), -1.0, mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)),
          mv(Lovov_.p, ix1(o * v), ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1)), 1.0,
          ovw(Fvv_.p, ix1(v), ix1(1)), 0, 2, "Fvv");
     // Fov[k][c] = f_ov + sum_ld Lovov[k,c,l,d] t1[l,d]
-    CCSD_CUDA(cudaMemcpyAsync(Fov_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
+    copy(Fov_.p, f_ov_.p, (size_t)(ov));
     gemm((int)ov, 1, (int)ov, 1.0, mv(Lovov_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
          ovw(Fov_.p, ix1(1), ix1(0)), 0, 0, "Fov");
     // Loo[k][i] = Foo + sum_c f_kc t1[i,c] + sum_lc Lovoo[l,c,k,i] t1[l,c]
-    CCSD_CUDA(cudaMemcpyAsync(Loo_.p, Foo_.p, sizeof(double) * o2, cudaMemcpyDeviceToDevice, st));
+    copy(Loo_.p, Foo_.p, (size_t)(o2));
     gemm(io, io, iv, 1.0, mv(f_ov_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
          ovw(Loo_.p, ix1(o), ix1(1)), 0, 0, "Loo_f");
     gemm((int)o2, 1, (int)ov, 1.0, mv(Lovoo_.p, ix1(1), ix1(o2)), mv(t1, ix1(0), ix1(1)), 1.0,
          ovw(Loo_.p, ix1(1), ix1(0)), 0, 0, "Loo_t1");
     // Lvv[a][c] = Fvv - sum_k t1[k,a] f_kc + sum_kd Lovvv[k,d,a,c] t1[k,d]
-    CCSD_CUDA(cudaMemcpyAsync(Lvv_.p, Fvv_.p, sizeof(double) * v2, cudaMemcpyDeviceToDevice, st));
+    copy(Lvv_.p, Fvv_.p, (size_t)(v2));
     gemm(iv, iv, io, -1.0, mv(t1, ix1(1), ix1(v)), mv(f_ov_.p, ix1(1), ix1(v)), 1.0,
          ovw(Lvv_.p, ix1(v), ix1(1)), 0, 0, "Lvv_f");
     gemm((int)v2, 1, (int)ov, 1.0, mv(Lovvv_.p, ix1(1), ix1(v2)), mv(t1, ix1(0), ix1(1)), 1.0,
          ovw(Lvv_.p, ix1(1), ix1(0)), 0, 0, "Lvv_t1");
 
     // ---- T1 numerator ----------------------------------------------------
-    CCSD_CUDA(cudaMemcpyAsync(R1_.p, f_ov_.p, sizeof(double) * ov, cudaMemcpyDeviceToDevice, st));
+    copy(R1_.p, f_ov_.p, (size_t)(ov));
     // -2 sum_kc f_kc t1[k,a] t1[i,c]: tmpo[i][k] = sum_c t1[i,c] f_kc
     gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(f_ov_.p, ix1(v), ix1(1)), 0.0,
          ovw(tmpo_.p, ix1(o), ix1(1)), 0, 0, "R1_ft1");
@@ -526,8 +562,8 @@ void Engine::residual() {
          ovw(R1_.p, ix1(v), ix1(1)), 4, 0, "R1_ovoo_tau");
 
     // ---- Woooo[k][l][i][j] ------------------------------------------------
-    axpby_view((int)o2, (int)o2, 1.0, mv(oooo_.p, ix2((uint32_t)o, o * o2, o), ix2((uint32_t)o, o2, 1)),
-               0.0, ovw(Woooo_.p, ix1(o2), ix1(1)), st);
+    axpby((int)o2, (int)o2, 1.0, mv(oooo_.p, ix2((uint32_t)o, o * o2, o), ix2((uint32_t)o, o2, 1)),
+               0.0, ovw(Woooo_.p, ix1(o2), ix1(1)));
     // + sum_c (lc|ki) t1[j,c]: M = (k,l,i), N = j, K = c
     gemm((int)(o * o2), io, iv, 1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, o, v * o2, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
@@ -542,7 +578,7 @@ void Engine::residual() {
          mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
 
     // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
-    CCSD_CUDA(cudaMemcpyAsync(Wvoov_.p, ovov_.p, sizeof(double) * ov * ov, cudaMemcpyDeviceToDevice, st));
+    copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
     // + sum_d (kc|ad) t1[i,d]: M = (k,c,a), N = i, K = d
     gemm((int)(ov * v), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
          ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0, "Wvoov_t1v");
@@ -550,8 +586,9 @@ void Engine::residual() {
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, v * o2, o2, 1), ix1(o)), mv(t1, ix1(1), ix1(v)),
          1.0, ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)), 0, 0, "Wvoov_t1o");
-    // + sum_ld th1[i,a,l,d] (ld|kc)
-    gemm((int)ov, (int)ov, (int)ov, 1.0, mv(th1_.p, ix1(ov), ix1(1)), mv(ovov_.p, ix1(ov), ix1(1)),
+    // + sum_ld th1[i,a,l,d] (ld|kc), read at ovov[l][d][k][c] (the position the closed-shell
+    // equations name, so that dE/d(pq|rs) is assigned per element like the oracle's)
+    gemm((int)ov, (int)ov, (int)ov, 1.0, mv(th1_.p, ix1(ov), ix1(1)), mv(ovov_.p, ix1(1), ix1(ov)),
          1.0, ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 7, "Wvoov_th1");
     // - 1/2 sum_ld (lc|kd) t2[i,l,a,d]
     gemm((int)ov, (int)ov, (int)ov, -0.5, mv(t2, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)),
@@ -559,8 +596,8 @@ void Engine::residual() {
          ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 8, "Wvoov_t2");
 
     // ---- Wvovo_s[i][a][k][c] = W_akci ------------------------------------
-    axpby_view((int)ov, (int)ov, 1.0, mv(oovv_.p, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)),
-               0.0, ovw(Wvovo_.p, ix1(ov), ix1(1)), st);
+    axpby((int)ov, (int)ov, 1.0, mv(oovv_.p, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)),
+               0.0, ovw(Wvovo_.p, ix1(ov), ix1(1)));
     // + sum_d (kd|ac) t1[i,d]: M = (k,a,c), N = i, K = d
     gemm((int)(ov * v), io, iv, 1.0,
          mv(ovvv_.p, ix3((uint32_t)v, (uint32_t)v, v * v2, v, 1), ix1(v2)), mv(t1, ix1(v), ix1(1)),
@@ -574,14 +611,14 @@ void Engine::residual() {
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
          ovw(Wvovo_.p, ix1(ov), ix1(1)), 0, 8, "Wvovo_th2");
     // Wa = 2 Wvoov - Wvovo
-    axpby_view((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
-    axpby_view((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)), st);
+    axpby((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)));
+    axpby((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)));
 
     // ---- R (symmetric terms) ---------------------------------------------
     // (ia|jb)
-    axpby_view((int)o2, (int)v2, 1.0,
+    axpby((int)o2, (int)v2, 1.0,
                mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
-               ovw(R_.p, ix1(v2), ix1(1)), st);
+               ovw(R_.p, ix1(v2), ix1(1)));
     // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b]
     gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
          1.0, ovw(R_.p, ix1(v2), ix1(1)), 0, 0, "hh_ladder");
@@ -600,9 +637,9 @@ void Engine::residual() {
          mv(Vk_.p, ix3((uint32_t)v, (uint32_t)o, v * o, o, 1), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
          1.0, ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)o, ov2, 1, v2), ix1(v)), 0, 0, "Rp_oovv_t1t1");
     // - sum_k tmpB[k,i,a,j] t1[k,b], tmpB = (ia|jk) + sum_c (kc|ia) t1[j,c]
-    axpby_view((int)(o * ov), io, 1.0,
+    axpby((int)(o * ov), io, 1.0,
                mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), 0.0,
-               ovw(tmpB_.p, ix1(o), ix1(1)), st);
+               ovw(tmpB_.p, ix1(o), ix1(1)));
     gemm((int)(o * ov), io, iv, 1.0,
          mv(ovov_.p, ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1), ix1(o * v)), mv(t1, ix1(v), ix1(1)),
          1.0, ovw(tmpB_.p, ix1(o), ix1(1)), 0, 0, "Rp_ovov_t1");
@@ -824,6 +861,8 @@ void Engine::solve(ccsd_result *res) {
     }
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
+    solved_ = true;
+    last_e_ = e_new;
     res->e_corr = e_new;
     res->residual_norm = last_resid_;
     res->iterations = updates;

@@ -25,7 +25,22 @@ struct DBuf {
     DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
     DBuf &operator=(DBuf &&o) noexcept;
     void alloc(size_t count);
+    void ensure(size_t count) {
+        if (!p || n != count) alloc(count);
+    }
     void zero(cudaStream_t st);
+};
+
+// One recorded operation of the forward computation (build or residual),
+// replayed backwards for the adjoint (Lambda) equations and the gradient.
+struct TapeOp {
+    enum Kind { Gemm, Axpby, Copy, Tau, Theta } kind;
+    int M = 0, N = 0, K = 0;  // Gemm: sizes; Axpby: R = M, C = N; Copy: count = M
+    double alpha = 0.0, beta = 0.0;
+    MatView A, B;  // Gemm operands; Axpby/Copy: A = source
+    OutView C;     // destination
+    const double *t1 = nullptr, *t2 = nullptr;  // Tau/Theta inputs
+    double *out1 = nullptr, *out2 = nullptr;    // Tau: out1 = tau; Theta: out1 = th1, out2 = th2
 };
 
 class Engine {
@@ -34,6 +49,8 @@ class Engine {
     ~Engine();
     void set_options(const ccsd_options &opts);
     void solve(ccsd_result *res);
+    // Lambda equations at the last solution and dE_corr/d(inputs); see abi.cpp.
+    void lambda_grad(const ccsd_problem &prob, ccsd_grad *out);
 
     int nocc() const { return o_; }
     int nvir() const { return v_; }
@@ -80,6 +97,33 @@ class Engine {
 
     // one amplitude update: residual numerators from (t1_, t2_)
     void residual();
+
+    // recordable element-wise operations (every op of build and residual goes
+    // through these or through gemm())
+    void axpby(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y);
+    void copy(double *dst, const double *src, size_t n);
+    void tau_op(const double *t1, const double *t2, double *tau);
+    void theta_op(const double *t1, const double *t2, double *th1, double *th2);
+
+    // reverse mode
+    std::vector<TapeOp> *tape_ = nullptr;  // recording target, or null
+    struct Reg {
+        DBuf *buf;
+        bool active;  // depends on the amplitudes (Lambda mode propagates into these only)
+    };
+    std::vector<Reg> regs_;
+    std::map<DBuf *, DBuf> adj_;
+    bool full_adjoint_ = false;
+    void reg(DBuf &b, bool active) { regs_.push_back(Reg{&b, active}); }
+    // adjoint pointer for a forward pointer, or null when no adjoint is kept
+    double *adj_of(const double *p, bool *active = nullptr);
+    void reverse(const std::vector<TapeOp> &tape);
+    void zero_adjoints();
+    std::vector<std::unique_ptr<DBuf>> keep_;  // inputs kept alive for a recorded build
+    DBuf *input_eri_ = nullptr, *input_df_ = nullptr, *input_c_ = nullptr;
+    DBuf qtmp_;                                // scratch of the Theta adjoint
+    bool solved_ = false;
+    double last_e_ = 0.0;
     double energy_of(const double *t1, const double *t2);  // uses tau_ as scratch
     double reduce_sum(int nparts);
     void diis_step(int update_index);

@@ -103,6 +103,24 @@ typedef struct ccsd_result {
     double flops_per_update;   /* algorithmic FLOP of one update (fixed count) */
 } ccsd_result;
 
+/* Output of ccsd_lambda_grad.  Every array is optional (NULL = not wanted)
+ * and caller-owned host memory.  Derivatives are taken with respect to each
+ * element of the input arrays as given to ccsd_create, each element treated
+ * as independent (an element the engine never reads has derivative 0). */
+typedef struct ccsd_grad {
+    double *d_fock;      /* n x n: dE_corr / d fock[p][q]                         */
+    double *d_eri;       /* MO_DENSE: n^4, AO_DENSE: nao^4: dE_corr / d eri[...]  */
+    double *d_df;        /* DF: naux*n*n: dE_corr / d B[Q][p][q]                  */
+    double *d_mo_coeff;  /* AO_DENSE: nao*n: dE_corr / d C[mu][p]                 */
+    double *lambda1;     /* o*v: Lambda amplitudes l1[i][a]                       */
+    double *lambda2;     /* o^2 v^2: l2[i][j][a][b]                               */
+    double tol;          /* in: stop when ||l_new - l||_2 < tol (0: 1e-10)        */
+    int32_t max_iter;    /* in: cap on Lambda updates (0: 500)                    */
+    int32_t iterations;  /* out: Lambda updates performed                         */
+    double residual_norm;/* out: ||l_new - l||_2 of the last update               */
+    double e_corr;       /* out: E_corr of the solution the gradient belongs to   */
+} ccsd_grad;
+
 typedef struct ccsd_handle ccsd_handle;
 
 /* Defaults: energy_tol 1e-10, max_iter 999, FP64, no DIIS (reference rules). */
@@ -116,6 +134,15 @@ int ccsd_create(const ccsd_problem *problem, const ccsd_options *opts, ccsd_hand
 /* Run the amplitude iteration from the MP2 guess (T1 = 0) and fill `res`.
  * Replaces ccsd_memory_optimized.cpp:473-566 (MP2 guess, loop, E_new). */
 int ccsd_solve(ccsd_handle *h, ccsd_result *res);
+
+/* Backward pass of a converged ccsd_solve: solves the CCSD Lambda (adjoint)
+ * equations  Lambda = (dE/dT + J^T Lambda) / D  with the same contraction
+ * kernels, transposed, and returns dE_corr/d(fock) and dE_corr/d(integrals):
+ * the one- and two-particle response densities of the correlation energy in
+ * the input representation.  `problem` must be the problem the handle was
+ * created with (its arrays are read again).  No counterpart in the reference,
+ * which has no Lambda equations or gradients. */
+int ccsd_lambda_grad(ccsd_handle *h, const ccsd_problem *problem, ccsd_grad *grad);
 
 /* Change options (precision, tolerances, DIIS, stream) between solves. */
 int ccsd_set_options(ccsd_handle *h, const ccsd_options *opts);
