@@ -24,7 +24,7 @@ from ._abi import (CCSD_INTS_AO_DENSE, CCSD_INTS_DF, CCSD_INTS_MO_DENSE, CCSD_PR
 PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD_PREC_SPLIT3,
               "split4": CCSD_PREC_SPLIT4}
 
-__all__ = ["Solver", "solve", "make_synthetic", "flops_per_update", "CCSD_Memory_optimized",
+__all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "CCSD_Memory_optimized",
            "CCSDError", "PRECISIONS"]
 
 
@@ -67,32 +67,39 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     return o
 
 
+def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None):
+    """ccsd_problem over host arrays; returns (problem, arrays to keep alive)."""
+    fock = _f64(fock)
+    n = fock.shape[0]
+    p = _abi.Problem()
+    p.nocc, p.nvir = nocc, n - nocc
+    keep = [fock]
+    p.fock = _ptr(fock)
+    if df is not None:
+        df = _f64(df)
+        p.integral_kind, p.naux, p.df = CCSD_INTS_DF, df.shape[0], _ptr(df)
+        keep.append(df)
+    elif ao_eri is not None:
+        ao_eri, mo_coeff = _f64(ao_eri), _f64(mo_coeff)
+        p.integral_kind, p.nao = CCSD_INTS_AO_DENSE, ao_eri.shape[0]
+        p.eri, p.mo_coeff = _ptr(ao_eri), _ptr(mo_coeff)
+        keep += [ao_eri, mo_coeff]
+    elif eri is not None:
+        eri = _f64(eri)
+        p.integral_kind, p.eri = CCSD_INTS_MO_DENSE, _ptr(eri)
+        keep.append(eri)
+    else:
+        raise ValueError("one of eri / df / ao_eri is required")
+    return p, keep
+
+
 class Solver:
     """One device-resident system (integrals uploaded/transformed once)."""
 
     def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, **opts):
-        fock = _f64(fock)
-        n = fock.shape[0]
+        p, self._keep = _problem(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff)
+        n = p.nocc + p.nvir
         self.nocc, self.nvir = nocc, n - nocc
-        p = _abi.Problem()
-        p.nocc, p.nvir = nocc, n - nocc
-        self._keep = [fock]
-        p.fock = _ptr(fock)
-        if df is not None:
-            df = _f64(df)
-            p.integral_kind, p.naux, p.df = CCSD_INTS_DF, df.shape[0], _ptr(df)
-            self._keep.append(df)
-        elif ao_eri is not None:
-            ao_eri, mo_coeff = _f64(ao_eri), _f64(mo_coeff)
-            p.integral_kind, p.nao = CCSD_INTS_AO_DENSE, ao_eri.shape[0]
-            p.eri, p.mo_coeff = _ptr(ao_eri), _ptr(mo_coeff)
-            self._keep += [ao_eri, mo_coeff]
-        elif eri is not None:
-            eri = _f64(eri)
-            p.integral_kind, p.eri = CCSD_INTS_MO_DENSE, _ptr(eri)
-            self._keep.append(eri)
-        else:
-            raise ValueError("one of eri / df / ao_eri is required")
         self._opts = _options(**opts)
         h = C.c_void_p()
         _abi.check(_abi.lib().ccsd_create(C.byref(p), C.byref(self._opts), C.byref(h)))
@@ -173,6 +180,88 @@ class Solver:
 def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, amplitudes=True, **opts):
     with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, **opts) as s:
         return s.solve(amplitudes=amplitudes)
+
+
+class Batch:
+    """Many systems of uneven nocc/nvir iterated together (ccsd_batch_*).
+
+    ``systems`` is a sequence of dicts with the keyword arguments of
+    :class:`Solver` (``fock``, ``nocc`` and one of ``eri`` / ``df`` /
+    ``ao_eri`` + ``mo_coeff``).  Every operation of the amplitude update runs
+    as one grouped launch over the batch, replayed from a CUDA graph."""
+
+    def __init__(self, systems, **opts):
+        probs, self._keep = [], []
+        for sysd in systems:
+            p, keep = _problem(**sysd)
+            probs.append(p)
+            self._keep += keep
+        self._probs = probs
+        self._arr = (C.POINTER(_abi.Problem) * len(probs))(*[C.pointer(p) for p in probs])
+        self._opts = _options(**opts)
+        h = C.c_void_p()
+        _abi.check(_abi.lib().ccsd_batch_create(self._arr, len(probs), C.byref(self._opts), C.byref(h)))
+        self._h = h
+
+    def __len__(self):
+        return len(self._probs)
+
+    def solve(self, amplitudes: bool = True, history: int = 1001) -> list:
+        res = (_abi.Result * len(self._probs))()
+        bufs = []
+        for r, p in zip(res, self._probs):
+            o, v = p.nocc, p.nvir
+            t1 = np.empty((o, v)) if amplitudes else None
+            t2 = np.empty((o, o, v, v)) if amplitudes else None
+            eh, ms = np.zeros(history), np.zeros(history)
+            r.t1, r.t2 = _ptr(t1), _ptr(t2)
+            r.energy_history, r.update_ms, r.history_capacity = _ptr(eh), _ptr(ms), history
+            bufs.append((t1, t2, eh, ms))
+        rc = _abi.lib().ccsd_batch_solve(self._h, res)
+        out = []
+        for r, (t1, t2, eh, ms) in zip(res, bufs):
+            out.append(dict(e_corr=r.e_corr, iterations=r.iterations, converged=bool(r.converged),
+                            residual_norm=r.residual_norm, energies=eh[:r.history_len].copy(),
+                            update_ms=ms[:r.iterations].copy(), flops_per_update=r.flops_per_update,
+                            t1=t1, t2=t2))
+        if rc != 0:
+            err = CCSDError(rc, _abi.last_error())
+            err.results = out
+            raise err
+        return out
+
+    def report(self) -> dict:
+        """Grouped operations, tile plans, autotuning and launches per update."""
+        import json
+        n = _abi.lib().ccsd_batch_report(self._h, None, 0)
+        if n < 0:
+            _abi.check(n)
+        buf = C.create_string_buffer(n + 1)
+        _abi.lib().ccsd_batch_report(self._h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.lib().ccsd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def solve_batched(systems, amplitudes=True, **opts) -> list:
+    """Solve many systems in one batch; one result dict per system."""
+    with Batch(systems, **opts) as b:
+        return b.solve(amplitudes=amplitudes)
 
 
 class CCSD_Memory_optimized:

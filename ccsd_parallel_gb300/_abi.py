@@ -82,6 +82,13 @@ SIGNATURES = {
     "ccsd_gemm": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                             C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,
                             C.c_void_p]),
+    "ccsd_batch_create": (C.c_int, [C.POINTER(C.POINTER(Problem)), C.c_int32, C.POINTER(Options),
+                                    C.POINTER(C.c_void_p)]),
+    "ccsd_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(Result)]),
+    "ccsd_batch_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "ccsd_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ccsd_solve_batched": (C.c_int, [C.POINTER(C.POINTER(Problem)), C.c_int32, C.POINTER(Options),
+                                     C.POINTER(Result)]),
     "ccsd_gemm_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                                     C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,
                                     C.c_void_p]),

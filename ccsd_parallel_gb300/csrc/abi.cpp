@@ -5,10 +5,15 @@
 #include <new>
 #include <string>
 
+#include "batched.h"
 #include "engine.h"
 
 struct ccsd_handle {
     ccsd::Engine *engine = nullptr;
+};
+
+struct ccsd_batch {
+    ccsd::Batch *batch = nullptr;
 };
 
 namespace {
@@ -98,6 +103,64 @@ int ccsd_destroy(ccsd_handle *h) {
     if (!h) return CCSD_OK;
     int rc = guarded([&] { delete h->engine; });
     delete h;
+    return rc;
+}
+
+int ccsd_batch_create(const ccsd_problem *const *problems, int32_t n, const ccsd_options *opts, ccsd_batch **out) {
+    if (!problems || !out || n <= 0) return fail(CCSD_ERR_INVALID_ARG, "problems/out is NULL or n <= 0");
+    *out = nullptr;
+    ccsd_options o;
+    if (opts)
+        o = *opts;
+    else
+        ccsd_default_options(&o);
+    return guarded([&] {
+        ccsd::Batch *b = new ccsd::Batch(problems, n, o);
+        ccsd_batch *h = new (std::nothrow) ccsd_batch;
+        if (!h) {
+            delete b;
+            throw std::bad_alloc();
+        }
+        h->batch = b;
+        *out = h;
+    });
+}
+
+int ccsd_batch_solve(ccsd_batch *b, ccsd_result *results) {
+    if (!b || !b->batch || !results) return fail(CCSD_ERR_INVALID_ARG, "batch/results is NULL");
+    return guarded([&] { b->batch->solve(results); });
+}
+
+int ccsd_batch_report(ccsd_batch *b, char *buf, size_t len) {
+    if (!b || !b->batch) return fail(CCSD_ERR_INVALID_ARG, "batch is NULL");
+    std::string s;
+    int rc = guarded([&] { s = b->batch->report(); });
+    if (rc != CCSD_OK) return rc;
+    if (buf && len > 0) {
+        size_t c = std::min(len - 1, s.size());
+        std::memcpy(buf, s.data(), c);
+        buf[c] = '\0';
+    }
+    return (int)s.size();
+}
+
+int ccsd_batch_destroy(ccsd_batch *b) {
+    if (!b) return CCSD_OK;
+    int rc = guarded([&] { delete b->batch; });
+    delete b;
+    return rc;
+}
+
+int ccsd_solve_batched(const ccsd_problem *const *problems, int32_t n, const ccsd_options *opts,
+                       ccsd_result *results) {
+    if (!results) return fail(CCSD_ERR_INVALID_ARG, "results is NULL");
+    ccsd_batch *b = nullptr;
+    int rc = ccsd_batch_create(problems, n, opts, &b);
+    if (rc != CCSD_OK) return rc;
+    rc = ccsd_batch_solve(b, results);
+    std::string keep = g_last_error;
+    ccsd_batch_destroy(b);
+    g_last_error = keep;
     return rc;
 }
 

@@ -49,6 +49,7 @@ void Engine::axpby(int R, int C, double alpha, const MatView &X, double beta, co
         op.A = X;
         op.C = Y;
         tape_->push_back(op);
+        if (record_only_) return;
     }
     axpby_view(R, C, alpha, X, beta, Y, st_);
 }
@@ -61,6 +62,7 @@ void Engine::copy(double *dst, const double *src, size_t n) {
         op.A = mv(src, ix1(0), ix1(1));
         op.C = ovw(dst, ix1(0), ix1(1));
         tape_->push_back(op);
+        if (record_only_) return;
     }
     CCSD_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st_));
 }
@@ -73,6 +75,7 @@ void Engine::tau_op(const double *t1, const double *t2, double *tau) {
         op.t2 = t2;
         op.out1 = tau;
         tape_->push_back(op);
+        if (record_only_) return;
     }
     k_tau(o_, v_, t1, t2, tau, st_);
 }
@@ -86,6 +89,7 @@ void Engine::theta_op(const double *t1, const double *t2, double *th1, double *t
         op.out1 = th1;
         op.out2 = th2;
         tape_->push_back(op);
+        if (record_only_) return;
     }
     k_theta(o_, v_, t1, t2, th1, th2, st_);
 }

@@ -396,7 +396,9 @@ void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const Mat
         op.A = A;
         op.B = B;
         op.C = C;
+        op.site = site;
         tape_->push_back(op);
+        if (record_only_) return;
         std::vector<TapeOp> *t = tape_;
         tape_ = nullptr;
         gemm(M, N, K, alpha, A, B, beta, C, cache_a, cache_b, site);

@@ -41,9 +41,14 @@ struct TapeOp {
     OutView C;     // destination
     const double *t1 = nullptr, *t2 = nullptr;  // Tau/Theta inputs
     double *out1 = nullptr, *out2 = nullptr;    // Tau: out1 = tau; Theta: out1 = th1, out2 = th2
+    const char *site = nullptr;                 // Gemm: contraction site name
 };
 
+class Batch;
+
 class Engine {
+    friend class Batch;  // the batched solve groups the recorded residuals of many engines
+
   public:
     Engine(const ccsd_problem &prob, const ccsd_options &opts);
     ~Engine();
@@ -107,6 +112,7 @@ class Engine {
 
     // reverse mode
     std::vector<TapeOp> *tape_ = nullptr;  // recording target, or null
+    bool record_only_ = false;             // record into tape_ without running
     struct Reg {
         DBuf *buf;
         bool active;  // depends on the amplitudes (Lambda mode propagates into these only)

@@ -149,6 +149,30 @@ int ccsd_set_options(ccsd_handle *h, const ccsd_options *opts);
 
 int ccsd_destroy(ccsd_handle *h);
 
+/* ---- batched solve: many systems of uneven nocc/nvir iterated together ----
+ * No counterpart in the reference, which solves one molecule per process.
+ * Every operation of the amplitude update runs as one grouped launch over all
+ * systems of the batch (contractions on a persistent grouped FP64 kernel
+ * whose tile shape and split-K are chosen per operation by timing candidates
+ * on the batch's own shapes), and the update is replayed from a captured CUDA
+ * graph.  Each system follows exactly the single-system rules of ccsd_solve
+ * (MP2 start, its own |dE| stop, cap, DIIS); a stopped system is masked off
+ * on the device and keeps its last iterate.  precision must be FP64.
+ * results[i] is filled like ccsd_solve's result (caller-provided t1/t2/
+ * history arrays per system).  When a system diverges, every result is still
+ * filled and the call returns CCSD_ERR_DIVERGED naming the first such system. */
+typedef struct ccsd_batch ccsd_batch;
+int ccsd_batch_create(const ccsd_problem *const *problems, int32_t n, const ccsd_options *opts,
+                      ccsd_batch **out);
+int ccsd_batch_solve(ccsd_batch *b, ccsd_result *results);
+/* JSON: grouped operations with their tile plans, autotuning times and the
+ * kernel launches of one update.  Returns the report length. */
+int ccsd_batch_report(ccsd_batch *b, char *buf, size_t len);
+int ccsd_batch_destroy(ccsd_batch *b);
+/* create + solve + destroy. */
+int ccsd_solve_batched(const ccsd_problem *const *problems, int32_t n, const ccsd_options *opts,
+                       ccsd_result *results);
+
 /* JSON report of the last solve when options.profile was set: per
  * contraction site the calls, device ms of the contraction kernel, device ms
  * of the operand splitting (split modes), algorithmic FLOP and the path that

@@ -38,6 +38,36 @@ def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
 
 
+def test_struct_layouts_match_compiled_header(tmp_path):
+    """Size and every field offset of the ctypes mirrors equal what a C
+    compiler makes of include/ccsd_gb300.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"ccsd_problem": _abi.Problem, "ccsd_options": _abi.Options, "ccsd_result": _abi.Result,
+               "ccsd_grad": _abi.Grad}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ccsd_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, val = line.split()
+        got[(s, f)] = int(val)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_default_options_follow_reference_rules():
     o = _abi.Options()
     assert _abi.lib().ccsd_default_options(C.byref(o)) == 0
