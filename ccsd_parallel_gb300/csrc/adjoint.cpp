@@ -94,6 +94,45 @@ void Engine::theta_op(const double *t1, const double *t2, double *th1, double *t
     k_theta(o_, v_, t1, t2, th1, th2, st_);
 }
 
+void Engine::tau_sym_op(const double *tau, double *tp, double *tm) {
+    if (tape_) {
+        TapeOp op;
+        op.kind = TapeOp::TauSym;
+        op.t1 = tau;
+        op.out1 = tp;
+        op.out2 = tm;
+        tape_->push_back(op);
+        if (record_only_) return;
+    }
+    k_tau_sym(o_, v_, tau, tp, tm, st_);
+}
+
+void Engine::unpack_op(const double *sp, const double *sm, double *R) {
+    if (tape_) {
+        TapeOp op;
+        op.kind = TapeOp::Unpack;
+        op.t1 = sp;
+        op.t2 = sm;
+        op.out1 = R;
+        tape_->push_back(op);
+        if (record_only_) return;
+    }
+    k_ladder_unpack(o_, v_, sp, sm, R, st_);
+}
+
+void Engine::w_sym_op(const double *W, double *wp, double *wm) {
+    if (tape_) {
+        TapeOp op;
+        op.kind = TapeOp::WSym;
+        op.t1 = W;
+        op.out1 = wp;
+        op.out2 = wm;
+        tape_->push_back(op);
+        if (record_only_) return;
+    }
+    k_w_sym(v_, W, wp, wm, st_);
+}
+
 // ---- adjoint storage ------------------------------------------------------------
 double *Engine::adj_of(const double *p, bool *active) {
     if (!p) return nullptr;
@@ -121,6 +160,8 @@ void Engine::zero_adjoints() {
 void Engine::reverse(const std::vector<TapeOp> &tape) {
     const int64_t o = o_, v = v_, ov = o * v, v2 = v * v, ov2 = o * v2;
     const size_t nT2 = (size_t)(o * o * v * v);
+    const size_t pair_o = (size_t)(o * (o + 1) / 2), spair_o = (size_t)(o * (o - 1) / 2);
+    const size_t pair_v = (size_t)(v * (v + 1) / 2), spair_v = (size_t)(v * (v - 1) / 2);
     auto scale = [&](int R, int C, double beta, const OutView &Y) {  // Ybar_old = beta Ybar
         if (beta == 1.0) return;
         axpby_view(R, C, 0.0, mv(Y.p, Y.row, Y.col), beta, Y, st_);
@@ -199,6 +240,29 @@ void Engine::reverse(const std::vector<TapeOp> &tape) {
                 if (h2) CCSD_CUDA(cudaMemsetAsync(h2, 0, nT2 * sizeof(double), st_));
                 break;
             }
+            case TapeOp::TauSym: {  // (tau+, tau-) = P(tau): taubar += P^T (tau+bar, tau-bar)
+                double *pb = adj_of(op.out1), *mb = adj_of(op.out2);
+                if (!pb) break;
+                if (double *tb = adj_of(op.t1)) k_tau_sym_adj((int)o, (int)v, pb, mb, tb, st_);
+                CCSD_CUDA(cudaMemsetAsync(pb, 0, sizeof(double) * pair_o * pair_v, st_));
+                if (mb) CCSD_CUDA(cudaMemsetAsync(mb, 0, sizeof(double) * spair_o * spair_v, st_));
+                break;
+            }
+            case TapeOp::Unpack: {  // R += U(S+, S-): (S+bar, S-bar) += U^T Rbar; Rbar unchanged
+                double *Rb = adj_of(op.out1);
+                if (!Rb) break;
+                double *pb = adj_of(op.t1), *mb = adj_of(op.t2);
+                if (pb) k_ladder_unpack_adj((int)o, (int)v, Rb, pb, mb, st_);
+                break;
+            }
+            case TapeOp::WSym: {  // (W+, W-) = Q(W): Wbar += Q^T (W+bar, W-bar)
+                double *pb = adj_of(op.out1), *mb = adj_of(op.out2);
+                if (!pb) break;
+                if (double *Wb = adj_of(op.t1)) k_w_sym_adj((int)v, pb, mb, Wb, st_);
+                CCSD_CUDA(cudaMemsetAsync(pb, 0, sizeof(double) * pair_v * pair_v, st_));
+                if (mb) CCSD_CUDA(cudaMemsetAsync(mb, 0, sizeof(double) * spair_v * spair_v, st_));
+                break;
+            }
         }
     }
 }
@@ -220,15 +284,16 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
             e->regs_.clear();
             e->keep_.clear();
             e->build_split_.reset();
+            e->wv_.alloc(0);  // (ac|bd) was rebuilt for the recorded build only
         }
     } cleanup{this};
 
     regs_.clear();
     adj_.clear();
     for (DBuf *b : {&t1_, &t2_, &tau_, &th1_, &th2_, &R1_, &R_, &Rp_, &Foo_, &Fvv_, &Fov_, &Loo_, &Lvv_, &tmpo_,
-                    &tmpo2_, &Woooo_, &Wvoov_, &Wvovo_, &Wa_, &Z_, &tmpB_, &Vk_})
+                    &tmpo2_, &Woooo_, &Wvoov_, &Wvovo_, &Wa_, &Z_, &tmpB_, &Vk_, &taup_, &taum_, &Sp_, &Sm_})
         reg(*b, true);
-    for (DBuf *b : {&ovov_, &oovv_, &ovoo_, &oooo_, &ovvv_, &wv_, &Lovov_, &Lovoo_, &Lovvv_, &LT1_, &Lijab_,
+    for (DBuf *b : {&ovov_, &oovv_, &ovoo_, &oooo_, &ovvv_, &wv_, &Lovov_, &Lovoo_, &Lovvv_, &LT1_, &Lijab_, &Wp_, &Wm_,
                     &f_oo_off_, &f_vv_off_, &f_ov_})
         reg(*b, false);
 

@@ -312,7 +312,9 @@ void Batch::build_ops() {
                 break;
             }
             case TapeOp::Tau:
-            case TapeOp::Theta: {
+            case TapeOp::Theta:
+            case TapeOp::TauSym:
+            case TapeOp::Unpack: {
                 std::vector<GAmp> parts(n);
                 for (int s = 0; s < n; ++s) {
                     const TapeOp &t = tapes_[s][k];
@@ -324,11 +326,16 @@ void Batch::build_ops() {
                     g.o = eng_[s]->o_;
                     g.v = eng_[s]->v_;
                     g.sys = s;
-                    op.max_elems = std::max(op.max_elems, (size_t)g.o * g.o * g.v * g.v);
+                    const size_t elems = op.kind == TapeOp::TauSym
+                                             ? (size_t)g.o * (g.o + 1) / 2 * ((size_t)g.v * (g.v + 1) / 2)
+                                             : (size_t)g.o * g.o * g.v * g.v;
+                    op.max_elems = std::max(op.max_elems, elems);
                 }
                 op.off = append(blob_, parts);
                 break;
             }
+            case TapeOp::WSym:
+                throw Error(CCSD_ERR_INVALID_ARG, "batched residual tape holds an integral-build operation");
         }
     }
     CCSD_CUDA(cudaEventRecord(b, st_));
@@ -420,6 +427,14 @@ void Batch::launch_op(const GOp &op) {
             break;
         case TapeOp::Theta:
             launch_grouped_theta(reinterpret_cast<const GAmp *>(desc_ + op.off), n, op.max_elems, active_, st_);
+            break;
+        case TapeOp::TauSym:
+            launch_grouped_tau_sym(reinterpret_cast<const GAmp *>(desc_ + op.off), n, op.max_elems, active_, st_);
+            break;
+        case TapeOp::Unpack:
+            launch_grouped_unpack(reinterpret_cast<const GAmp *>(desc_ + op.off), n, op.max_elems, active_, st_);
+            break;
+        case TapeOp::WSym:
             break;
     }
 }
@@ -574,11 +589,14 @@ std::string Batch::report() const {
     bool first = true;
     for (size_t k = 0; k < ops_.size(); ++k) {
         const GOp &op = ops_[k];
-        const char *kind = op.kind == TapeOp::Gemm    ? "contraction"
-                           : op.kind == TapeOp::Axpby ? "axpby"
-                           : op.kind == TapeOp::Copy  ? "copy"
-                           : op.kind == TapeOp::Tau   ? "tau"
-                                                      : "theta";
+        const char *kind = op.kind == TapeOp::Gemm     ? "contraction"
+                           : op.kind == TapeOp::Axpby  ? "axpby"
+                           : op.kind == TapeOp::Copy   ? "copy"
+                           : op.kind == TapeOp::Tau    ? "tau"
+                           : op.kind == TapeOp::Theta  ? "theta"
+                           : op.kind == TapeOp::TauSym ? "tau_pairs"
+                           : op.kind == TapeOp::Unpack ? "ladder_unpack"
+                                                       : "w_pairs";
         if (op.kind == TapeOp::Gemm)
             std::snprintf(buf, sizeof buf,
                           "%s{\"op\": %zu, \"kind\": \"%s\", \"site\": \"%s\", \"path\": \"%s\", \"tile\": \"%s\", "

@@ -105,6 +105,17 @@ void k_dot(size_t n, const double *x, const double *y, double *partials, int nbl
            cudaStream_t st);
 // sum of `n` partials into out[0] (single block, deterministic order).
 void k_sum(int n, const double *partials, double *out, cudaStream_t st);
+// Symmetric/antisymmetric particle-particle ladder (ladder_sym.cu); pair
+// indices tri(p>=q) = p(p+1)/2 + q and stri(p>q) = p(p-1)/2 + q.
+// tau+[tri(i,j)][tri(c,d)], tau-[stri(i,j)][stri(c,d)] from tau[i][j][c][d]
+void k_tau_sym(int o, int v, const double *tau, double *tp, double *tm, cudaStream_t st);
+void k_tau_sym_adj(int o, int v, const double *tpb, const double *tmb, double *taub, cudaStream_t st);
+// R[i][j][a][b] += S+[tri(i,j)][tri(a,b)] + sgn(i-j) sgn(a-b) S-[stri(i,j)][stri(a,b)]
+void k_ladder_unpack(int o, int v, const double *sp, const double *sm, double *R, cudaStream_t st);
+void k_ladder_unpack_adj(int o, int v, const double *Rb, double *spb, double *smb, cudaStream_t st);
+// W+[tri(a,b)][tri(c,d)], W-[stri(a,b)][stri(c,d)] from W[a][b][c][d] = (ac|bd)
+void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st);
+void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaStream_t st);
 void k_fill(size_t n, double val, double *p, cudaStream_t st);
 void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st);
 int reduce_blocks();

@@ -107,9 +107,15 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     build_derived();
     CCSD_CUDA(cudaStreamSynchronize(st_));
     build_split_.reset();
+    wv_.alloc(0);  // the ladder reads W+ and W- (a gradient rebuilds (ac|bd) from the inputs)
 
     const size_t o = o_, v = v_;
     const size_t nT2 = o * o * v * v, nT1 = o * v;
+    const size_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
+    taup_.alloc(To * Tv);
+    taum_.alloc(Tmo * Tmv);
+    Sp_.alloc(To * Tv);
+    Sm_.alloc(Tmo * Tmv);
     t1_.alloc(nT1);
     t2_.alloc(nT2);
     t1n_.alloc(nT1);
@@ -375,6 +381,11 @@ void Engine::build_derived() {
     axpby((int)(o * o), (int)(v * v), -1.0,
           mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
           ovw(Lijab_.p, ix1(v * v), ix1(1)));
+    // W+ [tri(a,b)][tri(c,d)] and W- [stri(a,b)][stri(c,d)] of the pair-form ladder
+    const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
+    Wp_.ensure(Tv * Tv);
+    Wm_.ensure(Tmv * Tmv);
+    w_sym_op(wv_.p, Wp_.p, Wm_.p);
 }
 
 // ---------------------------------------------------------------------------
@@ -624,9 +635,18 @@ void Engine::residual() {
     // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b]
     gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
          1.0, ovw(R_.p, ix1(v2), ix1(1)), 0, 0, "hh_ladder");
-    // + sum_cd (ac|bd) tau[i,j,c,d]: the v^4 particle-particle ladder, M = (a,b), N = (i,j)
-    gemm((int)v2, (int)o2, (int)v2, 1.0, mv(wv_.p, ix1(v2), ix1(1)), mv(tau, ix1(v2), ix1(1)), 1.0,
-         ovw(R_.p, ix1(1), ix1(v2)), 10, -1, "pp_ladder");
+    // + sum_cd (ac|bd) tau[i,j,c,d]: the v^4 particle-particle ladder in pair form
+    // (ladder_sym.cu): S+ = W+ tau+^T over (a>=b, i>=j, c>=d), S- = W- tau-^T over strict
+    // pairs, a quarter of the plain 2 o^2 v^4; R += unpack(S+, S-).  S is stored [ij][ab].
+    {
+        const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
+        tau_sym_op(tau, taup_.p, taum_.p);
+        gemm((int)Tv, (int)To, (int)Tv, 1.0, mv(Wp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
+             ovw(Sp_.p, ix1(1), ix1(Tv)), 10, -3, "pp_ladder_sym");
+        gemm((int)Tmv, (int)Tmo, (int)Tmv, 1.0, mv(Wm_.p, ix1(Tmv), ix1(1)), mv(taum_.p, ix1(Tmv), ix1(1)), 0.0,
+             ovw(Sm_.p, ix1(1), ix1(Tmv)), 11, -4, "pp_ladder_anti");
+        unpack_op(Sp_.p, Sm_.p, R_.p);
+    }
 
     // ---- Rp (terms under P(ij,ab)) -----------------------------------------
     // + sum_c (ia|bc) t1[j,c]: M = (i,a,b), N = j, K = c

@@ -34,7 +34,9 @@ struct DBuf {
 // One recorded operation of the forward computation (build or residual),
 // replayed backwards for the adjoint (Lambda) equations and the gradient.
 struct TapeOp {
-    enum Kind { Gemm, Axpby, Copy, Tau, Theta } kind;
+    // TauSym: (t1 = tau) -> out1 = tau+, out2 = tau-;  Unpack: (t1 = S+, t2 = S-) -> out1 = R (+=);
+    // WSym: (t1 = W) -> out1 = W+, out2 = W-   (ladder_sym.cu)
+    enum Kind { Gemm, Axpby, Copy, Tau, Theta, TauSym, Unpack, WSym } kind;
     int M = 0, N = 0, K = 0;  // Gemm: sizes; Axpby: R = M, C = N; Copy: count = M
     double alpha = 0.0, beta = 0.0;
     MatView A, B;  // Gemm operands; Axpby/Copy: A = source
@@ -109,6 +111,9 @@ class Engine {
     void copy(double *dst, const double *src, size_t n);
     void tau_op(const double *t1, const double *t2, double *tau);
     void theta_op(const double *t1, const double *t2, double *th1, double *th2);
+    void tau_sym_op(const double *tau, double *tp, double *tm);
+    void unpack_op(const double *sp, const double *sm, double *R);
+    void w_sym_op(const double *W, double *wp, double *wm);
 
     // reverse mode
     std::vector<TapeOp> *tape_ = nullptr;  // recording target, or null
@@ -144,8 +149,10 @@ class Engine {
     // integral blocks (chemist): ovov[i][a][j][b], oovv[i][j][a][b], ovoo[i][a][j][k],
     // oooo[i][j][k][l], ovvv[i][a][b][c], Wv[a][b][c][d] = (ac|bd)
     DBuf ovov_, oovv_, ovoo_, oooo_, ovvv_, wv_;
-    // derived: L-combinations
-    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_;
+    // derived: L-combinations; W+ [tri(a,b)][tri(c,d)] and W- [stri][stri] of the ladder
+    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_, Wp_, Wm_;
+    // ladder pair forms per update: tau+-, S+- (S stored [ij pair][ab pair])
+    DBuf taup_, taum_, Sp_, Sm_;
     // amplitudes and intermediates
     DBuf t1_, t2_, t1n_, t2n_, tau_, th1_, th2_;
     DBuf R1_, R_, Rp_;

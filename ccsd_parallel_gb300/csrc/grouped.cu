@@ -9,6 +9,7 @@
 #include <algorithm>
 
 #include "grouped.h"
+#include "ladder_sym.cuh"
 
 namespace ccsd {
 
@@ -238,6 +239,24 @@ __global__ void gtheta_kernel(const GAmp *__restrict__ parts, const int *__restr
     }
 }
 
+__global__ void gtau_sym_kernel(const GAmp *__restrict__ parts, const int *__restrict__ active) {
+    const GAmp &g = parts[blockIdx.y];
+    if (!active[g.sys]) return;
+    const int64_t total = (int64_t)g.o * (g.o + 1) / 2 * ((int64_t)g.v * (g.v + 1) / 2);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        pair::tau_sym_elem(g.o, g.v, g.t1, g.out1, g.out2, idx);
+}
+
+__global__ void gunpack_kernel(const GAmp *__restrict__ parts, const int *__restrict__ active) {
+    const GAmp &g = parts[blockIdx.y];
+    if (!active[g.sys]) return;
+    const int64_t total = (int64_t)g.o * g.o * g.v * g.v;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        pair::unpack_elem(g.o, g.v, g.t1, g.t2, g.out1, idx);
+}
+
 __device__ double gblock_sum(double x) {
     __shared__ double sh[32];
     for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
@@ -456,6 +475,18 @@ void launch_grouped_tau(const GAmp *d, int nparts, size_t max_elems, const int *
 void launch_grouped_theta(const GAmp *d, int nparts, size_t max_elems, const int *active, cudaStream_t st) {
     if (nparts <= 0) return;
     gtheta_kernel<<<dim3(grid_x(max_elems), nparts), kThreads, 0, st>>>(d, active);
+    CCSD_LAUNCH_CHECK();
+}
+
+void launch_grouped_tau_sym(const GAmp *d, int nparts, size_t max_elems, const int *active, cudaStream_t st) {
+    if (nparts <= 0) return;
+    gtau_sym_kernel<<<dim3(grid_x(max_elems), nparts), kThreads, 0, st>>>(d, active);
+    CCSD_LAUNCH_CHECK();
+}
+
+void launch_grouped_unpack(const GAmp *d, int nparts, size_t max_elems, const int *active, cudaStream_t st) {
+    if (nparts <= 0) return;
+    gunpack_kernel<<<dim3(grid_x(max_elems), nparts), kThreads, 0, st>>>(d, active);
     CCSD_LAUNCH_CHECK();
 }
 

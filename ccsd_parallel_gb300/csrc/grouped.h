@@ -80,6 +80,11 @@ void launch_grouped_axpby(const GAxpby *d_parts, int nparts, size_t max_elems, c
 void launch_grouped_tau(const GAmp *d_parts, int nparts, size_t max_elems, const int *active, cudaStream_t st);
 void launch_grouped_theta(const GAmp *d_parts, int nparts, size_t max_elems, const int *active,
                           cudaStream_t st);
+// pair-form ladder: tau (t1) -> tau+ (out1), tau- (out2); R (out1) += unpack(S+ (t1), S- (t2))
+void launch_grouped_tau_sym(const GAmp *d_parts, int nparts, size_t max_elems, const int *active,
+                            cudaStream_t st);
+void launch_grouped_unpack(const GAmp *d_parts, int nparts, size_t max_elems, const int *active,
+                           cudaStream_t st);
 // partials: nparts x grouped_partials_per_part(); part p's |dT|^2 pieces at p * per.
 int grouped_partials_per_part();
 void launch_grouped_update(const GUpdate *d_parts, int nparts, const int *active, double *partials,

@@ -13,6 +13,16 @@ hand-written adjoint tape:
 with theta = (fock[n][n], eri[n][n][n][n]) as given, every element treated as
 independent (the closed-shell equations read each block from fixed positions
 of the dense tensor, exactly as the engine does).
+
+Per-element derivatives depend on which of several equal-valued symmetric
+copies a term reads.  The engine's particle-particle ladder works on
+(ij,ab)-pairs and reads symmetrised inputs: the ladder of tau and
+W[a][b][c][d] = (ac|bd) is sum_cd W_s[ab,cd] (P tau)[ij,cd] with
+W_s = (W[abcd] + W[badc]) / 2 and (P tau)[ijcd] = (tau[ijcd] + tau[jidc]) / 2.
+Both equal W and tau for symmetric integrals and amplitudes (energies and
+amplitudes are unchanged); this restatement reads them the same way, so its
+Lambda and per-element gradients are the engine's.  Sums of the gradient over
+the 8 permutations of an integral do not depend on this choice.
 """
 from __future__ import annotations
 
@@ -63,7 +73,9 @@ def numerators(t1, t2, fock, eri, o):
     X = E("abic,jc->ijab", tmpA, t1)
     tmpB = E("kcai,jc->akij", ovov.permute(0, 1, 3, 2), t1) + ovoo.permute(1, 3, 0, 2)
     Y = E("akij,kb->ijab", tmpB, t1)
-    R2 = ovov.permute(0, 2, 1, 3) + P(X - Y) + E("klij,klab->ijab", Woooo, tau) + E("acbd,ijcd->ijab", vvvv, tau)
+    vvvv_s = 0.5 * (vvvv + vvvv.permute(2, 3, 0, 1))      # W_s in (ac|bd) order
+    tau_s = 0.5 * (tau + tau.permute(1, 0, 3, 2))          # P tau
+    R2 = ovov.permute(0, 2, 1, 3) + P(X - Y) + E("klij,klab->ijab", Woooo, tau) + E("acbd,ijcd->ijab", vvvv_s, tau_s)
     Z = E("kdac,ijcd->ijka", ovvv, tau)
     R2 = R2 - P(E("ijka,kb->ijab", Z, t1)) + P(E("ac,ijcb->ijab", Lvv_p, t2)) - P(E("ki,kjab->ijab", Loo_p, t2))
     R2 = R2 + P(E("akic,kjcb->ijab", 2.0 * Wvoov - Wvovo.permute(0, 1, 3, 2), t2))
