@@ -418,7 +418,7 @@ void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const Mat
     }
     const bool prof = opt_.profile && site;
     const bool split = use_split(M, N, K);
-    if (split && SplitEngine::prefer_swap(M, N)) {
+    if (split && SplitEngine::prefer_swap(M, N, C)) {
         gemm(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, cache_b, cache_a, site);
         return;
     }
@@ -595,10 +595,10 @@ void Engine::residual() {
     // + sum_d (kc|ad) t1[i,d]: M = (k,c,a), N = i, K = d
     gemm((int)(ov * v), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
          ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0, "Wvoov_t1v");
-    // - sum_l (kc|li) t1[l,a]: M = (k,c,i), N = a, K = l
+    // - sum_l (kc|li) t1[l,a]: M = (i,k,c) (c, contiguous in Wvoov, innermost), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
-         mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, v * o2, o2, 1), ix1(o)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)), 0, 0, "Wvoov_t1o");
+         mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Wvoov_.p, ix3((uint32_t)o, (uint32_t)v, v * ov, v, 1), ix1(ov)), 13, 0, "Wvoov_t1o");
     // + sum_ld th1[i,a,l,d] (ld|kc), read at ovov[l][d][k][c] (the position the closed-shell
     // equations name, so that dE/d(pq|rs) is assigned per element like the oracle's)
     gemm((int)ov, (int)ov, (int)ov, 1.0, mv(th1_.p, ix1(ov), ix1(1)), mv(ovov_.p, ix1(1), ix1(ov)),
@@ -615,10 +615,10 @@ void Engine::residual() {
     gemm((int)(ov * v), io, iv, 1.0,
          mv(ovvv_.p, ix3((uint32_t)v, (uint32_t)v, v * v2, v, 1), ix1(v2)), mv(t1, ix1(v), ix1(1)),
          1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)v, v, ov, 1), ix1(v * ov)), 9, 0, "Wvovo_t1v");
-    // - sum_l (lc|ki) t1[l,a]: M = (k,c,i), N = a, K = l
+    // - sum_l (lc|ki) t1[l,a]: M = (i,k,c) (c innermost), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
-         mv(ovoo_.p, ix3((uint32_t)v, (uint32_t)o, o, o2, 1), ix1(v * o2)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)o, v, 1, v * ov), ix1(ov)), 0, 0, "Wvovo_t1o");
+         mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, o, o2), ix1(v * o2)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Wvovo_.p, ix3((uint32_t)o, (uint32_t)v, v * ov, v, 1), ix1(ov)), 14, 0, "Wvovo_t1o");
     // - sum_ld th2[i,a,l,d] (lc|kd)
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(th2_.p, ix1(ov), ix1(1)),
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
@@ -656,8 +656,8 @@ void Engine::residual() {
     gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
          ovw(Vk_.p, ix1(o), ix1(1)), 0, 0, "Rp_oovv_t1");
     gemm((int)(o * v * o), iv, io, -1.0,
-         mv(Vk_.p, ix3((uint32_t)v, (uint32_t)o, v * o, o, 1), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)o, ov2, 1, v2), ix1(v)), 0, 0, "Rp_oovv_t1t1");
+         mv(Vk_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
+         1.0, ovw(Rp_.p, ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1), ix1(v)), 0, 0, "Rp_oovv_t1t1");
     // - sum_k tmpB[k,i,a,j] t1[k,b], tmpB = (ia|jk) + sum_c (kc|ia) t1[j,c]
     axpby((int)(o * ov), io, 1.0,
                mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), 0.0,

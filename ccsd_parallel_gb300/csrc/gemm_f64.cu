@@ -138,8 +138,18 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int M, int K, double alph
         const int m = blockIdx.x * 32 + tx;
         double acc = 0.0;
         if (m < M) {
+            // four independent chains keep four loads per thread in flight
             const int64_t ro = dim_off(A.row, m);
-            for (int k = ty; k < K; k += 8) acc = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], acc);
+            double a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int k = ty;
+            for (; k + 24 < K; k += 32) {
+                acc = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], acc);
+                a1 = fma(A.p[ro + dim_off(A.col, k + 8)], X.p[dim_off(X.col, k + 8)], a1);
+                a2 = fma(A.p[ro + dim_off(A.col, k + 16)], X.p[dim_off(X.col, k + 16)], a2);
+                a3 = fma(A.p[ro + dim_off(A.col, k + 24)], X.p[dim_off(X.col, k + 24)], a3);
+            }
+            for (; k < K; k += 8) acc = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], acc);
+            acc = (acc + a1) + (a2 + a3);
         }
         part[ty][tx] = acc;
         __syncthreads();

@@ -56,13 +56,14 @@ struct alignas(8) Bars {
     int never;  // stays 0: a wait that must not be cut short by another role
 };
 
-template <int S, int BN>
-__global__ void __launch_bounds__(kThreads, 1)
+// NSTF: pipeline stages (0 = as many as fit one CTA per SM); MINB: CTAs per SM.
+template <int S, int BN, int NSTF, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       int M, int N, int tiles_m, int tiles_n, int rowsA_pad, int rowsB_pad, int nkb_total,
                       int kb_per_split, const double *__restrict__ scaleA, const double *__restrict__ scaleB,
                       double alpha, double beta, OutView C, double *ws, int *gerr) {
-    constexpr int NST = num_stages(S, BN);
+    constexpr int NST = NSTF > 0 ? NSTF : num_stages(S, BN);
     constexpr int SB = stage_bytes(S, BN);
     constexpr int A_TILE = BM * BK * 2;   // bytes per A plane tile
     constexpr int B_TILE = BN * BK * 2;
@@ -227,19 +228,32 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int j = 0; j < 32; ++j) r[j] = 0u;
                 }
+                // kCB columns at a time: their C loads (beta != 0) are issued
+                // together instead of one dependent load per column
+                constexpr int kCB = 4;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int n = n0 + g * 32 + j;
-                    if (!mval || n >= N) continue;
-                    const double val =
-                        sa * scaleB[n] * ((double)iacc[g * 32 + j] + (double)__uint_as_float(r[j]));
-                    if (direct) {
-                        double *cp = C.p + crow + dim_off(C.col, (uint32_t)n);
-                        double out = alpha * val;
-                        if (beta != 0.0) out = fma(beta, *cp, out);
-                        *cp = out;
-                    } else {
-                        wsz[(size_t)m * N + n] = val;
+                for (int j0 = 0; j0 < 32; j0 += kCB) {
+                    int64_t off[kCB];
+                    double cold[kCB];
+#pragma unroll
+                    for (int j = 0; j < kCB; ++j) {
+                        const int n = n0 + g * 32 + j0 + j;
+                        off[j] = (mval && n < N) ? crow + dim_off(C.col, (uint32_t)n) : -1;
+                        cold[j] = (direct && beta != 0.0 && off[j] >= 0) ? C.p[off[j]] : 0.0;
+                    }
+#pragma unroll
+                    for (int j = 0; j < kCB; ++j) {
+                        if (off[j] < 0) continue;
+                        const int n = n0 + g * 32 + j0 + j;
+                        const double val = sa * scaleB[n] *
+                                           ((double)iacc[g * 32 + j0 + j] + (double)__uint_as_float(r[j0 + j]));
+                        if (direct) {
+                            double out = alpha * val;
+                            if (beta != 0.0) out = fma(beta, cold[j], out);
+                            C.p[off[j]] = out;
+                        } else {
+                            wsz[(size_t)m * N + n] = val;
+                        }
                     }
                 }
             }
@@ -407,15 +421,19 @@ void encode(CUtensorMap *map, const SplitOperand &op, int box_rows) {
     if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int S, int BN>
+template <int S, int BN, int NSTF = 0, int MINB = 1>
 void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
               const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
-    constexpr int NST = num_stages(S, BN);
-    constexpr size_t smem = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
+    constexpr int NST = NSTF > 0 ? NSTF : num_stages(S, BN);
+    // two-per-SM variants request at least 80 KB so that no third CTA (and its
+    // TMEM allocation) can become resident on the SM
+    constexpr size_t smem_need = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
+    constexpr size_t smem = (MINB > 1 && smem_need < 80 * 1024) ? 80 * 1024 : smem_need;
+    static_assert(MINB * smem <= 227 * 1024 && MINB * tmem_cols(BN) <= 512, "co-resident CTAs must fit");
     static bool attr = false;
     if (!attr) {
-        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S, BN, NSTF, MINB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
     alignas(64) CUtensorMap ta, tb;
@@ -434,9 +452,9 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     int kbps = (nkb + splits - 1) / splits;
     splits = (nkb + kbps - 1) / kbps;
     dim3 grid((unsigned)(tiles_m * tiles_n), 1, splits);
-    split_gemm_kernel<S, BN><<<grid, kThreads, smem, st>>>(ta, tb, M, N, tiles_m, tiles_n, A.rows_pad,
-                                                           B.rows_pad, nkb, kbps, A.scale, B.scale, alpha, beta,
-                                                           C, ws, d_err);
+    // lanes along n when the output is contiguous in n (and for the row-major split-K partials)
+    split_gemm_kernel<S, BN, NSTF, MINB><<<grid, kThreads, smem, st>>>(
+        ta, tb, M, N, tiles_m, tiles_n, A.rows_pad, B.rows_pad, nkb, kbps, A.scale, B.scale, alpha, beta, C, ws, d_err);
     CCSD_LAUNCH_CHECK();
     if (splits > 1) {
         const size_t total = (size_t)M * N;
@@ -462,6 +480,21 @@ void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double
             best_w = w;
             bn = c;
         }
+    }
+    // short K on a narrow tile: a few stages and two CTAs per SM, so one CTA's
+    // pipeline fill and epilogue overlap the other's main loop
+    const int nkb = A.kpad / BK;
+    // K <= 128: the main loop is a few k-blocks and the epilogue's C traffic
+    // dominates, so the narrow two-per-SM tiles win even for wide N
+    if (nkb <= 4 && bn > 64) bn = 64;
+    if (nkb <= 64 && bn <= 64) {
+        constexpr int st32 = std::max(2, std::min(3, (100 * 1024) / stage_bytes(S, 32)));
+        constexpr int st64 = std::max(2, std::min(3, (100 * 1024) / stage_bytes(S, 64)));
+        if (bn == 32)
+            launch_t<S, 32, st32, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+        else
+            launch_t<S, 64, st64, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+        return;
     }
     switch (bn) {
         case 160: launch_t<S, 160>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
@@ -624,7 +657,7 @@ SplitOperand *SplitEngine::operand(int key, int rows, int K, const MatView &v, i
 
 void SplitEngine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
                        const OutView &C, int cache_a, int cache_b) {
-    if (prefer_swap(M, N)) {  // C^T = B A^T keeps the long side in the 128-row MMA tile
+    if (prefer_swap(M, N, C)) {  // C^T = B A^T: long side / unit-stride output index in the rows
         gemm(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, cache_b, cache_a);
         return;
     }
