@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--fp64-updates", type=int, default=6,
                     help="updates of the FP64 comparison run (0 skips it)")
     ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--extras", type=int, default=1,
+                    help="also measure the Lambda gradient at this workload and the 64-system batched solve")
     ap.add_argument("--sites-out", default="",
                     help="write the per-contraction-site device profile of the timed run (JSON) here")
     return ap.parse_args()
@@ -201,6 +203,51 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def measure_extras(cg, fock, df, o, precision):
+    """Untimed-by-the-headline extras: the Lambda gradient (dE/dB) at the bench
+    workload and the batched solve of 64 small systems (nocc 4..12, nvir 20..80)."""
+    out = {}
+    t0 = time.perf_counter()
+    with cg.Solver(fock, o, df=df, precision=precision, energy_tol=1e-9, diis_size=WORKLOAD["diis"],
+                   diis_start=2) as s:
+        r = s.solve(amplitudes=False)
+        t1 = time.perf_counter()
+        g = s.lambda_grad(tol=1e-8, max_iter=200)
+        t2 = time.perf_counter()
+    out["gradient"] = dict(workload="dE_corr/dB and dE_corr/dfock at this workload after a 1e-9 solve",
+                           precision=precision, solve_s=t1 - t0, solve_updates=r["iterations"],
+                           lambda_grad_s=t2 - t1, lambda_iterations=g["iterations"],
+                           lambda_residual=g["residual_norm"])
+    rng = np.random.default_rng(4)
+    systems = []
+    for k in range(64):
+        so, sv = int(rng.integers(4, 13)), int(rng.integers(20, 81))
+        f_k, b_k = cg.make_synthetic(so, sv, 3 * (so + sv) // 2, 1000 + k)
+        systems.append(dict(fock=f_k, nocc=so, df=b_k))
+    with cg.Batch(systems, energy_tol=1e-10) as b:
+        b.solve(amplitudes=False)                     # autotunes and captures the graphs
+        t0 = time.perf_counter()
+        rb = b.solve(amplitudes=False)
+        tb = time.perf_counter() - t0
+        rep = b.report()
+    solvers = [cg.Solver(**sy, energy_tol=1e-10) for sy in systems]
+    for sv_ in solvers:
+        sv_.solve(amplitudes=False)
+    t0 = time.perf_counter()
+    for sv_ in solvers:
+        sv_.solve(amplitudes=False)
+    ts = time.perf_counter() - t0
+    for sv_ in solvers:
+        sv_.close()
+    flops = sum(x["flops_per_update"] * x["iterations"] for x in rb)
+    out["batch_c4"] = dict(workload="64 synthetic systems, nocc in [4,12], nvir in [20,80], tol 1e-10, FP64",
+                           batched_s=tb, sequential_s=ts, speedup=ts / tb,
+                           system_updates=sum(x["iterations"] for x in rb),
+                           algorithmic_tflops=flops / tb / 1e12,
+                           launches_per_update=rep["launches_per_update"])
+    return out
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -269,6 +316,10 @@ def main():
                            f"on 3 of {v} virtual rows ({res[0]['ladder_sample_s']:.1f} s, scaled "
                            f"x{res[0]['ladder_scale']:.0f})"))
 
+    extras = {}
+    if args.extras and rank == 0:
+        extras = measure_extras(cg, fock, df, o, args.precision)
+
     if rank != 0:
         return
     h2d = fock.nbytes + df.nbytes
@@ -299,6 +350,7 @@ def main():
                  includes="ccsd_create (H2D of fock + DF factors, block build) + ccsd_solve + T1/T2 read-back"),
         gpu_launches=int(round(launches)),
         clocks=clk.summary(),
+        **extras,
     )
     print(json.dumps(line), flush=True)
 

@@ -13,6 +13,7 @@
 // Bbar += alpha Cbar^T A, i.e. the same view-based contraction kernels with
 // the row and column index groups exchanged (FP64 or split precision, as the
 // forward pass).  Lambda is iterated like the amplitudes (Jacobi on D).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -172,12 +173,16 @@ void Engine::reverse(const std::vector<TapeOp> &tape) {
             case TapeOp::Gemm: {
                 double *Cb = adj_of(op.C.p);
                 if (!Cb) break;
+                // The operand held fixed in each product (integrals, or amplitudes at the
+                // solution) does not change during the Lambda iteration: its transposed view
+                // is split once and cached under a key of its own (key +- 1000).
+                auto tkey = [](int k) { return k > 0 ? k + 1000 : (k < 0 ? k - 1000 : 0); };
                 if (double *Ab = adj_of(op.A.p))  // Abar(m,k) += alpha sum_n Cbar(m,n) B(n,k)
                     gemm(op.M, op.K, op.N, op.alpha, mv(Cb, op.C.row, op.C.col), mv(op.B.p, op.B.col, op.B.row),
-                         1.0, ovw(Ab, op.A.row, op.A.col));
+                         1.0, ovw(Ab, op.A.row, op.A.col), 0, tkey(op.key_b));
                 if (double *Bb = adj_of(op.B.p))  // Bbar(n,k) += alpha sum_m Cbar(m,n) A(m,k)
                     gemm(op.N, op.K, op.M, op.alpha, mv(Cb, op.C.col, op.C.row), mv(op.A.p, op.A.col, op.A.row),
-                         1.0, ovw(Bb, op.B.row, op.B.col));
+                         1.0, ovw(Bb, op.B.row, op.B.col), 0, tkey(op.key_a));
                 scale(op.M, op.N, op.beta, ovw(Cb, op.C.row, op.C.col));
                 break;
             }
@@ -267,6 +272,48 @@ void Engine::reverse(const std::vector<TapeOp> &tape) {
     }
 }
 
+// ---- the ladder's dE/dB for density-fitted inputs --------------------------------------
+// The ladder reads W[a][b][c][d] = (ac|bd) = sum_Q B[Q][a][c] B[Q][b][d] (virtual
+// indices, offset o) through its pair forms, i.e. the plain ladder on the
+// symmetrised inputs W_s and P tau.  With Rbar = Lambda2 (the adjoint of R at the
+// ladder), its contribution to dE/dB is
+//   Bbar[Q][x][y] += sum_{ij,b,d} Lh[ij][x][b] B[Q][b][d] (P tau)[ij][y][d],
+//   Lh[ij][x][b] = l2[ij][x][b] + l2[ji][b][x],  (P tau)[ij][y][d] = (tau[ijyd] + tau[jidy]) / 2,
+// evaluated as two contractions per block of Q, so neither (ac|bd), W+- nor
+// their adjoints (v^4 each) are formed.  Lh and P tau are split once per call
+// (per-update cache keys, dropped at the next residual).
+void Engine::ladder_df_grad(const double *lam2, int naux) {
+    const int64_t o = o_, v = v_, n = n_, o2 = o * o, v2 = v * v, nn = n * n;
+    double *Bb = adj_of(input_df_ ? input_df_->p : nullptr);
+    if (!Bb) return;
+    const double *B = input_df_->p;
+    DBuf lh((size_t)(o2 * v2)), pt((size_t)(o2 * v2));
+    // element (i,j | x,b) of a [j][i][b][x] read: row (i,j) strides (v2, o v2), column (x,b) strides (1, v)
+    const MatView lt = mv(lam2, ix2((uint32_t)o, v2, o * v2), ix2((uint32_t)v, 1, v));
+    axpby_view((int)o2, (int)v2, 1.0, mv(lam2, ix1(v2), ix1(1)), 0.0, ovw(lh.p, ix1(v2), ix1(1)), st_);
+    axpby_view((int)o2, (int)v2, 1.0, lt, 1.0, ovw(lh.p, ix1(v2), ix1(1)), st_);
+    const MatView tt = mv(tau_.p, ix2((uint32_t)o, v2, o * v2), ix2((uint32_t)v, 1, v));
+    axpby_view((int)o2, (int)v2, 0.5, mv(tau_.p, ix1(v2), ix1(1)), 0.0, ovw(pt.p, ix1(v2), ix1(1)), st_);
+    axpby_view((int)o2, (int)v2, 0.5, tt, 1.0, ovw(pt.p, ix1(v2), ix1(1)), st_);
+    // Q blocks so that U = Lh B stays near 2 GB
+    const int64_t per_q = o2 * v2;
+    const int qc_max = (int)std::max<int64_t>(1, std::min<int64_t>(naux, (int64_t)(2.0e9 / 8.0) / per_q));
+    DBuf U((size_t)(per_q * qc_max));
+    const double *Bvv = B + o * n + o;
+    double *Bbvv = Bb + o * n + o;
+    for (int q0 = 0; q0 < naux; q0 += qc_max) {
+        const int64_t qc = std::min<int64_t>(qc_max, naux - q0);
+        // U[(ij,x)][(Q,d)] = sum_b Lh[ij][x][b] B[q0+Q][b][d]
+        gemm((int)(o2 * v), (int)(qc * v), (int)v, 1.0, mv(lh.p, ix1(v), ix1(1)),
+             mv(Bvv + q0 * nn, ix2((uint32_t)v, nn, 1), ix1(n)), 0.0, ovw(U.p, ix1(qc * v), ix1(1)), -1101, 0);
+        // Bbar[q0+Q][x][y] += sum_{ij,d} U[(ij,x)][(Q,d)] (P tau)[ij][y][d]
+        gemm((int)(qc * v), (int)v, (int)(o2 * v), 1.0,
+             mv(U.p, ix2((uint32_t)v, v, qc * v), ix2((uint32_t)v, v * qc * v, 1)),
+             mv(pt.p, ix1(v), ix2((uint32_t)v, v2, 1)), 1.0, ovw(Bbvv + q0 * nn, ix2((uint32_t)v, nn, n), ix1(1)),
+             0, -1102);
+    }
+}
+
 // ---- Lambda equations and the gradient ----------------------------------------------
 void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     if (!solved_) throw Error(CCSD_ERR_INVALID_ARG, "ccsd_lambda_grad needs a completed ccsd_solve first");
@@ -285,6 +332,7 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
             e->keep_.clear();
             e->build_split_.reset();
             e->wv_.alloc(0);  // (ac|bd) was rebuilt for the recorded build only
+            e->grad_lean_vvvv_ = false;
         }
     } cleanup{this};
 
@@ -293,17 +341,24 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     for (DBuf *b : {&t1_, &t2_, &tau_, &th1_, &th2_, &R1_, &R_, &Rp_, &Foo_, &Fvv_, &Fov_, &Loo_, &Lvv_, &tmpo_,
                     &tmpo2_, &Woooo_, &Wvoov_, &Wvovo_, &Wa_, &Z_, &tmpB_, &Vk_, &taup_, &taum_, &Sp_, &Sm_})
         reg(*b, true);
-    for (DBuf *b : {&ovov_, &oovv_, &ovoo_, &oooo_, &ovvv_, &wv_, &Lovov_, &Lovoo_, &Lovvv_, &LT1_, &Lijab_, &Wp_, &Wm_,
-                    &f_oo_off_, &f_vv_off_, &f_ov_})
+    // DF inputs: the ladder's dE/dB comes from ladder_df_grad, so (ac|bd) and W+- get
+    // no adjoints (at large nvir they would not fit next to the forward tensors)
+    const bool lean = prob.integral_kind == CCSD_INTS_DF;
+    for (DBuf *b : {&ovov_, &oovv_, &ovoo_, &oooo_, &ovvv_, &Lovov_, &Lovoo_, &Lovvv_, &LT1_, &Lijab_, &f_oo_off_,
+                    &f_vv_off_, &f_ov_})
         reg(*b, false);
+    if (!lean)
+        for (DBuf *b : {&wv_, &Wp_, &Wm_}) reg(*b, false);
 
     // 1. record the integral build again (the inputs are re-read), then one residual at the solution
     std::vector<TapeOp> build_tape, res_tape;
     input_eri_ = input_df_ = input_c_ = nullptr;
     tape_ = &build_tape;
     if (opt_.precision != CCSD_PREC_FP64) build_split_.reset(new SplitEngine(CCSD_PREC_SPLIT4, st_));
+    grad_lean_vvvv_ = lean;
     build_integrals(prob);
     build_derived();
+    grad_lean_vvvv_ = false;
     tape_ = nullptr;
     CCSD_CUDA(cudaStreamSynchronize(st_));
     build_split_.reset();
@@ -366,6 +421,7 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
         axpby_view(1, (int)nT2, 1.0, mv(tau_.p, ix1(0), ix1(1)), 1.0, ovw(Lb, ix1(0), ix1(1)), st_);
     }
     reverse(build_tape);
+    if (lean) ladder_df_grad(l2.p, prob.naux);
     CCSD_CUDA(cudaStreamSynchronize(st_));
 
     // 5. host assembly: the denominator term and the Fock matrix

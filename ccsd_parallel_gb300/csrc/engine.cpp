@@ -300,7 +300,10 @@ void Engine::build_from_df(const double *B, int naux) {
     blk(ovoo_, 0, o, o, v, 0, o, 0, o);
     blk(oooo_, 0, o, 0, o, 0, o, 0, o);
     blk(ovvv_, 0, o, o, v, o, v, o, v);
-    // Wv[a][b][c][d] = (ac|bd): M = (a,c), N = (b,d), K = Q
+    // Wv[a][b][c][d] = (ac|bd): M = (a,c), N = (b,d), K = Q.  A gradient with DF
+    // inputs takes the ladder's dE/dB directly (Engine::ladder_df_grad) and
+    // records the build without this block and its pair forms.
+    if (grad_lean_vvvv_) return;
     wv_.ensure((size_t)(v * v * v * v));
     const double *bvv = B + o * n + o;
     gemm((int)(v * v), (int)(v * v), naux, 1.0, mv(bvv, ix2((uint32_t)v, n, 1), ix1(nn)),
@@ -382,6 +385,7 @@ void Engine::build_derived() {
           mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
           ovw(Lijab_.p, ix1(v * v), ix1(1)));
     // W+ [tri(a,b)][tri(c,d)] and W- [stri(a,b)][stri(c,d)] of the pair-form ladder
+    if (grad_lean_vvvv_) return;
     const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
     Wp_.ensure(Tv * Tv);
     Wm_.ensure(Tmv * Tmv);
@@ -408,6 +412,8 @@ void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const Mat
         op.B = B;
         op.C = C;
         op.site = site;
+        op.key_a = cache_a;
+        op.key_b = cache_b;
         tape_->push_back(op);
         if (record_only_) return;
         std::vector<TapeOp> *t = tape_;

@@ -44,6 +44,7 @@ struct TapeOp {
     const double *t1 = nullptr, *t2 = nullptr;  // Tau/Theta inputs
     double *out1 = nullptr, *out2 = nullptr;    // Tau: out1 = tau; Theta: out1 = th1, out2 = th2
     const char *site = nullptr;                 // Gemm: contraction site name
+    int key_a = 0, key_b = 0;                   // Gemm: split-cache keys of the operands
 };
 
 class Batch;
@@ -118,6 +119,9 @@ class Engine {
     // reverse mode
     std::vector<TapeOp> *tape_ = nullptr;  // recording target, or null
     bool record_only_ = false;             // record into tape_ without running
+    bool grad_lean_vvvv_ = false;          // DF gradient: no (ac|bd) / W+- in the recorded build
+    // dE/dB of the pp ladder for DF inputs without the v^4 adjoints (adjoint.cpp)
+    void ladder_df_grad(const double *lam2, int naux);
     struct Reg {
         DBuf *buf;
         bool active;  // depends on the amplitudes (Lambda mode propagates into these only)

@@ -148,3 +148,29 @@ def test_split_precision_gradient_close_to_fp64():
         d = np.abs(out["split3"][k] - out["fp64"][k]).max()
         print(f"split3 vs fp64 {k}: max |diff| {d:.3e}")
         assert d < 1e-8, (k, d)
+
+
+def test_c5_df_gradient_against_finite_differences():
+    """Config: the bench workload, synthetic nocc=24, nvir=300, naux=900, split3.
+    dE/dB on four DF entries (two in the virtual-virtual block, whose ladder
+    term is taken directly from Lambda without the v^4 adjoints) against
+    central differences of split3 solves (h = 1e-4); within 1e-6."""
+    o, v, q = 24, 300, 900
+    fock, b = cg.make_synthetic(o, v, q, 2024)
+    opts = dict(precision="split3", energy_tol=1e-11, diis_size=6, diis_start=2)
+    with cg.Solver(fock, o, df=b, **opts) as s:
+        s.solve(amplitudes=False)
+        G = s.lambda_grad(tol=1e-9)
+    n = o + v
+    pos = [(17, o + 5, o + 200), (401, o + 123, o + 7), (3, 2, o + 50), (650, 1, 20)]
+    h = 1e-4
+    worst = 0.0
+    for idx in pos:
+        bp, bm = b.copy(), b.copy()
+        bp[idx] += h
+        bm[idx] -= h
+        ep = cg.solve(fock, o, df=bp, amplitudes=False, **opts)["e_corr"]
+        em = cg.solve(fock, o, df=bm, amplitudes=False, **opts)["e_corr"]
+        worst = max(worst, abs((ep - em) / (2 * h) - G["d_df"][idx]))
+    print(f"C5 finite-difference check: {len(pos)} DF entries, max |fd - grad| {worst:.3e}")
+    assert worst < 1e-6
