@@ -18,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (CCSD_INTS_AO_DENSE, CCSD_INTS_DF, CCSD_INTS_MO_DENSE, CCSD_PREC_FP64,
+from ._abi import (CCSD_INTS_AO_DENSE, CCSD_INTS_DF, CCSD_INTS_MO_DENSE, CCSD_INTS_SO_ANTISYM, CCSD_PREC_FP64,
                    CCSD_PREC_SPLIT2, CCSD_PREC_SPLIT3, CCSD_PREC_SPLIT4, CCSDError)
 
 PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD_PREC_SPLIT3,
@@ -67,8 +67,12 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     return o
 
 
-def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None):
-    """ccsd_problem over host arrays; returns (problem, arrays to keep alive)."""
+def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None):
+    """ccsd_problem over host arrays; returns (problem, arrays to keep alive).
+
+    Integrals: ``eri`` spatial (pq|rs) [n]^4, ``df`` factors B[Q][p][q],
+    ``ao_eri`` + ``mo_coeff``, or ``so_eri`` = <PQ||RS> over 2n interleaved
+    spin orbitals (the reference's antisymmetrised integrals)."""
     fock = _f64(fock)
     n = fock.shape[0]
     p = _abi.Problem()
@@ -84,20 +88,26 @@ def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None):
         p.integral_kind, p.nao = CCSD_INTS_AO_DENSE, ao_eri.shape[0]
         p.eri, p.mo_coeff = _ptr(ao_eri), _ptr(mo_coeff)
         keep += [ao_eri, mo_coeff]
+    elif so_eri is not None:
+        so_eri = _f64(so_eri)
+        if so_eri.shape != (2 * n,) * 4:
+            raise ValueError("so_eri must be (2n)^4 spin-orbital integrals <PQ||RS>")
+        p.integral_kind, p.eri = CCSD_INTS_SO_ANTISYM, _ptr(so_eri)
+        keep.append(so_eri)
     elif eri is not None:
         eri = _f64(eri)
         p.integral_kind, p.eri = CCSD_INTS_MO_DENSE, _ptr(eri)
         keep.append(eri)
     else:
-        raise ValueError("one of eri / df / ao_eri is required")
+        raise ValueError("one of eri / df / ao_eri / so_eri is required")
     return p, keep
 
 
 class Solver:
     """One device-resident system (integrals uploaded/transformed once)."""
 
-    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, **opts):
-        p, self._keep = _problem(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff)
+    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, **opts):
+        p, self._keep = _problem(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri)
         n = p.nocc + p.nvir
         self.nocc, self.nvir = nocc, n - nocc
         self._opts = _options(**opts)
@@ -137,6 +147,8 @@ class Solver:
         elif p.integral_kind == CCSD_INTS_AO_DENSE:
             out["d_eri"] = np.zeros((p.nao,) * 4)
             out["d_mo_coeff"] = np.zeros((p.nao, n))
+        elif p.integral_kind == CCSD_INTS_SO_ANTISYM:
+            out["d_eri"] = np.zeros((2 * n,) * 4)
         else:
             out["d_eri"] = np.zeros((n,) * 4)
         if lambdas:
@@ -177,8 +189,8 @@ class Solver:
         self.close()
 
 
-def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, amplitudes=True, **opts):
-    with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, **opts) as s:
+def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, amplitudes=True, **opts):
+    with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri, **opts) as s:
         return s.solve(amplitudes=amplitudes)
 
 
@@ -281,8 +293,8 @@ class CCSD_Memory_optimized:
     """
 
     def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, E_HF=0.0,
-                 precision="fp64"):
-        self._solver = Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff,
+                 precision="fp64", so_eri=None):
+        self._solver = Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri,
                               precision=precision)
         self.n_Electrons = 2 * nocc
         self.unocc_orb = 2 * (np.asarray(fock).shape[0] - nocc)

@@ -24,6 +24,7 @@ CCSD_ERR_NOT_CONVERGED = -8
 CCSD_INTS_MO_DENSE = 0
 CCSD_INTS_DF = 1
 CCSD_INTS_AO_DENSE = 2
+CCSD_INTS_SO_ANTISYM = 3
 
 CCSD_PREC_FP64 = 0
 CCSD_PREC_SPLIT2 = 2

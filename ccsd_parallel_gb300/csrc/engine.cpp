@@ -255,9 +255,59 @@ void Engine::build_integrals(const ccsd_problem &prob) {
         keep(std::move(ao));
         keep(std::move(c));
         keep(std::move(mo));
+    } else if (prob.integral_kind == CCSD_INTS_SO_ANTISYM) {
+        // <PQ||RS> over N = 2n interleaved spin orbitals (ccsdt.cpp:1466-1478).  For a
+        // closed-shell determinant (pq|rs) = <p_alpha r_beta || q_alpha s_beta>
+        // = so[2p][2r+1][2q][2s+1]: one strided copy (recorded, so the gradient
+        // lands on these elements of the input).
+        if (!prob.eri) throw Error(CCSD_ERR_INVALID_ARG, "eri is NULL");
+        const int64_t N = 2 * (int64_t)n, nn = n;
+        if (!prob.device_inputs) check_closed_shell_so(prob.eri, n);
+        std::unique_ptr<DBuf> so(new DBuf((size_t)(N * N * N * N))), mo(new DBuf((size_t)(nn * nn * nn * nn)));
+        CCSD_CUDA(cudaMemcpyAsync(so->p, prob.eri, sizeof(double) * so->n, kind, st_));
+        axpby((int)(nn * nn), (int)(nn * nn), 1.0,
+              mv(so->p + N * N + 1, ix2((uint32_t)n, 2 * N * N * N, 2 * N), ix2((uint32_t)n, 2 * N * N, 2)), 0.0,
+              ovw(mo->p, ix1(nn * nn), ix1(1)));
+        build_from_mo_dense(mo->p);
+        CCSD_CUDA(cudaStreamSynchronize(st_));
+        input_eri_ = so.get();
+        keep(std::move(so));
+        keep(std::move(mo));
     } else {
         throw Error(CCSD_ERR_INVALID_ARG, "unknown integral_kind");
     }
+}
+
+// Host check that spin-orbital integrals belong to a closed-shell determinant:
+// a fixed sample of same-spin elements must equal (pr|qs) - (ps|qr) built from
+// the alpha-beta block, and the spin-forbidden <p_a q_b || r_a s_a> must vanish,
+// to 1e-4 of the largest sampled value (it catches open-shell or mis-ordered
+// integrals, not rounding).
+void Engine::check_closed_shell_so(const double *so, int n) {
+    const int64_t N = 2 * (int64_t)n;
+    auto at = [&](int64_t P, int64_t Q, int64_t R, int64_t S) { return so[((P * N + Q) * N + R) * N + S]; };
+    auto chem = [&](int p, int q, int r, int s) { return at(2 * p, 2 * r + 1, 2 * q, 2 * s + 1); };
+    double scale = 0.0, worst = 0.0;
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    for (int t = 0; t < 4096; ++t) {
+        int idx[4];
+        for (int &k : idx) {
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            k = (int)(x % (uint64_t)n);
+        }
+        const int p = idx[0], q = idx[1], r = idx[2], s = idx[3];
+        const double ref = chem(p, r, q, s) - chem(p, s, q, r);
+        scale = std::max(scale, std::fabs(ref));
+        worst = std::max(worst, std::fabs(at(2 * p, 2 * q, 2 * r, 2 * s) - ref));
+        worst = std::max(worst, std::fabs(at(2 * p + 1, 2 * q + 1, 2 * r + 1, 2 * s + 1) - ref));
+        worst = std::max(worst, std::fabs(at(2 * p, 2 * q + 1, 2 * r, 2 * s)));
+    }
+    if (worst > 1e-4 * std::max(scale, 1e-12))
+        throw Error(CCSD_ERR_INVALID_ARG,
+                    "spin-orbital integrals are not those of a closed-shell determinant (same-spin elements differ "
+                    "from (pr|qs) - (ps|qr) of the alpha-beta block by " + std::to_string(worst) + ")");
 }
 
 // Y[p'][q'][r'][s'] = eri[p0+p'][q0+q'][r0+r'][s0+s'] for every block.

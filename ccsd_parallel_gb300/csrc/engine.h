@@ -70,6 +70,7 @@ class Engine {
     void build_from_df(const double *b_dev, int naux);
     void ao_to_mo(const double *ao_dev, const double *c_dev, int nao, DBuf &mo_out);
     void build_derived();
+    static void check_closed_shell_so(const double *so_host, int n);
 
     // contractions: C(m,n) = alpha sum_k A(m,k) B(n,k) + beta C(m,n).
     // `cache_a/b` != 0 marks an operand view over constant integrals whose

@@ -55,6 +55,13 @@ extern "C" {
 #define CCSD_INTS_MO_DENSE 0 /* eri = n^4 MO (pq|rs), row-major p,q,r,s         */
 #define CCSD_INTS_DF 1       /* df  = naux*n*n factors B[Q][p][q], (pq|rs) = sum_Q B B */
 #define CCSD_INTS_AO_DENSE 2 /* eri = nao^4 AO (mu nu|la si), mo_coeff = C[mu][p] */
+/* eri = <PQ||RS> over N = 2n spin orbitals, physicist order, alpha/beta
+ * interleaved (spin orbital P -> spatial P/2, spin P%2), the reference's
+ * antisymmetrised spin-orbital integrals (ccsdt.cpp:1466-1478).  They must be
+ * those of a closed-shell determinant; the engine reads the alpha-beta block,
+ * (pq|rs) = <p_alpha r_beta || q_alpha s_beta>, and (host inputs) checks a
+ * sample of same-spin elements against (pr|qs) - (ps|qr). */
+#define CCSD_INTS_SO_ANTISYM 3
 
 /* ---- contraction precision ------------------------------------------- */
 #define CCSD_PREC_FP64 0      /* every contraction in FP64 (DFMA)              */
@@ -70,7 +77,7 @@ typedef struct ccsd_problem {
     int32_t nao;           /* AO_DENSE: number of basis functions (>= n)       */
     int32_t device_inputs; /* 0: pointers below are host memory; 1: device     */
     const double *fock;    /* n x n MO Fock matrix, n = nocc + nvir            */
-    const double *eri;     /* MO_DENSE: n^4; AO_DENSE: nao^4                   */
+    const double *eri;     /* MO_DENSE: n^4; AO_DENSE: nao^4; SO_ANTISYM: (2n)^4 */
     const double *df;      /* DF: naux * n * n                                 */
     const double *mo_coeff;/* AO_DENSE: nao x n, row-major C[mu][p]            */
 } ccsd_problem;
@@ -109,7 +116,7 @@ typedef struct ccsd_result {
  * as independent (an element the engine never reads has derivative 0). */
 typedef struct ccsd_grad {
     double *d_fock;      /* n x n: dE_corr / d fock[p][q]                         */
-    double *d_eri;       /* MO_DENSE: n^4, AO_DENSE: nao^4: dE_corr / d eri[...]  */
+    double *d_eri;       /* MO_DENSE: n^4, AO_DENSE: nao^4, SO_ANTISYM: (2n)^4   */
     double *d_df;        /* DF: naux*n*n: dE_corr / d B[Q][p][q]                  */
     double *d_mo_coeff;  /* AO_DENSE: nao*n: dE_corr / d C[mu][p]                 */
     double *lambda1;     /* o*v: Lambda amplitudes l1[i][a]                       */

@@ -174,3 +174,36 @@ def test_c5_df_gradient_against_finite_differences():
         worst = max(worst, abs((ep - em) / (2 * h) - G["d_df"][idx]))
     print(f"C5 finite-difference check: {len(pos)} DF entries, max |fd - grad| {worst:.3e}")
     assert worst < 1e-6
+
+
+def test_spin_orbital_input_gradient():
+    """dE/d<PQ||RS> for the spin-orbital input form: the alpha-beta block
+    carries the spatial gradient, every other element has derivative 0 (the
+    engine does not read it); central FD on alpha-beta entries (h = 1e-6, small
+    enough for the input's closed-shell check)."""
+    from oracle.ccsd_spinorb import spin_orbital_integrals
+    o, v = 2, 4
+    fock, eri = _system(o, v, 14, 8, 0.3)
+    g = spin_orbital_integrals(eri)
+    with cg.Solver(fock, o, so_eri=g, energy_tol=1e-13) as s:
+        s.solve(amplitudes=False)
+        G = s.lambda_grad(tol=1e-12)
+    with cg.Solver(fock, o, eri=eri, energy_tol=1e-13) as s:
+        s.solve(amplitudes=False)
+        Gs = s.lambda_grad(tol=1e-12)
+    n = o + v
+    ab = G["d_eri"][0::2, 1::2, 0::2, 1::2].transpose(0, 2, 1, 3)   # [p][r][q][s] -> [p][q][r][s]
+    np.testing.assert_allclose(ab, Gs["d_eri"], rtol=0, atol=1e-12)
+    mask = np.ones_like(G["d_eri"], dtype=bool)
+    mask[0::2, 1::2, 0::2, 1::2] = False
+    assert np.abs(G["d_eri"][mask]).max() == 0.0
+    h = 1e-6
+
+    def e(idx, dh):
+        gg = g.copy()
+        gg[idx] += dh
+        return cg.solve(fock, o, so_eri=gg, energy_tol=1e-13, amplitudes=False)["e_corr"]
+
+    for idx in [(0, 1, 2, 3), (2 * 1, 2 * 3 + 1, 2 * 1, 2 * 3 + 1), (2 * 3, 2 * 0 + 1, 2 * 5, 2 * 2 + 1)]:
+        fd = (e(idx, h) - e(idx, -h)) / (2 * h)
+        assert abs(fd - G["d_eri"][idx]) < 1e-6, (idx, fd, G["d_eri"][idx])

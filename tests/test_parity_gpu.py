@@ -149,3 +149,50 @@ def test_bad_shape_is_rejected():
     with pytest.raises(cg.CCSDError) as ei:
         cg.solve(fock, 0, df=b)
     assert ei.value.code == -1
+
+
+@pytest.mark.parametrize("o,v", [(1, 1), (1, 4), (3, 1), (2, 2), (1, 17)])
+def test_degenerate_shapes_match_oracle(o, v):
+    """nocc = 1 or nvir = 1 leave the antisymmetric ladder half empty (no i > j or
+    a > b pairs); single-system FP64 and split3 runs and the batched solve all
+    follow the oracle."""
+    from oracle.ccsd_rhf import RHFCCSD
+    eps = syn.orbital_energies(o, v, 40 + o + v)
+    fock = np.diag(eps)
+    b = syn.df_factors(o + v, 3 * (o + v), 40 + o + v, sigma=0.3)
+    ref = RHFCCSD(fock, o, df=b).run(toler=1e-11)
+    for prec, tol in (("fp64", 1e-11), ("split3", 1e-9)):
+        r = cg.solve(fock, o, df=b, energy_tol=1e-11, precision=prec)
+        assert abs(r["e_corr"] - ref["e_corr"]) < tol, (prec, r["e_corr"], ref["e_corr"])
+        np.testing.assert_allclose(r["t2"], ref["t2"], rtol=0, atol=100 * tol)
+    rb = cg.solve_batched([dict(fock=fock, nocc=o, df=b)] * 2, energy_tol=1e-11)
+    for x in rb:
+        assert abs(x["e_corr"] - ref["e_corr"]) < 1e-11
+
+
+def test_spin_orbital_input_matches_spatial_and_spin_orbital_oracle():
+    """The reference's antisymmetrised spin-orbital integrals <PQ||RS> as input
+    (CCSD_INTS_SO_ANTISYM): same iterates as the spatial input and as the
+    spin-orbital oracle (the reference's CCSD1 equations)."""
+    from oracle.ccsd_spinorb import SpinOrbitalCCSD, spin_orbital_integrals
+    o, v = 2, 4
+    eps = syn.orbital_energies(o, v, 8)
+    eri = syn.eri_from_df(syn.df_factors(o + v, 14, 8, sigma=0.3))
+    g = spin_orbital_integrals(eri)
+    r_so = cg.solve(np.diag(eps), o, so_eri=g, energy_tol=1e-11)
+    r_sp = cg.solve(np.diag(eps), o, eri=eri, energy_tol=1e-11)
+    ref = SpinOrbitalCCSD(np.diag(eps), eri, o).run(toler=1e-11)
+    assert r_so["iterations"] == r_sp["iterations"]
+    np.testing.assert_allclose(r_so["energies"], r_sp["energies"], rtol=0, atol=1e-14)
+    assert abs(r_so["e_corr"] - ref["e_corr"]) < 1e-10
+
+
+def test_spin_orbital_input_rejects_open_shell_integrals():
+    from oracle.ccsd_spinorb import spin_orbital_integrals
+    o, v = 2, 3
+    eri = syn.eri_from_df(syn.df_factors(o + v, 10, 9, sigma=0.3))
+    g = spin_orbital_integrals(eri)
+    g[0::2, 0::2, 0::2, 0::2] *= 1.1      # alpha-alpha block no longer (pr|qs) - (ps|qr)
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve(np.diag(syn.orbital_energies(o, v, 9)), o, so_eri=g)
+    assert ei.value.code == -1 and "closed-shell" in str(ei.value)
