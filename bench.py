@@ -224,12 +224,15 @@ def measure_extras(cg, fock, df, o, precision):
         so, sv = int(rng.integers(4, 13)), int(rng.integers(20, 81))
         f_k, b_k = cg.make_synthetic(so, sv, 3 * (so + sv) // 2, 1000 + k)
         systems.append(dict(fock=f_k, nocc=so, df=b_k))
-    with cg.Batch(systems, energy_tol=1e-10) as b:
-        b.solve(amplitudes=False)                     # autotunes and captures the graphs
-        t0 = time.perf_counter()
-        rb = b.solve(amplitudes=False)
-        tb = time.perf_counter() - t0
-        rep = b.report()
+    def timed_batch(prec):
+        with cg.Batch(systems, energy_tol=1e-10, precision=prec) as b:
+            b.solve(amplitudes=False)                 # autotunes, splits constants, captures the graphs
+            t0 = time.perf_counter()
+            res = b.solve(amplitudes=False)
+            return res, time.perf_counter() - t0, b.report()
+
+    rb, tb, rep = timed_batch("fp64")
+    rs, ts3, rep3 = timed_batch(precision)
     solvers = [cg.Solver(**sy, energy_tol=1e-10) for sy in systems]
     for sv_ in solvers:
         sv_.solve(amplitudes=False)
@@ -240,10 +243,14 @@ def measure_extras(cg, fock, df, o, precision):
     for sv_ in solvers:
         sv_.close()
     flops = sum(x["flops_per_update"] * x["iterations"] for x in rb)
-    out["batch_c4"] = dict(workload="64 synthetic systems, nocc in [4,12], nvir in [20,80], tol 1e-10, FP64",
-                           batched_s=tb, sequential_s=ts, speedup=ts / tb,
+    nsplit = sum(1 for op in rep3["ops"] if op["kind"] == "contraction" and op.get("path") == "split")
+    out["batch_c4"] = dict(workload="64 synthetic systems, nocc in [4,12], nvir in [20,80], tol 1e-10",
+                           batched_fp64_s=tb, sequential_fp64_s=ts, speedup_fp64=ts / tb,
+                           batched_split_s=ts3, split_precision=precision, speedup_split_vs_sequential=ts / ts3,
+                           split_contraction_sites=nsplit,
+                           max_abs_dE_split_vs_fp64=max(abs(x["e_corr"] - y["e_corr"]) for x, y in zip(rs, rb)),
                            system_updates=sum(x["iterations"] for x in rb),
-                           algorithmic_tflops=flops / tb / 1e12,
+                           algorithmic_tflops_fp64=flops / tb / 1e12, algorithmic_tflops_split=flops / ts3 / 1e12,
                            launches_per_update=rep["launches_per_update"])
     return out
 

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 
 namespace ccsd {
 
@@ -76,8 +77,6 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         cudaGetLastError();
         throw Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
     }
-    if (opts.precision != CCSD_PREC_FP64)
-        throw Error(CCSD_ERR_UNSUPPORTED, "the batched solve runs the FP64 contraction path (precision must be FP64)");
     opt_ = opts;
     if (opts.stream) {
         st_ = (cudaStream_t)opts.stream;
@@ -102,6 +101,8 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         CCSD_CUDA(cudaMallocHost(&h_e_, sizeof(double) * n));
         CCSD_CUDA(cudaMallocHost(&h_n2_, sizeof(double) * n));
         CCSD_CUDA(cudaMallocHost(&h_active_, sizeof(int) * n));
+        CCSD_CUDA(cudaMalloc(&d_err_, sizeof(int)));
+        CCSD_CUDA(cudaMemset(d_err_, 0, sizeof(int)));
         record();
     } catch (...) {
         release();
@@ -128,6 +129,10 @@ void Batch::release() {
     if (e_dev_) cudaFree(e_dev_);
     if (n2_dev_) cudaFree(n2_dev_);
     if (ws_) cudaFree(ws_);
+    for (Pack &P : packs_) packed_split_free(P.buf);
+    packs_.clear();
+    if (d_err_) cudaFree(d_err_);
+    d_err_ = nullptr;
     if (h_e_) cudaFreeHost(h_e_);
     if (h_n2_) cudaFreeHost(h_n2_);
     if (h_active_) cudaFreeHost(h_active_);
@@ -266,6 +271,11 @@ void Batch::build_ops() {
         GOp &op = ops_[k];
         switch (op.kind) {
             case TapeOp::Gemm: {
+                std::vector<GroupedSplitPart> sparts;
+                if (opt_.precision != CCSD_PREC_FP64 && plan_split(op, k, sparts)) {
+                    op.off = append(blob_, sparts);
+                    break;
+                }
                 std::vector<GGemm> parts(n);
                 for (int s = 0; s < n; ++s) {
                     const TapeOp &t = tapes_[s][k];
@@ -393,6 +403,7 @@ void Batch::build_ops() {
         dot[s].n = (long long)nT2;
         dot[s].sys = s;
     }
+    for (size_t i = 0; i < packs_.size(); ++i) packs_[i].off = append(blob_, pack_parts_[i]);
     upd_off_ = append(blob_, upd);
     cp1_off_ = append(blob_, cp1);
     cp2_off_ = append(blob_, cp2);
@@ -410,13 +421,115 @@ void Batch::build_ops() {
         CCSD_CUDA(cudaMalloc(&ws_, sizeof(double) * need_ws));
         ws_elems_ = need_ws;
     }
+    // operands over constant integrals are split once, here
+    for (Pack &P : packs_)
+        if (P.key > 0)
+            grouped_split_operand_launch(P.buf, reinterpret_cast<const GroupedSplitOperandPart *>(desc_ + P.off), n,
+                                         P.max_rows, P.max_kpad, P.rowc, active_, st_);
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+}
+
+// A contraction whose largest system has M N K >= 1e7 runs on the tensor
+// cores: operands split into packed buffers (rows and K padded with zeros, so
+// small systems need no minimum size), one grouped tcgen05 launch.  The
+// orientation (A/B swap) follows the single-system rule for the first system.
+bool Batch::plan_split(GOp &op, size_t k, std::vector<GroupedSplitPart> &sp) {
+    const int n = size();
+    long long maxmnk = 0;
+    for (int s = 0; s < n; ++s) {
+        const TapeOp &t = tapes_[s][k];
+        if (t.M < 1 || t.N < 1 || t.K < 1) return false;
+        maxmnk = std::max(maxmnk, (long long)t.M * t.N * t.K);
+    }
+    if (maxmnk < 10000000ll) return false;
+    const TapeOp &t0 = tapes_[0][k];
+    const bool swap = SplitEngine::prefer_swap(t0.M, t0.N, t0.C);
+    std::vector<GroupedSplitOperandPart> pa(n), pb(n);
+    int kmax = 0, nmax = 0;
+    for (int s = 0; s < n; ++s) {
+        const TapeOp &t = tapes_[s][k];
+        pa[s].v = swap ? t.B : t.A;
+        pa[s].rows = swap ? t.N : t.M;
+        pb[s].v = swap ? t.A : t.B;
+        pb[s].rows = swap ? t.M : t.N;
+        pa[s].K = pb[s].K = t.K;
+        pa[s].sys = pb[s].sys = s;
+        kmax = std::max(kmax, t.K);
+        nmax = std::max(nmax, pb[s].rows);
+    }
+    const int pitch = (kmax + 31) / 32 * 32;
+    op.packA = pack_for(swap ? t0.key_b : t0.key_a, pa, pitch);
+    op.packB = pack_for(swap ? t0.key_a : t0.key_b, pb, pitch);
+    op.bn = grouped_split_bn(nmax);
+    sp.assign(n, GroupedSplitPart());
+    int tiles = 0;
+    for (int s = 0; s < n; ++s) {
+        const TapeOp &t = tapes_[s][k];
+        GroupedSplitPart &g = sp[s];
+        g.C = swap ? OutView{t.C.p, t.C.col, t.C.row} : t.C;
+        g.alpha = t.alpha;
+        g.beta = t.beta;
+        g.M = pa[s].rows;
+        g.N = pb[s].rows;
+        g.nkb = (t.K + 31) / 32;
+        g.rowA0 = pack_parts_[op.packA][s].row0;
+        g.rowB0 = pack_parts_[op.packB][s].row0;
+        g.scaleA = packs_[op.packA].buf.scale + g.rowA0;
+        g.scaleB = packs_[op.packB].buf.scale + g.rowB0;
+        g.tiles_m = (g.M + 127) / 128;
+        g.tiles_n = (g.N + op.bn - 1) / op.bn;
+        g.tile_begin = tiles;
+        g.sys = s;
+        tiles += g.tiles_m * g.tiles_n;
+    }
+    op.total_tiles = tiles;
+    op.split = true;
+    return true;
+}
+
+// The packed buffer of one operand view; views with the same nonzero split-cache
+// key (the same tensor view in every system) share one buffer.
+int Batch::pack_for(int key, const std::vector<GroupedSplitOperandPart> &parts, int pitch) {
+    if (key != 0)
+        for (size_t i = 0; i < packs_.size(); ++i)
+            if (packs_[i].key == key && packs_[i].buf.kpad == pitch) return (int)i;
+    std::vector<GroupedSplitOperandPart> pp = parts;
+    int rows = 0, max_rows = 0;
+    for (GroupedSplitOperandPart &g : pp) {
+        g.row0 = rows;
+        rows += (g.rows + 127) / 128 * 128;
+        max_rows = std::max(max_rows, g.rows);
+    }
+    Pack P;
+    P.key = key;
+    P.max_rows = max_rows;
+    P.max_kpad = pitch;
+    P.rowc = pp[0].v.row.s2 == 1 && pp[0].v.col.s2 != 1;
+    packed_split_alloc(P.buf, rows, pitch, opt_.precision);
+    packs_.push_back(P);
+    pack_parts_.push_back(pp);
+    return (int)packs_.size() - 1;
 }
 
 void Batch::launch_op(const GOp &op) {
     const int n = size();
     switch (op.kind) {
         case TapeOp::Gemm:
-            launch_grouped_gemm(op.plan, reinterpret_cast<const GGemm *>(desc_ + op.off), n, active_, ws_, st_);
+            if (op.split) {
+                for (int pk : {op.packA, op.packB}) {
+                    Pack &P = packs_[pk];
+                    if (P.key > 0) continue;  // constant: split once at set-up
+                    if (P.key < 0 && split_done_.count(P.key)) continue;  // shared, already split this update
+                    grouped_split_operand_launch(P.buf, reinterpret_cast<const GroupedSplitOperandPart *>(desc_ + P.off),
+                                                 n, P.max_rows, P.max_kpad, P.rowc, active_, st_);
+                    if (P.key < 0) split_done_.insert(P.key);
+                }
+                grouped_split_gemm_launch(packs_[op.packA].buf, packs_[op.packB].buf, op.bn,
+                                          reinterpret_cast<const GroupedSplitPart *>(desc_ + op.off), n, op.total_tiles,
+                                          active_, d_err_, st_);
+            } else {
+                launch_grouped_gemm(op.plan, reinterpret_cast<const GGemm *>(desc_ + op.off), n, active_, ws_, st_);
+            }
             break;
         case TapeOp::Axpby:
         case TapeOp::Copy:
@@ -448,6 +561,7 @@ void Batch::capture() {
         CCSD_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         try {
             if (g == 0) {
+                split_done_.clear();
                 for (const GOp &op : ops_) launch_op(op);
                 launch_grouped_update(reinterpret_cast<const GUpdate *>(desc_ + upd_off_), n, active_, partials_, st_);
                 launch_grouped_sum(n, active_, partials_, n2_dev_, st_);
@@ -559,6 +673,11 @@ void Batch::solve(ccsd_result *res) {
     }
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
+    {
+        int err = 0;
+        CCSD_CUDA(cudaMemcpy(&err, d_err_, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) throw Error(CCSD_ERR_TIMEOUT, "split-precision kernel reported a bounded-wait timeout");
+    }
 
     int first_bad = -1;
     for (int s = 0; s < n; ++s) {
@@ -597,7 +716,12 @@ std::string Batch::report() const {
                            : op.kind == TapeOp::TauSym ? "tau_pairs"
                            : op.kind == TapeOp::Unpack ? "ladder_unpack"
                                                        : "w_pairs";
-        if (op.kind == TapeOp::Gemm)
+        if (op.kind == TapeOp::Gemm && op.split)
+            std::snprintf(buf, sizeof buf,
+                          "%s{\"op\": %zu, \"kind\": \"%s\", \"site\": \"%s\", \"path\": \"split\", "
+                          "\"bn\": %d, \"tiles\": %d}",
+                          first ? "" : ", ", k, kind, op.site ? op.site : "", op.bn, op.total_tiles);
+        else if (op.kind == TapeOp::Gemm)
             std::snprintf(buf, sizeof buf,
                           "%s{\"op\": %zu, \"kind\": \"%s\", \"site\": \"%s\", \"path\": \"%s\", \"tile\": \"%s\", "
                           "\"target\": %d, \"items\": %d, \"grid\": %d, \"candidates\": %d, \"cached\": %s, "

@@ -4,11 +4,13 @@
 #pragma once
 
 #include <memory>
+#include <set>
 #include <string>
 #include <vector>
 
 #include "engine.h"
 #include "grouped.h"
+#include "split_gemm.h"
 
 namespace ccsd {
 
@@ -38,10 +40,23 @@ class Batch {
         GGemmPlan plan;          // contractions
         double tuned_ms = 0.0;   // best autotuned time
         int candidates = 0;
+        // split-precision contraction on the tensor cores (packed operands)
+        bool split = false;
+        int packA = -1, packB = -1, bn = 0, total_tiles = 0;
+    };
+    // one packed split operand (all systems' rows of one operand view)
+    struct Pack {
+        PackedSplit buf;
+        size_t off = 0;      // GroupedSplitOperandPart[] in desc_
+        int key = 0;         // split-cache key of the view (> 0 constant, < 0 per update, 0 private)
+        int max_rows = 0, max_kpad = 0;
+        bool rowc = false;
     };
 
     void record();
     void build_ops();
+    bool plan_split(GOp &op, size_t k, std::vector<GroupedSplitPart> &parts);
+    int pack_for(int key, const std::vector<GroupedSplitOperandPart> &parts, int pitch);
     void tune(GOp &op, std::vector<GGemm> &parts);
     void capture();
     void launch_op(const GOp &op);
@@ -56,6 +71,10 @@ class Batch {
 
     std::vector<std::vector<TapeOp>> tapes_;
     std::vector<GOp> ops_;
+    std::vector<Pack> packs_;
+    std::vector<std::vector<GroupedSplitOperandPart>> pack_parts_;  // host copies until the upload
+    int *d_err_ = nullptr;  // split kernels' bounded-wait error word
+    std::set<int> split_done_;  // per-update shared packs already split in the graph being captured
     std::vector<char> blob_;   // host copy of every descriptor array
     char *desc_ = nullptr;     // device copy
     size_t upd_off_ = 0, cp1_off_ = 0, cp2_off_ = 0, tau_off_ = 0, dot_off_ = 0;

@@ -56,13 +56,101 @@ struct alignas(8) Bars {
     int never;  // stays 0: a wait that must not be cut short by another role
 };
 
+}  // namespace
+
+// What one CTA computes: a 128 x BN output tile of one contraction.  Rows of
+// the tile's A (B) operand start at plane row rowA0 + mt*128 (rowB0 + nt*BN).
+struct TileJob {
+    int rowA0, rowB0;    // first plane row of the contraction's A / B operand
+    int mt, nt;          // tile indices
+    int M, N;            // C bounds
+    int kb0, nkb;        // k-block range (32 K elements per block)
+    const double *scaleA, *scaleB;  // row scales, indexed by the C row / column
+    double alpha, beta;
+    OutView C;
+    double *wsz;  // split-K: partial-sum slab [M][N], else null (write C)
+    bool run;
+};
+
+// One contraction over the whole grid (grouped rasterisation, split-K over z).
+struct SingleJobs {
+    int M, N, tiles_m, tiles_n, nkb_total, kb_per_split;
+    const double *scaleA, *scaleB;
+    double alpha, beta;
+    OutView C;
+    double *ws;
+    __device__ TileJob job() const {
+        TileJob J;
+        // Grouped rasterisation: consecutive CTAs walk kGroupM row tiles across
+        // all column tiles, so the CTAs resident together share A and B tiles in L2.
+        const int t = blockIdx.x;
+        const int group = kGroupM * tiles_n;
+        const int g = t / group, first_m = g * kGroupM;
+        const int gm = min(tiles_m - first_m, kGroupM);
+        const int local = t - g * group;
+        J.mt = first_m + local % gm;
+        J.nt = local / gm;
+        J.rowA0 = J.rowB0 = 0;
+        J.M = M;
+        J.N = N;
+        J.kb0 = blockIdx.z * kb_per_split;
+        J.nkb = min(nkb_total, J.kb0 + kb_per_split) - J.kb0;
+        J.scaleA = scaleA;
+        J.scaleB = scaleB;
+        J.alpha = alpha;
+        J.beta = beta;
+        J.C = C;
+        J.wsz = gridDim.z == 1 ? nullptr : ws + (size_t)blockIdx.z * M * N;
+        J.run = true;
+        return J;
+    }
+};
+
+// Many systems' shares of one contraction (batched solve): part p's rows sit
+// at rowA0 / rowB0 of packed plane buffers with a common row pitch; a CTA
+// finds its part by binary search over the parts' first tiles.
+struct GroupedJobs {
+    const GroupedSplitPart *parts;
+    int nparts;
+    const int *active;
+    __device__ TileJob job() const {
+        TileJob J;
+        const int t = blockIdx.x;
+        int lo = 0, hi = nparts - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (parts[mid].tile_begin <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const GroupedSplitPart &P = parts[lo];
+        J.run = active[P.sys] != 0;
+        const int local = t - P.tile_begin;
+        J.mt = local % P.tiles_m;
+        J.nt = local / P.tiles_m;
+        J.rowA0 = P.rowA0;
+        J.rowB0 = P.rowB0;
+        J.M = P.M;
+        J.N = P.N;
+        J.kb0 = 0;
+        J.nkb = P.nkb;
+        J.scaleA = P.scaleA;
+        J.scaleB = P.scaleB;
+        J.alpha = P.alpha;
+        J.beta = P.beta;
+        J.C = P.C;
+        J.wsz = nullptr;
+        return J;
+    }
+};
+
+namespace {
+
 // NSTF: pipeline stages (0 = as many as fit one CTA per SM); MINB: CTAs per SM.
-template <int S, int BN, int NSTF, int MINB>
+// Jobs: SingleJobs (one contraction) or GroupedJobs (one per system).
+template <int S, int BN, int NSTF, int MINB, class Jobs>
 __global__ void __launch_bounds__(kThreads, MINB)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      int M, int N, int tiles_m, int tiles_n, int rowsA_pad, int rowsB_pad, int nkb_total,
-                      int kb_per_split, const double *__restrict__ scaleA, const double *__restrict__ scaleB,
-                      double alpha, double beta, OutView C, double *ws, int *gerr) {
+                      int rowsA_pad, int rowsB_pad, const Jobs jobs, int *gerr) {
     constexpr int NST = NSTF > 0 ? NSTF : num_stages(S, BN);
     constexpr int SB = stage_bytes(S, BN);
     constexpr int A_TILE = BM * BK * 2;   // bytes per A plane tile
@@ -70,28 +158,23 @@ __global__ void __launch_bounds__(kThreads, MINB)
     constexpr uint32_t IDESC = ptx::idesc_bf16_f32(BM, BN);
     constexpr int NCOLS = tmem_cols(BN);
 
+    const TileJob J = jobs.job();
+    if (!J.run) return;  // a stopped system: the whole CTA leaves before any set-up
+
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     Bars *bars = (Bars *)(smem + NST * SB);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // Grouped rasterisation: consecutive CTAs walk kGroupM row tiles across
-    // all column tiles, so the CTAs resident together share A and B tiles in L2.
-    int mt, nt;
-    {
-        const int t = blockIdx.x;
-        const int group = kGroupM * tiles_n;
-        const int g = t / group, first_m = g * kGroupM;
-        const int gm = min(tiles_m - first_m, kGroupM);
-        const int local = t - g * group;
-        mt = first_m + local % gm;
-        nt = local / gm;
-    }
-    const int m0 = mt * BM, n0 = nt * BN;
-    const int kb0 = blockIdx.z * kb_per_split;
-    const int kb1 = min(nkb_total, kb0 + kb_per_split);
-    const int nkb = kb1 - kb0;
+    const int m0 = J.mt * BM, n0 = J.nt * BN, M = J.M, N = J.N;
+    const int tma_m0 = J.rowA0 + m0, tma_n0 = J.rowB0 + n0;
+    const int kb0 = J.kb0;
+    const int nkb = J.nkb;
     const int nch = (nkb + CHUNK_KB - 1) / CHUNK_KB;
+    const double *__restrict__ scaleA = J.scaleA;
+    const double *__restrict__ scaleB = J.scaleB;
+    const double alpha = J.alpha, beta = J.beta;
+    const OutView C = J.C;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -132,8 +215,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
                 const int kx = (kb0 + l) * BK;
 #pragma unroll
                 for (int p = 0; p < S; ++p) {
-                    ptx::tma_load_2d(sa + p * A_TILE, &tmA, &bars->full[st], kx, p * rowsA_pad + m0);
-                    ptx::tma_load_2d(sb + p * B_TILE, &tmB, &bars->full[st], kx, p * rowsB_pad + n0);
+                    ptx::tma_load_2d(sa + p * A_TILE, &tmA, &bars->full[st], kx, p * rowsA_pad + tma_m0);
+                    ptx::tma_load_2d(sb + p * B_TILE, &tmB, &bars->full[st], kx, p * rowsB_pad + tma_n0);
                 }
                 issued = l + 1;
             }
@@ -216,8 +299,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
             const bool mval = m < M;
             const double sa = mval ? scaleA[m] * 0x1.0p-14 : 0.0;
             const int64_t crow = mval ? dim_off(C.row, (uint32_t)m) : 0;
-            const bool direct = gridDim.z == 1;
-            double *wsz = ws + (size_t)blockIdx.z * M * N;
+            const bool direct = J.wsz == nullptr;
+            double *wsz = J.wsz;
 #pragma unroll
             for (int g = 0; g < BN / 32; ++g) {
                 uint32_t r[32];
@@ -278,11 +361,11 @@ __global__ void __launch_bounds__(kThreads, MINB)
 // [-128, 128].  Plane p stores d_p * 2^(-8p), exact in BF16.
 constexpr int kRowmaxKT = 32;  // 32-wide k tiles per row-max block
 
+// Row maxima of one 32-row x (32 kRowmaxKT)-column block, from row r0 and
+// column kbeg, merged into rmax with atomicMax (32 x 8 threads).
 template <bool ROWC>
-__global__ void rowmax_kernel(int rows, int K, int nkg, MatView v, unsigned long long *rmax) {
+__device__ void rowmax_block(int rows, int K, const MatView &v, unsigned long long *rmax, int r0, int kbeg) {
     const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-    const int r0 = (int)(blockIdx.x / nkg) * 32;
-    const int kbeg = (int)(blockIdx.x % nkg) * 32 * kRowmaxKT;
     const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
     if (ROWC) {
         // thread owns row r0 + tx; the 8 thread rows split the k range
@@ -327,6 +410,12 @@ __global__ void rowmax_kernel(int rows, int K, int nkg, MatView v, unsigned long
             if (tx == 0 && r < rows && m) atomicMax(rmax + r, m);
         }
     }
+    __syncthreads();  // the shared row maxima are reused by the next block of a looping caller
+}
+
+template <bool ROWC>
+__global__ void rowmax_kernel(int rows, int K, int nkg, MatView v, unsigned long long *rmax) {
+    rowmax_block<ROWC>(rows, K, v, rmax, (int)(blockIdx.x / nkg) * 32, (int)(blockIdx.x % nkg) * 32 * kRowmaxKT);
 }
 
 template <bool ROWC>
@@ -347,15 +436,16 @@ __device__ __forceinline__ void load_tile(double (&t)[32][33], int rows, int K, 
     }
 }
 
+// Digits of one 32 x 32 block from row r0 and column k0.  Rows below rows_pad
+// and columns below kpad are written (zeros past rows / K); row r of plane p
+// sits at planes + p * plane + r * pitch.
 template <int S, bool ROWC>
-__global__ void split_planes_kernel(int rows, int rows_pad, int K, int kpad, int nkt, MatView v,
-                                    const unsigned long long *rmax, __nv_bfloat16 *planes, double *scale) {
+__device__ void planes_block(int rows, int rows_pad, int K, int kpad, int64_t pitch, size_t plane, const MatView &v,
+                             const unsigned long long *rmax, __nv_bfloat16 *planes, double *scale, int r0, int k0) {
     __shared__ double t[32][33];
-    const int k0 = (int)(blockIdx.x % nkt) * 32, r0 = (int)(blockIdx.x / nkt) * 32;
     load_tile<ROWC>(t, rows, K, v, r0, k0);
     __syncthreads();
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const size_t plane = (size_t)rows_pad * kpad;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int a = ty + 8 * j;
@@ -373,7 +463,7 @@ __global__ void split_planes_kernel(int rows, int rows_pad, int K, int kpad, int
             Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
             if (bits >> 63) Y = -Y;
         }
-        __nv_bfloat16 *dst = planes + (size_t)r * kpad + k;
+        __nv_bfloat16 *dst = planes + (size_t)r * pitch + k;
 #pragma unroll
         for (int p = S - 1; p >= 1; --p) {
             const long long d = ((Y + 128) & 255) - 128;
@@ -382,7 +472,42 @@ __global__ void split_planes_kernel(int rows, int rows_pad, int K, int kpad, int
         }
         dst[0] = __float2bfloat16_rn((float)Y);
     }
+    __syncthreads();  // t is reused by the next block of a looping caller
 }
+
+template <int S, bool ROWC>
+__global__ void split_planes_kernel(int rows, int rows_pad, int K, int kpad, int nkt, MatView v,
+                                    const unsigned long long *rmax, __nv_bfloat16 *planes, double *scale) {
+    planes_block<S, ROWC>(rows, rows_pad, K, kpad, kpad, (size_t)rows_pad * kpad, v, rmax, planes, scale,
+                          (int)(blockIdx.x / nkt) * 32, (int)(blockIdx.x % nkt) * 32);
+}
+
+// Grouped forms (batched solve): blockIdx.y = part; each part's rows go to
+// packed rows row0.. of the shared planes (row pitch = the packed kpad).
+template <bool ROWC>
+__global__ void grouped_rowmax_kernel(const GroupedSplitOperandPart *parts, const int *active,
+                                      unsigned long long *rmax) {
+    const GroupedSplitOperandPart &P = parts[blockIdx.y];
+    if (!active[P.sys]) return;
+    const int nkg = (P.K + 32 * kRowmaxKT - 1) / (32 * kRowmaxKT);
+    const int nblocks = (P.rows + 31) / 32 * nkg;
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x)
+        rowmax_block<ROWC>(P.rows, P.K, P.v, rmax + P.row0, (b / nkg) * 32, (b % nkg) * 32 * kRowmaxKT);
+}
+
+template <int S, bool ROWC>
+__global__ void grouped_planes_kernel(const GroupedSplitOperandPart *parts, const int *active, int total_rows,
+                                      int pitch, const unsigned long long *rmax, __nv_bfloat16 *planes,
+                                      double *scale) {
+    const GroupedSplitOperandPart &P = parts[blockIdx.y];
+    if (!active[P.sys]) return;
+    const int rows_pad = (P.rows + BM - 1) / BM * BM, kpad = (P.K + BK - 1) / BK * BK;
+    const int nkt = kpad / 32, nblocks = rows_pad / 32 * nkt;
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x)
+        planes_block<S, ROWC>(P.rows, rows_pad, P.K, kpad, pitch, (size_t)total_rows * pitch, P.v, rmax + P.row0,
+                              planes + (size_t)P.row0 * pitch, scale + P.row0, (b / nkt) * 32, (b % nkt) * 32);
+}
+
 __global__ void splitk_reduce(int M, int N, int splits, double alpha, const double *ws, double beta,
                               OutView C) {
     const size_t total = (size_t)M * N;
@@ -410,32 +535,47 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-void encode(CUtensorMap *map, const SplitOperand &op, int box_rows) {
-    cuuint64_t gdim[2] = {(cuuint64_t)op.kpad, (cuuint64_t)op.nslices * op.rows_pad};
-    cuuint64_t gstride[1] = {(cuuint64_t)op.kpad * 2};
+void encode_raw(CUtensorMap *map, void *planes, int kpad, int nslices, int rows, int box_rows) {
+    cuuint64_t gdim[2] = {(cuuint64_t)kpad, (cuuint64_t)nslices * rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)kpad * 2};
     cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
     cuuint32_t estride[2] = {1, 1};
-    CUresult r = get_encode()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, op.planes, gdim, gstride, box, estride,
+    CUresult r = get_encode()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, planes, gdim, gstride, box, estride,
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int S, int BN, int NSTF = 0, int MINB = 1>
-void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
-              const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+void encode(CUtensorMap *map, const SplitOperand &op, int box_rows) {
+    encode_raw(map, op.planes, op.kpad, op.nslices, op.rows_pad, box_rows);
+}
+
+template <int S, int BN, int NSTF, int MINB>
+constexpr size_t kernel_smem() {
     constexpr int NST = NSTF > 0 ? NSTF : num_stages(S, BN);
     // two-per-SM variants request at least 80 KB so that no third CTA (and its
     // TMEM allocation) can become resident on the SM
-    constexpr size_t smem_need = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
-    constexpr size_t smem = (MINB > 1 && smem_need < 80 * 1024) ? 80 * 1024 : smem_need;
-    static_assert(MINB * smem <= 227 * 1024 && MINB * tmem_cols(BN) <= 512, "co-resident CTAs must fit");
+    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
+    return (MINB > 1 && need < 80 * 1024) ? 80 * 1024 : need;
+}
+
+template <int S, int BN, int NSTF, int MINB, class Jobs>
+void set_smem_attr() {
     static bool attr = false;
     if (!attr) {
-        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S, BN, NSTF, MINB>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_kernel<S, BN, NSTF, MINB, Jobs>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kernel_smem<S, BN, NSTF, MINB>()));
         attr = true;
     }
+}
+
+template <int S, int BN, int NSTF = 0, int MINB = 1>
+void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+              const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+    constexpr size_t smem = kernel_smem<S, BN, NSTF, MINB>();
+    static_assert(MINB * smem <= 227 * 1024 && MINB * tmem_cols(BN) <= 512, "co-resident CTAs must fit");
+    set_smem_attr<S, BN, NSTF, MINB, SingleJobs>();
     alignas(64) CUtensorMap ta, tb;
     encode(&ta, A, BM);
     encode(&tb, B, BN);
@@ -452,9 +592,21 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     int kbps = (nkb + splits - 1) / splits;
     splits = (nkb + kbps - 1) / kbps;
     dim3 grid((unsigned)(tiles_m * tiles_n), 1, splits);
-    // lanes along n when the output is contiguous in n (and for the row-major split-K partials)
-    split_gemm_kernel<S, BN, NSTF, MINB><<<grid, kThreads, smem, st>>>(
-        ta, tb, M, N, tiles_m, tiles_n, A.rows_pad, B.rows_pad, nkb, kbps, A.scale, B.scale, alpha, beta, C, ws, d_err);
+    SingleJobs jobs;
+    jobs.M = M;
+    jobs.N = N;
+    jobs.tiles_m = tiles_m;
+    jobs.tiles_n = tiles_n;
+    jobs.nkb_total = nkb;
+    jobs.kb_per_split = kbps;
+    jobs.scaleA = A.scale;
+    jobs.scaleB = B.scale;
+    jobs.alpha = alpha;
+    jobs.beta = beta;
+    jobs.C = C;
+    jobs.ws = ws;
+    split_gemm_kernel<S, BN, NSTF, MINB, SingleJobs><<<grid, kThreads, smem, st>>>(ta, tb, A.rows_pad, B.rows_pad,
+                                                                                 jobs, d_err);
     CCSD_LAUNCH_CHECK();
     if (splits > 1) {
         const size_t total = (size_t)M * N;
@@ -505,7 +657,106 @@ void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     }
 }
 
+template <int S, int BN>
+void launch_grouped(const PackedSplit &A, const PackedSplit &B, const GroupedSplitPart *d_parts, int nparts,
+                    int total_tiles, const int *active, int *d_err, cudaStream_t st) {
+    constexpr size_t smem = kernel_smem<S, BN, 0, 1>();
+    set_smem_attr<S, BN, 0, 1, GroupedJobs>();
+    alignas(64) CUtensorMap ta, tb;
+    encode_raw(&ta, A.planes, A.kpad, A.nslices, A.rows, BM);
+    encode_raw(&tb, B.planes, B.kpad, B.nslices, B.rows, BN);
+    GroupedJobs jobs;
+    jobs.parts = d_parts;
+    jobs.nparts = nparts;
+    jobs.active = active;
+    split_gemm_kernel<S, BN, 0, 1, GroupedJobs><<<total_tiles, kThreads, smem, st>>>(ta, tb, A.rows, B.rows, jobs,
+                                                                                   d_err);
+    CCSD_LAUNCH_CHECK();
+}
+
 }  // namespace
+
+// ---------------------------------------------------------------------------
+void packed_split_alloc(PackedSplit &op, int rows, int kpad, int nslices) {
+    packed_split_free(op);
+    const size_t bytes = (size_t)nslices * rows * kpad * 2;
+    cudaError_t e = cudaMalloc(&op.planes, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        op.planes = nullptr;
+        throw Error(-3, "packed split planes: cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    CCSD_CUDA(cudaMemset(op.planes, 0, bytes));
+    CCSD_CUDA(cudaMalloc(&op.scale, sizeof(double) * rows));
+    CCSD_CUDA(cudaMalloc(&op.rmax, sizeof(unsigned long long) * rows));
+    op.rows = rows;
+    op.kpad = kpad;
+    op.nslices = nslices;
+    op.bytes = bytes;
+}
+
+void packed_split_free(PackedSplit &op) {
+    if (op.planes) cudaFree(op.planes);
+    if (op.scale) cudaFree(op.scale);
+    if (op.rmax) cudaFree(op.rmax);
+    op = PackedSplit();
+}
+
+void grouped_split_operand_launch(PackedSplit &op, const GroupedSplitOperandPart *d_parts, int nparts,
+                                  int max_rows, int max_kpad, bool rowc, const int *active, cudaStream_t st) {
+    if (nparts <= 0) return;
+    const dim3 thr(32, 8);
+    CCSD_CUDA(cudaMemsetAsync(op.rmax, 0, sizeof(unsigned long long) * op.rows, st));
+    const int nkg = (max_kpad + 32 * kRowmaxKT - 1) / (32 * kRowmaxKT);
+    const int rblocks = std::max(1, std::min(1024, (max_rows + 31) / 32 * nkg));
+    const int pblocks = std::max(1, std::min(4096, (max_rows + BM - 1) / BM * (BM / 32) * (max_kpad / 32)));
+    if (rowc)
+        grouped_rowmax_kernel<true><<<dim3(rblocks, nparts), thr, 0, st>>>(d_parts, active, op.rmax);
+    else
+        grouped_rowmax_kernel<false><<<dim3(rblocks, nparts), thr, 0, st>>>(d_parts, active, op.rmax);
+    CCSD_LAUNCH_CHECK();
+    __nv_bfloat16 *pl = (__nv_bfloat16 *)op.planes;
+#define CCSD_GSPLIT_CASE(S_)                                                                                     \
+    case S_:                                                                                                     \
+        if (rowc)                                                                                                \
+            grouped_planes_kernel<S_, true><<<dim3(pblocks, nparts), thr, 0, st>>>(d_parts, active, op.rows,    \
+                                                                                   op.kpad, op.rmax, pl, op.scale); \
+        else                                                                                                     \
+            grouped_planes_kernel<S_, false><<<dim3(pblocks, nparts), thr, 0, st>>>(d_parts, active, op.rows,   \
+                                                                                    op.kpad, op.rmax, pl, op.scale); \
+        break;
+    switch (op.nslices) {
+        CCSD_GSPLIT_CASE(2)
+        CCSD_GSPLIT_CASE(3)
+        CCSD_GSPLIT_CASE(4)
+        default: throw Error(-1, "nslices must be 2, 3 or 4");
+    }
+#undef CCSD_GSPLIT_CASE
+    CCSD_LAUNCH_CHECK();
+}
+
+int grouped_split_bn(int max_n) { return max_n <= 64 ? 64 : 128; }
+
+void grouped_split_gemm_launch(const PackedSplit &A, const PackedSplit &B, int bn, const GroupedSplitPart *d_parts,
+                               int nparts, int total_tiles, const int *active, int *d_err, cudaStream_t st) {
+    if (nparts <= 0 || total_tiles <= 0) return;
+    if (A.kpad != B.kpad || A.nslices != B.nslices) throw Error(-1, "grouped split operands disagree");
+    if (bn != 64 && bn != 128) throw Error(-1, "grouped split tile width must be 64 or 128");
+#define CCSD_GGEMM_CASE(S_)                                                                                 \
+    case S_:                                                                                                \
+        if (bn == 64)                                                                                       \
+            launch_grouped<S_, 64>(A, B, d_parts, nparts, total_tiles, active, d_err, st);                  \
+        else                                                                                                \
+            launch_grouped<S_, 128>(A, B, d_parts, nparts, total_tiles, active, d_err, st);                 \
+        break;
+    switch (A.nslices) {
+        CCSD_GGEMM_CASE(2)
+        CCSD_GGEMM_CASE(3)
+        CCSD_GGEMM_CASE(4)
+        default: throw Error(-1, "nslices must be 2, 3 or 4");
+    }
+#undef CCSD_GGEMM_CASE
+}
 
 // ---------------------------------------------------------------------------
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st) {

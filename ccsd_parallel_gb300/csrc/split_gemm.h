@@ -86,6 +86,42 @@ class SplitEngine {
     size_t ws_elems_ = 0;
 };
 
+// ---- grouped split contractions (batched solve) -------------------------------
+// Many systems' operands of one contraction, split into one packed buffer:
+// part p's rows occupy rows row0 .. row0 + roundup(rows, 128) of every plane,
+// all with the same row pitch kpad (>= every part's K rounded up to 32).
+struct PackedSplit {
+    void *planes = nullptr;  // __nv_bfloat16*, [nslices][rows][kpad]
+    double *scale = nullptr;
+    unsigned long long *rmax = nullptr;
+    int rows = 0, kpad = 0, nslices = 0;
+    size_t bytes = 0;
+};
+void packed_split_alloc(PackedSplit &op, int rows, int kpad, int nslices);
+void packed_split_free(PackedSplit &op);
+
+struct GroupedSplitOperandPart {  // one system's operand view
+    MatView v;
+    int rows = 0, K = 0, row0 = 0, sys = 0;
+};
+// Split every active part into `op` (rowmax, then digits); rowc: the views'
+// row index is the contiguous one.
+void grouped_split_operand_launch(PackedSplit &op, const GroupedSplitOperandPart *d_parts, int nparts,
+                                  int max_rows, int max_kpad, bool rowc, const int *active, cudaStream_t st);
+
+struct GroupedSplitPart {  // one system's share of a grouped split contraction
+    OutView C;
+    const double *scaleA = nullptr, *scaleB = nullptr;  // at the part's first packed row
+    double alpha = 0.0, beta = 0.0;
+    int M = 0, N = 0, nkb = 0, rowA0 = 0, rowB0 = 0, tiles_m = 0, tiles_n = 0, tile_begin = 0, sys = 0;
+};
+// Column tile width of grouped launches (64 or 128) for the parts' largest N.
+int grouped_split_bn(int max_n);
+// C_p = alpha_p A_p B_p^T + beta_p C_p for every active part, one CTA per 128 x bn
+// tile (parts[].tile_begin: prefix of tiles_m * tiles_n); no split-K (K < 131072).
+void grouped_split_gemm_launch(const PackedSplit &A, const PackedSplit &B, int bn, const GroupedSplitPart *d_parts,
+                               int nparts, int total_tiles, const int *active, int *d_err, cudaStream_t st);
+
 // FP64 view -> split operand (S BF16 planes + row scales).
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st);
 // C = alpha * A B^T + beta C for split operands with equal kpad and nslices;

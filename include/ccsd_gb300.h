@@ -164,7 +164,9 @@ int ccsd_destroy(ccsd_handle *h);
  * on the batch's own shapes), and the update is replayed from a captured CUDA
  * graph.  Each system follows exactly the single-system rules of ccsd_solve
  * (MP2 start, its own |dE| stop, cap, DIIS); a stopped system is masked off
- * on the device and keeps its last iterate.  precision must be FP64.
+ * on the device and keeps its last iterate.  In split precision the larger
+ * contractions run as grouped tcgen05 launches over packed split operands;
+ * in FP64 on a persistent grouped DFMA kernel.
  * results[i] is filled like ccsd_solve's result (caller-provided t1/t2/
  * history arrays per system).  When a system diverges, every result is still
  * filled and the call returns CCSD_ERR_DIVERGED naming the first such system. */

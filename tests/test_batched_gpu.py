@@ -123,7 +123,27 @@ def test_divergent_system_reported_after_filling_the_rest():
     _compare([ei.value.results[0], ei.value.results[2]], singles)
 
 
-def test_batch_rejects_split_precision():
-    with pytest.raises(cg.CCSDError) as ei:
-        cg.solve_batched(_c4_systems(count=2), precision="split3")
-    assert ei.value.code == -7
+def test_split_batch_runs_contractions_on_tensor_cores():
+    """precision split3: the larger grouped contractions run as one grouped
+    tcgen05 launch over packed split operands; every system follows its own
+    split3 single-system solve (same updates, energies within 1e-9) and stays
+    within 1e-8 of the FP64 batch."""
+    rng = np.random.default_rng(13)
+    systems = []
+    for k in range(12):
+        o, v = int(rng.integers(6, 13)), int(rng.integers(40, 81))
+        fock, b = cg.make_synthetic(o, v, 3 * (o + v) // 2, 2000 + k)
+        systems.append(dict(fock=fock, nocc=o, df=b))
+    with cg.Batch(systems, precision="split3", energy_tol=1e-10) as bt:
+        rb = bt.solve()
+        rep = bt.report()
+    split_ops = [op for op in rep["ops"] if op["kind"] == "contraction" and op["path"] == "split"]
+    assert len(split_ops) >= 8, [op["site"] for op in split_ops]
+    assert {"pp_ladder_sym", "ring1"} <= {op["site"] for op in split_ops}
+    singles = [cg.solve(**s, precision="split3", energy_tol=1e-10) for s in systems]
+    fp64 = cg.solve_batched(systems, energy_tol=1e-10)
+    for k, (x, y, z) in enumerate(zip(rb, singles, fp64)):
+        assert x["iterations"] == y["iterations"], k
+        assert abs(x["e_corr"] - y["e_corr"]) < 1e-9, (k, x["e_corr"], y["e_corr"])
+        assert abs(x["e_corr"] - z["e_corr"]) < 1e-8, (k, x["e_corr"], z["e_corr"])
+        assert np.abs(x["t2"] - y["t2"]).max() < 1e-8
