@@ -13,6 +13,13 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
   antisymmetric copies)                                        ``ccsdt.cpp:625-727``
 * tau = t2 + t1 t1 - t1 t1                                     ``ccsdt.cpp:2603-2620``
 * MP2 initial T2, T1 = 0                                       ``ccsdt.cpp:172-192``
+* CCSDT-1a (``Method_Nr == 1``): T3 from the bare integrals and T2
+  (X1(b,c)(k,e) = <bc||ek>, X2(c,m)(j,k) = <mc||jk>)            ``ccsdt.cpp:1960-2042, 995-1290``
+  T3 -> T1: + 1/4 <jk||bc> t_ijk^abc                            ``ccsdt.cpp:419-434``
+  T3 -> T2: + 1/2 P(ab) <bk||cd> t_ijk^acd - 1/2 P(ij) <km||jc> t_ikm^abc
+                                                                ``ccsdt.cpp:640-670``
+  Each pass forms T1/T2 from the previous T3 and T3 from the previous T2
+  (``ccsdt.cpp:255-271``); T3 starts at zero.
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -56,8 +63,12 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 
 
 class SpinOrbitalCCSD:
-    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int):
-        """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial."""
+    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
+        """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
+        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a (the reference's Method_Nr)."""
+        if method not in (-1, 1):
+            raise ValueError("method must be -1 (CCSD1) or 1 (CCSDT-1a)")
+        self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
         self.O = 2 * nocc
@@ -117,8 +128,22 @@ class SpinOrbitalCCSD:
         ``ccsd_memory_optimized.cpp:646``."""
         return 0.25 * np.einsum("ijab,abij->", self.goovv, self.tau(t1, t2))
 
-    def update(self, t1, t2):
-        """One Jacobi pass: returns (t1_new, t2_new)."""
+    def triples(self, t2):
+        """CCSDT-1a T3 from T2 (``ccsdt.cpp:1016-1058`` with X1, X2 bare): t3[a,b,c,i,j,k] =
+        [P(a/bc) P(k/ij) sum_e <bc||ek> t2(a,e)(i,j) - P(c/ab) P(i/jk) sum_m <mc||jk> t2(a,b)(i,m)] / D3."""
+        A = np.einsum("bcek,aeij->abcijk", self.gvvvo, t2, **ES)
+        B = np.einsum("mcjk,abim->abcijk", self.govoo, t2, **ES)
+        PA = A - A.transpose(1, 0, 2, 3, 4, 5) - A.transpose(2, 1, 0, 3, 4, 5)     # P(a/bc)
+        PA = PA - PA.transpose(0, 1, 2, 5, 4, 3) - PA.transpose(0, 1, 2, 3, 5, 4)  # P(k/ij)
+        PB = B - B.transpose(2, 1, 0, 3, 4, 5) - B.transpose(0, 2, 1, 3, 4, 5)     # P(c/ab)
+        PB = PB - PB.transpose(0, 1, 2, 4, 3, 5) - PB.transpose(0, 1, 2, 5, 4, 3)  # P(i/jk)
+        d = self.den
+        D3 = (d[:, None, None, :, None, None] + d[None, :, None, None, :, None] + d[None, None, :, None, None, :])
+        return (PA - PB) / D3
+
+    def update(self, t1, t2, t3=None):
+        """One Jacobi pass: returns (t1_new, t2_new), or (t1_new, t2_new, t3_new)
+        for CCSDT-1a (T1/T2 from the given t3, T3 from the given t2)."""
         fs_vo, f_oo, f_vv = self.f_vo, self.f_oo, self.f_vv
         O, V = self.O, self.V
         tau = self.tau(t1, t2)
@@ -156,6 +181,8 @@ class SpinOrbitalCCSD:
               + np.einsum("acik,ck->ai", t2, D1, **ES)
               - 0.5 * np.einsum("cakl,cikl->ai", t2, W3, **ES)
               + 0.5 * np.einsum("kacd,cdki->ai", self.govvv, tau, **ES))
+        if self.method >= 0 and t3 is not None:
+            R1 = R1 + 0.25 * np.einsum("jkbc,abcijk->ai", self.goovv, t3, **ES)
         t1_new = np.where(self.t1_mask, R1 / self.den, 0.0)
         # T2  ccsdt.cpp:630-727 (Method_Nr < 0 branch)
         ring = np.einsum("bcjk,akic->abij", t2, W4, **ES)
@@ -172,23 +199,34 @@ class SpinOrbitalCCSD:
               + np.einsum("abcj,ci->abij", self.gvvvo, t1, **ES)
               - np.einsum("abci,cj->abij", self.gvvvo, t1, **ES)
               + 0.5 * np.einsum("abcd,cdij->abij", self.gvvvv, tau, **ES))
+        if self.method >= 0 and t3 is not None:
+            R2 = (R2 + 0.5 * np.einsum("bkcd,acdijk->abij", self.gvovv, t3, **ES)
+                  - 0.5 * np.einsum("akcd,bcdijk->abij", self.gvovv, t3, **ES)
+                  - 0.5 * np.einsum("kmjc,abcikm->abij", self.gooov, t3, **ES)
+                  + 0.5 * np.einsum("kmic,abcjkm->abij", self.gooov, t3, **ES))
         d2 = self.den[:, None, :, None] + self.den[None, :, None, :]
         val = np.where(self.t2_write, R2 / np.where(self.t2_write, d2, 1.0), 0.0)
         # symmetric copies (ccsdt.cpp:720-723)
         t2_new = val - val.transpose(1, 0, 2, 3) - val.transpose(0, 1, 3, 2) + val.transpose(1, 0, 3, 2)
+        if self.method >= 0:
+            return t1_new, t2_new, self.triples(t2)
         return t1_new, t2_new
 
     def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None):
         """Reference driver loop. Returns dict with e_corr, energies (per
         ``iter``), iter (reference counter), t1, t2."""
         t1, t2 = self.mp2_guess()
+        t3 = np.zeros((self.V,) * 3 + (self.O,) * 3) if self.method >= 0 else None
         e_new = self.energy(t1, t2)
         energies = [e_new]
         it = 1
         passes = 0
         while True:
             e_old = e_new
-            t1, t2 = self.update(t1, t2)
+            if self.method >= 0:
+                t1, t2, t3 = self.update(t1, t2, t3)
+            else:
+                t1, t2 = self.update(t1, t2)
             e_new = self.energy(t1, t2)
             it += 1
             passes += 1
@@ -197,4 +235,4 @@ class SpinOrbitalCCSD:
                 break
             if max_passes is not None and passes >= max_passes:
                 break
-        return dict(e_corr=e_new, energies=np.array(energies), iter=it, t1=t1, t2=t2)
+        return dict(e_corr=e_new, energies=np.array(energies), iter=it, t1=t1, t2=t2, t3=t3)

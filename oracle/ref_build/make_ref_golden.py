@@ -2,7 +2,8 @@
 oracle/_ref/ by build_ref.py (TEST INFRASTRUCTURE ONLY; needs the reference
 sources, so it runs in the development container, not on the GPU host).
 
-    python -m oracle.ref_build.make_ref_golden
+    python -m oracle.ref_build.make_ref_golden            # CCSD fixtures
+    python -m oracle.ref_build.make_ref_golden ccsdt-1a   # CCSDT-1a fixtures
 
 Writes
 * tests/golden/h2o_<basis>_<geometry>_tol<k>.npz: the RHF outputs the
@@ -12,7 +13,10 @@ Writes
 * tests/golden/reference_runs.json: the reference's CCSD on the seeded
   synthetic systems of synthetic_oracle.json, from both of its CCSD codes:
   "mo" = CCSD_Memory_optimized::CCSD (the "CCSD" method) and
-  "ccsd1" = CCSDT::Calc_Energy(toler, -1) (the dense spin-orbital "CCSD1").
+  "ccsd1" = CCSDT::Calc_Energy(toler, -1) (the dense spin-orbital "CCSD1");
+* tests/golden/reference_ccsdt1a.json (with the ccsdt-1a argument): the
+  reference's CCSDT-1a, CCSDT::Calc_Energy(toler, 1), on small seeded
+  synthetic systems and on the H2O inputs of the .npz fixtures above.
 """
 from __future__ import annotations
 
@@ -46,10 +50,10 @@ def _parse(out: str):
     return d
 
 
-def run_h2o(basis, geom, tol):
+def run_h2o(basis, geom, tol, mode="ccsd1"):
     with tempfile.TemporaryDirectory() as td:
         dump = Path(td) / "h2o.bin"
-        out = subprocess.run([str(REF / "ref_h2o"), basis, geom, str(tol), str(dump), "ccsd1"],
+        out = subprocess.run([str(REF / "ref_h2o"), basis, geom, str(tol), str(dump), mode],
                              capture_output=True, text=True, check=True).stdout
         res = _parse(out)
         c1 = [l for l in out.splitlines() if l.startswith("ccsd1_iter")][-1].split()
@@ -102,5 +106,27 @@ def main():
     (GOLD / "reference_runs.json").write_text(json.dumps(runs, indent=1))
 
 
+CCSDT1A_SYNTHETIC = [  # (nocc, nvir, naux, seed, sigma); sigma 0.2-0.3 gives visible triples
+    (2, 4, 12, 5, 0.3), (3, 6, 20, 6, 0.3), (2, 8, 20, 7, 0.25), (4, 6, 24, 11, 0.2)]
+
+
+def main_ccsdt1a():
+    runs = {"synthetic": {}, "h2o": {}}
+    for o, v, q, seed, sigma in CCSDT1A_SYNTHETIC:
+        r = run_synthetic(o, v, q, seed, sigma, -10, "ccsdt-1")
+        runs["synthetic"][f"o{o}_v{v}_s{seed}"] = dict(nocc=o, nvir=v, naux=q, seed=seed, sigma=sigma, log10_tol=-10,
+                                                        iter=r["iter"], e_corr=r["ecorr"])
+    for basis, geom, tol in H2O:
+        res = run_h2o(basis, geom, tol, "ccsdt-1")[0]
+        tag = "incarsym" if geom.startswith("yz:1.079252") else geom
+        name = f"h2o_{basis.lower().replace('-', '')}_{tag}_tol{-tol}.npz"
+        runs["h2o"][name] = dict(iter=res["ccsd1_iter"], e_corr=res["ccsd1_ecorr"])
+    (GOLD / "reference_ccsdt1a.json").write_text(json.dumps(runs, indent=1))
+    print(json.dumps(runs, indent=1))
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "ccsdt-1a":
+        main_ccsdt1a()
+    else:
+        main()

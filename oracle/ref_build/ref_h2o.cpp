@@ -54,11 +54,14 @@ int main(int argc, char **argv) {
     const double e = cc.CCSD(toler, false);
     const double ehf = e - cc.E_new;
     std::printf("iter %d ecorr %.17e ehf %.17e etotal %.17e\n", cc.iter, cc.E_new, ehf, e);
-    if (argc > 5 && std::string(argv[5]) == "ccsd1") {
-        // the reference's dense spin-orbital CCSD on the same RHF (its SCF reruns to the same result)
+    if (argc > 5 && (std::string(argv[5]) == "ccsd1" || std::string(argv[5]).rfind("ccsdt-", 0) == 0)) {
+        // the reference's dense spin-orbital CCSD ("ccsd1", method -1) or CCSDT-n ("ccsdt-<n>")
+        // on the same RHF (its SCF reruns to the same result)
+        const std::string m = argv[5];
+        const int method = m == "ccsd1" ? -1 : std::atoi(m.c_str() + 6);
         Hartree_Fock_Solver hf1(3, Z, R, basis, n_elec, false, 0, 1, false);
         CCSDT c1(3, Z, R, basis, n_elec, 0, 1, &hf1, false);
-        const double e1 = c1.Calc_Energy(toler, -1);
+        const double e1 = c1.Calc_Energy(toler, method);
         std::printf("ccsd1_iter %d ccsd1_ecorr %.17e\n", c1.iter, e1 - ehf);
     }
 

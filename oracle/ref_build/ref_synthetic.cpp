@@ -10,9 +10,11 @@
 // E_HF = 0, C = identity, orbital energies and chemist (pq|rs) read from a
 // binary file, so Prepear_AOs passes the integrals through unchanged.
 //
-//   usage: ref_synthetic <input.bin> <log10 tolerance> [mo|ccsd1]
-//     mo     CCSD_Memory_optimized::CCSD (the reference's "CCSD" method)
-//     ccsd1  CCSDT::Calc_Energy(toler, -1), the dense spin-orbital CCSD ("CCSD1")
+//   usage: ref_synthetic <input.bin> <log10 tolerance> [mo|ccsd1|ccsdt-<n>]
+//     mo         CCSD_Memory_optimized::CCSD (the reference's "CCSD" method)
+//     ccsd1      CCSDT::Calc_Energy(toler, -1), the dense spin-orbital CCSD ("CCSD1")
+//     ccsdt-<n>  CCSDT::Calc_Energy(toler, n): 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2,
+//                4 = CCSDT-3, 5 = CCSDT-4, 6 = CCSDT (initializer.cpp:98-128)
 //   input: int32 n, int32 nocc, float64 eps[n], float64 eri[n^4] (p,q,r,s row-major)
 //   prints: "iter <reference iter> ecorr <E_corr %.17e>"
 #include <cstdio>
@@ -90,9 +92,10 @@ int main(int argc, char **argv) {
     vec Z = zeros(1);
     mat R = zeros(1, 3);
     Hartree_Fock_Solver hf(1, Z, R, "synthetic", 2 * g_nocc, false, 0, 1, false);
-    if (argc > 3 && std::strcmp(argv[3], "ccsd1") == 0) {
+    if (argc > 3 && (std::strcmp(argv[3], "ccsd1") == 0 || std::strncmp(argv[3], "ccsdt-", 6) == 0)) {
+        const int method = std::strcmp(argv[3], "ccsd1") == 0 ? -1 : std::atoi(argv[3] + 6);
         CCSDT cc(1, Z, R, "synthetic", 2 * g_nocc, 0, 1, &hf, false);
-        const double e = cc.Calc_Energy(toler, -1);
+        const double e = cc.Calc_Energy(toler, method);
         std::printf("iter %d ecorr %.17e etotal %.17e\n", cc.iter, e, e);
     } else {
         CCSD_Memory_optimized cc(1, Z, R, "synthetic", 2 * g_nocc, 0, 1, &hf, false);
