@@ -49,9 +49,12 @@ def flops_per_update(nocc: int, nvir: int) -> float:
     return float(_abi.lib().ccsd_flops_per_update(nocc, nvir))
 
 
+METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A}
+
+
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
              fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, profile=False,
-             stream=None):
+             stream=None, method="ccsd"):
     o = _abi.Options()
     _abi.check(_abi.lib().ccsd_default_options(C.byref(o)))
     o.energy_tol = energy_tol
@@ -63,6 +66,7 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.verbose = int(bool(verbose))
     o.profile = int(bool(profile))
+    o.method = METHODS[method] if isinstance(method, str) else int(method)
     o.stream = stream
     return o
 

@@ -26,6 +26,9 @@ CCSD_INTS_DF = 1
 CCSD_INTS_AO_DENSE = 2
 CCSD_INTS_SO_ANTISYM = 3
 
+CCSD_METHOD_CCSD = 0
+CCSD_METHOD_CCSDT1A = 1
+
 CCSD_PREC_FP64 = 0
 CCSD_PREC_SPLIT2 = 2
 CCSD_PREC_SPLIT3 = 3
@@ -47,7 +50,7 @@ class Options(C.Structure):
         ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
         ("fixed_iterations", C.c_int32), ("diis_size", C.c_int32), ("diis_start", C.c_int32),
         ("precision", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
-        ("stream", C.c_void_p),
+        ("method", C.c_int32), ("stream", C.c_void_p),
     ]
 
 

@@ -317,6 +317,8 @@ void Engine::ladder_df_grad(const double *lam2, int naux) {
 // ---- Lambda equations and the gradient ----------------------------------------------
 void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     if (!solved_) throw Error(CCSD_ERR_INVALID_ARG, "ccsd_lambda_grad needs a completed ccsd_solve first");
+    if (opt_.method != CCSD_METHOD_CCSD)
+        throw Error(CCSD_ERR_UNSUPPORTED, "ccsd_lambda_grad is built for CCSD (method CCSD_METHOD_CCSD)");
     if (prob.nocc != o_ || prob.nvir != v_) throw Error(CCSD_ERR_INVALID_ARG, "problem shape differs from the handle's");
     const int o = o_, v = v_;
     const int64_t ov = (int64_t)o * v, v2 = (int64_t)v * v, ov2 = (int64_t)o * v2, o2 = (int64_t)o * o;

@@ -77,6 +77,8 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         cudaGetLastError();
         throw Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
     }
+    if (opts.method != CCSD_METHOD_CCSD)
+        throw Error(CCSD_ERR_UNSUPPORTED, "the batched solve runs CCSD (method CCSD_METHOD_CCSD)");
     opt_ = opts;
     if (opts.stream) {
         st_ = (cudaStream_t)opts.stream;

@@ -116,6 +116,16 @@ void k_ladder_unpack_adj(int o, int v, const double *Rb, double *spb, double *sm
 // W+[tri(a,b)][tri(c,d)], W-[stri(a,b)][stri(c,d)] from W[a][b][c][d] = (ac|bd)
 void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st);
 void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaStream_t st);
+// CCSDT-1a triples (triples.cu), spin orbitals O = 2o, V = 2v:
+// <PQ||RS> blocks from the spatial ovov/ovoo/ovvv blocks; kind 0: vvvo [b][c][e][k],
+// 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c]
+void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv, double *out,
+                cudaStream_t st);
+// t2so[a][b][i][j] (spin orbitals) from the spatial t2[i][j][a][b]
+void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st);
+// t3 = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / D3, all [a][b][c][i][j][k]
+void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *eo, const double *ev, double *t3,
+                   cudaStream_t st);
 void k_fill(size_t n, double val, double *p, cudaStream_t st);
 void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st);
 int reduce_blocks();

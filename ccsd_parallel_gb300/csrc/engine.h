@@ -106,6 +106,11 @@ class Engine {
 
     // one amplitude update: residual numerators from (t1_, t2_)
     void residual();
+    // CCSDT-1a (triples.cpp): spin-orbital T3, its contraction intermediates and
+    // the spin-orbital integral blocks it reads
+    void triples_setup();
+    void triples_step();
+    DBuf t3_, y3_, z3_, t2so_, so_vvvo_, so_ovoo_, so_oovv_, so_vovv_, so_ooov_;
 
     // recordable element-wise operations (every op of build and residual goes
     // through these or through gemm())

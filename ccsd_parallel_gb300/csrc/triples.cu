@@ -1,0 +1,176 @@
+// CCSDT-1a triples (the reference's CCSDT method Method_Nr 1, ccsdt.cpp:735-1318)
+// on top of the closed-shell CCSD engine, in the reference's spin-orbital form:
+// spin orbital P = 2p + spin (alpha/beta interleaved, ccsdt.cpp:1466-1478).
+//
+//   t3[a][b][c][i][j][k] = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / D3
+//   Y[abc][ijk] = sum_e t2(a,e)(i,j) <bc||ek>,  Z[abc][ijk] = sum_m t2(a,b)(i,m) <mc||jk>
+//
+// Y and Z are contractions (engine kernels); this file builds the
+// spin-orbital integral blocks from the spatial ones, expands the spatial T2
+// into spin orbitals, and assembles T3 (both antisymmetrisers and D3 in one
+// pass, one thread per element).  Sizes: O = 2 nocc, V = 2 nvir.
+#include "common.h"
+
+namespace ccsd {
+
+namespace {
+
+inline int blocks_for(size_t n) {
+    size_t b = (n + 255) / 256;
+    if (b > 8 * 152 * 4) b = 8 * 152 * 4;
+    return b < 1 ? 1 : (int)b;
+}
+
+// spatial chemist blocks: ovov[i][a][j][b], ovoo[i][a][j][k], ovvv[i][a][b][c]
+struct Blocks {
+    int o, v;
+    const double *ovov, *ovoo, *ovvv;
+    __device__ double OVOV(int i, int a, int j, int b) const {
+        return ovov[(((int64_t)i * v + a) * o + j) * v + b];
+    }
+    __device__ double OVOO(int i, int a, int j, int k) const {
+        return ovoo[(((int64_t)i * v + a) * o + j) * o + k];
+    }
+    __device__ double OVVV(int i, int a, int b, int c) const {
+        return ovvv[(((int64_t)i * v + a) * v + b) * v + c];
+    }
+};
+
+// <PQ||RS> = (pr|qs) d(sp,sr) d(sq,ss) - (ps|qr) d(sp,ss) d(sq,sr), per block kind:
+//   0: vvvo [b][c][e][k] = (be|ck) - (bk|ce)
+//   1: ovoo [m][c][j][k] = (mj|ck) - (mk|cj)
+//   2: oovv [j][k][b][c] = (jb|kc) - (jc|kb)
+//   3: vovv [b][k][c][d] = (bc|kd) - (bd|kc)
+//   4: ooov [k][m][j][c] = (kj|mc) - (kc|mj)
+__global__ void so_block_kernel(int kind, Blocks B, double *out) {
+    const int O = 2 * B.o, V = 2 * B.v;
+    int e0, e1, e2, e3;  // extents of the four indices
+    switch (kind) {
+        case 0: e0 = V; e1 = V; e2 = V; e3 = O; break;
+        case 1: e0 = O; e1 = V; e2 = O; e3 = O; break;
+        case 2: e0 = O; e1 = O; e2 = V; e3 = V; break;
+        case 3: e0 = V; e1 = O; e2 = V; e3 = V; break;
+        default: e0 = O; e1 = O; e2 = O; e3 = V; break;
+    }
+    const int64_t total = (int64_t)e0 * e1 * e2 * e3;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int P3 = (int)(idx % e3);
+        int64_t r = idx / e3;
+        const int P2 = (int)(r % e2);
+        r /= e2;
+        const int P1 = (int)(r % e1);
+        const int P0 = (int)(r / e1);
+        const int p0 = P0 >> 1, p1 = P1 >> 1, p2 = P2 >> 1, p3 = P3 >> 1;
+        const int s0 = P0 & 1, s1 = P1 & 1, s2 = P2 & 1, s3 = P3 & 1;
+        double d = 0.0, x = 0.0;
+        switch (kind) {
+            case 0:  // <bc||ek>: (be|ck) = ovvv[k][c][b][e], (bk|ce) = ovvv[k][b][c][e]
+                if (s0 == s2 && s1 == s3) d = B.OVVV(p3, p1, p0, p2);
+                if (s0 == s3 && s1 == s2) x = B.OVVV(p3, p0, p1, p2);
+                break;
+            case 1:  // <mc||jk>: (mj|ck) = ovoo[k][c][m][j], (mk|cj) = ovoo[j][c][m][k]
+                if (s0 == s2 && s1 == s3) d = B.OVOO(p3, p1, p0, p2);
+                if (s0 == s3 && s1 == s2) x = B.OVOO(p2, p1, p0, p3);
+                break;
+            case 2:  // <jk||bc>: (jb|kc) = ovov[j][b][k][c], (jc|kb) = ovov[j][c][k][b]
+                if (s0 == s2 && s1 == s3) d = B.OVOV(p0, p2, p1, p3);
+                if (s0 == s3 && s1 == s2) x = B.OVOV(p0, p3, p1, p2);
+                break;
+            case 3:  // <bk||cd>: (bc|kd) = ovvv[k][d][b][c], (bd|kc) = ovvv[k][c][b][d]
+                if (s0 == s2 && s1 == s3) d = B.OVVV(p1, p3, p0, p2);
+                if (s0 == s3 && s1 == s2) x = B.OVVV(p1, p2, p0, p3);
+                break;
+            default:  // <km||jc>: (kj|mc) = ovoo[m][c][k][j], (kc|mj) = ovoo[k][c][m][j]
+                if (s0 == s2 && s1 == s3) d = B.OVOO(p1, p3, p0, p2);
+                if (s0 == s3 && s1 == s2) x = B.OVOO(p0, p3, p1, p2);
+                break;
+        }
+        out[idx] = d - x;
+    }
+}
+
+// t2so[a][b][i][j] (spin orbitals) from the spatial t2[i][j][a][b]:
+// t2[ij ab] d(sa,si) d(sb,sj) - t2[ji ab] d(sa,sj) d(sb,si)
+__global__ void t2_spin_kernel(int o, int v, const double *__restrict__ t2, double *__restrict__ t2so) {
+    const int O = 2 * o, V = 2 * v;
+    const int64_t total = (int64_t)V * V * O * O;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int J = (int)(idx % O);
+        int64_t r = idx / O;
+        const int I = (int)(r % O);
+        r /= O;
+        const int Bv = (int)(r % V);
+        const int A = (int)(r / V);
+        const int a = A >> 1, b = Bv >> 1, i = I >> 1, j = J >> 1;
+        const int sa = A & 1, sb = Bv & 1, si = I & 1, sj = J & 1;
+        double val = 0.0;
+        if (sa == si && sb == sj) val += t2[(((int64_t)i * o + j) * v + a) * v + b];
+        if (sa == sj && sb == si) val -= t2[(((int64_t)j * o + i) * v + a) * v + b];
+        t2so[idx] = val;
+    }
+}
+
+// t3[a][b][c][i][j][k] = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / (D(a,i) + D(b,j) + D(c,k)),
+// D(a,i) = f_ii - f_aa, with P(a/bc) = 1 - (ab) - (ac), P(k/ij) = 1 - (ik) - (jk),
+// P(c/ab) = 1 - (ac) - (bc), P(i/jk) = 1 - (ij) - (ik) (ccsdt.cpp:1016-1058, 1235-1238)
+__global__ void t3_assemble_kernel(int o, int v, const double *__restrict__ Y, const double *__restrict__ Z,
+                                   const double *__restrict__ eo, const double *__restrict__ ev,
+                                   double *__restrict__ t3) {
+    const int O = 2 * o, V = 2 * v;
+    const int64_t O3 = (int64_t)O * O * O;
+    const int64_t total = (int64_t)V * V * V * O3;
+    auto at = [&](const double *X, int a, int b, int c, int i, int j, int k) {
+        return X[(((int64_t)a * V + b) * V + c) * O3 + ((int64_t)i * O + j) * O + k];
+    };
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % O);
+        int64_t r = idx / O;
+        const int j = (int)(r % O);
+        r /= O;
+        const int i = (int)(r % O);
+        r /= O;
+        const int c = (int)(r % V);
+        r /= V;
+        const int b = (int)(r % V);
+        const int a = (int)(r / V);
+        // P(a/bc) applied to each of P(k/ij)'s three index orders
+        auto pa = [&](int p, int q, int s) {
+            return at(Y, a, b, c, p, q, s) - at(Y, b, a, c, p, q, s) - at(Y, c, b, a, p, q, s);
+        };
+        const double y = pa(i, j, k) - pa(k, j, i) - pa(i, k, j);
+        auto pc = [&](int p, int q, int s) {
+            return at(Z, a, b, c, p, q, s) - at(Z, c, b, a, p, q, s) - at(Z, a, c, b, p, q, s);
+        };
+        const double z = pc(i, j, k) - pc(j, i, k) - pc(k, j, i);
+        const double den = (eo[i >> 1] - ev[a >> 1]) + (eo[j >> 1] - ev[b >> 1]) + (eo[k >> 1] - ev[c >> 1]);
+        t3[idx] = (y - z) / den;
+    }
+}
+
+}  // namespace
+
+void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv, double *out,
+                cudaStream_t st) {
+    Blocks B{o, v, ovov, ovoo, ovvv};
+    const size_t O = 2 * (size_t)o, V = 2 * (size_t)v;
+    const size_t sizes[5] = {V * V * V * O, O * V * O * O, O * O * V * V, V * O * V * V, O * O * O * V};
+    so_block_kernel<<<blocks_for(sizes[kind]), 256, 0, st>>>(kind, B, out);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st) {
+    t2_spin_kernel<<<blocks_for((size_t)16 * o * o * v * v), 256, 0, st>>>(o, v, t2, t2so);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *eo, const double *ev, double *t3,
+                   cudaStream_t st) {
+    const size_t n = (size_t)64 * o * o * o * v * v * v;
+    t3_assemble_kernel<<<blocks_for(n), 256, 0, st>>>(o, v, Y, Z, eo, ev, t3);
+    CCSD_LAUNCH_CHECK();
+}
+
+}  // namespace ccsd

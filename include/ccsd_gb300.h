@@ -93,8 +93,19 @@ typedef struct ccsd_options {
     int32_t precision;         /* CCSD_PREC_*                                   */
     int32_t verbose;           /* print one line per update to stdout          */
     int32_t profile;           /* 1: time every contraction with CUDA events   */
+    int32_t method;            /* CCSD_METHOD_*                                 */
     void *stream;              /* cudaStream_t, or NULL for a private stream   */
 } ccsd_options;
+
+/* ---- coupled-cluster method (ccsd_options.method) ------------------------ */
+#define CCSD_METHOD_CCSD 0     /* CCSD (the reference's CCSD / CCSD1)            */
+/* CCSDT-1a, the reference's CCSDT::Calc_Energy(toler, 1) (initializer.cpp:104-108):
+ * T3 from T2 and the bare integrals, T3 terms in T1/T2 (ccsdt.cpp:419-434,
+ * 640-670, 995-1290), iterated with T1/T2 (Jacobi; DIIS, when set, acts on T1/T2).
+ * T3 is kept in the reference's spin-orbital form, 3 (2 nocc)^3 (2 nvir)^3
+ * doubles of device memory with its two contraction intermediates.  Single
+ * systems only (no batched solve, no ccsd_lambda_grad). */
+#define CCSD_METHOD_CCSDT1A 1
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */

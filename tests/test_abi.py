@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8
-    assert C.sizeof(_abi.Options) == 2 * 8 + 7 * 4 + 4 + 8
+    assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8
     assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
 
 

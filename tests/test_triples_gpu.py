@@ -1,0 +1,103 @@
+"""CCSDT-1a on the GPU engine (the reference's CCSDT::Calc_Energy(toler, 1),
+ccsdt.cpp:255-271) against the spin-orbital oracle and the reference's own
+runs (tests/golden/reference_ccsdt1a.json): FP64 energies to 1e-11 with the
+reference's iteration counter, amplitudes to 1e-12 after a fixed number of
+updates, split precision within 1e-8."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ccsd_parallel_gb300 as cg
+from ccsd_parallel_gb300 import _abi
+from oracle import synthetic as syn
+from oracle.ccsd_spinorb import SpinOrbitalCCSD
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).parent / "golden"
+CCSDT1A = json.loads((GOLD / "reference_ccsdt1a.json").read_text())
+
+
+def _case(c):
+    eps = syn.orbital_energies(c["nocc"], c["nvir"], c["seed"])
+    b = syn.df_factors(c["nocc"] + c["nvir"], c["naux"], c["seed"], sigma=c["sigma"])
+    return np.diag(eps), b
+
+
+@pytest.mark.parametrize("key", sorted(CCSDT1A["synthetic"]))
+def test_ccsdt1a_matches_reference_synthetic(key):
+    c = CCSDT1A["synthetic"][key]
+    fock, b = _case(c)
+    r = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=10.0 ** c["log10_tol"])
+    assert r["iterations"] + 1 == c["iter"]
+    assert abs(r["e_corr"] - c["e_corr"]) < 1e-11
+
+
+@pytest.mark.parametrize("name", sorted(CCSDT1A["h2o"]))
+def test_ccsdt1a_matches_reference_h2o(name):
+    """The reference's RHF outputs for H2O through the AO input."""
+    d = np.load(GOLD / name)
+    ref = CCSDT1A["h2o"][name]
+    r = cg.solve(np.diag(d["eps"]), int(d["nocc"]), ao_eri=d["ao_eri"], mo_coeff=d["mo_coeff"],
+                 method="ccsdt-1a", energy_tol=10.0 ** float(d["log10_tol"]))
+    assert r["iterations"] + 1 == ref["iter"]
+    assert abs(r["e_corr"] - ref["e_corr"]) < 1e-11
+
+
+def test_ccsdt1a_amplitudes_match_oracle_every_update():
+    """Energies of every update and the final T1/T2 equal the oracle's; the
+    closed-shell amplitudes are the alpha-beta blocks of the spin-orbital ones,
+    t1[i,a] = t1so[2a,2i], t2[i,j,a,b] = t2so[2a,2b+1,2i,2j+1]."""
+    o, v = 3, 7
+    fock, b = _case(dict(nocc=o, nvir=v, naux=22, seed=17, sigma=0.3))
+    eri = syn.eri_from_df(b)
+    ref = SpinOrbitalCCSD(fock, eri, o, method=1).run(toler=1e-13, max_passes=8)
+    r = cg.solve(fock, o, df=b, method="ccsdt-1a", fixed_iterations=8)
+    np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
+    t1 = ref["t1"][0::2, 0::2].T
+    t2 = ref["t2"][0::2, 1::2, 0::2, 1::2].transpose(2, 3, 0, 1)
+    np.testing.assert_allclose(r["t1"], t1, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r["t2"], t2, rtol=0, atol=1e-12)
+    # the triples change the answer: CCSD's own fixed point differs
+    rc = cg.solve(fock, o, df=b, fixed_iterations=8)
+    assert abs(rc["e_corr"] - r["e_corr"]) > 1e-6
+
+
+@pytest.mark.parametrize("prec", ["split3", "split2"])
+def test_ccsdt1a_split_precision(prec):
+    """Split precision on the same method: the FP64 answer within 1e-8."""
+    c = CCSDT1A["synthetic"]["o3_v6_s6"]
+    fock, b = _case(c)
+    ref = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=1e-11)
+    r = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=1e-11, precision=prec)
+    assert abs(r["e_corr"] - ref["e_corr"]) < 1e-8
+
+
+def test_ccsdt1a_spin_orbital_input():
+    """The reference's own input form (<PQ||RS>) gives the same iterates."""
+    from oracle.ccsd_spinorb import spin_orbital_integrals
+    c = CCSDT1A["synthetic"]["o2_v4_s5"]
+    fock, b = _case(c)
+    g = spin_orbital_integrals(syn.eri_from_df(b))
+    r_so = cg.solve(fock, c["nocc"], so_eri=g, method="ccsdt-1a", energy_tol=1e-10)
+    r_df = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=1e-10)
+    assert r_so["iterations"] == r_df["iterations"] == c["iter"] - 1
+    np.testing.assert_allclose(r_so["energies"], r_df["energies"], rtol=0, atol=1e-13)
+
+
+def test_ccsdt1a_unsupported_paths_fail_loudly():
+    c = CCSDT1A["synthetic"]["o2_v4_s5"]
+    fock, b = _case(c)
+    with cg.Solver(fock, c["nocc"], df=b, method="ccsdt-1a") as s:
+        s.solve()
+        with pytest.raises(cg.CCSDError) as ei:
+            s.lambda_grad()
+        assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve_batched([dict(fock=fock, nocc=c["nocc"], df=b)] * 2, method="ccsdt-1a")
+    assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve(fock, c["nocc"], df=b, method=7)
+    assert ei.value.code == _abi.CCSD_ERR_INVALID_ARG
