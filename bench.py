@@ -255,6 +255,59 @@ def measure_extras(cg, fock, df, o, precision):
     return out
 
 
+def measure_ccsdt1a(cg, precision, pk):
+    """CCSDT-1a (the reference's CCSDT::Calc_Energy(toler, 1), T3 in spin
+    orbitals) at a synthetic nocc=6, nvir=40 system: per-update device time in
+    FP64 and split precision, the T3 assembly's HBM roofline, and at a small
+    size (nocc=4, nvir=16) the update time of the spin-orbital oracle on the
+    host beside the GPU's."""
+    from oracle.ccsd_spinorb import SpinOrbitalCCSD
+    from oracle.cpu_baseline import cores
+    o, v = 6, 40
+    O, V = 2 * o, 2 * v
+    n3 = V ** 3 * O ** 3
+    fock, b = cg.make_synthetic(o, v, 3 * (o + v) // 2, 77)
+    out = dict(workload=f"synthetic nocc={o} nvir={v} naux={3 * (o + v) // 2} (seed 77), CCSDT-1a, "
+                        f"T3 = {n3 * 8 / 1e9:.1f} GB in spin orbitals, 5 updates from the MP2 start")
+    e = {}
+    for prec in ("fp64", precision):
+        with cg.Solver(fock, o, df=b, precision=prec, method="ccsdt-1a", fixed_iterations=5, profile=True) as s:
+            r = s.solve(amplitudes=False)
+            prof = s.profile()
+        e[prec] = r["e_corr"]
+        upd = float(np.median(r["update_ms"][1:]))
+        sites = {x["site"]: x for x in prof["sites"]}
+        t3 = {k: sites[k]["ms"] / sites[k]["calls"] for k in sites if k.startswith(("T3_", "R1_T3", "R2_T3"))}
+        out[prec] = dict(update_ms=upd, triples_sites_ms=t3)
+        if prec == "fp64":
+            asm = t3["T3_assemble"]
+            # per virtual triple a<b<c: three Y and three Z slabs of O^3 read, six t3 slabs written
+            triples = V * (V - 1) * (V - 2) // 6
+            bytes_alg = 8.0 * 12 * triples * O ** 3
+            out["assemble_roofline"] = dict(bound="hbm", achieved=bytes_alg / asm / 1e6, peak=pk["hbm_gbs"],
+                                            unit="GB/s", frac=bytes_alg / asm / 1e6 / pk["hbm_gbs"],
+                                            basis="12 O^3 doubles per virtual triple a<b<c (3 Y + 3 Z slabs "
+                                                  "read, 6 t3 slabs written) / CUDA-event time",
+                                            bytes_per_launch=bytes_alg, ms=asm)
+    out["abs_dE_split_vs_fp64"] = abs(e[precision] - e["fp64"])
+    so, sv = 4, 16
+    f_s, b_s = cg.make_synthetic(so, sv, 3 * (so + sv) // 2, 78)
+    eri = np.einsum("Qpq,Qrs->pqrs", b_s, b_s)
+    ref = SpinOrbitalCCSD(f_s, eri, so, method=1)
+    t1, t2 = ref.mp2_guess()
+    t3 = np.zeros((2 * sv,) * 3 + (2 * so,) * 3)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        t1, t2, t3 = ref.update(t1, t2, t3)
+    cpu_ms = (time.perf_counter() - t0) / 3 * 1e3
+    with cg.Solver(f_s, so, df=b_s, method="ccsdt-1a", fixed_iterations=5) as s:
+        r = s.solve(amplitudes=False)
+    out["small"] = dict(workload=f"synthetic nocc={so} nvir={sv} (seed 78)", gpu_fp64_update_ms=float(
+        np.median(r["update_ms"][1:])), cpu_port_update_ms=cpu_ms, cpu_kind="port (numpy, spin orbitals)",
+        cpu_cores=cores())
+    return out
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -326,6 +379,7 @@ def main():
     extras = {}
     if args.extras and rank == 0:
         extras = measure_extras(cg, fock, df, o, args.precision)
+        extras["ccsdt1a"] = measure_ccsdt1a(cg, args.precision, pk)
 
     if rank != 0:
         return

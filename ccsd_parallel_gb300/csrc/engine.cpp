@@ -447,7 +447,7 @@ void Engine::build_derived() {
 // ---------------------------------------------------------------------------
 bool Engine::use_split(int M, int N, int K) const {
     if (opt_.precision == CCSD_PREC_FP64 || (!split_ && !build_split_)) return false;
-    return M >= 16 && N >= 16 && K >= 16 && (double)M * N * K >= 1.0e7;
+    return M >= 16 && N >= 16 && K >= 4 && (double)M * N * K >= 1.0e7;
 }
 
 void Engine::gemm(int M, int N, int K, double alpha, const MatView &A, const MatView &B,

@@ -179,7 +179,111 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int M, int K, double alph
     }
 }
 
+// Skinny form (N <= 16 columns, long K): the contraction streams A once and is
+// memory-bound.  A block covers 32 rows (4 per warp) and one K range; for each
+// 128-wide k chunk it stages B(0..N-1, k) in shared memory, and every lane
+// accumulates 4 rows x NN columns over k = lane + 32 q, so consecutive lanes read
+// consecutive k of A (coalesced when A is K-contiguous) and one column offset
+// serves four rows.  Lanes meet in a warp reduction at the end; a K-split writes
+// per-range partial sums that splitk_reduce_kernel adds in a fixed order.
+constexpr int SK_ROWS = 4, SK_KC = 128;
+
+template <int NN>
+__global__ void __launch_bounds__(256) gemm_skinny_f64_kernel(int M, int N, int K, int kchunk, double alpha,
+                                                              MatView A, MatView B, double beta, OutView C,
+                                                              double *ws) {
+    __shared__ double Bs[NN][SK_KC];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m0 = blockIdx.x * (8 * SK_ROWS) + warp * SK_ROWS;
+    const int kbeg = blockIdx.y * kchunk;
+    const int kend = min(K, kbeg + kchunk);
+    int64_t arow[SK_ROWS];
+    bool aok[SK_ROWS];
+#pragma unroll
+    for (int r = 0; r < SK_ROWS; ++r) {
+        aok[r] = m0 + r < M;
+        arow[r] = aok[r] ? dim_off(A.row, m0 + r) : 0;
+    }
+    double acc[SK_ROWS][NN];
+#pragma unroll
+    for (int r = 0; r < SK_ROWS; ++r)
+#pragma unroll
+        for (int n = 0; n < NN; ++n) acc[r][n] = 0.0;
+
+    for (int k0 = kbeg; k0 < kend; k0 += SK_KC) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < NN * SK_KC; e += blockDim.x) {
+            const int n = e / SK_KC, kk = e % SK_KC, k = k0 + kk;
+            Bs[n][kk] = (n < N && k < kend) ? B.p[dim_off(B.row, n) + dim_off(B.col, k)] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < SK_KC / 32; ++q) {
+            const int kk = lane + 32 * q, k = k0 + kk;
+            if (k < kend) {
+                const int64_t co = dim_off(A.col, k);
+                double a[SK_ROWS];
+#pragma unroll
+                for (int r = 0; r < SK_ROWS; ++r) a[r] = aok[r] ? A.p[arow[r] + co] : 0.0;
+#pragma unroll
+                for (int n = 0; n < NN; ++n) {
+                    const double b = Bs[n][kk];
+#pragma unroll
+                    for (int r = 0; r < SK_ROWS; ++r) acc[r][n] = fma(a[r], b, acc[r][n]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < SK_ROWS; ++r)
+#pragma unroll
+        for (int n = 0; n < NN; ++n)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[r][n] += __shfl_down_sync(0xffffffffu, acc[r][n], off);
+    if (lane != 0) return;
+#pragma unroll
+    for (int r = 0; r < SK_ROWS; ++r) {
+        const int m = m0 + r;
+        if (m >= M) continue;
+        if (gridDim.y == 1) {
+            const int64_t ro = dim_off(C.row, m);
+#pragma unroll
+            for (int n = 0; n < NN; ++n) {
+                if (n >= N) break;
+                double *c = C.p + ro + dim_off(C.col, n);
+                double v = alpha * acc[r][n];
+                if (beta != 0.0) v = fma(beta, *c, v);
+                *c = v;
+            }
+        } else {
+            double *w = ws + (size_t)blockIdx.y * M * N + (size_t)m * N;
+#pragma unroll
+            for (int n = 0; n < NN; ++n)
+                if (n < N) w[n] = acc[r][n];
+        }
+    }
+}
+
 constexpr int kTargetBlocks = 2 * 152;
+constexpr int kSkinnyMaxN = 16;
+
+// K ranges for the skinny form: enough blocks to cover the SMs four times over.
+int choose_skinny_splits(int M, int K) {
+    const long mblocks = (M + 8 * SK_ROWS - 1) / (8 * SK_ROWS);
+    const long want = (4 * 152 + mblocks - 1) / mblocks;
+    const long maxk = (K + 4 * SK_KC - 1) / (4 * SK_KC);  // at least four chunks per range
+    long s = want < maxk ? want : maxk;
+    if (s > 128) s = 128;
+    return s < 1 ? 1 : (int)s;
+}
+
+// The skinny form takes a shape whose short side is at most 16 and whose other
+// sides are long enough for it to matter (the tiled kernel wastes most of a 64-wide
+// tile there); returns the number of columns after orienting the short side to N.
+bool skinny_shape(int M, int N, int K) {
+    const int lo = M < N ? M : N, hi = M < N ? N : M;
+    return lo <= kSkinnyMaxN && hi >= 64 && K >= 256;
+}
 
 int choose_splits(int M, int N, int K) {
     long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
@@ -194,10 +298,36 @@ int choose_splits(int M, int N, int K) {
 }  // namespace
 
 size_t gemm_f64_ws_elems(int M, int N, int K) {
+    if (skinny_shape(M, N, K)) {
+        const int Ml = M < N ? N : M;
+        int s = choose_skinny_splits(Ml, K);
+        return s > 1 ? (size_t)s * M * N : 0;
+    }
     if (M == 1 || N == 1) return 0;
     int s = choose_splits(M, N, K);
     return s > 1 ? (size_t)s * M * N : 0;
 }
+
+namespace {
+template <int NN>
+void launch_skinny(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+                   const OutView &C, double *ws, size_t ws_elems, cudaStream_t st) {
+    int splits = choose_skinny_splits(M, K);
+    while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
+    int kchunk = (K + splits - 1) / splits;
+    kchunk = (kchunk + SK_KC - 1) / SK_KC * SK_KC;
+    splits = (K + kchunk - 1) / kchunk;
+    dim3 grid((M + 8 * SK_ROWS - 1) / (8 * SK_ROWS), splits);
+    gemm_skinny_f64_kernel<NN><<<grid, 256, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    CCSD_LAUNCH_CHECK();
+    if (splits > 1) {
+        size_t total = (size_t)M * N;
+        int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+        splitk_reduce_kernel<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
+        CCSD_LAUNCH_CHECK();
+    }
+}
+}  // namespace
 
 void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
               const OutView &C, double *ws, size_t ws_elems, cudaStream_t st) {
@@ -212,11 +342,27 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         const MatView &Xv = N == 1 ? B : A;
         const OutView Y = N == 1 ? C : OutView{C.p, C.col, C.row};
         const int R = N == 1 ? M : N;
-        if (Am.row.s2 == 1 && Am.col.s2 != 1)
+        if (Am.row.s2 == 1 && Am.col.s2 != 1) {
             gemv_f64_kernel<true><<<(R + 31) / 32, 256, 0, st>>>(R, K, alpha, Am, Xv, beta, Y);
-        else
+        } else if (skinny_shape(R, 1, K) && R < 8 * 152 * 8) {
+            // few rows of a long K: the K-split skinny form keeps every SM busy
+            launch_skinny<1>(R, 1, K, alpha, Am, Xv, beta, Y, ws, ws_elems, st);
+            return;
+        } else {
             gemv_f64_kernel<false><<<(R + 7) / 8, 256, 0, st>>>(R, K, alpha, Am, Xv, beta, Y);
+        }
         CCSD_LAUNCH_CHECK();
+        return;
+    }
+    if (skinny_shape(M, N, K)) {
+        if (M < N) {  // the short side goes to the columns
+            gemm_f64(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, ws, ws_elems, st);
+            return;
+        }
+        if (N <= 2) launch_skinny<2>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
+        else if (N <= 4) launch_skinny<4>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
+        else if (N <= 8) launch_skinny<8>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
+        else launch_skinny<16>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
         return;
     }
     int splits = choose_splits(M, N, K);

@@ -40,6 +40,8 @@ void Engine::triples_setup() {
     DBuf *blocks[5] = {&so_vvvo_, &so_ovoo_, &so_oovv_, &so_vovv_, &so_ooov_};
     for (int kind = 0; kind < 5; ++kind) k_so_block(kind, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, blocks[kind]->p, st_);
     t3_.zero(st_);  // T3 starts at zero (the first update is CCSD-like)
+    y3_.zero(st_);  // spin-forbidden blocks of Y and Z are never written
+    z3_.zero(st_);
 }
 
 void Engine::triples_step() {
@@ -54,44 +56,120 @@ void Engine::triples_step() {
          mv(t3, ix2((uint32_t)v, 2 * O2, 2 * V2O3), ix3((uint32_t)V, (uint32_t)O2, VO3, O3, 1)),
          mv(so_oovv_.p, ix1(0), ix3((uint32_t)V, (uint32_t)O2, V, 1, V * V)), 1.0,
          ovw(R1_.p, ix2((uint32_t)v, v, 1), ix1(0)), 0, 0, "R1_T3");
-    // R[i][j][a][b] += 1/2 sum_{c,d,k} <bk||cd> t3[a][c][d][i][j][k]   (a = 2a', b = 2b'+1, i = 2i', j = 2j'+1)
-    const Dim K_cdk = ix3((uint32_t)V, (uint32_t)O, VO3, O3, 1);
-    const Dim Kv_cdk = ix3((uint32_t)V, (uint32_t)O, V, 1, V * V);
-    gemm(io * io * iv, iv, (int)(V * V * O), 0.5, mv(t3 + O, ix3((uint32_t)o, (uint32_t)v, 2 * O2, 2 * O, 2 * V2O3), K_cdk),
-         mv(so_vovv_.p + O * V * V, ix1(2 * O * V * V), Kv_cdk), 1.0,
-         ovw(R_.p, ix3((uint32_t)o, (uint32_t)v, o * v * v, v * v, v), ix1(1)), 0, 23, "R2_T3_vovv_b");
-    // - 1/2 sum_{c,d,k} <ak||cd> t3[b][c][d][i][j][k]
-    gemm(io * io * iv, iv, (int)(V * V * O), -0.5,
-         mv(t3 + V2O3 + O, ix3((uint32_t)o, (uint32_t)v, 2 * O2, 2 * O, 2 * V2O3), K_cdk),
-         mv(so_vovv_.p, ix1(2 * O * V * V), Kv_cdk), 1.0,
-         ovw(R_.p, ix3((uint32_t)o, (uint32_t)v, o * v * v, v * v, 1), ix1(v)), 0, 24, "R2_T3_vovv_a");
-    // - 1/2 sum_{c,km} <km||jc> t3[a][b][c][i][k][m]
-    const Dim K_ckm = ix2((uint32_t)O2, O3, 1);
-    const Dim Ko_ckm = ix2((uint32_t)O2, 1, O * V);
-    gemm(io * iv * iv, io, (int)(V * O2), -0.5,
-         mv(t3 + VO3, ix3((uint32_t)v, (uint32_t)v, 2 * O2, 2 * V2O3, 2 * VO3), K_ckm),
-         mv(so_ooov_.p + V, ix1(2 * V), Ko_ckm), 1.0,
-         ovw(R_.p, ix3((uint32_t)v, (uint32_t)v, o * v * v, v, 1), ix1(v * v)), 0, 25, "R2_T3_ooov_j");
-    // + 1/2 sum_{c,km} <km||ic> t3[a][b][c][j][k][m]
-    gemm(io * iv * iv, io, (int)(V * O2), 0.5,
-         mv(t3 + VO3 + O2, ix3((uint32_t)v, (uint32_t)v, 2 * O2, 2 * V2O3, 2 * VO3), K_ckm),
-         mv(so_ooov_.p, ix1(2 * V), Ko_ckm), 1.0,
-         ovw(R_.p, ix3((uint32_t)v, (uint32_t)v, v * v, v, 1), ix1(o * v * v)), 0, 26, "R2_T3_ooov_i");
+    // R[i][j][a][b] (a = 2a', b = 2b'+1, i = 2i', j = 2j'+1) from the previous t3, by
+    // spin blocks of the summed indices (3 of the 8 spin triples conserve spin):
+    struct Spins {
+        int s0, s1, s2;
+    };
+    const uint32_t uo = (uint32_t)o, uv = (uint32_t)v;
+    const Dim rows_ija = ix3(uo, uv, 2 * O2, 2 * O, 2 * V2O3);  // t3 rows (i', j', a') at fixed spins
+    const Dim rows_iab = ix3(uv, uv, 2 * O2, 2 * V2O3, 2 * VO3);
+    //   + 1/2 sum_{c,d,k} <bk||cd> t3[a][c][d][i][j][k]    (sc + sd = 1 + sk)
+    const Spins vb[3] = {{0, 1, 0}, {1, 0, 0}, {1, 1, 1}};
+    //   - 1/2 sum_{c,d,k} <ak||cd> t3[b][c][d][i][j][k]    (sc + sd = sk)
+    const Spins va[3] = {{0, 0, 0}, {0, 1, 1}, {1, 0, 1}};
+    for (int q = 0; q < 3; ++q) {
+        const Dim K_cdk = ix3(uv, uo, 2 * VO3, 2 * O3, 2);   // (c', d', k') in t3
+        const Dim Kv_cdk = ix3(uv, uo, 2 * V, 2, 2 * V * V);  // (c', d', k') in <bk||cd>
+        const OutView Rb = ovw(R_.p, ix3(uo, uv, o * v * v, v * v, v), ix1(1));
+        const OutView Ra = ovw(R_.p, ix3(uo, uv, o * v * v, v * v, 1), ix1(v));
+        {
+            const Spins &sp = vb[q];
+            const int64_t t3o = sp.s0 * VO3 + sp.s1 * O3 + sp.s2, io_ = sp.s0 * V + sp.s1 + sp.s2 * V * V;
+            gemm(io * io * iv, iv, (int)(v * v * o), 0.5, mv(t3 + O + t3o, rows_ija, K_cdk),
+                 mv(so_vovv_.p + O * V * V + io_, ix1(2 * O * V * V), Kv_cdk), 1.0, Rb, 0, 400 + q, "R2_T3_vovv_b");
+        }
+        {
+            const Spins &sp = va[q];
+            const int64_t t3o = sp.s0 * VO3 + sp.s1 * O3 + sp.s2, io_ = sp.s0 * V + sp.s1 + sp.s2 * V * V;
+            gemm(io * io * iv, iv, (int)(v * v * o), -0.5, mv(t3 + V2O3 + O + t3o, rows_ija, K_cdk),
+                 mv(so_vovv_.p + io_, ix1(2 * O * V * V), Kv_cdk), 1.0, Ra, 0, 403 + q, "R2_T3_vovv_a");
+        }
+    }
+    //   - 1/2 sum_{c,k,m} <km||jc> t3[a][b][c][i][k][m]    (sk + sm = 1 + sc)
+    const Spins oj[3] = {{0, 0, 1}, {0, 1, 0}, {1, 1, 1}};
+    //   + 1/2 sum_{c,k,m} <km||ic> t3[a][b][c][j][k][m]    (sk + sm = sc)
+    const Spins oi[3] = {{0, 0, 0}, {1, 0, 1}, {1, 1, 0}};
+    for (int q = 0; q < 3; ++q) {
+        const Dim K_ckm = ix3(uo, uo, 2 * O3, 2 * O, 2);              // (c', k', m') in t3
+        const Dim Ko_ckm = ix3(uo, uo, 2, 2 * O2 * V, 2 * O * V);     // (c', k', m') in <km||jc>
+        {
+            const Spins &sp = oj[q];
+            const int64_t t3o = sp.s0 * O3 + sp.s1 * O + sp.s2, io_ = sp.s0 + sp.s1 * O2 * V + sp.s2 * O * V;
+            gemm(io * iv * iv, io, (int)(v * o * o), -0.5, mv(t3 + VO3 + t3o, rows_iab, K_ckm),
+                 mv(so_ooov_.p + V + io_, ix1(2 * V), Ko_ckm), 1.0,
+                 ovw(R_.p, ix3(uv, uv, o * v * v, v, 1), ix1(v * v)), 0, 406 + q, "R2_T3_ooov_j");
+        }
+        {
+            const Spins &sp = oi[q];
+            const int64_t t3o = sp.s0 * O3 + sp.s1 * O + sp.s2, io_ = sp.s0 + sp.s1 * O2 * V + sp.s2 * O * V;
+            gemm(io * iv * iv, io, (int)(v * o * o), 0.5, mv(t3 + VO3 + O2 + t3o, rows_iab, K_ckm),
+                 mv(so_ooov_.p + io_, ix1(2 * V), Ko_ckm), 1.0,
+                 ovw(R_.p, ix3(uv, uv, v * v, v, 1), ix1(o * v * v)), 0, 409 + q, "R2_T3_ooov_i");
+        }
+    }
 
-    // ---- T3 from the previous T2 (ccsdt.cpp:1016-1058, 1235-1238)
-    // Y[a][b][c][i][j][k] = sum_e t2so[a][e][i][j] <bc||ek>:  M = (a,i,j), N = (b,c,k), K = e
-    gemm((int)(V * O2), (int)(V * V * O), (int)V, 1.0,
-         mv(t2so_.p, ix3((uint32_t)O, (uint32_t)O, V * O2, O, 1), ix1(O2)),
-         mv(so_vvvo_.p, ix3((uint32_t)V, (uint32_t)O, V * V * O, V * O, 1), ix1(O)), 0.0,
-         ovw(y3_.p, ix3((uint32_t)O, (uint32_t)O, V2O3, O2, O), ix3((uint32_t)V, (uint32_t)O, VO3, O3, 1)), -21, 21,
-         "T3_Y");
-    // Z[a][b][c][i][j][k] = sum_m t2so[a][b][i][m] <mc||jk>:  M = (a,b,i), N = (c,j,k), K = m
-    gemm((int)(V * V * O), (int)(V * O2), (int)O, 1.0,
-         mv(t2so_.p, ix3((uint32_t)V, (uint32_t)O, V * O2, O2, O), ix1(1)),
-         mv(so_ovoo_.p, ix3((uint32_t)O, (uint32_t)O, O2, O, 1), ix1(V * O2)), 0.0,
-         ovw(z3_.p, ix3((uint32_t)V, (uint32_t)O, V2O3, VO3, O2), ix3((uint32_t)O, (uint32_t)O, O3, O, 1)), -22, 22,
-         "T3_Z");
+    // ---- T3 from the previous T2 (ccsdt.cpp:1016-1058, 1235-1238), by spin blocks.
+    // Spin orbital X = 2x + s, so a block of fixed spins is a stride-2 view of
+    // spatial indices.  t2so and the integral blocks conserve spin, so of the
+    // 2^7 spin assignments of each product only 18 are non-zero; each is one
+    // contraction over spatial indices (1/7 of the dense spin-orbital flops).  The
+    // other blocks of Y and Z are zero and stay at the zero set in triples_setup.
+    for (int sa = 0; sa < 2; ++sa)
+        for (int si = 0; si < 2; ++si)
+            for (int sj = 0; sj < 2; ++sj) {
+                // Y[a][b][c][i][j][k] = sum_e t2so[a][e][i][j] <bc||ek>: se = si + sj - sa,
+                // (sb, sc, sk) with sb + sc = se + sk;  M = (a,i,j), N = (b,c,k), K = e (spatial)
+                const int se = si + sj - sa;
+                if (se < 0 || se > 1) continue;
+                const double *A = t2so_.p + sa * V * O2 + se * O2 + si * O + sj;
+                const MatView Av = mv(A, ix3(uo, uo, 2 * V * O2, 2 * O, 2), ix1(2 * O2));
+                for (int sb = 0; sb < 2; ++sb)
+                    for (int sc = 0; sc < 2; ++sc) {
+                        const int sk = sb + sc - se;
+                        if (sk < 0 || sk > 1) continue;
+                        const double *B = so_vvvo_.p + sb * V * V * O + sc * V * O + se * O + sk;
+                        double *Cp = y3_.p + sa * V2O3 + si * O2 + sj * O + sb * VO3 + sc * O3 + sk;
+                        gemm((int)(v * o * o), (int)(v * v * o), (int)v, 1.0, Av,
+                             mv(B, ix3(uv, uo, 2 * V * V * O, 2 * V * O, 2), ix1(2 * O)), 0.0,
+                             ovw(Cp, ix3(uo, uo, 2 * V2O3, 2 * O2, 2 * O), ix3(uv, uo, 2 * VO3, 2 * O3, 2)),
+                             -(300 + sa * 4 + si * 2 + sj), 310 + se * 8 + sb * 4 + sc * 2 + sk, "T3_Y");
+                    }
+            }
+    for (int sa = 0; sa < 2; ++sa)
+        for (int sb = 0; sb < 2; ++sb)
+            for (int si = 0; si < 2; ++si) {
+                // Z[a][b][c][i][j][k] = sum_m t2so[a][b][i][m] <mc||jk>: sm = sa + sb - si,
+                // (sc, sj, sk) with sm + sc = sj + sk;  M = (a,b,i), N = (c,j,k), K = m (spatial)
+                const int sm = sa + sb - si;
+                if (sm < 0 || sm > 1) continue;
+                const double *A = t2so_.p + sa * V * O2 + sb * O2 + si * O + sm;
+                const MatView Av = mv(A, ix3(uv, uo, 2 * V * O2, 2 * O2, 2 * O), ix1(2));
+                for (int sj = 0; sj < 2; ++sj)
+                    for (int sk = 0; sk < 2; ++sk) {
+                        const int sc = sj + sk - sm;
+                        if (sc < 0 || sc > 1) continue;
+                        const double *B = so_ovoo_.p + sm * V * O2 + sc * O2 + sj * O + sk;
+                        double *Cp = z3_.p + sa * V2O3 + sb * VO3 + si * O2 + sc * O3 + sj * O + sk;
+                        gemm((int)(v * v * o), (int)(v * o * o), (int)o, 1.0, Av,
+                             mv(B, ix3(uo, uo, 2 * O2, 2 * O, 2), ix1(2 * V * O2)), 0.0,
+                             ovw(Cp, ix3(uv, uo, 2 * V2O3, 2 * VO3, 2 * O2), ix3(uo, uo, 2 * O3, 2 * O, 2)),
+                             -(330 + sa * 4 + sb * 2 + si), 340 + sm * 8 + sc * 4 + sj * 2 + sk, "T3_Z");
+                    }
+            }
+    cudaEvent_t ea = nullptr, eb = nullptr, ec = nullptr;
+    if (opt_.profile) {  // a site of its own in the contraction profile (no flops)
+        ea = prof_event();
+        eb = prof_event();
+        ec = prof_event();
+        CCSD_CUDA(cudaEventRecord(ea, st_));
+        CCSD_CUDA(cudaEventRecord(eb, st_));
+    }
     k_t3_assemble(io, iv, y3_.p, z3_.p, eo_.p, ev_.p, t3_.p, st_);
+    if (opt_.profile) {
+        CCSD_CUDA(cudaEventRecord(ec, st_));
+        prof_pending_.push_back(ProfPending{"T3_assemble", ea, eb, ec, 0.0, false});
+    }
 }
 
 }  // namespace ccsd

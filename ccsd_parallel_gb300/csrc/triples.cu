@@ -8,7 +8,8 @@
 // Y and Z are contractions (engine kernels); this file builds the
 // spin-orbital integral blocks from the spatial ones, expands the spatial T2
 // into spin orbitals, and assembles T3 (both antisymmetrisers and D3 in one
-// pass, one thread per element).  Sizes: O = 2 nocc, V = 2 nvir.
+// pass, one thread per element, spin-forbidden elements left at zero).
+// Sizes: O = 2 nocc, V = 2 nvir.
 #include "common.h"
 
 namespace ccsd {
@@ -136,6 +137,10 @@ __global__ void t3_assemble_kernel(int o, int v, const double *__restrict__ Y, c
         r /= V;
         const int b = (int)(r % V);
         const int a = (int)(r / V);
+        // spin conservation: Y, Z and t3 vanish unless abc and ijk carry the same
+        // number of beta spins (20 of the 64 spin blocks); those stay at the zero
+        // the buffer was set to
+        if ((a & 1) + (b & 1) + (c & 1) != (i & 1) + (j & 1) + (k & 1)) continue;
         // P(a/bc) applied to each of P(k/ij)'s three index orders
         auto pa = [&](int p, int q, int s) {
             return at(Y, a, b, c, p, q, s) - at(Y, b, a, c, p, q, s) - at(Y, c, b, a, p, q, s);
@@ -147,6 +152,171 @@ __global__ void t3_assemble_kernel(int o, int v, const double *__restrict__ Y, c
         const double z = pc(i, j, k) - pc(j, i, k) - pc(k, j, i);
         const double den = (eo[i >> 1] - ev[a >> 1]) + (eo[j >> 1] - ev[b >> 1]) + (eo[k >> 1] - ev[c >> 1]);
         t3[idx] = (y - z) / den;
+    }
+}
+
+// The same T3 as t3_assemble_kernel, one CTA per virtual triple a < b < c
+// (C(V,3) CTAs).  Y is antisymmetric in its last two virtual indices and Z in
+// its first two, so P(a/bc) Y and P(c/ab) Z, and with them t3, are antisymmetric
+// in abc: the CTA forms the O^3 slab of (a,b,c) and writes it, with the sign of
+// each permutation, into the six slabs abc, acb, bac, bca, cab, cba.  Slabs with a
+// repeated virtual index are zero and stay at the zero the buffer was set to.
+//   ys[ijk] = Y[abc][ijk] - Y[bac][ijk] - Y[cba][ijk]     P(a/bc), slab-contiguous reads
+//   zs[ijk] = Z[abc][ijk] - Z[cba][ijk] - Z[acb][ijk]     P(c/ab)
+//   t3[abc][ijk] = ([ys(ijk) - ys(kji) - ys(ikj)] - [zs(ijk) - zs(jik) - zs(kji)]) / D3
+// The occupied permutations read shared memory at stride s_i or s_j; both are odd
+// (s_j = O + 1, s_i = O s_j + 1, O even), so a half-warp of doubles hits 16
+// distinct bank pairs.  Every global read and write is of a contiguous slab.
+__device__ __forceinline__ int64_t c3(int64_t n) { return n * (n - 1) * (n - 2) / 6; }
+
+__global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, const double *__restrict__ Y,
+                                                               const double *__restrict__ Z,
+                                                               const double *__restrict__ eo,
+                                                               const double *__restrict__ ev,
+                                                               double *__restrict__ t3) {
+    extern __shared__ double sm[];
+    const int O = 2 * o, V = 2 * v;
+    const int O3 = O * O * O, sj = O + 1, si = O * sj + 1;
+    double *ys = sm, *zs = sm + (size_t)O * si;
+    // blockIdx.x -> (a < b < c): c3(c) <= t < c3(c + 1), then r = t - c3(c) = b(b-1)/2 + a
+    const int64_t t = blockIdx.x;
+    int c = (int)cbrt(6.0 * (double)t);
+    if (c < 2) c = 2;
+    while (c3(c + 1) <= t) ++c;
+    while (c > 2 && c3(c) > t) --c;
+    const int64_t r = t - c3(c);
+    int b = (int)sqrt(2.0 * (double)r);
+    if (b < 1) b = 1;
+    while ((int64_t)(b + 1) * b / 2 <= r) ++b;
+    while (b > 1 && (int64_t)b * (b - 1) / 2 > r) --b;
+    const int a = (int)(r - (int64_t)b * (b - 1) / 2);
+    auto slab = [&](int x, int y, int z) { return (((int64_t)x * V + y) * V + z) * O3; };
+    const double *y0 = Y + slab(a, b, c), *y1 = Y + slab(b, a, c), *y2 = Y + slab(c, b, a);
+    const double *z0 = Z + slab(a, b, c), *z1 = Z + slab(c, b, a), *z2 = Z + slab(a, c, b);
+    for (int e = threadIdx.x; e < O3; e += blockDim.x) {
+        const int k = e % O, j = (e / O) % O, i = e / (O * O);
+        const int p = i * si + j * sj + k;
+        ys[p] = (y0[e] - y1[e]) - y2[e];
+        zs[p] = (z0[e] - z1[e]) - z2[e];
+    }
+    __syncthreads();
+    const int64_t s_abc = slab(a, b, c), s_acb = slab(a, c, b), s_bac = slab(b, a, c);
+    const int64_t s_bca = slab(b, c, a), s_cab = slab(c, a, b), s_cba = slab(c, b, a);
+    const double fa = ev[a >> 1], fb = ev[b >> 1], fc = ev[c >> 1];
+    for (int e = threadIdx.x; e < O3; e += blockDim.x) {
+        const int k = e % O, j = (e / O) % O, i = e / (O * O);
+        const double y = (ys[i * si + j * sj + k] - ys[k * si + j * sj + i]) - ys[i * si + k * sj + j];
+        const double z = (zs[i * si + j * sj + k] - zs[j * si + i * sj + k]) - zs[k * si + j * sj + i];
+        const double den = ((eo[i >> 1] - fa) + (eo[j >> 1] - fb)) + (eo[k >> 1] - fc);
+        const double u = (y - z) / den;
+        t3[s_abc + e] = u;
+        t3[s_acb + e] = -u;
+        t3[s_bac + e] = -u;
+        t3[s_bca + e] = u;
+        t3[s_cab + e] = u;
+        t3[s_cba + e] = -u;
+    }
+}
+
+// The kernel above spends about 30 FP64 instructions on every element, and FP64
+// issue is GB300's narrow resource (about 0.6 T instructions/s for the whole
+// GPU).  This form does the same work with far fewer: t3 is also antisymmetric
+// in ijk (Y in ij, Z in jk), so only i < j < k are evaluated and the six orders
+// filled with signs in a shared-memory output slab; elements whose occupied spins
+// do not balance the virtual ones (both sides must carry the same number of beta
+// spins) are zero and skip their loads and arithmetic.  Phases:
+//   1. ys, zs as above (spin-allowed elements only), output slab us = 0
+//   2. i < j < k: u = ([ys(ijk) - ys(kji) - ys(ikj)] - [zs(ijk) - zs(jik) - zs(kji)]) / D3,
+//      us at the six orders of ijk with their signs
+//   3. us written to the six slabs of abc with their signs (contiguous)
+__device__ __forceinline__ void decode_triple(int64_t t, int &a, int &b, int &c) {
+    c = (int)cbrt(6.0 * (double)t);
+    if (c < 2) c = 2;
+    while (c3(c + 1) <= t) ++c;
+    while (c > 2 && c3(c) > t) --c;
+    const int64_t r = t - c3(c);
+    b = (int)sqrt(2.0 * (double)r);
+    if (b < 1) b = 1;
+    while ((int64_t)(b + 1) * b / 2 <= r) ++b;
+    while (b > 1 && (int64_t)b * (b - 1) / 2 > r) --b;
+    a = (int)(r - (int64_t)b * (b - 1) / 2);
+}
+
+__global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, const double *__restrict__ Y,
+                                                                 const double *__restrict__ Z,
+                                                                 const double *__restrict__ eo,
+                                                                 const double *__restrict__ ev,
+                                                                 double *__restrict__ t3) {
+    extern __shared__ double sm[];
+    const int O = 2 * o, V = 2 * v;
+    const int O3 = O * O * O, sj = O + 1, si = O * sj + 1, P = O * si;
+    double *ys = sm, *zs = sm + P, *us = sm + 2 * P;
+    int a, b, c;
+    decode_triple(blockIdx.x, a, b, c);
+    const int sv = (a & 1) + (b & 1) + (c & 1);
+    auto slab = [&](int x, int y, int z) { return (((int64_t)x * V + y) * V + z) * O3; };
+    const double *y0 = Y + slab(a, b, c), *y1 = Y + slab(b, a, c), *y2 = Y + slab(c, b, a);
+    const double *z0 = Z + slab(a, b, c), *z1 = Z + slab(c, b, a), *z2 = Z + slab(a, c, b);
+    for (int e = threadIdx.x; e < O3; e += blockDim.x) {
+        const int k = e % O, j = (e / O) % O, i = e / (O * O);
+        const int p = i * si + j * sj + k;
+        double yv = 0.0, zv = 0.0;
+        if ((i & 1) + (j & 1) + (k & 1) == sv) {
+            yv = (y0[e] - y1[e]) - y2[e];
+            zv = (z0[e] - z1[e]) - z2[e];
+        }
+        ys[p] = yv;
+        zs[p] = zv;
+        us[p] = 0.0;
+    }
+    __syncthreads();
+    const double fa = ev[a >> 1], fb = ev[b >> 1], fc = ev[c >> 1];
+    const int nu = O * (O - 1) * (O - 2) / 6;
+    for (int t = threadIdx.x; t < nu; t += blockDim.x) {
+        int i, j, k;
+        decode_triple(t, i, j, k);
+        double u = 0.0;
+        if ((i & 1) + (j & 1) + (k & 1) == sv) {
+            const double y = (ys[i * si + j * sj + k] - ys[k * si + j * sj + i]) - ys[i * si + k * sj + j];
+            const double z = (zs[i * si + j * sj + k] - zs[j * si + i * sj + k]) - zs[k * si + j * sj + i];
+            const double den = ((eo[i >> 1] - fa) + (eo[j >> 1] - fb)) + (eo[k >> 1] - fc);
+            u = (y - z) / den;
+        }
+        us[i * si + j * sj + k] = u;
+        us[i * si + k * sj + j] = -u;
+        us[j * si + i * sj + k] = -u;
+        us[j * si + k * sj + i] = u;
+        us[k * si + i * sj + j] = u;
+        us[k * si + j * sj + i] = -u;
+    }
+    __syncthreads();
+    const int64_t s_abc = slab(a, b, c), s_acb = slab(a, c, b), s_bac = slab(b, a, c);
+    const int64_t s_bca = slab(b, c, a), s_cab = slab(c, a, b), s_cba = slab(c, b, a);
+    for (int e = threadIdx.x; e < O3; e += blockDim.x) {
+        const int k = e % O, j = (e / O) % O, i = e / (O * O);
+        const double u = us[i * si + j * sj + k];
+        t3[s_abc + e] = u;
+        t3[s_acb + e] = -u;
+        t3[s_bac + e] = -u;
+        t3[s_bca + e] = u;
+        t3[s_cab + e] = u;
+        t3[s_cba + e] = -u;
+    }
+}
+
+size_t slab_smem_bytes(int o, int arrays) {
+    const size_t O = 2 * (size_t)o, si = O * (O + 1) + 1;
+    return arrays * O * si * sizeof(double);
+}
+constexpr size_t kSlabSmemMax = 227 * 1024;
+
+template <typename Kern>
+void opt_in_smem(Kern kern, int &configured) {  // the opt-in above 48 KB is per device function
+    int dev = 0;
+    CCSD_CUDA(cudaGetDevice(&dev));
+    if (configured != dev) {
+        CCSD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlabSmemMax));
+        configured = dev;
     }
 }
 
@@ -168,6 +338,21 @@ void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st) {
 
 void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *eo, const double *ev, double *t3,
                    cudaStream_t st) {
+    const int64_t V = 2 * (int64_t)v, triples = V * (V - 1) * (V - 2) / 6;
+    static int configured_unique = -1, configured_slab = -1;
+    if (V >= 3 && slab_smem_bytes(o, 3) <= kSlabSmemMax) {  // O <= 20
+        opt_in_smem(t3_assemble_unique_kernel, configured_unique);
+        t3_assemble_unique_kernel<<<(unsigned)triples, 256, slab_smem_bytes(o, 3), st>>>(o, v, Y, Z, eo, ev, t3);
+        CCSD_LAUNCH_CHECK();
+        return;
+    }
+    if (V >= 3 && slab_smem_bytes(o, 2) <= kSlabSmemMax) {  // O <= 24
+        opt_in_smem(t3_assemble_slab_kernel, configured_slab);
+        t3_assemble_slab_kernel<<<(unsigned)triples, 256, slab_smem_bytes(o, 2), st>>>(o, v, Y, Z, eo, ev, t3);
+        CCSD_LAUNCH_CHECK();
+        return;
+    }
+    // fewer than three virtual spin orbitals (t3 is zero) or O^3 slabs beyond shared memory
     const size_t n = (size_t)64 * o * o * o * v * v * v;
     t3_assemble_kernel<<<blocks_for(n), 256, 0, st>>>(o, v, Y, Z, eo, ev, t3);
     CCSD_LAUNCH_CHECK();

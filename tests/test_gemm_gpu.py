@@ -41,7 +41,13 @@ SHAPES = [(1, 1, 1), (5, 7, 3), (128, 128, 32), (200, 70, 1000), (130, 33, 2500)
           (1000, 20, 64), (64, 513, 4097), (5000, 1, 300), (1, 700, 9000), (40, 1000, 500)]
 
 
-@pytest.mark.parametrize("M,N,K", SHAPES)
+# short side <= 16 with a long K: the skinny form (K-split, B staged in shared
+# memory), with the short side in M, in N, or a single column
+SKINNY = [(2000, 6, 3000), (7, 900, 1200), (240, 1, 100000), (3000, 16, 257), (100, 9, 256), (64, 3, 5000),
+          (33, 2, 70000)]
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES + SKINNY)
 def test_fp64_kernel(M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 13 + K)
     A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)

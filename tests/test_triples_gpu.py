@@ -65,6 +65,18 @@ def test_ccsdt1a_amplitudes_match_oracle_every_update():
     assert abs(rc["e_corr"] - r["e_corr"]) > 1e-6
 
 
+@pytest.mark.parametrize("o,v", [(11, 3), (13, 2), (1, 3), (2, 1)])
+def test_ccsdt1a_assembly_forms_match_oracle(o, v):
+    """Every form of the T3 assembly against the oracle: O = 2 nocc = 22 takes the
+    two-slab form, 26 the element-wise one, O = 2 the unique-ijk form with no
+    occupied triple, and nvir = 1 leaves fewer than three virtual spin orbitals
+    (element-wise form, T3 = 0)."""
+    fock, b = _case(dict(nocc=o, nvir=v, naux=2 * (o + v), seed=o + 5 * v, sigma=0.2))
+    ref = SpinOrbitalCCSD(fock, syn.eri_from_df(b), o, method=1).run(toler=1e-14, max_passes=4)
+    r = cg.solve(fock, o, df=b, method="ccsdt-1a", fixed_iterations=4)
+    np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
+
+
 @pytest.mark.parametrize("prec", ["split3", "split2"])
 def test_ccsdt1a_split_precision(prec):
     """Split precision on the same method: the FP64 answer within 1e-8."""
