@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--extras", type=int, default=1,
                     help="also measure the Lambda gradient at this workload and the 64-system batched solve")
+    ap.add_argument("--method", default="ccsd", choices=["ccsd", "ccsdt-1a"],
+                    help="amplitude equations of the timed run (ccsdt-1a: no DIIS, as the reference runs it)")
     ap.add_argument("--sites-out", default="",
                     help="write the per-contraction-site device profile of the timed run (JSON) here")
     return ap.parse_args()
@@ -325,8 +327,9 @@ def main():
     barrier(world)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         t0 = time.perf_counter()
+        diis = WORKLOAD["diis"] if args.method == "ccsd" else 0
         s = cg.Solver(fock, o, df=df, precision=args.precision, fixed_iterations=U,
-                      diis_size=WORKLOAD["diis"], diis_start=2, profile=True)
+                      diis_size=diis, diis_start=2, profile=True, method=args.method)
         r = s.solve(amplitudes=True)
         t1 = time.perf_counter()
     prof = s.profile()
@@ -356,8 +359,8 @@ def main():
     fp64 = {}
     nf = min(args.fp64_updates, U)
     if nf > 0:
-        with cg.Solver(fock, o, df=df, precision="fp64", fixed_iterations=nf, diis_size=WORKLOAD["diis"],
-                       diis_start=2) as s64:
+        with cg.Solver(fock, o, df=df, precision="fp64", fixed_iterations=nf, diis_size=diis,
+                       diis_start=2, method=args.method) as s64:
             r64 = s64.solve(amplitudes=True)
         ms64 = np.asarray(r64["update_ms"])
         f64_s = float(ms64[min(2, nf - 1):].mean()) / 1e3
@@ -389,7 +392,7 @@ def main():
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=K, warmup=W,
         ms_per_step=value * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
         dtype=f"bf16x{nprod}-products/fp32-acc + f64 ({args.precision})", data="synthetic",
-        config=dict(workload=f"synthetic closed-shell CCSD nocc={o} nvir={v} naux={q} (seed "
+        config=dict(workload=f"synthetic closed-shell {args.method.upper()} nocc={o} nvir={v} naux={q} (seed "
                              f"{WORKLOAD['seed']}), DIIS({WORKLOAD['diis']}), 1 step = 1 amplitude update",
                     precision=args.precision, l2="inputs larger than L2: split W+/W- planes "
                     f"{SLICES_PLANES.get(args.precision, 0) * 2 * (v * (v + 1) // 2) ** 2 * 2 / 1e9:.0f} GB "

@@ -56,6 +56,12 @@ struct alignas(8) Bars {
     int never;  // stays 0: a wait that must not be cut short by another role
 };
 
+// Behind the barriers: the tile's output column offsets and column scales, set
+// once by the epilogue warps instead of per element (a 3-level column view costs
+// tens of integer instructions per offset).
+__host__ __device__ constexpr size_t epi_offset() { return (sizeof(Bars) + 15) / 16 * 16; }
+__host__ __device__ constexpr size_t epi_bytes(int BN) { return (size_t)BN * (sizeof(int64_t) + sizeof(double)); }
+
 }  // namespace
 
 // What one CTA computes: a 128 x BN output tile of one contraction.  Rows of
@@ -268,6 +274,14 @@ __global__ void __launch_bounds__(kThreads, MINB)
         // epilogue warps 2..5; TMEM lane quarter = warp % 4
         const int q = warp & 3;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        int64_t *s_coff = (int64_t *)((unsigned char *)bars + epi_offset());
+        double *s_sb = (double *)(s_coff + BN);
+        for (int j = threadIdx.x - 64; j < BN; j += 128) {
+            const int n = n0 + j;
+            s_coff[j] = n < N ? dim_off(C.col, (uint32_t)n) : -1;
+            s_sb[j] = n < N ? scaleB[n] : 0.0;
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps only
         int32_t iacc[BN];
 #pragma unroll
         for (int j = 0; j < BN; ++j) iacc[j] = 0;
@@ -320,15 +334,15 @@ __global__ void __launch_bounds__(kThreads, MINB)
                     double cold[kCB];
 #pragma unroll
                     for (int j = 0; j < kCB; ++j) {
-                        const int n = n0 + g * 32 + j0 + j;
-                        off[j] = (mval && n < N) ? crow + dim_off(C.col, (uint32_t)n) : -1;
+                        const int64_t co = s_coff[g * 32 + j0 + j];
+                        off[j] = (mval && co >= 0) ? crow + co : -1;
                         cold[j] = (direct && beta != 0.0 && off[j] >= 0) ? C.p[off[j]] : 0.0;
                     }
 #pragma unroll
                     for (int j = 0; j < kCB; ++j) {
                         if (off[j] < 0) continue;
                         const int n = n0 + g * 32 + j0 + j;
-                        const double val = sa * scaleB[n] *
+                        const double val = sa * s_sb[g * 32 + j0 + j] *
                                            ((double)iacc[g * 32 + j0 + j] + (double)__uint_as_float(r[j0 + j]));
                         if (direct) {
                             double out = alpha * val;
@@ -555,7 +569,7 @@ constexpr size_t kernel_smem() {
     constexpr int NST = NSTF > 0 ? NSTF : num_stages(S, BN);
     // two-per-SM variants request at least 80 KB so that no third CTA (and its
     // TMEM allocation) can become resident on the SM
-    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + sizeof(Bars) + 1024;
+    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + epi_offset() + epi_bytes(BN) + 1024;
     return (MINB > 1 && need < 80 * 1024) ? 80 * 1024 : need;
 }
 

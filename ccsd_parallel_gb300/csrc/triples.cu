@@ -169,6 +169,27 @@ __global__ void t3_assemble_kernel(int o, int v, const double *__restrict__ Y, c
 // distinct bank pairs.  Every global read and write is of a contiguous slab.
 __device__ __forceinline__ int64_t c3(int64_t n) { return n * (n - 1) * (n - 2) / 6; }
 
+// -x by flipping the sign bit on the integer pipe (the same value as -x for every
+// input), so the six signed copies of each element cost no FP64 issue slots.
+__device__ __forceinline__ double negd(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+
+// Single-precision estimates (FP32 issue is cheap, FP64 is not); the integer loops
+// make the result exact.
+__device__ __forceinline__ void decode_triple(int64_t t, int &a, int &b, int &c) {
+    c = (int)cbrtf(6.0f * (float)t);
+    if (c < 2) c = 2;
+    while (c3(c + 1) <= t) ++c;
+    while (c > 2 && c3(c) > t) --c;
+    const int64_t r = t - c3(c);
+    b = (int)sqrtf(2.0f * (float)r);
+    if (b < 1) b = 1;
+    while ((int64_t)(b + 1) * b / 2 <= r) ++b;
+    while (b > 1 && (int64_t)b * (b - 1) / 2 > r) --b;
+    a = (int)(r - (int64_t)b * (b - 1) / 2);
+}
+
 __global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, const double *__restrict__ Y,
                                                                const double *__restrict__ Z,
                                                                const double *__restrict__ eo,
@@ -179,17 +200,8 @@ __global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, con
     const int O3 = O * O * O, sj = O + 1, si = O * sj + 1;
     double *ys = sm, *zs = sm + (size_t)O * si;
     // blockIdx.x -> (a < b < c): c3(c) <= t < c3(c + 1), then r = t - c3(c) = b(b-1)/2 + a
-    const int64_t t = blockIdx.x;
-    int c = (int)cbrt(6.0 * (double)t);
-    if (c < 2) c = 2;
-    while (c3(c + 1) <= t) ++c;
-    while (c > 2 && c3(c) > t) --c;
-    const int64_t r = t - c3(c);
-    int b = (int)sqrt(2.0 * (double)r);
-    if (b < 1) b = 1;
-    while ((int64_t)(b + 1) * b / 2 <= r) ++b;
-    while (b > 1 && (int64_t)b * (b - 1) / 2 > r) --b;
-    const int a = (int)(r - (int64_t)b * (b - 1) / 2);
+    int a, b, c;
+    decode_triple(blockIdx.x, a, b, c);
     auto slab = [&](int x, int y, int z) { return (((int64_t)x * V + y) * V + z) * O3; };
     const double *y0 = Y + slab(a, b, c), *y1 = Y + slab(b, a, c), *y2 = Y + slab(c, b, a);
     const double *z0 = Z + slab(a, b, c), *z1 = Z + slab(c, b, a), *z2 = Z + slab(a, c, b);
@@ -209,12 +221,13 @@ __global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, con
         const double z = (zs[i * si + j * sj + k] - zs[j * si + i * sj + k]) - zs[k * si + j * sj + i];
         const double den = ((eo[i >> 1] - fa) + (eo[j >> 1] - fb)) + (eo[k >> 1] - fc);
         const double u = (y - z) / den;
+        const double nu_ = negd(u);
         t3[s_abc + e] = u;
-        t3[s_acb + e] = -u;
-        t3[s_bac + e] = -u;
+        t3[s_acb + e] = nu_;
+        t3[s_bac + e] = nu_;
         t3[s_bca + e] = u;
         t3[s_cab + e] = u;
-        t3[s_cba + e] = -u;
+        t3[s_cba + e] = nu_;
     }
 }
 
@@ -229,19 +242,6 @@ __global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, con
 //   2. i < j < k: u = ([ys(ijk) - ys(kji) - ys(ikj)] - [zs(ijk) - zs(jik) - zs(kji)]) / D3,
 //      us at the six orders of ijk with their signs
 //   3. us written to the six slabs of abc with their signs (contiguous)
-__device__ __forceinline__ void decode_triple(int64_t t, int &a, int &b, int &c) {
-    c = (int)cbrt(6.0 * (double)t);
-    if (c < 2) c = 2;
-    while (c3(c + 1) <= t) ++c;
-    while (c > 2 && c3(c) > t) --c;
-    const int64_t r = t - c3(c);
-    b = (int)sqrt(2.0 * (double)r);
-    if (b < 1) b = 1;
-    while ((int64_t)(b + 1) * b / 2 <= r) ++b;
-    while (b > 1 && (int64_t)b * (b - 1) / 2 > r) --b;
-    a = (int)(r - (int64_t)b * (b - 1) / 2);
-}
-
 __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, const double *__restrict__ Y,
                                                                  const double *__restrict__ Z,
                                                                  const double *__restrict__ eo,
@@ -282,12 +282,13 @@ __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, c
             const double den = ((eo[i >> 1] - fa) + (eo[j >> 1] - fb)) + (eo[k >> 1] - fc);
             u = (y - z) / den;
         }
+        const double nu_ = negd(u);
         us[i * si + j * sj + k] = u;
-        us[i * si + k * sj + j] = -u;
-        us[j * si + i * sj + k] = -u;
+        us[i * si + k * sj + j] = nu_;
+        us[j * si + i * sj + k] = nu_;
         us[j * si + k * sj + i] = u;
         us[k * si + i * sj + j] = u;
-        us[k * si + j * sj + i] = -u;
+        us[k * si + j * sj + i] = nu_;
     }
     __syncthreads();
     const int64_t s_abc = slab(a, b, c), s_acb = slab(a, c, b), s_bac = slab(b, a, c);
@@ -295,12 +296,13 @@ __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, c
     for (int e = threadIdx.x; e < O3; e += blockDim.x) {
         const int k = e % O, j = (e / O) % O, i = e / (O * O);
         const double u = us[i * si + j * sj + k];
+        const double nu_ = negd(u);
         t3[s_abc + e] = u;
-        t3[s_acb + e] = -u;
-        t3[s_bac + e] = -u;
+        t3[s_acb + e] = nu_;
+        t3[s_bac + e] = nu_;
         t3[s_bca + e] = u;
         t3[s_cab + e] = u;
-        t3[s_cba + e] = -u;
+        t3[s_cba + e] = nu_;
     }
 }
 
