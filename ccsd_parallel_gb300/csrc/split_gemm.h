@@ -54,11 +54,13 @@ class SplitEngine {
     // The tensor-core tile is 128 rows by at most 128 columns: a product whose
     // row count is short and column count long runs faster transposed.
     static bool prefer_swap(int M, int N) { return M < 128 && N > M; }
-    // also put C's unit-stride index in the rows (TMEM lanes), so that the
-    // epilogue's lanes write consecutive addresses; N >= 128 keeps the swapped
-    // problem's row dimension a full MMA tile
+    // also put the index of C with the smaller innermost stride in the rows
+    // (TMEM lanes), so that the epilogue's lanes write the fewest sectors per
+    // store; N >= 128 keeps the swapped problem's row dimension a full MMA tile
     static bool prefer_swap(int M, int N, const OutView &C) {
-        return prefer_swap(M, N) || (C.col.s2 == 1 && C.row.s2 != 1 && N >= 128);
+        const int64_t rs = C.row.s2 < 0 ? -C.row.s2 : C.row.s2;
+        const int64_t cs = C.col.s2 < 0 ? -C.col.s2 : C.col.s2;
+        return prefer_swap(M, N) || (cs < rs && N >= 128);
     }
     // Negative cache keys name amplitude-derived operands that several
     // contractions of one update share; begin_update() invalidates them.
