@@ -567,18 +567,20 @@ void Engine::residual() {
     tau_op(t1, t2, tau_.p);
     theta_op(t1, t2, th1_.p, th2_.p);
     // the split forms of tau as (ij|cd) (key -1) and of the ring view of t2
-    // (key -2) are shared by several contractions of this update
+    // (key -2) are shared by several contractions of this update, and so are
+    // tau read as [i][(l,c,d)] (key -5: Foo, R1_ovvv_tau) and as [a][(k,l,d)]
+    // (key -6: Fvv, R1_ovoo_tau)
     if (split_ && opt_.precision != CCSD_PREC_FP64) split_->begin_update();
 
     // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d]
     copy(Foo_.p, f_oo_off_.p, (size_t)(o2));
     gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
-         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, 0, "Foo");
+         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, -5, "Foo");
     // Fvv[a][c] = f_vv' - sum_{kld} Lovov[k,c,l,d] tau[k,l,a,d]
     copy(Fvv_.p, f_vv_off_.p, (size_t)(v2));
     gemm(iv, iv, (int)(o * o * v), -1.0, mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)),
          mv(Lovov_.p, ix1(o * v), ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1)), 1.0,
-         ovw(Fvv_.p, ix1(v), ix1(1)), 0, 2, "Fvv");
+         ovw(Fvv_.p, ix1(v), ix1(1)), -6, 2, "Fvv");
     // Fov[k][c] = f_ov + sum_ld Lovov[k,c,l,d] t1[l,d]
     copy(Fov_.p, f_ov_.p, (size_t)(ov));
     gemm((int)ov, 1, (int)ov, 1.0, mv(Lovov_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
@@ -625,12 +627,12 @@ void Engine::residual() {
     // + sum_kcd Lovvv[k,d,a,c] tau[i,k,c,d]
     gemm(io, iv, (int)(o * v2), 1.0, mv(tau, ix1(ov2), ix1(1)),
          mv(Lovvv_.p, ix1(v), ix3((uint32_t)v, (uint32_t)v, v * v2, 1, v2)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)), 0, 3, "R1_ovvv_tau");
+         ovw(R1_.p, ix1(v), ix1(1)), -5, 3, "R1_ovvv_tau");
     // - sum_klc Lovoo[l,c,k,i] tau[k,l,a,c]
     gemm(io, iv, (int)(o2 * v), -1.0,
          mv(Lovoo_.p, ix1(1), ix3((uint32_t)o, (uint32_t)v, o, v * o2, o2)),
          mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)), 1.0,
-         ovw(R1_.p, ix1(v), ix1(1)), 4, 0, "R1_ovoo_tau");
+         ovw(R1_.p, ix1(v), ix1(1)), 4, -6, "R1_ovoo_tau");
 
     // ---- Woooo[k][l][i][j] ------------------------------------------------
     axpby((int)o2, (int)o2, 1.0, mv(oooo_.p, ix2((uint32_t)o, o * o2, o), ix2((uint32_t)o, o2, 1)),
@@ -863,9 +865,10 @@ void Engine::diis_step(int update_index) {
 void Engine::solve(ccsd_result *res) {
     const int o = o_, v = v_;
     const size_t nT1 = (size_t)o * v, nT2 = nT1 * o * v;
-    diis_t_.clear();
-    diis_e_.clear();
+    // the DIIS vectors stay allocated between solves (2 m amplitude-sized
+    // cudaMallocs cost tens of ms at the bench size); only the history restarts
     diis_count_ = diis_next_ = 0;
+    std::fill(diis_b_.begin(), diis_b_.end(), 0.0);
     prof_.clear();
     prof_pending_.clear();
     prof_update_ms_ = 0.0;

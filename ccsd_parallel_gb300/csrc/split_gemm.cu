@@ -862,8 +862,19 @@ void SplitEngine::free_op(SplitOperand &op) {
     op.bytes = 0;
 }
 
+// Rows are padded to a multiple of 32 for the splitter's tiles, not to the MMA
+// tile: TMA boxes that run past an operand's rows read the next plane (or the
+// map's zero fill after the last one), and those rows only reach output rows or
+// columns the epilogue discards.  The planes together keep at least 160 rows so
+// that no box (128 rows for A, at most 160 for B) is taller than the map.
+static int split_rows_pad(int rows, int nslices) {
+    const int r32 = (rows + 31) / 32 * 32;
+    const int min_rows = ((160 + nslices - 1) / nslices + 31) / 32 * 32;
+    return r32 > min_rows ? r32 : min_rows;
+}
+
 void SplitEngine::ensure(SplitOperand &op, int rows, int K) {
-    const int rows_pad = (rows + BM - 1) / BM * BM;
+    const int rows_pad = split_rows_pad(rows, nslices_);
     const int kpad = (K + BK - 1) / BK * BK;
     const size_t need = (size_t)nslices_ * rows_pad * kpad * 2;
     if (!op.planes || need > op.bytes || (size_t)rows_pad > op.scale_cap) {
