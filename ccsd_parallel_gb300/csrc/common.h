@@ -32,26 +32,56 @@ struct Error : std::runtime_error {
 // An unused level keeps the extent UINT32_MAX, so a 1-level dim is i2 = idx
 // and a 2-level dim is (i1, i2).  This lets a GEMM read a 4-index tensor in
 // any grouping without a copy.
+// The divisions by e2 and e1 are multiply-highs with precomputed constants
+// (Granlund & Montgomery 1994, the round-up form for 32-bit operands):
+// n / e = (umulhi(m, n) + n) >> l with l = ceil(log2 e) and
+// m = floor(2^32 (2^l - e) / e) + 1, exact for every 32-bit n.  A 1-level dim
+// skips the divisions altogether; these offsets are computed per element in the
+// splitter, the FP64 kernels and the epilogues.
 struct Dim {
     uint32_t e1 = 0xFFFFFFFFu, e2 = 0xFFFFFFFFu;
     int64_t s0 = 0, s1 = 0, s2 = 0;
+    uint32_t m1 = 0, m2 = 0, l1 = 0, l2 = 0;  // division constants for e1, e2
 };
 
+__host__ __device__ inline uint32_t dim_udiv(uint32_t n, uint32_t m, uint32_t l) {
+#ifdef __CUDA_ARCH__
+    const uint32_t t = __umulhi(m, n);
+#else
+    const uint32_t t = (uint32_t)(((uint64_t)m * n) >> 32);
+#endif
+    return (uint32_t)(((uint64_t)t + n) >> l);
+}
+
 __host__ __device__ inline int64_t dim_off(const Dim &d, uint32_t idx) {
-    uint32_t i2 = idx % d.e2;
-    uint32_t r = idx / d.e2;
-    uint32_t i1 = r % d.e1;
-    uint32_t i0 = r / d.e1;
+    if (d.e2 == 0xFFFFFFFFu) return (int64_t)idx * d.s2;
+    const uint32_t q = dim_udiv(idx, d.m2, d.l2), i2 = idx - q * d.e2;
+    if (d.e1 == 0xFFFFFFFFu) return (int64_t)q * d.s1 + (int64_t)i2 * d.s2;
+    const uint32_t i0 = dim_udiv(q, d.m1, d.l1), i1 = q - i0 * d.e1;
     return (int64_t)i0 * d.s0 + (int64_t)i1 * d.s1 + (int64_t)i2 * d.s2;
+}
+
+inline void dim_magic(uint32_t e, uint32_t &m, uint32_t &l) {
+    m = l = 0;
+    if (e == 0) return;  // an empty view: no index reaches the division
+    uint32_t ll = 0;
+    while (ll < 32 && (1ull << ll) < e) ++ll;
+    l = ll;
+    m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << ll) - e)) / e + 1);
 }
 
 // Helpers to build dims.
 inline Dim ix1(int64_t s) { Dim d; d.s2 = s; return d; }
 inline Dim ix2(uint32_t e_inner, int64_t s_outer, int64_t s_inner) {
-    Dim d; d.e2 = e_inner; d.s1 = s_outer; d.s2 = s_inner; return d;
+    Dim d; d.e2 = e_inner; d.s1 = s_outer; d.s2 = s_inner;
+    dim_magic(e_inner, d.m2, d.l2);
+    return d;
 }
 inline Dim ix3(uint32_t e_mid, uint32_t e_inner, int64_t s_outer, int64_t s_mid, int64_t s_inner) {
-    Dim d; d.e1 = e_mid; d.e2 = e_inner; d.s0 = s_outer; d.s1 = s_mid; d.s2 = s_inner; return d;
+    Dim d; d.e1 = e_mid; d.e2 = e_inner; d.s0 = s_outer; d.s1 = s_mid; d.s2 = s_inner;
+    dim_magic(e_mid, d.m1, d.l1);
+    dim_magic(e_inner, d.m2, d.l2);
+    return d;
 }
 
 // A read-only matrix view rows x cols over a tensor.

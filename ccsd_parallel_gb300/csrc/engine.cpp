@@ -714,7 +714,7 @@ void Engine::residual() {
          ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
     // - sum_k t1[k,a] sum_c (ki|bc) t1[j,c]: Vk[k][i][b][j] = sum_c oovv[k,i,b,c] t1[j,c]
     gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
-         ovw(Vk_.p, ix1(o), ix1(1)), 0, 0, "Rp_oovv_t1");
+         ovw(Vk_.p, ix1(o), ix1(1)), 15, 0, "Rp_oovv_t1");
     gemm((int)(o * v * o), iv, io, -1.0,
          mv(Vk_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
          1.0, ovw(Rp_.p, ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1), ix1(v)), 0, 0, "Rp_oovv_t1t1");
@@ -724,7 +724,7 @@ void Engine::residual() {
                ovw(tmpB_.p, ix1(o), ix1(1)));
     gemm((int)(o * ov), io, iv, 1.0,
          mv(ovov_.p, ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1), ix1(o * v)), mv(t1, ix1(v), ix1(1)),
-         1.0, ovw(tmpB_.p, ix1(o), ix1(1)), 0, 0, "Rp_ovov_t1");
+         1.0, ovw(tmpB_.p, ix1(o), ix1(1)), 16, 0, "Rp_ovov_t1");
     gemm((int)(o2 * v), iv, io, -1.0,
          mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
          1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
