@@ -652,9 +652,13 @@ void Engine::residual() {
 
     // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
     copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
-    // + sum_d (kc|ad) t1[i,d]: M = (k,c,a), N = i, K = d
-    gemm((int)(ov * v), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
-         ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)), 6, 0, "Wvoov_t1v");
+    // + sum_d (kc|ad) t1[i,d] is the product Y[(p,q,r)][j] = sum_s (pq|rs) t1[j,s] that
+    // also opens Rp (Rp[i][j][a][b] = Y[(i,a,b)][j], its first write of the update):
+    // Y is formed once, into Rp, and Wvoov[i][a][k][c] += Y[(k,c,a)][i] = Rp[k][i][c][a]
+    gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
+         ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
+    axpby((int)(ov * v), io, 1.0, mv(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 1.0,
+          ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)));
     // - sum_l (kc|li) t1[l,a]: M = (i,k,c) (c, contiguous in Wvoov, innermost), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), mv(t1, ix1(1), ix1(v)),
@@ -709,9 +713,7 @@ void Engine::residual() {
     }
 
     // ---- Rp (terms under P(ij,ab)) -----------------------------------------
-    // + sum_c (ia|bc) t1[j,c]: M = (i,a,b), N = j, K = c
-    gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
-         ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
+    // + sum_c (ia|bc) t1[j,c] is already in Rp (formed with Wvoov above)
     // - sum_k t1[k,a] sum_c (ki|bc) t1[j,c]: Vk[k][i][b][j] = sum_c oovv[k,i,b,c] t1[j,c]
     gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
          ovw(Vk_.p, ix1(o), ix1(1)), 15, 0, "Rp_oovv_t1");

@@ -34,6 +34,20 @@ __global__ void axpby_view_kernel(int R, int C, double alpha, MatView X, double 
     }
 }
 
+// R * C < 2^32: 32-bit indices, and (r, c) = divmod(idx, C) as a multiply-high
+// with the constants (cm, cl) of C (the same form as the view offsets)
+__global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, double alpha, MatView X, double beta,
+                                    OutView Y) {
+    const uint32_t total = (uint32_t)R * (uint32_t)C;
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const uint32_t r = dim_udiv(idx, cm, cl), c = idx - r * (uint32_t)C;
+        double *y = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
+        double v = alpha == 0.0 ? 0.0 : alpha * X.p[dim_off(X.row, r) + dim_off(X.col, c)];
+        if (beta != 0.0) v = fma(beta, *y, v);
+        *y = v;
+    }
+}
+
 __global__ void tau_kernel(int o, int v, const double *t1, const double *t2, double *tau) {
     size_t total = (size_t)o * o * v * v;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
@@ -181,7 +195,13 @@ long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
                 cudaStream_t st) {
     if (R <= 0 || C <= 0) return;
-    axpby_view_kernel<<<grid_for((size_t)R * C), 256, 0, st>>>(R, C, alpha, X, beta, Y);
+    if ((size_t)R * C < ((size_t)1 << 32) - ((size_t)1 << 22)) {  // idx + grid stride stays below 2^32
+        uint32_t cm, cl;
+        dim_magic((uint32_t)C, cm, cl);
+        axpby_view32_kernel<<<grid_for((size_t)R * C), 256, 0, st>>>(R, C, cm, cl, alpha, X, beta, Y);
+    } else {
+        axpby_view_kernel<<<grid_for((size_t)R * C), 256, 0, st>>>(R, C, alpha, X, beta, Y);
+    }
     CCSD_LAUNCH_CHECK();
 }
 
