@@ -34,6 +34,49 @@ __global__ void axpby_view_kernel(int R, int C, double alpha, MatView X, double 
     }
 }
 
+// Y = alpha X + beta Y as a permutation over four indices (three row levels and
+// the column) whose X strides and Y strides differ: a 32 x 32 tile over the
+// index that is unit-stride in X (p) and the one unit-stride in Y (q) goes
+// through shared memory, so that reads run along p and writes along q.  The
+// other two indices and the tile numbers come from blockIdx.x.
+struct PermIndex {
+    uint32_t ext[4];
+    int64_t xs[4], ys[4];
+};
+
+__global__ void __launch_bounds__(256) permute_axpby_kernel(PermIndex P, int p, int q, int u, int w, uint32_t tp,
+                                                            uint32_t tq, double alpha, const double *__restrict__ X,
+                                                            double beta, double *__restrict__ Y) {
+    __shared__ double t[32][33];
+    uint32_t b = blockIdx.x;
+    const uint32_t ip0 = (b % tp) * 32;
+    b /= tp;
+    const uint32_t iq0 = (b % tq) * 32;
+    b /= tq;
+    const uint32_t iu = b % P.ext[u], iw = b / P.ext[u];
+    const int64_t xb = (int64_t)iu * P.xs[u] + (int64_t)iw * P.xs[w];
+    const int64_t yb = (int64_t)iu * P.ys[u] + (int64_t)iw * P.ys[w];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+        const uint32_t ip = ip0 + tx, iq = iq0 + ty + j;
+        double v = 0.0;
+        if (ip < P.ext[p] && iq < P.ext[q]) v = X[xb + (int64_t)ip * P.xs[p] + (int64_t)iq * P.xs[q]];
+        t[ty + j][tx] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+        const uint32_t iq = iq0 + tx, ip = ip0 + ty + j;
+        if (ip < P.ext[p] && iq < P.ext[q]) {
+            double *y = Y + yb + (int64_t)ip * P.ys[p] + (int64_t)iq * P.ys[q];
+            double v = alpha == 0.0 ? 0.0 : alpha * t[tx][ty + j];
+            if (beta != 0.0) v = fma(beta, *y, v);
+            *y = v;
+        }
+    }
+}
+
 // R * C < 2^32: 32-bit indices, and (r, c) = divmod(idx, C) as a multiply-high
 // with the constants (cm, cl) of C (the same form as the view offsets)
 __global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, double alpha, MatView X, double beta,
@@ -192,9 +235,66 @@ std::atomic<long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+namespace {
+// Row levels (outer, middle, inner) of a view over R rows: extents and strides.
+bool row_levels(int R, const Dim &d, uint32_t ext[3], int64_t str[3]) {
+    if (d.e2 == 0xFFFFFFFFu) {
+        ext[0] = 1; ext[1] = 1; ext[2] = (uint32_t)R;
+        str[0] = 0; str[1] = 0; str[2] = d.s2;
+        return true;
+    }
+    if (d.e1 == 0xFFFFFFFFu) {
+        if (R % d.e2) return false;
+        ext[0] = 1; ext[1] = (uint32_t)(R / d.e2); ext[2] = d.e2;
+        str[0] = 0; str[1] = d.s1; str[2] = d.s2;
+        return true;
+    }
+    const uint64_t inner = (uint64_t)d.e1 * d.e2;
+    if (R % inner) return false;
+    ext[0] = (uint32_t)(R / inner); ext[1] = d.e1; ext[2] = d.e2;
+    str[0] = d.s0; str[1] = d.s1; str[2] = d.s2;
+    return true;
+}
+
+// The permute form when both views are plain 4-index views with the same row
+// levels and 1-level columns, and their unit-stride indices differ.
+bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y, cudaStream_t st) {
+    if (X.col.e2 != 0xFFFFFFFFu || Y.col.e2 != 0xFFFFFFFFu) return false;
+    if (X.row.e1 != Y.row.e1 || X.row.e2 != Y.row.e2) return false;
+    PermIndex P;
+    int64_t xr[3], yr[3];
+    uint32_t ex[3], ey[3];
+    if (!row_levels(R, X.row, ex, xr) || !row_levels(R, Y.row, ey, yr)) return false;
+    for (int i = 0; i < 3; ++i) {
+        P.ext[i] = ex[i];
+        P.xs[i] = xr[i];
+        P.ys[i] = yr[i];
+    }
+    P.ext[3] = (uint32_t)C;
+    P.xs[3] = X.col.s2;
+    P.ys[3] = Y.col.s2;
+    int p = -1, q = -1;
+    for (int i = 0; i < 4; ++i) {
+        if (P.ext[i] > 1 && P.xs[i] == 1 && p < 0) p = i;
+        if (P.ext[i] > 1 && P.ys[i] == 1 && q < 0) q = i;
+    }
+    if (p < 0 || q < 0 || p == q || P.ext[p] < 8 || P.ext[q] < 8) return false;
+    int rest[2], nr = 0;
+    for (int i = 0; i < 4; ++i)
+        if (i != p && i != q) rest[nr++] = i;
+    const uint32_t tp = (P.ext[p] + 31) / 32, tq = (P.ext[q] + 31) / 32;
+    const uint64_t blocks = (uint64_t)tp * tq * P.ext[rest[0]] * P.ext[rest[1]];
+    if (blocks >= (1ull << 31)) return false;
+    permute_axpby_kernel<<<(unsigned)blocks, 256, 0, st>>>(P, p, q, rest[0], rest[1], tp, tq, alpha, X.p, beta, Y.p);
+    CCSD_LAUNCH_CHECK();
+    return true;
+}
+}  // namespace
+
 void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
                 cudaStream_t st) {
     if (R <= 0 || C <= 0) return;
+    if (try_permute_axpby(R, C, alpha, X, beta, Y, st)) return;
     if ((size_t)R * C < ((size_t)1 << 32) - ((size_t)1 << 22)) {  // idx + grid stride stays below 2^32
         uint32_t cm, cl;
         dim_magic((uint32_t)C, cm, cl);
