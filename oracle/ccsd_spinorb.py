@@ -20,6 +20,10 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
                                                                 ``ccsdt.cpp:640-670``
   Each pass forms T1/T2 from the previous T3 and T3 from the previous T2
   (``ccsdt.cpp:255-271``); T3 starts at zero.
+* CCSDT-1b (``Method_Nr == 2``): CCSDT-1a plus the T3 T1 term of T2
+  (``ccsdt.cpp:676-700``):
+  + 1/2 <kl||cd> [- t_ikj^acd t_l^b + t_ikj^bcd t_l^a - t_klj^adb t_i^c
+                  + t_kli^adb t_j^c + 2 t_ijk^abc t_l^d]
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -65,9 +69,9 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 class SpinOrbitalCCSD:
     def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
-        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a (the reference's Method_Nr)."""
-        if method not in (-1, 1):
-            raise ValueError("method must be -1 (CCSD1) or 1 (CCSDT-1a)")
+        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b (the reference's Method_Nr)."""
+        if method not in (-1, 1, 2):
+            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a) or 2 (CCSDT-1b)")
         self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
@@ -204,6 +208,13 @@ class SpinOrbitalCCSD:
                   - 0.5 * np.einsum("akcd,bcdijk->abij", self.gvovv, t3, **ES)
                   - 0.5 * np.einsum("kmjc,abcikm->abij", self.gooov, t3, **ES)
                   + 0.5 * np.einsum("kmic,abcjkm->abij", self.gooov, t3, **ES))
+        if self.method >= 2 and t3 is not None:  # ccsdt.cpp:676-700
+            g = self.goovv
+            R2 = R2 + 0.5 * (-np.einsum("klcd,acdikj,bl->abij", g, t3, t1, **ES)
+                             + np.einsum("klcd,bcdikj,al->abij", g, t3, t1, **ES)
+                             - np.einsum("klcd,adbklj,ci->abij", g, t3, t1, **ES)
+                             + np.einsum("klcd,adbkli,cj->abij", g, t3, t1, **ES)
+                             + 2.0 * np.einsum("klcd,abcijk,dl->abij", g, t3, t1, **ES))
         d2 = self.den[:, None, :, None] + self.den[None, :, None, :]
         val = np.where(self.t2_write, R2 / np.where(self.t2_write, d2, 1.0), 0.0)
         # symmetric copies (ccsdt.cpp:720-723)

@@ -110,23 +110,30 @@ CCSDT1A_SYNTHETIC = [  # (nocc, nvir, naux, seed, sigma); sigma 0.2-0.3 gives vi
     (2, 4, 12, 5, 0.3), (3, 6, 20, 6, 0.3), (2, 8, 20, 7, 0.25), (4, 6, 24, 11, 0.2)]
 
 
-def main_ccsdt1a():
+CCSDT_METHODS = {"ccsdt-1a": (1, "reference_ccsdt1a.json"), "ccsdt-1b": (2, "reference_ccsdt1b.json")}
+
+
+def main_ccsdt(name="ccsdt-1a"):
+    """The reference's CCSDT::Calc_Energy(toler, Method_Nr) on the synthetic
+    systems and on H2O; Method_Nr 1 = CCSDT-1a, 2 = CCSDT-1b."""
+    method, out = CCSDT_METHODS[name]
+    mode = f"ccsdt-{method}"
     runs = {"synthetic": {}, "h2o": {}}
     for o, v, q, seed, sigma in CCSDT1A_SYNTHETIC:
-        r = run_synthetic(o, v, q, seed, sigma, -10, "ccsdt-1")
+        r = run_synthetic(o, v, q, seed, sigma, -10, mode)
         runs["synthetic"][f"o{o}_v{v}_s{seed}"] = dict(nocc=o, nvir=v, naux=q, seed=seed, sigma=sigma, log10_tol=-10,
                                                         iter=r["iter"], e_corr=r["ecorr"])
     for basis, geom, tol in H2O:
-        res = run_h2o(basis, geom, tol, "ccsdt-1")[0]
+        res = run_h2o(basis, geom, tol, mode)[0]
         tag = "incarsym" if geom.startswith("yz:1.079252") else geom
         name = f"h2o_{basis.lower().replace('-', '')}_{tag}_tol{-tol}.npz"
         runs["h2o"][name] = dict(iter=res["ccsd1_iter"], e_corr=res["ccsd1_ecorr"])
-    (GOLD / "reference_ccsdt1a.json").write_text(json.dumps(runs, indent=1))
+    (GOLD / out).write_text(json.dumps(runs, indent=1))
     print(json.dumps(runs, indent=1))
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] == "ccsdt-1a":
-        main_ccsdt1a()
+    if len(sys.argv) > 1 and sys.argv[1] in CCSDT_METHODS:
+        main_ccsdt(sys.argv[1])
     else:
         main()

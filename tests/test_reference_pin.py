@@ -101,26 +101,36 @@ def test_live_reference_run_matches_oracle(tmp_path):
     assert abs(float(line[3]) - r["e_corr"]) < 1e-13
 
 
-CCSDT1A = json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1a.json").read_text())
+CCSDT = {1: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1a.json").read_text()),
+         2: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1b.json").read_text())}
 
 
-@pytest.mark.parametrize("key", sorted(CCSDT1A["synthetic"]))
-def test_oracle_ccsdt1a_matches_reference_synthetic(key):
-    """The spin-orbital oracle's CCSDT-1a against the reference's own
-    CCSDT::Calc_Energy(toler, 1), compiled unchanged: same iteration counter,
-    energies to 1e-13."""
-    c = CCSDT1A["synthetic"][key]
+@pytest.mark.parametrize("method", [1, 2], ids=["ccsdt1a", "ccsdt1b"])
+@pytest.mark.parametrize("key", sorted(CCSDT[1]["synthetic"]))
+def test_oracle_ccsdt_matches_reference_synthetic(method, key):
+    """The spin-orbital oracle's CCSDT-1a / -1b against the reference's own
+    CCSDT::Calc_Energy(toler, Method_Nr), compiled unchanged: same iteration
+    counter, energies to 1e-13."""
+    c = CCSDT[method]["synthetic"][key]
     eps = syn.orbital_energies(c["nocc"], c["nvir"], c["seed"])
     eri = syn.eri_from_df(syn.df_factors(c["nocc"] + c["nvir"], c["naux"], c["seed"], sigma=c["sigma"]))
-    r = SpinOrbitalCCSD(np.diag(eps), eri, c["nocc"], method=1).run(toler=10.0 ** c["log10_tol"])
+    r = SpinOrbitalCCSD(np.diag(eps), eri, c["nocc"], method=method).run(toler=10.0 ** c["log10_tol"])
     assert r["iter"] == c["iter"]
     assert abs(r["e_corr"] - c["e_corr"]) < 1e-13
 
 
-@pytest.mark.parametrize("name", sorted(CCSDT1A["h2o"]))
-def test_oracle_ccsdt1a_matches_reference_h2o(name):
+@pytest.mark.parametrize("method", [1, 2], ids=["ccsdt1a", "ccsdt1b"])
+@pytest.mark.parametrize("name", sorted(CCSDT[1]["h2o"]))
+def test_oracle_ccsdt_matches_reference_h2o(method, name):
     d, fock, mo = _h2o(Path(__file__).parent / "golden" / name)
-    ref = CCSDT1A["h2o"][name]
-    r = SpinOrbitalCCSD(fock, mo, int(d["nocc"]), method=1).run(toler=10.0 ** float(d["log10_tol"]))
+    ref = CCSDT[method]["h2o"][name]
+    r = SpinOrbitalCCSD(fock, mo, int(d["nocc"]), method=method).run(toler=10.0 ** float(d["log10_tol"]))
     assert r["iter"] == ref["iter"]
     assert abs(r["e_corr"] - ref["e_corr"]) < 1e-12
+
+
+def test_ccsdt1b_term_is_visible():
+    """The T3 T1 term of CCSDT-1b moves the reference's own energies by more than
+    the pin tolerance, so the pins above distinguish the two methods."""
+    for key in CCSDT[1]["synthetic"]:
+        assert abs(CCSDT[1]["synthetic"][key]["e_corr"] - CCSDT[2]["synthetic"][key]["e_corr"]) > 1e-9
