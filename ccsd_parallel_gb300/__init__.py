@@ -49,7 +49,8 @@ def flops_per_update(nocc: int, nvir: int) -> float:
     return float(_abi.lib().ccsd_flops_per_update(nocc, nvir))
 
 
-METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A}
+METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A,
+           "ccsdt-1b": _abi.CCSD_METHOD_CCSDT1B}
 
 
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,

@@ -151,6 +151,8 @@ void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaSt
 // 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c]
 void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv, double *out,
                 cudaStream_t st);
+// t1so[a][i] (spin orbitals) from the spatial t1[i][a]
+void k_t1_spin(int o, int v, const double *t1, double *t1so, cudaStream_t st);
 // t2so[a][b][i][j] (spin orbitals) from the spatial t2[i][j][a][b]
 void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st);
 // t3 = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / D3, all [a][b][c][i][j][k]

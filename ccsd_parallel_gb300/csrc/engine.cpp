@@ -166,7 +166,7 @@ void Engine::set_options(const ccsd_options &opts) {
         throw Error(CCSD_ERR_INVALID_ARG, "diis_size must be in [0, 16]");
     if (opts.max_iter < 0 || opts.fixed_iterations < 0)
         throw Error(CCSD_ERR_INVALID_ARG, "iteration counts must be >= 0");
-    if (opts.method != CCSD_METHOD_CCSD && opts.method != CCSD_METHOD_CCSDT1A)
+    if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT1B)
         throw Error(CCSD_ERR_INVALID_ARG, "unknown method");
     if (opts.stream) {
         if (own_stream_ && st_) cudaStreamDestroy(st_);
@@ -879,7 +879,7 @@ void Engine::solve(ccsd_result *res) {
     // T1 = 0, T2 = MP2 (ccsd_memory_optimized.cpp:473-490)
     t1_.zero(st_);
     k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
-    if (opt_.method == CCSD_METHOD_CCSDT1A) triples_setup();  // T3 = 0
+    if (opt_.method != CCSD_METHOD_CCSD) triples_setup();  // T3 = 0
     double e_new = energy_of(t1_.p, t2_.p);
     int hist = 0;
     if (res->energy_history && res->history_capacity > 0) res->energy_history[hist] = e_new;
@@ -897,7 +897,7 @@ void Engine::solve(ccsd_result *res) {
             const long launches0 = launch_count();
             CCSD_CUDA(cudaEventRecord(ev0, st_));
             residual();
-            if (opt_.method == CCSD_METHOD_CCSDT1A) triples_step();  // T3 terms, then T3 from this T2
+            if (opt_.method != CCSD_METHOD_CCSD) triples_step();  // T3 terms, then T3 from this T2
             k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
             k_update_t1(o, v, R1_.p, eo_.p, ev_.p, t1_.p, t1n_.p, partials_.p + reduce_blocks(), st_);
             const double rn2 = reduce_sum(reduce_blocks() + 1);

@@ -111,6 +111,8 @@ class Engine {
     void triples_setup();
     void triples_step();
     DBuf t3_, y3_, z3_, t2so_, so_vvvo_, so_ovoo_, so_oovv_, so_vovv_, so_ooov_;
+    DBuf t1so_, g1b_, g2b_, h3b_, h4b_, f1b_, w5b_;  // CCSDT-1b T3 T1 intermediates
+    void triples_1b_terms();
 
     // recordable element-wise operations (every op of build and residual goes
     // through these or through gemm())

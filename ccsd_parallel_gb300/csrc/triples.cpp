@@ -42,6 +42,96 @@ void Engine::triples_setup() {
     t3_.zero(st_);  // T3 starts at zero (the first update is CCSD-like)
     y3_.zero(st_);  // spin-forbidden blocks of Y and Z are never written
     z3_.zero(st_);
+    if (opt_.method >= CCSD_METHOD_CCSDT1B) {
+        const size_t o = o_, v = v_;
+        t1so_.ensure(V * O);
+        g1b_.ensure(v * o * o * o);
+        g2b_.ensure(v * o * o * o);
+        h3b_.ensure(v * v * o * v);
+        h4b_.ensure(v * v * o * v);
+        f1b_.ensure(O * V);
+        w5b_.ensure(v * v * O * O);
+    }
+}
+
+// CCSDT-1b (ccsdt.cpp:676-700): R2 += 1/2 sum_{c,d,k,l} <kl||cd> [- t3(acd,ikj) t1(b,l)
+//   + t3(bcd,ikj) t1(a,l) - t3(adb,klj) t1(c,i) + t3(adb,kli) t1(c,j) + 2 t3(abc,ijk) t1(d,l)]
+// from the previous t3 and t1, in the alpha-beta block (a = 2a', b = 2b'+1, i = 2i',
+// j = 2j'+1), where t1(b,l) fixes l = 2l'+1, t1(a,l) l = 2l', t1(c,i) c = 2c' and
+// t1(c,j) c = 2c'+1.  Intermediates (spatial primed indices, the other spins summed
+// over the spin-conserving blocks):
+//   G1(a',i',j',l') = sum_{c,d,k} <k,2l'+1||c,d> t3[2a'][c][d][2i'][k][2j'+1]
+//   G2(b',i',j',l') = sum_{c,d,k} <k,2l'||c,d>   t3[2b'+1][c][d][2i'][k][2j'+1]
+//   H3(a',b',j',c') = sum_{d,k,l} <k,l||2c',d>   t3[2a'][d][2b'+1][k][l][2j'+1]
+//   H4(a',b',i',c') = sum_{d,k,l} <k,l||2c'+1,d> t3[2a'][d][2b'+1][k][l][2i']
+//   f(k,c) = sum_{d,l} <kl||cd> t1(d,l),  W5[a'][b'][i][j] = sum_{c,k} t3[2a'][2b'+1][c][i][j][k] f(k,c)
+void Engine::triples_1b_terms() {
+    const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
+    const int io = (int)o, iv = (int)v;
+    const uint32_t uo = (uint32_t)o, uv = (uint32_t)v;
+    const double *t3 = t3_.p, *t1 = t1_.p, *g = so_oovv_.p;  // g = <kl||cd> at [k][l][c][d]
+    const int64_t gk = O * V * V, gl = V * V, gc = V;
+    struct Spins {
+        int s0, s1, s2;
+    };
+    // G1: (sc, sd, sk) with sc + sd = sk + 1;  G2: sc + sd = sk
+    const Spins s1[3] = {{0, 1, 0}, {1, 0, 0}, {1, 1, 1}};
+    const Spins s2[3] = {{0, 0, 0}, {0, 1, 1}, {1, 0, 1}};
+    const Dim rows_xij = ix3(uo, uo, 2 * V2O3, 2 * O2, 2);  // (x', i', j') of t3[x][.][.][i][.][j]
+    const Dim K_cdk = ix3(uv, uo, 2 * VO3, 2 * O3, 2 * O);  // (c', d', k') in t3[.][c][d][.][k][.]
+    const Dim Kg_cdk = ix3(uv, uo, 2 * gc, 2, 2 * gk);      // (c', d', k') in <kl||cd>
+    const Dim rows_G = ix3(uo, uo, o * o * o, o * o, o);     // G[x'][i'][j'][l']
+    for (int q = 0; q < 3; ++q) {
+        const Spins &p = s1[q], &r = s2[q];
+        gemm(iv * io * io, io, (int)(v * v * o), 1.0, mv(t3 + p.s0 * VO3 + p.s1 * O3 + p.s2 * O + 1, rows_xij, K_cdk),
+             mv(g + p.s2 * gk + gl + p.s0 * gc + p.s1, ix1(2 * gl), Kg_cdk), q ? 1.0 : 0.0,
+             ovw(g1b_.p, rows_G, ix1(1)), 0, 420 + q, "T3T1_G1");
+        gemm(iv * io * io, io, (int)(v * v * o), 1.0,
+             mv(t3 + V2O3 + r.s0 * VO3 + r.s1 * O3 + r.s2 * O + 1, rows_xij, K_cdk),
+             mv(g + r.s2 * gk + r.s0 * gc + r.s1, ix1(2 * gl), Kg_cdk), q ? 1.0 : 0.0, ovw(g2b_.p, rows_G, ix1(1)),
+             0, 423 + q, "T3T1_G2");
+    }
+    // R[i'][j'][a'][b'] += -1/2 sum_l' G1(a',i',j',l') t1[l'][b'] + 1/2 sum_l' G2(b',i',j',l') t1[l'][a']
+    const Dim G_ijx = ix3(uo, uv, o * o, o, o * o * o);  // rows (i', j', x') of G
+    gemm(io * io * iv, iv, io, -0.5, mv(g1b_.p, G_ijx, ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+         ovw(R_.p, ix3(uo, uv, o * v * v, v * v, v), ix1(1)), 0, 0, "T3T1_G1t1");
+    gemm(io * io * iv, iv, io, 0.5, mv(g2b_.p, G_ijx, ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+         ovw(R_.p, ix3(uo, uv, o * v * v, v * v, 1), ix1(v)), 0, 0, "T3T1_G2t1");
+
+    // H3: (sd, sk, sl) with sd = sk + sl;  H4: sk + sl = sd + 1
+    const Spins s3[3] = {{0, 0, 0}, {1, 0, 1}, {1, 1, 0}};
+    const Spins s4[3] = {{0, 0, 1}, {0, 1, 0}, {1, 1, 1}};
+    const Dim rows_abx = ix3(uv, uo, 2 * V2O3, 2 * O3, 2);   // (a', b', x') of t3[a][.][b][.][.][x]
+    const Dim K_dkl = ix3(uo, uo, 2 * VO3, 2 * O2, 2 * O);   // (d', k', l') in t3[.][d][.][k][l][.]
+    const Dim Kg_dkl = ix3(uo, uo, 2, 2 * gk, 2 * gl);       // (d', k', l') in <kl||cd>
+    const Dim rows_H = ix3(uv, uo, v * o * v, o * v, v);     // H[a'][b'][x'][c']
+    for (int q = 0; q < 3; ++q) {
+        const Spins &p = s3[q], &r = s4[q];
+        gemm(iv * iv * io, iv, (int)(v * o * o), 1.0,
+             mv(t3 + p.s0 * VO3 + O3 + p.s1 * O2 + p.s2 * O + 1, rows_abx, K_dkl),
+             mv(g + p.s1 * gk + p.s2 * gl + p.s0, ix1(2 * gc), Kg_dkl), q ? 1.0 : 0.0, ovw(h3b_.p, rows_H, ix1(1)), 0,
+             426 + q, "T3T1_H3");
+        gemm(iv * iv * io, iv, (int)(v * o * o), 1.0, mv(t3 + r.s0 * VO3 + O3 + r.s1 * O2 + r.s2 * O, rows_abx, K_dkl),
+             mv(g + r.s1 * gk + r.s2 * gl + gc + r.s0, ix1(2 * gc), Kg_dkl), q ? 1.0 : 0.0,
+             ovw(h4b_.p, rows_H, ix1(1)), 0, 429 + q, "T3T1_H4");
+    }
+    // R[i'][j'][a'][b'] += -1/2 sum_c' H3(a',b',j',c') t1[i'][c'] + 1/2 sum_c' H4(a',b',i',c') t1[j'][c']
+    gemm(iv * iv * io, io, iv, -0.5, mv(h3b_.p, rows_H, ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
+         ovw(R_.p, ix3(uv, uo, v, 1, v * v), ix1(o * v * v)), 0, 0, "T3T1_H3t1");
+    gemm(iv * iv * io, io, iv, 0.5, mv(h4b_.p, rows_H, ix1(1)), mv(t1, ix1(v), ix1(1)), 1.0,
+         ovw(R_.p, ix3(uv, uo, v, 1, o * v * v), ix1(v * v)), 0, 0, "T3T1_H4t1");
+
+    // f(k,c) = sum_{l,d} <kl||cd> t1so[d][l]  (O x V; zero unless sk = sc)
+    k_t1_spin(io, iv, t1, t1so_.p, st_);
+    gemm((int)(O * V), 1, (int)(O * V), 1.0, mv(g, ix2((uint32_t)V, gk, gc), ix2((uint32_t)V, gl, 1)),
+         mv(t1so_.p, ix1(0), ix2((uint32_t)V, 1, O)), 0.0, ovw(f1b_.p, ix1(1), ix1(0)), 0, 0, "T3T1_f");
+    // W5[a'][b'][i][j] = sum_{c,k} t3[2a'][2b'+1][c][i][j][k] f(k,c), rows (a', b', i O + j)
+    gemm((int)(v * v * O2), 1, (int)(V * O), 1.0,
+         mv(t3 + VO3, ix3(uv, (uint32_t)O2, 2 * V2O3, 2 * VO3, O), ix2((uint32_t)O, O3, 1)),
+         mv(f1b_.p, ix1(0), ix2((uint32_t)O, 1, V)), 0.0, ovw(w5b_.p, ix1(1), ix1(0)), 0, 0, "T3T1_ft3");
+    // R[i'][j'][a'][b'] += W5[a'][b'][2i'][2j'+1]  (1/2 x 2)
+    axpby(io * io * iv, iv, 1.0, mv(w5b_.p + 1, ix3(uo, uv, 2 * O, 2, v * O2), ix1(O2)), 1.0,
+          ovw(R_.p, ix3(uo, uv, o * v * v, v * v, v), ix1(1)));
 }
 
 void Engine::triples_step() {
@@ -108,6 +198,8 @@ void Engine::triples_step() {
                  ovw(R_.p, ix3(uv, uv, v * v, v, 1), ix1(o * v * v)), 0, 409 + q, "R2_T3_ooov_i");
         }
     }
+
+    if (opt_.method >= CCSD_METHOD_CCSDT1B) triples_1b_terms();  // also from the previous t3
 
     // ---- T3 from the previous T2 (ccsdt.cpp:1016-1058, 1235-1238), by spin blocks.
     // Spin orbital X = 2x + s, so a block of fixed spins is a stride-2 view of

@@ -113,6 +113,15 @@ __global__ void t2_spin_kernel(int o, int v, const double *__restrict__ t2, doub
     }
 }
 
+// t1so[a][i] (spin orbitals) from the spatial t1[i][a]: t1[i a] d(sa, si)
+__global__ void t1_spin_kernel(int o, int v, const double *__restrict__ t1, double *__restrict__ t1so) {
+    const int O = 2 * o, V = 2 * v;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < V * O; idx += gridDim.x * blockDim.x) {
+        const int I = idx % O, A = idx / O;
+        t1so[idx] = ((A & 1) == (I & 1)) ? t1[(I >> 1) * v + (A >> 1)] : 0.0;
+    }
+}
+
 // t3[a][b][c][i][j][k] = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / (D(a,i) + D(b,j) + D(c,k)),
 // D(a,i) = f_ii - f_aa, with P(a/bc) = 1 - (ab) - (ac), P(k/ij) = 1 - (ik) - (jk),
 // P(c/ab) = 1 - (ac) - (bc), P(i/jk) = 1 - (ij) - (ik) (ccsdt.cpp:1016-1058, 1235-1238)
@@ -330,6 +339,11 @@ void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, 
     const size_t O = 2 * (size_t)o, V = 2 * (size_t)v;
     const size_t sizes[5] = {V * V * V * O, O * V * O * O, O * O * V * V, V * O * V * V, O * O * O * V};
     so_block_kernel<<<blocks_for(sizes[kind]), 256, 0, st>>>(kind, B, out);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_t1_spin(int o, int v, const double *t1, double *t1so, cudaStream_t st) {
+    t1_spin_kernel<<<blocks_for((size_t)4 * o * v), 256, 0, st>>>(o, v, t1, t1so);
     CCSD_LAUNCH_CHECK();
 }
 

@@ -106,6 +106,9 @@ typedef struct ccsd_options {
  * doubles of device memory with its two contraction intermediates.  Single
  * systems only (no batched solve, no ccsd_lambda_grad). */
 #define CCSD_METHOD_CCSDT1A 1
+/* CCSDT-1b, CCSDT::Calc_Energy(toler, 2) (initializer.cpp:110-114): CCSDT-1a plus
+ * the T3 T1 term of T2 (ccsdt.cpp:676-700).  Same memory and restrictions. */
+#define CCSD_METHOD_CCSDT1B 2
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */

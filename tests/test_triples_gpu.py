@@ -1,8 +1,9 @@
-"""CCSDT-1a on the GPU engine (the reference's CCSDT::Calc_Energy(toler, 1),
-ccsdt.cpp:255-271) against the spin-orbital oracle and the reference's own
-runs (tests/golden/reference_ccsdt1a.json): FP64 energies to 1e-11 with the
-reference's iteration counter, amplitudes to 1e-12 after a fixed number of
-updates, split precision within 1e-8."""
+"""CCSDT-1a and CCSDT-1b on the GPU engine (the reference's
+CCSDT::Calc_Energy(toler, 1 | 2), ccsdt.cpp:255-271) against the spin-orbital
+oracle and the reference's own runs (tests/golden/reference_ccsdt1a.json,
+reference_ccsdt1b.json): FP64 energies to 1e-11 with the reference's iteration
+counter, amplitudes to 1e-12 after a fixed number of updates, split precision
+within 1e-8."""
 import json
 from pathlib import Path
 
@@ -18,6 +19,8 @@ pytestmark = pytest.mark.gpu
 
 GOLD = Path(__file__).parent / "golden"
 CCSDT1A = json.loads((GOLD / "reference_ccsdt1a.json").read_text())
+GOLDEN = {"ccsdt-1a": CCSDT1A, "ccsdt-1b": json.loads((GOLD / "reference_ccsdt1b.json").read_text())}
+METHOD_NR = {"ccsdt-1a": 1, "ccsdt-1b": 2}
 
 
 def _case(c):
@@ -26,35 +29,38 @@ def _case(c):
     return np.diag(eps), b
 
 
+@pytest.mark.parametrize("method", sorted(GOLDEN))
 @pytest.mark.parametrize("key", sorted(CCSDT1A["synthetic"]))
-def test_ccsdt1a_matches_reference_synthetic(key):
-    c = CCSDT1A["synthetic"][key]
+def test_ccsdt_matches_reference_synthetic(method, key):
+    c = GOLDEN[method]["synthetic"][key]
     fock, b = _case(c)
-    r = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=10.0 ** c["log10_tol"])
+    r = cg.solve(fock, c["nocc"], df=b, method=method, energy_tol=10.0 ** c["log10_tol"])
     assert r["iterations"] + 1 == c["iter"]
     assert abs(r["e_corr"] - c["e_corr"]) < 1e-11
 
 
+@pytest.mark.parametrize("method", sorted(GOLDEN))
 @pytest.mark.parametrize("name", sorted(CCSDT1A["h2o"]))
-def test_ccsdt1a_matches_reference_h2o(name):
+def test_ccsdt_matches_reference_h2o(method, name):
     """The reference's RHF outputs for H2O through the AO input."""
     d = np.load(GOLD / name)
-    ref = CCSDT1A["h2o"][name]
+    ref = GOLDEN[method]["h2o"][name]
     r = cg.solve(np.diag(d["eps"]), int(d["nocc"]), ao_eri=d["ao_eri"], mo_coeff=d["mo_coeff"],
-                 method="ccsdt-1a", energy_tol=10.0 ** float(d["log10_tol"]))
+                 method=method, energy_tol=10.0 ** float(d["log10_tol"]))
     assert r["iterations"] + 1 == ref["iter"]
     assert abs(r["e_corr"] - ref["e_corr"]) < 1e-11
 
 
-def test_ccsdt1a_amplitudes_match_oracle_every_update():
+@pytest.mark.parametrize("method", sorted(GOLDEN))
+def test_ccsdt_amplitudes_match_oracle_every_update(method):
     """Energies of every update and the final T1/T2 equal the oracle's; the
     closed-shell amplitudes are the alpha-beta blocks of the spin-orbital ones,
     t1[i,a] = t1so[2a,2i], t2[i,j,a,b] = t2so[2a,2b+1,2i,2j+1]."""
     o, v = 3, 7
     fock, b = _case(dict(nocc=o, nvir=v, naux=22, seed=17, sigma=0.3))
     eri = syn.eri_from_df(b)
-    ref = SpinOrbitalCCSD(fock, eri, o, method=1).run(toler=1e-13, max_passes=8)
-    r = cg.solve(fock, o, df=b, method="ccsdt-1a", fixed_iterations=8)
+    ref = SpinOrbitalCCSD(fock, eri, o, method=METHOD_NR[method]).run(toler=1e-13, max_passes=8)
+    r = cg.solve(fock, o, df=b, method=method, fixed_iterations=8)
     np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
     t1 = ref["t1"][0::2, 0::2].T
     t2 = ref["t2"][0::2, 1::2, 0::2, 1::2].transpose(2, 3, 0, 1)
@@ -66,24 +72,26 @@ def test_ccsdt1a_amplitudes_match_oracle_every_update():
 
 
 @pytest.mark.parametrize("o,v", [(11, 3), (13, 2), (1, 3), (2, 1)])
-def test_ccsdt1a_assembly_forms_match_oracle(o, v):
+def test_ccsdt_assembly_forms_match_oracle(o, v):
     """Every form of the T3 assembly against the oracle: O = 2 nocc = 22 takes the
     two-slab form, 26 the element-wise one, O = 2 the unique-ijk form with no
     occupied triple, and nvir = 1 leaves fewer than three virtual spin orbitals
     (element-wise form, T3 = 0)."""
     fock, b = _case(dict(nocc=o, nvir=v, naux=2 * (o + v), seed=o + 5 * v, sigma=0.2))
-    ref = SpinOrbitalCCSD(fock, syn.eri_from_df(b), o, method=1).run(toler=1e-14, max_passes=4)
-    r = cg.solve(fock, o, df=b, method="ccsdt-1a", fixed_iterations=4)
-    np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
+    for method in sorted(GOLDEN):
+        ref = SpinOrbitalCCSD(fock, syn.eri_from_df(b), o, method=METHOD_NR[method]).run(toler=1e-14, max_passes=4)
+        r = cg.solve(fock, o, df=b, method=method, fixed_iterations=4)
+        np.testing.assert_allclose(r["energies"], ref["energies"], rtol=0, atol=1e-12)
 
 
+@pytest.mark.parametrize("method", sorted(GOLDEN))
 @pytest.mark.parametrize("prec", ["split3", "split2"])
-def test_ccsdt1a_split_precision(prec):
+def test_ccsdt_split_precision(prec, method):
     """Split precision on the same method: the FP64 answer within 1e-8."""
     c = CCSDT1A["synthetic"]["o3_v6_s6"]
     fock, b = _case(c)
-    ref = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=1e-11)
-    r = cg.solve(fock, c["nocc"], df=b, method="ccsdt-1a", energy_tol=1e-11, precision=prec)
+    ref = cg.solve(fock, c["nocc"], df=b, method=method, energy_tol=1e-11)
+    r = cg.solve(fock, c["nocc"], df=b, method=method, energy_tol=1e-11, precision=prec)
     assert abs(r["e_corr"] - ref["e_corr"]) < 1e-8
 
 
@@ -109,6 +117,9 @@ def test_ccsdt1a_unsupported_paths_fail_loudly():
         assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
     with pytest.raises(cg.CCSDError) as ei:
         cg.solve_batched([dict(fock=fock, nocc=c["nocc"], df=b)] * 2, method="ccsdt-1a")
+    assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.solve_batched([dict(fock=fock, nocc=c["nocc"], df=b)] * 2, method="ccsdt-1b")
     assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
     with pytest.raises(cg.CCSDError) as ei:
         cg.solve(fock, c["nocc"], df=b, method=7)
