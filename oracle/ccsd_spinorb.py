@@ -24,6 +24,8 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
   (``ccsdt.cpp:676-700``):
   + 1/2 <kl||cd> [- t_ikj^acd t_l^b + t_ikj^bcd t_l^a - t_klj^adb t_i^c
                   + t_kli^adb t_j^c + 2 t_ijk^abc t_l^d]
+* CCSDT-2 (``Method_Nr == 3``): CCSDT-1b with T2-dressed X1/X2 and the X12/X13
+  terms of T3 (``triples``).
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -69,9 +71,9 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 class SpinOrbitalCCSD:
     def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
-        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b (the reference's Method_Nr)."""
-        if method not in (-1, 1, 2):
-            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a) or 2 (CCSDT-1b)")
+        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2 (the reference's Method_Nr)."""
+        if method not in (-1, 1, 2, 3):
+            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a), 2 (CCSDT-1b) or 3 (CCSDT-2)")
         self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
@@ -133,17 +135,43 @@ class SpinOrbitalCCSD:
         return 0.25 * np.einsum("ijab,abij->", self.goovv, self.tau(t1, t2))
 
     def triples(self, t2):
-        """CCSDT-1a T3 from T2 (``ccsdt.cpp:1016-1058`` with X1, X2 bare): t3[a,b,c,i,j,k] =
-        [P(a/bc) P(k/ij) sum_e <bc||ek> t2(a,e)(i,j) - P(c/ab) P(i/jk) sum_m <mc||jk> t2(a,b)(i,m)] / D3."""
-        A = np.einsum("bcek,aeij->abcijk", self.gvvvo, t2, **ES)
-        B = np.einsum("mcjk,abim->abcijk", self.govoo, t2, **ES)
+        """T3 from T2 (``ccsdt.cpp:995-1290``): t3[a,b,c,i,j,k] =
+        [P(a/bc) P(k/ij) sum_e X1(b,c)(k,e) t2(a,e)(i,j) - P(c/ab) P(i/jk) sum_m X2(c,m)(j,k) t2(a,b)(i,m)
+         (+ for CCSDT-2, Method_Nr 3: P(i/jk) P(abc) sum_e X12(a,b)(i,e) t2(e,c)(j,k)
+                                    + P(a/bc) P(ijk) sum_m X13(a,m)(i,j) t2(b,c)(m,k))] / D3
+        X1(b,c)(k,e) = <bc||ek> and X2(c,m)(j,k) = <mc||jk> for CCSDT-1a/1b; CCSDT-2
+        dresses them with T2 (``ccsdt.cpp:1960-2040``):
+          X1 += 1/2 sum_lm <lm||ek> t2(b,c)(l,m),  X2 += 1/2 sum_de t2(d,e)(j,k) <mc||de>
+          X12(a,b)(i,d) = sum_le <lb||ed> t2(a,e)(i,l),  X13(a,l)(i,j) = -sum_md <ml||dj> t2(a,d)(i,m)
+                                                                      ``ccsdt.cpp:2301-2390``"""
+        X1, X2 = self.gvvvo, self.govoo  # X1 at [b,c,e,k], X2 at [m,c,j,k]
+        if self.method >= 3:
+            X1 = X1 + 0.5 * np.einsum("lmek,bclm->bcek", self.goovo, t2, **ES)
+            X2 = X2 + 0.5 * np.einsum("dejk,mcde->mcjk", t2, self.govvv, **ES)
+        A = np.einsum("bcek,aeij->abcijk", X1, t2, **ES)
+        B = np.einsum("mcjk,abim->abcijk", X2, t2, **ES)
         PA = A - A.transpose(1, 0, 2, 3, 4, 5) - A.transpose(2, 1, 0, 3, 4, 5)     # P(a/bc)
         PA = PA - PA.transpose(0, 1, 2, 5, 4, 3) - PA.transpose(0, 1, 2, 3, 5, 4)  # P(k/ij)
         PB = B - B.transpose(2, 1, 0, 3, 4, 5) - B.transpose(0, 2, 1, 3, 4, 5)     # P(c/ab)
         PB = PB - PB.transpose(0, 1, 2, 4, 3, 5) - PB.transpose(0, 1, 2, 5, 4, 3)  # P(i/jk)
+        num = PA - PB
+        if self.method >= 3:
+            X12 = np.einsum("lbed,aeil->abid", self.govvv, t2, **ES)
+            X13 = -np.einsum("mldj,adim->alij", self.goovo, t2, **ES)
+            Q = np.einsum("abie,ecjk->abcijk", X12, t2, **ES)
+            # P(abc): all six orders of the virtual indices with their signs
+            Q = (Q - Q.transpose(1, 0, 2, 3, 4, 5) - Q.transpose(2, 1, 0, 3, 4, 5) - Q.transpose(0, 2, 1, 3, 4, 5)
+                 + Q.transpose(1, 2, 0, 3, 4, 5) + Q.transpose(2, 0, 1, 3, 4, 5))
+            Q = Q - Q.transpose(0, 1, 2, 4, 3, 5) - Q.transpose(0, 1, 2, 5, 4, 3)  # P(i/jk)
+            S = np.einsum("amij,bcmk->abcijk", X13, t2, **ES)
+            S = S - S.transpose(1, 0, 2, 3, 4, 5) - S.transpose(2, 1, 0, 3, 4, 5)  # P(a/bc)
+            # P(ijk): all six orders of the occupied indices with their signs
+            S = (S - S.transpose(0, 1, 2, 4, 3, 5) - S.transpose(0, 1, 2, 5, 4, 3) - S.transpose(0, 1, 2, 3, 5, 4)
+                 + S.transpose(0, 1, 2, 4, 5, 3) + S.transpose(0, 1, 2, 5, 3, 4))
+            num = num + Q + S
         d = self.den
         D3 = (d[:, None, None, :, None, None] + d[None, :, None, None, :, None] + d[None, None, :, None, None, :])
-        return (PA - PB) / D3
+        return num / D3
 
     def update(self, t1, t2, t3=None):
         """One Jacobi pass: returns (t1_new, t2_new), or (t1_new, t2_new, t3_new)

@@ -110,12 +110,13 @@ CCSDT1A_SYNTHETIC = [  # (nocc, nvir, naux, seed, sigma); sigma 0.2-0.3 gives vi
     (2, 4, 12, 5, 0.3), (3, 6, 20, 6, 0.3), (2, 8, 20, 7, 0.25), (4, 6, 24, 11, 0.2)]
 
 
-CCSDT_METHODS = {"ccsdt-1a": (1, "reference_ccsdt1a.json"), "ccsdt-1b": (2, "reference_ccsdt1b.json")}
+CCSDT_METHODS = {"ccsdt-1a": (1, "reference_ccsdt1a.json"), "ccsdt-1b": (2, "reference_ccsdt1b.json"),
+                 "ccsdt-2": (3, "reference_ccsdt2.json")}
 
 
 def main_ccsdt(name="ccsdt-1a"):
     """The reference's CCSDT::Calc_Energy(toler, Method_Nr) on the synthetic
-    systems and on H2O; Method_Nr 1 = CCSDT-1a, 2 = CCSDT-1b."""
+    systems and on H2O; Method_Nr 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2."""
     method, out = CCSDT_METHODS[name]
     mode = f"ccsdt-{method}"
     runs = {"synthetic": {}, "h2o": {}}
