@@ -155,9 +155,10 @@ void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, 
 void k_t1_spin(int o, int v, const double *t1, double *t1so, cudaStream_t st);
 // t2so[a][b][i][j] (spin orbitals) from the spatial t2[i][j][a][b]
 void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st);
-// t3 = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z] / D3, all [a][b][c][i][j][k]
-void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *eo, const double *ev, double *t3,
-                   cudaStream_t st);
+// t3 = [P(a/bc) P(k/ij) Y - P(c/ab) P(i/jk) Z (+ P(i/jk) P(abc) Q12 + P(a/bc) P(ijk) Q13
+// when Q12 is given)] / D3, all [a][b][c][i][j][k]
+void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *Q12, const double *Q13,
+                   const double *eo, const double *ev, double *t3, cudaStream_t st);
 void k_fill(size_t n, double val, double *p, cudaStream_t st);
 void k_copy_diag(int n, const double *fock, int off, int cnt, double *out, cudaStream_t st);
 int reduce_blocks();

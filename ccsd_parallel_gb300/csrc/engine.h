@@ -112,7 +112,9 @@ class Engine {
     void triples_step();
     DBuf t3_, y3_, z3_, t2so_, so_vvvo_, so_ovoo_, so_oovv_, so_vovv_, so_ooov_;
     DBuf t1so_, g1b_, g2b_, h3b_, h4b_, f1b_, w5b_;  // CCSDT-1b T3 T1 intermediates
+    DBuf x1d_, x2d_, x12_, x13_, q12_, q13_;         // CCSDT-2: dressed X1/X2, X12/X13 and their products
     void triples_1b_terms();
+    void triples_m3_products();
 
     // recordable element-wise operations (every op of build and residual goes
     // through these or through gemm())

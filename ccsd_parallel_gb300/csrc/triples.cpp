@@ -42,6 +42,16 @@ void Engine::triples_setup() {
     t3_.zero(st_);  // T3 starts at zero (the first update is CCSD-like)
     y3_.zero(st_);  // spin-forbidden blocks of Y and Z are never written
     z3_.zero(st_);
+    if (opt_.method >= CCSD_METHOD_CCSDT2) {
+        x1d_.ensure(V * V * V * O);
+        x2d_.ensure(O * V * O * O);
+        x12_.ensure(V * V * O * V);
+        x13_.ensure(V * O * O * O);
+        q12_.ensure(n3);
+        q13_.ensure(n3);
+        q12_.zero(st_);  // spin-forbidden blocks are never written
+        q13_.zero(st_);
+    }
     if (opt_.method >= CCSD_METHOD_CCSDT1B) {
         const size_t o = o_, v = v_;
         t1so_.ensure(V * O);
@@ -134,6 +144,69 @@ void Engine::triples_1b_terms() {
           ovw(R_.p, ix3(uo, uv, o * v * v, v * v, v), ix1(1)));
 }
 
+// CCSDT-2 (ccsdt.cpp:1078-1130, 2301-2390): from this T2,
+//   X12[a][b][i][d] = sum_{l,e} <lb||ed> t2so[a][e][i][l]    (<lb||ed> = -<bl||ed>)
+//   X13[a][l][i][j] = -sum_{m,d} <ml||dj> t2so[a][d][i][m]   (<ml||dj> = -<ml||jd>)
+//   Q12[a][b][c][i][j][k] = sum_e X12[a][b][i][e] t2so[e][c][j][k]
+//   Q13[a][b][c][i][j][k] = sum_m X13[a][m][i][j] t2so[b][c][m][k]
+// Q12 and Q13 conserve spin like Y and Z: 18 spin blocks each, as stride-2 views.
+void Engine::triples_m3_products() {
+    const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
+    const uint32_t uo = (uint32_t)o, uv = (uint32_t)v;
+    const int64_t VO2 = V * O2;
+    // X12: M = (a,i), N = (b,d), K = (l,e)
+    gemm((int)(V * O), (int)(V * V), (int)(O * V), -1.0,
+         mv(t2so_.p, ix2((uint32_t)O, VO2, O), ix2((uint32_t)V, 1, O2)),
+         mv(so_vovv_.p, ix2((uint32_t)V, O * V * V, 1), ix2((uint32_t)V, V * V, V)), 0.0,
+         ovw(x12_.p, ix2((uint32_t)O, V * O * V, V), ix2((uint32_t)V, O * V, 1)), 0, 0, "T3_X12");
+    // X13: M = (a,i), N = (l,j), K = (m,d)
+    gemm((int)(V * O), (int)O2, (int)(O * V), 1.0,
+         mv(t2so_.p, ix2((uint32_t)O, VO2, O), ix2((uint32_t)V, 1, O2)),
+         mv(so_ooov_.p, ix2((uint32_t)O, O * V, V), ix2((uint32_t)V, O2 * V, 1)), 0.0,
+         ovw(x13_.p, ix2((uint32_t)O, O3, O), ix2((uint32_t)O, O2, 1)), 0, 0, "T3_X13");
+    const int64_t X12a = V * O * V, X12b = O * V, X12i = V;  // X12[a][b][i][d] strides
+    for (int sa = 0; sa < 2; ++sa)
+        for (int sb = 0; sb < 2; ++sb)
+            for (int si = 0; si < 2; ++si) {
+                // Q12: se = sa + sb - si, (sc, sj, sk) with se + sc = sj + sk;  M = (a,b,i), N = (c,j,k), K = e
+                const int se = sa + sb - si;
+                if (se < 0 || se > 1) continue;
+                const MatView Av = mv(x12_.p + sa * X12a + sb * X12b + si * X12i + se,
+                                      ix3(uv, uo, 2 * X12a, 2 * X12b, 2 * X12i), ix1(2));
+                for (int sj = 0; sj < 2; ++sj)
+                    for (int sk = 0; sk < 2; ++sk) {
+                        const int sc = sj + sk - se;
+                        if (sc < 0 || sc > 1) continue;
+                        const double *B = t2so_.p + se * VO2 + sc * O2 + sj * O + sk;
+                        double *Cp = q12_.p + sa * V2O3 + sb * VO3 + si * O2 + sc * O3 + sj * O + sk;
+                        gemm((int)(v * v * o), (int)(v * o * o), (int)v, 1.0, Av,
+                             mv(B, ix3(uo, uo, 2 * O2, 2 * O, 2), ix1(2 * VO2)), 0.0,
+                             ovw(Cp, ix3(uv, uo, 2 * V2O3, 2 * VO3, 2 * O2), ix3(uo, uo, 2 * O3, 2 * O, 2)),
+                             -(500 + sa * 4 + sb * 2 + si), -(510 + se * 8 + sc * 4 + sj * 2 + sk), "T3_Q12");
+                    }
+            }
+    for (int sa = 0; sa < 2; ++sa)
+        for (int si = 0; si < 2; ++si)
+            for (int sj = 0; sj < 2; ++sj) {
+                // Q13: sm = si + sj - sa, (sb, sc, sk) with sb + sc = sm + sk;  M = (a,i,j), N = (b,c,k), K = m
+                const int sm = si + sj - sa;
+                if (sm < 0 || sm > 1) continue;
+                const MatView Av = mv(x13_.p + sa * O3 + sm * O2 + si * O + sj, ix3(uo, uo, 2 * O3, 2 * O, 2),
+                                      ix1(2 * O2));
+                for (int sb = 0; sb < 2; ++sb)
+                    for (int sc = 0; sc < 2; ++sc) {
+                        const int sk = sb + sc - sm;
+                        if (sk < 0 || sk > 1) continue;
+                        const double *B = t2so_.p + sb * VO2 + sc * O2 + sm * O + sk;
+                        double *Cp = q13_.p + sa * V2O3 + si * O2 + sj * O + sb * VO3 + sc * O3 + sk;
+                        gemm((int)(v * o * o), (int)(v * v * o), (int)o, 1.0, Av,
+                             mv(B, ix3(uv, uo, 2 * VO2, 2 * O2, 2), ix1(2 * O)), 0.0,
+                             ovw(Cp, ix3(uo, uo, 2 * V2O3, 2 * O2, 2 * O), ix3(uv, uo, 2 * VO3, 2 * O3, 2)),
+                             -(520 + sa * 4 + si * 2 + sj), -(530 + sm * 8 + sb * 4 + sc * 2 + sk), "T3_Q13");
+                    }
+            }
+}
+
 void Engine::triples_step() {
     const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
     const int io = (int)o, iv = (int)v;
@@ -201,6 +274,25 @@ void Engine::triples_step() {
 
     if (opt_.method >= CCSD_METHOD_CCSDT1B) triples_1b_terms();  // also from the previous t3
 
+    // CCSDT-2 dresses X1 and X2 with this T2 (ccsdt.cpp:1960-2040):
+    //   X1[b][c][e][k] = <bc||ek> + 1/2 sum_lm <lm||ek> t2so[b][c][l][m],  <lm||ek> = -<lm||ke>
+    //   X2[m][c][j][k] = <mc||jk> + 1/2 sum_de t2so[d][e][j][k] <mc||de>,  <mc||de> = -<cm||de>
+    const bool m3 = opt_.method >= CCSD_METHOD_CCSDT2;
+    const double *X1 = so_vvvo_.p, *X2 = so_ovoo_.p;
+    if (m3) {
+        copy(x1d_.p, so_vvvo_.p, (size_t)(V * V * V * O));
+        gemm((int)(V * V), (int)(V * O), (int)O2, -0.5, mv(t2so_.p, ix1(O2), ix1(1)),
+             mv(so_ooov_.p, ix2((uint32_t)O, 1, V), ix1(O * V)), 1.0, ovw(x1d_.p, ix1(V * O), ix1(1)), 0, 0,
+             "T3_X1_dress");
+        copy(x2d_.p, so_ovoo_.p, (size_t)(O * V * O2));
+        gemm((int)(O * V), (int)O2, (int)(V * V), -0.5, mv(so_vovv_.p, ix2((uint32_t)V, V * V, O * V * V), ix1(1)),
+             mv(t2so_.p, ix1(1), ix1(O2)), 1.0, ovw(x2d_.p, ix1(O2), ix1(1)), 0, 0, "T3_X2_dress");
+        X1 = x1d_.p;
+        X2 = x2d_.p;
+    }
+    // integral operands are split once (positive keys) unless they change every update
+    const int ksign = m3 ? -1 : 1;
+
     // ---- T3 from the previous T2 (ccsdt.cpp:1016-1058, 1235-1238), by spin blocks.
     // Spin orbital X = 2x + s, so a block of fixed spins is a stride-2 view of
     // spatial indices.  t2so and the integral blocks conserve spin, so of the
@@ -220,12 +312,12 @@ void Engine::triples_step() {
                     for (int sc = 0; sc < 2; ++sc) {
                         const int sk = sb + sc - se;
                         if (sk < 0 || sk > 1) continue;
-                        const double *B = so_vvvo_.p + sb * V * V * O + sc * V * O + se * O + sk;
+                        const double *B = X1 + sb * V * V * O + sc * V * O + se * O + sk;
                         double *Cp = y3_.p + sa * V2O3 + si * O2 + sj * O + sb * VO3 + sc * O3 + sk;
                         gemm((int)(v * o * o), (int)(v * v * o), (int)v, 1.0, Av,
                              mv(B, ix3(uv, uo, 2 * V * V * O, 2 * V * O, 2), ix1(2 * O)), 0.0,
                              ovw(Cp, ix3(uo, uo, 2 * V2O3, 2 * O2, 2 * O), ix3(uv, uo, 2 * VO3, 2 * O3, 2)),
-                             -(300 + sa * 4 + si * 2 + sj), 310 + se * 8 + sb * 4 + sc * 2 + sk, "T3_Y");
+                             -(300 + sa * 4 + si * 2 + sj), ksign * (310 + se * 8 + sb * 4 + sc * 2 + sk), "T3_Y");
                     }
             }
     for (int sa = 0; sa < 2; ++sa)
@@ -241,14 +333,16 @@ void Engine::triples_step() {
                     for (int sk = 0; sk < 2; ++sk) {
                         const int sc = sj + sk - sm;
                         if (sc < 0 || sc > 1) continue;
-                        const double *B = so_ovoo_.p + sm * V * O2 + sc * O2 + sj * O + sk;
+                        const double *B = X2 + sm * V * O2 + sc * O2 + sj * O + sk;
                         double *Cp = z3_.p + sa * V2O3 + sb * VO3 + si * O2 + sc * O3 + sj * O + sk;
                         gemm((int)(v * v * o), (int)(v * o * o), (int)o, 1.0, Av,
                              mv(B, ix3(uo, uo, 2 * O2, 2 * O, 2), ix1(2 * V * O2)), 0.0,
                              ovw(Cp, ix3(uv, uo, 2 * V2O3, 2 * VO3, 2 * O2), ix3(uo, uo, 2 * O3, 2 * O, 2)),
-                             -(330 + sa * 4 + sb * 2 + si), 340 + sm * 8 + sc * 4 + sj * 2 + sk, "T3_Z");
+                             -(330 + sa * 4 + sb * 2 + si), ksign * (340 + sm * 8 + sc * 4 + sj * 2 + sk), "T3_Z");
                     }
             }
+    if (m3) triples_m3_products();
+
     cudaEvent_t ea = nullptr, eb = nullptr, ec = nullptr;
     if (opt_.profile) {  // a site of its own in the contraction profile (no flops)
         ea = prof_event();
@@ -257,7 +351,7 @@ void Engine::triples_step() {
         CCSD_CUDA(cudaEventRecord(ea, st_));
         CCSD_CUDA(cudaEventRecord(eb, st_));
     }
-    k_t3_assemble(io, iv, y3_.p, z3_.p, eo_.p, ev_.p, t3_.p, st_);
+    k_t3_assemble(io, iv, y3_.p, z3_.p, m3 ? q12_.p : nullptr, m3 ? q13_.p : nullptr, eo_.p, ev_.p, t3_.p, st_);
     if (opt_.profile) {
         CCSD_CUDA(cudaEventRecord(ec, st_));
         prof_pending_.push_back(ProfPending{"T3_assemble", ea, eb, ec, 0.0, false});

@@ -251,15 +251,21 @@ __global__ void __launch_bounds__(256) t3_assemble_slab_kernel(int o, int v, con
 //   2. i < j < k: u = ([ys(ijk) - ys(kji) - ys(ikj)] - [zs(ijk) - zs(jik) - zs(kji)]) / D3,
 //      us at the six orders of ijk with their signs
 //   3. us written to the six slabs of abc with their signs (contiguous)
+template <bool M3>
 __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, const double *__restrict__ Y,
                                                                  const double *__restrict__ Z,
+                                                                 const double *__restrict__ Q12,
+                                                                 const double *__restrict__ Q13,
                                                                  const double *__restrict__ eo,
                                                                  const double *__restrict__ ev,
                                                                  double *__restrict__ t3) {
+    // M3 (CCSDT-2): ws also carries P(abc) Q12 (both under P(i/jk)), and qs = P(a/bc) Q13
+    // under the full P(ijk).  Without M3, ws = -P(c/ab) Z and the arithmetic is that of
+    // [P(k/ij) ys - P(i/jk) zs] exactly.
     extern __shared__ double sm[];
     const int O = 2 * o, V = 2 * v;
     const int O3 = O * O * O, sj = O + 1, si = O * sj + 1, P = O * si;
-    double *ys = sm, *zs = sm + P, *us = sm + 2 * P;
+    double *ys = sm, *ws = sm + P, *us = sm + 2 * P, *qs = sm + 3 * P;
     int a, b, c;
     decode_triple(blockIdx.x, a, b, c);
     const int sv = (a & 1) + (b & 1) + (c & 1);
@@ -269,14 +275,21 @@ __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, c
     for (int e = threadIdx.x; e < O3; e += blockDim.x) {
         const int k = e % O, j = (e / O) % O, i = e / (O * O);
         const int p = i * si + j * sj + k;
-        double yv = 0.0, zv = 0.0;
+        double yv = 0.0, wv = 0.0, qv = 0.0;
         if ((i & 1) + (j & 1) + (k & 1) == sv) {
             yv = (y0[e] - y1[e]) - y2[e];
-            zv = (z0[e] - z1[e]) - z2[e];
+            wv = negd((z0[e] - z1[e]) - z2[e]);
+            if (M3) {
+                const double q = ((((Q12[slab(a, b, c) + e] - Q12[slab(b, a, c) + e]) - Q12[slab(c, b, a) + e]) -
+                                   Q12[slab(a, c, b) + e]) + Q12[slab(b, c, a) + e]) + Q12[slab(c, a, b) + e];
+                wv = q + wv;
+                qv = (Q13[slab(a, b, c) + e] - Q13[slab(b, a, c) + e]) - Q13[slab(c, b, a) + e];
+            }
         }
         ys[p] = yv;
-        zs[p] = zv;
+        ws[p] = wv;
         us[p] = 0.0;
+        if (M3) qs[p] = qv;
     }
     __syncthreads();
     const double fa = ev[a >> 1], fb = ev[b >> 1], fc = ev[c >> 1];
@@ -287,9 +300,15 @@ __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, c
         double u = 0.0;
         if ((i & 1) + (j & 1) + (k & 1) == sv) {
             const double y = (ys[i * si + j * sj + k] - ys[k * si + j * sj + i]) - ys[i * si + k * sj + j];
-            const double z = (zs[i * si + j * sj + k] - zs[j * si + i * sj + k]) - zs[k * si + j * sj + i];
+            const double w = (ws[i * si + j * sj + k] - ws[j * si + i * sj + k]) - ws[k * si + j * sj + i];
+            double num = y + w;
+            if (M3) {
+                const double q = ((((qs[i * si + j * sj + k] - qs[j * si + i * sj + k]) - qs[k * si + j * sj + i]) -
+                                   qs[i * si + k * sj + j]) + qs[j * si + k * sj + i]) + qs[k * si + i * sj + j];
+                num = num + q;
+            }
             const double den = ((eo[i >> 1] - fa) + (eo[j >> 1] - fb)) + (eo[k >> 1] - fc);
-            u = (y - z) / den;
+            u = num / den;
         }
         const double nu_ = negd(u);
         us[i * si + j * sj + k] = u;
@@ -312,6 +331,51 @@ __global__ void __launch_bounds__(256) t3_assemble_unique_kernel(int o, int v, c
         t3[s_bca + e] = u;
         t3[s_cab + e] = u;
         t3[s_cba + e] = nu_;
+    }
+}
+
+// The CCSDT-2 numerator element by element (any O): global reads of every permuted
+// operand, for O^3 slabs beyond shared memory or V < 3.
+__global__ void t3_assemble_m3_kernel(int o, int v, const double *__restrict__ Y, const double *__restrict__ Z,
+                                      const double *__restrict__ Q12, const double *__restrict__ Q13,
+                                      const double *__restrict__ eo, const double *__restrict__ ev,
+                                      double *__restrict__ t3) {
+    const int O = 2 * o, V = 2 * v;
+    const int64_t O3 = (int64_t)O * O * O;
+    const int64_t total = (int64_t)V * V * V * O3;
+    auto at = [&](const double *X, int a, int b, int c, int i, int j, int k) {
+        return X[(((int64_t)a * V + b) * V + c) * O3 + ((int64_t)i * O + j) * O + k];
+    };
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % O);
+        int64_t r = idx / O;
+        const int j = (int)(r % O);
+        r /= O;
+        const int i = (int)(r % O);
+        r /= O;
+        const int c = (int)(r % V);
+        r /= V;
+        const int b = (int)(r % V);
+        const int a = (int)(r / V);
+        if ((a & 1) + (b & 1) + (c & 1) != (i & 1) + (j & 1) + (k & 1)) continue;
+        auto pa = [&](int p, int q, int s) {
+            return (at(Y, a, b, c, p, q, s) - at(Y, b, a, c, p, q, s)) - at(Y, c, b, a, p, q, s);
+        };
+        const double y = (pa(i, j, k) - pa(k, j, i)) - pa(i, k, j);
+        auto pw = [&](int p, int q, int s) {
+            const double z = (at(Z, a, b, c, p, q, s) - at(Z, c, b, a, p, q, s)) - at(Z, a, c, b, p, q, s);
+            const double q12 = ((((at(Q12, a, b, c, p, q, s) - at(Q12, b, a, c, p, q, s)) - at(Q12, c, b, a, p, q, s)) -
+                                 at(Q12, a, c, b, p, q, s)) + at(Q12, b, c, a, p, q, s)) + at(Q12, c, a, b, p, q, s);
+            return q12 + negd(z);
+        };
+        const double w = (pw(i, j, k) - pw(j, i, k)) - pw(k, j, i);
+        auto pq = [&](int p, int q, int s) {
+            return (at(Q13, a, b, c, p, q, s) - at(Q13, b, a, c, p, q, s)) - at(Q13, c, b, a, p, q, s);
+        };
+        const double qq = ((((pq(i, j, k) - pq(j, i, k)) - pq(k, j, i)) - pq(i, k, j)) + pq(j, k, i)) + pq(k, i, j);
+        const double den = (eo[i >> 1] - ev[a >> 1]) + (eo[j >> 1] - ev[b >> 1]) + (eo[k >> 1] - ev[c >> 1]);
+        t3[idx] = ((y + w) + qq) / den;
     }
 }
 
@@ -352,13 +416,26 @@ void k_t2_spin(int o, int v, const double *t2, double *t2so, cudaStream_t st) {
     CCSD_LAUNCH_CHECK();
 }
 
-void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *eo, const double *ev, double *t3,
-                   cudaStream_t st) {
+void k_t3_assemble(int o, int v, const double *Y, const double *Z, const double *Q12, const double *Q13,
+                   const double *eo, const double *ev, double *t3, cudaStream_t st) {
     const int64_t V = 2 * (int64_t)v, triples = V * (V - 1) * (V - 2) / 6;
-    static int configured_unique = -1, configured_slab = -1;
+    static int configured_unique = -1, configured_unique3 = -1, configured_slab = -1;
+    if (Q12) {  // CCSDT-2 terms
+        if (V >= 3 && slab_smem_bytes(o, 4) <= kSlabSmemMax) {  // O <= 18
+            opt_in_smem(t3_assemble_unique_kernel<true>, configured_unique3);
+            t3_assemble_unique_kernel<true><<<(unsigned)triples, 256, slab_smem_bytes(o, 4), st>>>(o, v, Y, Z, Q12, Q13,
+                                                                                                 eo, ev, t3);
+        } else {
+            const size_t n = (size_t)64 * o * o * o * v * v * v;
+            t3_assemble_m3_kernel<<<blocks_for(n), 256, 0, st>>>(o, v, Y, Z, Q12, Q13, eo, ev, t3);
+        }
+        CCSD_LAUNCH_CHECK();
+        return;
+    }
     if (V >= 3 && slab_smem_bytes(o, 3) <= kSlabSmemMax) {  // O <= 20
-        opt_in_smem(t3_assemble_unique_kernel, configured_unique);
-        t3_assemble_unique_kernel<<<(unsigned)triples, 256, slab_smem_bytes(o, 3), st>>>(o, v, Y, Z, eo, ev, t3);
+        opt_in_smem(t3_assemble_unique_kernel<false>, configured_unique);
+        t3_assemble_unique_kernel<false><<<(unsigned)triples, 256, slab_smem_bytes(o, 3), st>>>(o, v, Y, Z, nullptr,
+                                                                                              nullptr, eo, ev, t3);
         CCSD_LAUNCH_CHECK();
         return;
     }

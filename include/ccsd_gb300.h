@@ -109,6 +109,10 @@ typedef struct ccsd_options {
 /* CCSDT-1b, CCSDT::Calc_Energy(toler, 2) (initializer.cpp:110-114): CCSDT-1a plus
  * the T3 T1 term of T2 (ccsdt.cpp:676-700).  Same memory and restrictions. */
 #define CCSD_METHOD_CCSDT1B 2
+/* CCSDT-2, CCSDT::Calc_Energy(toler, 3) (initializer.cpp:116-120): CCSDT-1b with
+ * T2-dressed X1/X2 and the X12/X13 terms of T3 (ccsdt.cpp:1078-1130, 1960-2040,
+ * 2301-2390).  Two more V^3 O^3 arrays (5 in all); same restrictions. */
+#define CCSD_METHOD_CCSDT2 3
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */
