@@ -292,6 +292,16 @@ def measure_ccsdt1a(cg, precision, pk):
                                                   "read, 6 t3 slabs written) / CUDA-event time",
                                             bytes_per_launch=bytes_alg, ms=asm)
     out["abs_dE_split_vs_fp64"] = abs(e[precision] - e["fp64"])
+    # CCSDT-1b (Method_Nr 2: + the T3 T1 term of T2) and CCSDT-2 (Method_Nr 3: + dressed
+    # X1/X2 and the X12/X13 terms of T3) on the same system
+    for meth in ("ccsdt-1b", "ccsdt-2"):
+        ms = {}
+        for prec in ("fp64", precision):
+            with cg.Solver(fock, o, df=b, precision=prec, method=meth, fixed_iterations=5) as s:
+                r = s.solve(amplitudes=False)
+            ms[prec + "_update_ms"] = float(np.median(r["update_ms"][1:]))
+            ms[prec + "_e_corr"] = r["e_corr"]
+        out[meth.replace("-", "")] = ms
     so, sv = 4, 16
     f_s, b_s = cg.make_synthetic(so, sv, 3 * (so + sv) // 2, 78)
     eri = np.einsum("Qpq,Qrs->pqrs", b_s, b_s)
