@@ -26,6 +26,8 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
                   + t_kli^adb t_j^c + 2 t_ijk^abc t_l^d]
 * CCSDT-2 (``Method_Nr == 3``): CCSDT-1b with T2-dressed X1/X2 and the X12/X13
   terms of T3 (``triples``).
+* CCSDT-3 (``Method_Nr == 4``): CCSDT-2 with T1 terms in X12/X13 and the X14/X15
+  terms of T3 (``triples``).
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -71,9 +73,10 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 class SpinOrbitalCCSD:
     def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
-        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2 (the reference's Method_Nr)."""
-        if method not in (-1, 1, 2, 3):
-            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a), 2 (CCSDT-1b) or 3 (CCSDT-2)")
+        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3 (the
+        reference's Method_Nr)."""
+        if method not in (-1, 1, 2, 3, 4):
+            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a), 2 (CCSDT-1b), 3 (CCSDT-2) or 4 (CCSDT-3)")
         self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
@@ -134,7 +137,7 @@ class SpinOrbitalCCSD:
         ``ccsd_memory_optimized.cpp:646``."""
         return 0.25 * np.einsum("ijab,abij->", self.goovv, self.tau(t1, t2))
 
-    def triples(self, t2):
+    def triples(self, t2, t1=None):
         """T3 from T2 (``ccsdt.cpp:995-1290``): t3[a,b,c,i,j,k] =
         [P(a/bc) P(k/ij) sum_e X1(b,c)(k,e) t2(a,e)(i,j) - P(c/ab) P(i/jk) sum_m X2(c,m)(j,k) t2(a,b)(i,m)
          (+ for CCSDT-2, Method_Nr 3: P(i/jk) P(abc) sum_e X12(a,b)(i,e) t2(e,c)(j,k)
@@ -143,13 +146,32 @@ class SpinOrbitalCCSD:
         dresses them with T2 (``ccsdt.cpp:1960-2040``):
           X1 += 1/2 sum_lm <lm||ek> t2(b,c)(l,m),  X2 += 1/2 sum_de t2(d,e)(j,k) <mc||de>
           X12(a,b)(i,d) = sum_le <lb||ed> t2(a,e)(i,l),  X13(a,l)(i,j) = -sum_md <ml||dj> t2(a,d)(i,m)
-                                                                      ``ccsdt.cpp:2301-2390``"""
+                                                                      ``ccsdt.cpp:2301-2390``
+        CCSDT-3 (Method_Nr 4) adds T1 terms to X12/X13 and, with the antisymmetrisers
+        of X1 and X2, P(c/ab) P(i/jk) sum_e X14(a,b)(i,e) t2(e,c)(j,k) and
+        P(a/bc) P(k/ij) sum_m X15(a,m)(i,j) t2(b,c)(m,k)       ``ccsdt.cpp:1028-1070, 2043-2125``
+          X14(a,b)(i,d) = sum_e <ab||ed> t1(e,i) + sum_elm <lm||ed> [t1(e,i) t1(a,l) t1(b,m)
+                          - t1(e,l) t2(a,b)(i,m) + 1/2 t1(e,i) t2(a,b)(l,m)] + sum_lm <lm||id> t1(a,l) t1(b,m)
+          X15(a,l)(i,j) = -sum_de <al||de> t1(d,i) t1(e,j) + sum_m <ml||ij> t1(a,m)
+                          + 1/2 sum_mde <ml||de> t1(a,m) tau(d,e)(i,j)"""
         X1, X2 = self.gvvvo, self.govoo  # X1 at [b,c,e,k], X2 at [m,c,j,k]
         if self.method >= 3:
             X1 = X1 + 0.5 * np.einsum("lmek,bclm->bcek", self.goovo, t2, **ES)
             X2 = X2 + 0.5 * np.einsum("dejk,mcde->mcjk", t2, self.govvv, **ES)
         A = np.einsum("bcek,aeij->abcijk", X1, t2, **ES)
         B = np.einsum("mcjk,abim->abcijk", X2, t2, **ES)
+        if self.method >= 4:
+            tau = self.tau(t1, t2)
+            X14 = (np.einsum("abed,ei->abid", self.gvvvv, t1, **ES)
+                   + np.einsum("lmed,ei,al,bm->abid", self.goovv, t1, t1, t1, **ES)
+                   - np.einsum("lmed,el,abim->abid", self.goovv, t1, t2, **ES)
+                   + 0.5 * np.einsum("lmed,ei,ablm->abid", self.goovv, t1, t2, **ES)
+                   + np.einsum("lmid,al,bm->abid", self.gooov, t1, t1, **ES))
+            X15 = (-np.einsum("alde,di,ej->alij", self.gvovv, t1, t1, **ES)
+                   + np.einsum("mlij,am->alij", self.goooo, t1, **ES)
+                   + 0.5 * np.einsum("mlde,am,deij->alij", self.goovv, t1, tau, **ES))
+            A = A + np.einsum("amij,bcmk->abcijk", X15, t2, **ES)   # same antisymmetriser as the X1 term
+            B = B - np.einsum("abie,ecjk->abcijk", X14, t2, **ES)   # same as the X2 term, opposite sign
         PA = A - A.transpose(1, 0, 2, 3, 4, 5) - A.transpose(2, 1, 0, 3, 4, 5)     # P(a/bc)
         PA = PA - PA.transpose(0, 1, 2, 5, 4, 3) - PA.transpose(0, 1, 2, 3, 5, 4)  # P(k/ij)
         PB = B - B.transpose(2, 1, 0, 3, 4, 5) - B.transpose(0, 2, 1, 3, 4, 5)     # P(c/ab)
@@ -158,6 +180,13 @@ class SpinOrbitalCCSD:
         if self.method >= 3:
             X12 = np.einsum("lbed,aeil->abid", self.govvv, t2, **ES)
             X13 = -np.einsum("mldj,adim->alij", self.goovo, t2, **ES)
+            if self.method >= 4:  # ccsdt.cpp:2321-2333, 2365-2383
+                X12 = (X12 - np.einsum("alid,bl->abid", self.gvoov, t1, **ES)
+                       - np.einsum("lbed,ei,al->abid", self.govvv, t1, t1, **ES)
+                       - np.einsum("lmed,bm,aeil->abid", self.goovv, t1, t2, **ES))
+                X13 = (X13 + np.einsum("mldj,di,am->alij", self.goovo, t1, t1, **ES)
+                       - np.einsum("mlde,adim,ej->alij", self.goovv, t2, t1, **ES)
+                       - np.einsum("alid,dj->alij", self.gvoov, t1, **ES))
             Q = np.einsum("abie,ecjk->abcijk", X12, t2, **ES)
             # P(abc): all six orders of the virtual indices with their signs
             Q = (Q - Q.transpose(1, 0, 2, 3, 4, 5) - Q.transpose(2, 1, 0, 3, 4, 5) - Q.transpose(0, 2, 1, 3, 4, 5)
@@ -248,7 +277,7 @@ class SpinOrbitalCCSD:
         # symmetric copies (ccsdt.cpp:720-723)
         t2_new = val - val.transpose(1, 0, 2, 3) - val.transpose(0, 1, 3, 2) + val.transpose(1, 0, 3, 2)
         if self.method >= 0:
-            return t1_new, t2_new, self.triples(t2)
+            return t1_new, t2_new, self.triples(t2, t1)
         return t1_new, t2_new
 
     def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None):

@@ -103,14 +103,15 @@ def test_live_reference_run_matches_oracle(tmp_path):
 
 CCSDT = {1: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1a.json").read_text()),
          2: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1b.json").read_text()),
-         3: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt2.json").read_text())}
-CCSDT_IDS = ["ccsdt1a", "ccsdt1b", "ccsdt2"]
+         3: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt2.json").read_text()),
+         4: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt3.json").read_text())}
+CCSDT_IDS = ["ccsdt1a", "ccsdt1b", "ccsdt2", "ccsdt3"]
 
 
-@pytest.mark.parametrize("method", [1, 2, 3], ids=CCSDT_IDS)
+@pytest.mark.parametrize("method", [1, 2, 3, 4], ids=CCSDT_IDS)
 @pytest.mark.parametrize("key", sorted(CCSDT[1]["synthetic"]))
 def test_oracle_ccsdt_matches_reference_synthetic(method, key):
-    """The spin-orbital oracle's CCSDT-1a / -1b / -2 against the reference's own
+    """The spin-orbital oracle's CCSDT-1a / -1b / -2 / -3 against the reference's own
     CCSDT::Calc_Energy(toler, Method_Nr), compiled unchanged: same iteration
     counter, energies to 1e-13."""
     c = CCSDT[method]["synthetic"][key]
@@ -121,7 +122,7 @@ def test_oracle_ccsdt_matches_reference_synthetic(method, key):
     assert abs(r["e_corr"] - c["e_corr"]) < 1e-13
 
 
-@pytest.mark.parametrize("method", [1, 2, 3], ids=CCSDT_IDS)
+@pytest.mark.parametrize("method", [1, 2, 3, 4], ids=CCSDT_IDS)
 @pytest.mark.parametrize("name", sorted(CCSDT[1]["h2o"]))
 def test_oracle_ccsdt_matches_reference_h2o(method, name):
     d, fock, mo = _h2o(Path(__file__).parent / "golden" / name)
@@ -133,7 +134,8 @@ def test_oracle_ccsdt_matches_reference_h2o(method, name):
 
 def test_ccsdt_methods_are_distinct():
     """Each method's extra terms move the reference's own energies by more than
-    the pin tolerance, so the pins above distinguish the methods."""
+    1e-10 (the smallest step, CCSDT-2 -> -3 at o4v6, is 8.8e-10), far above the
+    1e-13 pin tolerance, so the pins above distinguish the methods."""
     for key in CCSDT[1]["synthetic"]:
-        e = [CCSDT[m]["synthetic"][key]["e_corr"] for m in (1, 2, 3)]
-        assert abs(e[0] - e[1]) > 1e-9 and abs(e[1] - e[2]) > 1e-9
+        e = [CCSDT[m]["synthetic"][key]["e_corr"] for m in (1, 2, 3, 4)]
+        assert all(abs(e[m] - e[m + 1]) > 1e-10 for m in range(3))
