@@ -148,9 +148,13 @@ void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st);
 void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaStream_t st);
 // CCSDT-1a triples (triples.cu), spin orbitals O = 2o, V = 2v:
 // <PQ||RS> blocks from the spatial ovov/ovoo/ovvv blocks; kind 0: vvvo [b][c][e][k],
-// 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c]
-void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv, double *out,
-                cudaStream_t st);
+// 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c],
+// 5: voov [a][l][i][d], 6: oooo [m][l][i][j], 7: vvvv [a][b][e][d] (kinds 5-7 read oovv, oooo and
+// wv[a][b][c][d] = (ac|bd); the others may pass them as NULL)
+void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv,
+                const double *oovv, const double *oooo, const double *wv, double *out, cudaStream_t st);
+// tauso[a][b][i][j] = t2so + t1so[a][i] t1so[b][j] - t1so[a][j] t1so[b][i]
+void k_tau_spin(int o, int v, const double *t2so, const double *t1so, double *tauso, cudaStream_t st);
 // t1so[a][i] (spin orbitals) from the spatial t1[i][a]
 void k_t1_spin(int o, int v, const double *t1, double *t1so, cudaStream_t st);
 // t2so[a][b][i][j] (spin orbitals) from the spatial t2[i][j][a][b]

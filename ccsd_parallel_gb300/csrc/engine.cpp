@@ -107,7 +107,9 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     build_derived();
     CCSD_CUDA(cudaStreamSynchronize(st_));
     build_split_.reset();
-    wv_.alloc(0);  // the ladder reads W+ and W- (a gradient rebuilds (ac|bd) from the inputs)
+    // the ladder reads W+ and W- (a gradient rebuilds (ac|bd) from the inputs); CCSDT-3
+    // builds its spin-orbital <ab||cd> block from (ac|bd) and keeps it
+    if (opt_.method < CCSD_METHOD_CCSDT3) wv_.alloc(0);
 
     const size_t o = o_, v = v_;
     const size_t nT2 = o * o * v * v, nT1 = o * v;
@@ -166,7 +168,7 @@ void Engine::set_options(const ccsd_options &opts) {
         throw Error(CCSD_ERR_INVALID_ARG, "diis_size must be in [0, 16]");
     if (opts.max_iter < 0 || opts.fixed_iterations < 0)
         throw Error(CCSD_ERR_INVALID_ARG, "iteration counts must be >= 0");
-    if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT2)
+    if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT3)
         throw Error(CCSD_ERR_INVALID_ARG, "unknown method");
     if (opts.stream) {
         if (own_stream_ && st_) cudaStreamDestroy(st_);

@@ -113,6 +113,9 @@ class Engine {
     DBuf t3_, y3_, z3_, t2so_, so_vvvo_, so_ovoo_, so_oovv_, so_vovv_, so_ooov_;
     DBuf t1so_, g1b_, g2b_, h3b_, h4b_, f1b_, w5b_;  // CCSDT-1b T3 T1 intermediates
     DBuf x1d_, x2d_, x12_, x13_, q12_, q13_;         // CCSDT-2: dressed X1/X2, X12/X13 and their products
+    DBuf so_voov_, so_oooo_, so_vvvv_, tauso_;       // CCSDT-3
+    DBuf p1_, p2_, p3_, p4_, a1_, d14_, e15_, g15_, x14_, x15_;
+    void triples_m4_terms();
     void triples_1b_terms();
     void triples_m3_products();
 

@@ -38,7 +38,25 @@ void Engine::triples_setup() {
     so_vovv_.ensure(V * O * V * V);
     so_ooov_.ensure(O * O * O * V);
     DBuf *blocks[5] = {&so_vvvo_, &so_ovoo_, &so_oovv_, &so_vovv_, &so_ooov_};
-    for (int kind = 0; kind < 5; ++kind) k_so_block(kind, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, blocks[kind]->p, st_);
+    for (int kind = 0; kind < 5; ++kind)
+        k_so_block(kind, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, nullptr, nullptr, nullptr, blocks[kind]->p, st_);
+    if (opt_.method >= CCSD_METHOD_CCSDT3) {
+        if (wv_.n < (size_t)v_ * v_ * v_ * v_)
+            throw Error(CCSD_ERR_INVALID_ARG, "CCSDT-3 needs (ac|bd): set method CCSD_METHOD_CCSDT3 at ccsd_create");
+        so_voov_.ensure(V * O * O * V);
+        so_oooo_.ensure(O * O * O * O);
+        so_vvvv_.ensure(V * V * V * V);
+        k_so_block(5, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, oovv_.p, oooo_.p, wv_.p, so_voov_.p, st_);
+        k_so_block(6, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, oovv_.p, oooo_.p, wv_.p, so_oooo_.p, st_);
+        k_so_block(7, o_, v_, ovov_.p, ovoo_.p, ovvv_.p, oovv_.p, oooo_.p, wv_.p, so_vvvv_.p, st_);
+        tauso_.ensure(V * V * O * O);
+        for (DBuf *b : {&p1_, &p2_, &p4_, &d14_, &e15_}) b->ensure(V * O * O * V);
+        p3_.ensure(O * O * O * O);
+        g15_.ensure(O * O * O * O);
+        a1_.ensure(O * O * O * V);
+        x14_.ensure(V * V * O * V);
+        x15_.ensure(V * O * O * O);
+    }
     t3_.zero(st_);  // T3 starts at zero (the first update is CCSD-like)
     y3_.zero(st_);  // spin-forbidden blocks of Y and Z are never written
     z3_.zero(st_);
@@ -164,6 +182,7 @@ void Engine::triples_m3_products() {
          mv(t2so_.p, ix2((uint32_t)O, VO2, O), ix2((uint32_t)V, 1, O2)),
          mv(so_ooov_.p, ix2((uint32_t)O, O * V, V), ix2((uint32_t)V, O2 * V, 1)), 0.0,
          ovw(x13_.p, ix2((uint32_t)O, O3, O), ix2((uint32_t)O, O2, 1)), 0, 0, "T3_X13");
+    if (opt_.method >= CCSD_METHOD_CCSDT3) triples_m4_terms();  // T1 terms of X12/X13, X14/X15 into Z/Y
     const int64_t X12a = V * O * V, X12b = O * V, X12i = V;  // X12[a][b][i][d] strides
     for (int sa = 0; sa < 2; ++sa)
         for (int sb = 0; sb < 2; ++sb)
@@ -203,6 +222,114 @@ void Engine::triples_m3_products() {
                              mv(B, ix3(uv, uo, 2 * VO2, 2 * O2, 2), ix1(2 * O)), 0.0,
                              ovw(Cp, ix3(uo, uo, 2 * V2O3, 2 * O2, 2 * O), ix3(uv, uo, 2 * VO3, 2 * O3, 2)),
                              -(520 + sa * 4 + si * 2 + sj), -(530 + sm * 8 + sb * 4 + sc * 2 + sk), "T3_Q13");
+                    }
+            }
+}
+
+// CCSDT-3 (ccsdt.cpp:1028-1070, 2043-2125, 2321-2383), from this T1 and T2 (t1so, t2so):
+//   X12[a][b][i][d] -= sum_l <al||id> t1[b][l] + sum_l t1[a][l] P1[l][b][i][d] + sum_m t1[b][m] P2[a][i][m][d]
+//   X13[a][l][i][j] += sum_m t1[a][m] P3[m][l][i][j] - sum_e P2[a][i][l][e] t1[e][j] - sum_d <al||id> t1[d][j]
+//     P1[l][b][i][d] = sum_e <lb||ed> t1[e][i]           (<lb||ed> = -<bl||ed>)
+//     P2[a][i][m][d] = sum_{l,e} t2[a][e][i][l] <lm||ed>
+//     P3[m][l][i][j] = sum_d <ml||dj> t1[d][i]           (<ml||dj> = -<ml||jd>)
+//   X14[a][b][i][d] = sum_e <ab||ed> t1[e][i] + 1/2 sum_{l,m} t2[a][b][l][m] A1[l][m][i][d]
+//                     - sum_m t2[a][b][i][m] f[m][d] + sum_{l,m} t1[a][l] t1[b][m] (A1 + <lm||id>)[l][m][i][d]
+//     A1[l][m][i][d] = sum_e <lm||ed> t1[e][i],  f[m][d] = sum_{l,e} <ml||de> t1[e][l] (the CCSDT-1b f)
+//   X15[a][l][i][j] = -sum_e E[a][l][i][e] t1[e][j] + sum_m t1[a][m] G[m][l][i][j]
+//     E[a][l][i][e] = sum_d <al||de> t1[d][i],  G = <ml||ij> + 1/2 sum_{d,e} <ml||de> tau[d][e][i][j]
+//   Z -= sum_e X14[a][b][i][e] t2[e][c][j][k]   (the antisymmetriser of X2's term, opposite sign)
+//   Y += sum_m X15[a][m][i][j] t2[b][c][m][k]   (the antisymmetriser of X1's term)
+void Engine::triples_m4_terms() {
+    const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
+    const int64_t VO2 = V * O2, OV = O * V, VOV = V * O * V, O2V = O2 * V, V2 = V * V;
+    const uint32_t uO = (uint32_t)O, uV = (uint32_t)V, uo = (uint32_t)o, uv = (uint32_t)v;
+    const int iO = (int)O, iV = (int)V;
+    const double *t1s = t1so_.p, *t2s = t2so_.p;
+    const MatView t1_xl = mv(t1s, ix1(O), ix1(1));  // t1[x][l]: rows x, K l
+    const MatView t1_ie = mv(t1s, ix1(1), ix1(O));  // t1[e][i]: rows i, K e
+    const Dim rows_aid_x12 = ix3(uO, uV, VOV, V, 1);  // (a,i,d) of a [a][b][i][d] array
+    // ---- X12
+    gemm(iV * iO * iV, iV, iO, -1.0, mv(so_voov_.p, ix3(uO, uV, O2V, V, 1), ix1(OV)), t1_xl, 1.0,
+         ovw(x12_.p, rows_aid_x12, ix1(OV)), 0, 0, "T3_X12_voov_t1");
+    gemm(iO * iV * iV, iO, iV, -1.0, mv(so_vovv_.p, ix3(uV, uV, V2, O * V2, 1), ix1(V)), t1_ie, 0.0,
+         ovw(p1_.p, ix3(uV, uV, VOV, OV, 1), ix1(V)), 0, 0, "T3_P1");
+    gemm(iV * iO * iV, iV, iO, -1.0, mv(p1_.p, ix1(1), ix1(VOV)), t1_xl, 1.0, ovw(x12_.p, ix1(1), ix1(VOV)), 0, 0,
+         "T3_X12_P1");
+    gemm(iV * iO, iO * iV, iO * iV, 1.0, mv(t2s, ix2(uO, VO2, O), ix2(uV, 1, O2)),
+         mv(so_oovv_.p, ix2(uV, V2, 1), ix2(uV, O * V2, V)), 0.0, ovw(p2_.p, ix2(uO, O2V, OV), ix1(1)), 0, 0, "T3_P2");
+    gemm(iV * iO * iV, iV, iO, -1.0, mv(p2_.p, ix3(uO, uV, O2V, OV, 1), ix1(V)), t1_xl, 1.0,
+         ovw(x12_.p, rows_aid_x12, ix1(OV)), 0, 0, "T3_X12_P2");
+    // ---- X13
+    gemm((int)O3, iO, iV, -1.0, mv(so_ooov_.p, ix1(V), ix1(1)), t1_ie, 0.0,
+         ovw(p3_.p, ix3(uO, uO, O3, O2, 1), ix1(O)), 0, 0, "T3_P3");
+    gemm((int)O3, iV, iO, 1.0, mv(p3_.p, ix1(1), ix1(O3)), t1_xl, 1.0, ovw(x13_.p, ix1(1), ix1(O3)), 0, 0,
+         "T3_X13_P3");
+    gemm(iV * iO * iO, iO, iV, -1.0, mv(p2_.p, ix3(uO, uO, O2V, V, OV), ix1(1)), t1_ie, 1.0,
+         ovw(x13_.p, ix3(uO, uO, O3, O2, O), ix1(1)), 0, 0, "T3_X13_P2");
+    gemm(iV * iO * iO, iO, iV, -1.0, mv(so_voov_.p, ix1(V), ix1(1)), t1_ie, 1.0, ovw(x13_.p, ix1(O), ix1(1)), 0, 0,
+         "T3_X13_voov_t1");
+    // ---- X14
+    gemm(iV * iV * iV, iO, iV, 1.0, mv(so_vvvv_.p, ix2(uV, V2, 1), ix1(V)), t1_ie, 0.0,
+         ovw(x14_.p, ix2(uV, OV, 1), ix1(V)), 0, 0, "T3_X14_vvvv_t1");
+    gemm(iO * iO * iV, iO, iV, 1.0, mv(so_oovv_.p, ix2(uV, V2, 1), ix1(V)), t1_ie, 0.0,
+         ovw(a1_.p, ix2(uV, OV, 1), ix1(V)), 0, 0, "T3_A1");
+    gemm(iV * iV, iO * iV, (int)O2, 0.5, mv(t2s, ix1(O2), ix1(1)), mv(a1_.p, ix1(1), ix1(OV)), 1.0,
+         ovw(x14_.p, ix1(OV), ix1(1)), 0, 0, "T3_X14_t2A1");
+    gemm(iV * iV * iO, iV, iO, -1.0, mv(t2s, ix1(O), ix1(1)), mv(f1b_.p, ix1(1), ix1(V)), 1.0,
+         ovw(x14_.p, ix1(V), ix1(1)), 0, 0, "T3_X14_t2f");
+    axpby((int)O3, iV, 1.0, mv(so_ooov_.p, ix1(V), ix1(1)), 1.0, ovw(a1_.p, ix1(V), ix1(1)));  // A1 + <lm||id>
+    gemm(iO * iO * iV, iV, iO, 1.0, mv(a1_.p, ix1(1), ix1(O2V)), t1_xl, 0.0, ovw(d14_.p, ix1(1), ix1(O2V)), 0, 0,
+         "T3_D14");
+    gemm(iV * iO * iV, iV, iO, 1.0, mv(d14_.p, ix3(uO, uV, O2V, V, 1), ix1(OV)), t1_xl, 1.0,
+         ovw(x14_.p, rows_aid_x12, ix1(OV)), 0, 0, "T3_X14_t1t1");
+    // ---- X15
+    gemm(iV * iO * iV, iO, iV, 1.0, mv(so_vovv_.p, ix2(uV, V2, 1), ix1(V)), t1_ie, 0.0,
+         ovw(e15_.p, ix2(uV, OV, 1), ix1(V)), 0, 0, "T3_E15");
+    gemm(iV * iO * iO, iO, iV, -1.0, mv(e15_.p, ix1(V), ix1(1)), t1_ie, 0.0, ovw(x15_.p, ix1(O), ix1(1)), 0, 0,
+         "T3_X15_E");
+    k_tau_spin((int)o, (int)v, t2s, t1s, tauso_.p, st_);
+    copy(g15_.p, so_oooo_.p, (size_t)(O2 * O2));
+    gemm((int)O2, (int)O2, (int)V2, 0.5, mv(so_oovv_.p, ix1(V2), ix1(1)), mv(tauso_.p, ix1(1), ix1(O2)), 1.0,
+         ovw(g15_.p, ix1(O2), ix1(1)), 0, 0, "T3_G15");
+    gemm((int)O3, iV, iO, 1.0, mv(g15_.p, ix1(1), ix1(O3)), t1_xl, 1.0, ovw(x15_.p, ix1(1), ix1(O3)), 0, 0,
+         "T3_X15_G");
+    // ---- Q14 into Z, Q15 into Y (the spin blocks and t2 views of Q12 and Q13)
+    for (int sa = 0; sa < 2; ++sa)
+        for (int sb = 0; sb < 2; ++sb)
+            for (int si = 0; si < 2; ++si) {
+                const int se = sa + sb - si;
+                if (se < 0 || se > 1) continue;
+                const MatView Av =
+                    mv(x14_.p + sa * VOV + sb * OV + si * V + se, ix3(uv, uo, 2 * VOV, 2 * OV, 2 * V), ix1(2));
+                for (int sj = 0; sj < 2; ++sj)
+                    for (int sk = 0; sk < 2; ++sk) {
+                        const int sc = sj + sk - se;
+                        if (sc < 0 || sc > 1) continue;
+                        const double *B = t2s + se * VO2 + sc * O2 + sj * O + sk;
+                        double *Cp = z3_.p + sa * V2O3 + sb * VO3 + si * O2 + sc * O3 + sj * O + sk;
+                        gemm((int)(v * v * o), (int)(v * o * o), (int)v, -1.0, Av,
+                             mv(B, ix3(uo, uo, 2 * O2, 2 * O, 2), ix1(2 * VO2)), 1.0,
+                             ovw(Cp, ix3(uv, uo, 2 * V2O3, 2 * VO3, 2 * O2), ix3(uo, uo, 2 * O3, 2 * O, 2)),
+                             -(560 + sa * 4 + sb * 2 + si), -(510 + se * 8 + sc * 4 + sj * 2 + sk), "T3_Q14");
+                    }
+            }
+    for (int sa = 0; sa < 2; ++sa)
+        for (int si = 0; si < 2; ++si)
+            for (int sj = 0; sj < 2; ++sj) {
+                const int sm = si + sj - sa;
+                if (sm < 0 || sm > 1) continue;
+                const MatView Av =
+                    mv(x15_.p + sa * O3 + sm * O2 + si * O + sj, ix3(uo, uo, 2 * O3, 2 * O, 2), ix1(2 * O2));
+                for (int sb = 0; sb < 2; ++sb)
+                    for (int sc = 0; sc < 2; ++sc) {
+                        const int sk = sb + sc - sm;
+                        if (sk < 0 || sk > 1) continue;
+                        const double *B = t2s + sb * VO2 + sc * O2 + sm * O + sk;
+                        double *Cp = y3_.p + sa * V2O3 + si * O2 + sj * O + sb * VO3 + sc * O3 + sk;
+                        gemm((int)(v * o * o), (int)(v * v * o), (int)o, 1.0, Av,
+                             mv(B, ix3(uv, uo, 2 * VO2, 2 * O2, 2), ix1(2 * O)), 1.0,
+                             ovw(Cp, ix3(uo, uo, 2 * V2O3, 2 * O2, 2 * O), ix3(uv, uo, 2 * VO3, 2 * O3, 2)),
+                             -(570 + sa * 4 + si * 2 + sj), -(530 + sm * 8 + sb * 4 + sc * 2 + sk), "T3_Q15");
                     }
             }
 }

@@ -22,10 +22,20 @@ inline int blocks_for(size_t n) {
     return b < 1 ? 1 : (int)b;
 }
 
-// spatial chemist blocks: ovov[i][a][j][b], ovoo[i][a][j][k], ovvv[i][a][b][c]
+// spatial chemist blocks: ovov[i][a][j][b], ovoo[i][a][j][k], ovvv[i][a][b][c], and for the
+// CCSDT-3 blocks oovv[i][j][a][b], oooo[i][j][k][l], wv[a][b][c][d] = (ac|bd)
 struct Blocks {
     int o, v;
-    const double *ovov, *ovoo, *ovvv;
+    const double *ovov, *ovoo, *ovvv, *oovv, *oooo, *wv;
+    __device__ double OOVV(int i, int j, int a, int b) const {
+        return oovv[(((int64_t)i * o + j) * v + a) * v + b];
+    }
+    __device__ double OOOO(int i, int j, int k, int l) const {
+        return oooo[(((int64_t)i * o + j) * o + k) * o + l];
+    }
+    __device__ double WV(int a, int b, int c, int d) const {  // (ac|bd)
+        return wv[(((int64_t)a * v + b) * v + c) * v + d];
+    }
     __device__ double OVOV(int i, int a, int j, int b) const {
         return ovov[(((int64_t)i * v + a) * o + j) * v + b];
     }
@@ -43,6 +53,9 @@ struct Blocks {
 //   2: oovv [j][k][b][c] = (jb|kc) - (jc|kb)
 //   3: vovv [b][k][c][d] = (bc|kd) - (bd|kc)
 //   4: ooov [k][m][j][c] = (kj|mc) - (kc|mj)
+//   5: voov [a][l][i][d] = (ai|ld) - (ad|li)
+//   6: oooo [m][l][i][j] = (mi|lj) - (mj|li)
+//   7: vvvv [a][b][e][d] = (ae|bd) - (ad|be)
 __global__ void so_block_kernel(int kind, Blocks B, double *out) {
     const int O = 2 * B.o, V = 2 * B.v;
     int e0, e1, e2, e3;  // extents of the four indices
@@ -51,7 +64,10 @@ __global__ void so_block_kernel(int kind, Blocks B, double *out) {
         case 1: e0 = O; e1 = V; e2 = O; e3 = O; break;
         case 2: e0 = O; e1 = O; e2 = V; e3 = V; break;
         case 3: e0 = V; e1 = O; e2 = V; e3 = V; break;
-        default: e0 = O; e1 = O; e2 = O; e3 = V; break;
+        case 4: e0 = O; e1 = O; e2 = O; e3 = V; break;
+        case 5: e0 = V; e1 = O; e2 = O; e3 = V; break;
+        case 6: e0 = O; e1 = O; e2 = O; e3 = O; break;
+        default: e0 = V; e1 = V; e2 = V; e3 = V; break;
     }
     const int64_t total = (int64_t)e0 * e1 * e2 * e3;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -82,9 +98,21 @@ __global__ void so_block_kernel(int kind, Blocks B, double *out) {
                 if (s0 == s2 && s1 == s3) d = B.OVVV(p1, p3, p0, p2);
                 if (s0 == s3 && s1 == s2) x = B.OVVV(p1, p2, p0, p3);
                 break;
-            default:  // <km||jc>: (kj|mc) = ovoo[m][c][k][j], (kc|mj) = ovoo[k][c][m][j]
+            case 4:  // <km||jc>: (kj|mc) = ovoo[m][c][k][j], (kc|mj) = ovoo[k][c][m][j]
                 if (s0 == s2 && s1 == s3) d = B.OVOO(p1, p3, p0, p2);
                 if (s0 == s3 && s1 == s2) x = B.OVOO(p0, p3, p1, p2);
+                break;
+            case 5:  // <al||id>: (ai|ld) = ovov[i][a][l][d], (ad|li) = oovv[l][i][a][d]
+                if (s0 == s2 && s1 == s3) d = B.OVOV(p2, p0, p1, p3);
+                if (s0 == s3 && s1 == s2) x = B.OOVV(p1, p2, p0, p3);
+                break;
+            case 6:  // <ml||ij>: (mi|lj) = oooo[m][i][l][j], (mj|li) = oooo[m][j][l][i]
+                if (s0 == s2 && s1 == s3) d = B.OOOO(p0, p2, p1, p3);
+                if (s0 == s3 && s1 == s2) x = B.OOOO(p0, p3, p1, p2);
+                break;
+            default:  // <ab||ed>: (ae|bd) = wv[a][b][e][d], (ad|be) = wv[a][b][d][e]
+                if (s0 == s2 && s1 == s3) d = B.WV(p0, p1, p2, p3);
+                if (s0 == s3 && s1 == s2) x = B.WV(p0, p1, p3, p2);
                 break;
         }
         out[idx] = d - x;
@@ -110,6 +138,23 @@ __global__ void t2_spin_kernel(int o, int v, const double *__restrict__ t2, doub
         if (sa == si && sb == sj) val += t2[(((int64_t)i * o + j) * v + a) * v + b];
         if (sa == sj && sb == si) val -= t2[(((int64_t)j * o + i) * v + a) * v + b];
         t2so[idx] = val;
+    }
+}
+
+// tauso[a][b][i][j] = t2so[a][b][i][j] + t1so[a][i] t1so[b][j] - t1so[a][j] t1so[b][i]
+__global__ void tau_spin_kernel(int o, int v, const double *__restrict__ t2so, const double *__restrict__ t1so,
+                                double *__restrict__ tauso) {
+    const int O = 2 * o, V = 2 * v;
+    const int64_t total = (int64_t)V * V * O * O;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(idx % O);
+        int64_t r = idx / O;
+        const int i = (int)(r % O);
+        r /= O;
+        const int b = (int)(r % V);
+        const int a = (int)(r / V);
+        tauso[idx] = t2so[idx] + (t1so[a * O + i] * t1so[b * O + j] - t1so[a * O + j] * t1so[b * O + i]);
     }
 }
 
@@ -397,12 +442,18 @@ void opt_in_smem(Kern kern, int &configured) {  // the opt-in above 48 KB is per
 
 }  // namespace
 
-void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv, double *out,
-                cudaStream_t st) {
-    Blocks B{o, v, ovov, ovoo, ovvv};
+void k_so_block(int kind, int o, int v, const double *ovov, const double *ovoo, const double *ovvv,
+                const double *oovv, const double *oooo, const double *wv, double *out, cudaStream_t st) {
+    Blocks B{o, v, ovov, ovoo, ovvv, oovv, oooo, wv};
     const size_t O = 2 * (size_t)o, V = 2 * (size_t)v;
-    const size_t sizes[5] = {V * V * V * O, O * V * O * O, O * O * V * V, V * O * V * V, O * O * O * V};
+    const size_t sizes[8] = {V * V * V * O, O * V * O * O, O * O * V * V, V * O * V * V,
+                             O * O * O * V, V * O * O * V, O * O * O * O, V * V * V * V};
     so_block_kernel<<<blocks_for(sizes[kind]), 256, 0, st>>>(kind, B, out);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_tau_spin(int o, int v, const double *t2so, const double *t1so, double *tauso, cudaStream_t st) {
+    tau_spin_kernel<<<blocks_for((size_t)16 * o * o * v * v), 256, 0, st>>>(o, v, t2so, t1so, tauso);
     CCSD_LAUNCH_CHECK();
 }
 

@@ -113,6 +113,11 @@ typedef struct ccsd_options {
  * T2-dressed X1/X2 and the X12/X13 terms of T3 (ccsdt.cpp:1078-1130, 1960-2040,
  * 2301-2390).  Two more V^3 O^3 arrays (5 in all); same restrictions. */
 #define CCSD_METHOD_CCSDT2 3
+/* CCSDT-3, CCSDT::Calc_Energy(toler, 4) (initializer.cpp:122-126): CCSDT-2 with T1
+ * terms in X12/X13 and the X14/X15 terms of T3 (ccsdt.cpp:1028-1070, 2043-2125,
+ * 2321-2383).  Also keeps the spin-orbital <ab||cd> block ((2 nvir)^4 doubles);
+ * the method must be set at ccsd_create. */
+#define CCSD_METHOD_CCSDT3 4
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */
