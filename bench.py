@@ -292,9 +292,9 @@ def measure_ccsdt1a(cg, precision, pk):
                                                   "read, 6 t3 slabs written) / CUDA-event time",
                                             bytes_per_launch=bytes_alg, ms=asm)
     out["abs_dE_split_vs_fp64"] = abs(e[precision] - e["fp64"])
-    # CCSDT-1b (Method_Nr 2: + the T3 T1 term of T2) and CCSDT-2 (Method_Nr 3: + dressed
-    # X1/X2 and the X12/X13 terms of T3) on the same system
-    for meth in ("ccsdt-1b", "ccsdt-2"):
+    # CCSDT-1b (Method_Nr 2: + the T3 T1 term of T2), CCSDT-2 (Method_Nr 3: + dressed
+    # X1/X2 and the X12/X13 terms of T3) and CCSDT-3 (Method_Nr 4: + T1 terms and X14/X15)
+    for meth in ("ccsdt-1b", "ccsdt-2", "ccsdt-3"):
         ms = {}
         for prec in ("fp64", precision):
             with cg.Solver(fock, o, df=b, precision=prec, method=meth, fixed_iterations=5) as s:
