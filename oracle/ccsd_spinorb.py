@@ -28,6 +28,8 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
   terms of T3 (``triples``).
 * CCSDT-3 (``Method_Nr == 4``): CCSDT-2 with T1 terms in X12/X13 and the X14/X15
   terms of T3 (``triples``).
+* CCSDT-4 (``Method_Nr == 5``): CCSDT-3 with the X3/X4/X6 terms of the previous T3
+  in T3 (``triples``).
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -73,10 +75,10 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 class SpinOrbitalCCSD:
     def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
-        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3 (the
-        reference's Method_Nr)."""
-        if method not in (-1, 1, 2, 3, 4):
-            raise ValueError("method must be -1 (CCSD1), 1 (CCSDT-1a), 2 (CCSDT-1b), 3 (CCSDT-2) or 4 (CCSDT-3)")
+        method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3,
+        5 = CCSDT-4 (the reference's Method_Nr)."""
+        if method not in (-1, 1, 2, 3, 4, 5):
+            raise ValueError("method must be -1 (CCSD1) or 1-5 (CCSDT-1a, -1b, -2, -3, -4)")
         self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
@@ -137,7 +139,7 @@ class SpinOrbitalCCSD:
         ``ccsd_memory_optimized.cpp:646``."""
         return 0.25 * np.einsum("ijab,abij->", self.goovv, self.tau(t1, t2))
 
-    def triples(self, t2, t1=None):
+    def triples(self, t2, t1=None, t3=None):
         """T3 from T2 (``ccsdt.cpp:995-1290``): t3[a,b,c,i,j,k] =
         [P(a/bc) P(k/ij) sum_e X1(b,c)(k,e) t2(a,e)(i,j) - P(c/ab) P(i/jk) sum_m X2(c,m)(j,k) t2(a,b)(i,m)
          (+ for CCSDT-2, Method_Nr 3: P(i/jk) P(abc) sum_e X12(a,b)(i,e) t2(e,c)(j,k)
@@ -153,7 +155,12 @@ class SpinOrbitalCCSD:
           X14(a,b)(i,d) = sum_e <ab||ed> t1(e,i) + sum_elm <lm||ed> [t1(e,i) t1(a,l) t1(b,m)
                           - t1(e,l) t2(a,b)(i,m) + 1/2 t1(e,i) t2(a,b)(l,m)] + sum_lm <lm||id> t1(a,l) t1(b,m)
           X15(a,l)(i,j) = -sum_de <al||de> t1(d,i) t1(e,j) + sum_m <ml||ij> t1(a,m)
-                          + 1/2 sum_mde <ml||de> t1(a,m) tau(d,e)(i,j)"""
+                          + 1/2 sum_mde <ml||de> t1(a,m) tau(d,e)(i,j)
+        CCSDT-4 (Method_Nr 5) adds terms of the previous T3 (``ccsdt.cpp:1134-1180``) with the
+        bare X3(i,j)(l,m) = 1/2 <ij||lm>, X4(a,b)(d,e) = 1/2 <ab||de>, X6(a,l)(i,d) = <al||id>
+        (``ccsdt.cpp:2185-2300``):
+          P(c/ab) sum_de X4(a,b)(d,e) t3(dec,ijk) + P(k/ij) sum_lm X3(i,j)(l,m) t3(abc,lmk)
+          + P(i/jk) P(a/bc) sum_ld X6(a,l)(i,d) t3(dbc,ljk)"""
         X1, X2 = self.gvvvo, self.govoo  # X1 at [b,c,e,k], X2 at [m,c,j,k]
         if self.method >= 3:
             X1 = X1 + 0.5 * np.einsum("lmek,bclm->bcek", self.goovo, t2, **ES)
@@ -198,6 +205,14 @@ class SpinOrbitalCCSD:
             S = (S - S.transpose(0, 1, 2, 4, 3, 5) - S.transpose(0, 1, 2, 5, 4, 3) - S.transpose(0, 1, 2, 3, 5, 4)
                  + S.transpose(0, 1, 2, 4, 5, 3) + S.transpose(0, 1, 2, 5, 3, 4))
             num = num + Q + S
+        if self.method >= 5 and t3 is not None:
+            W = 0.5 * np.einsum("abde,decijk->abcijk", self.gvvvv, t3, **ES)
+            num = num + W - W.transpose(2, 1, 0, 3, 4, 5) - W.transpose(0, 2, 1, 3, 4, 5)      # P(c/ab)
+            W = 0.5 * np.einsum("ijlm,abclmk->abcijk", self.goooo, t3, **ES)
+            num = num + W - W.transpose(0, 1, 2, 5, 4, 3) - W.transpose(0, 1, 2, 3, 5, 4)      # P(k/ij)
+            W = np.einsum("alid,dbcljk->abcijk", self.gvoov, t3, **ES)
+            W = W - W.transpose(1, 0, 2, 3, 4, 5) - W.transpose(2, 1, 0, 3, 4, 5)              # P(a/bc)
+            num = num + W - W.transpose(0, 1, 2, 4, 3, 5) - W.transpose(0, 1, 2, 5, 4, 3)      # P(i/jk)
         d = self.den
         D3 = (d[:, None, None, :, None, None] + d[None, :, None, None, :, None] + d[None, None, :, None, None, :])
         return num / D3
@@ -277,7 +292,7 @@ class SpinOrbitalCCSD:
         # symmetric copies (ccsdt.cpp:720-723)
         t2_new = val - val.transpose(1, 0, 2, 3) - val.transpose(0, 1, 3, 2) + val.transpose(1, 0, 3, 2)
         if self.method >= 0:
-            return t1_new, t2_new, self.triples(t2, t1)
+            return t1_new, t2_new, self.triples(t2, t1, t3)
         return t1_new, t2_new
 
     def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None):
