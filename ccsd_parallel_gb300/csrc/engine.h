@@ -116,6 +116,7 @@ class Engine {
     DBuf so_voov_, so_oooo_, so_vvvv_, tauso_;       // CCSDT-3
     DBuf p1_, p2_, p3_, p4_, a1_, d14_, e15_, g15_, x14_, x15_;
     void triples_m4_terms();
+    void triples_m5_terms();
     void triples_1b_terms();
     void triples_m3_products();
 

@@ -334,6 +334,34 @@ void Engine::triples_m4_terms() {
             }
 }
 
+// CCSDT-4 (ccsdt.cpp:1134-1180): terms of the previous t3 with X3 = 1/2 <ij||lm>,
+// X4 = 1/2 <ab||de>, X6 = <al||id>, added to Y so that the assembly's P(a/bc) P(k/ij)
+// produces them:
+//   P(k/ij) sum_lm X3(i,j)(l,m) t3(abc,lmk): W is antisymmetric in abc, where P(a/bc) W = 3 W,
+//     so Y += W / 3;
+//   P(c/ab) sum_de X4(a,b)(d,e) t3(dec,ijk): W is antisymmetric in ab and ijk; with the cyclic
+//     relabelling W'(a,b,c) = W(b,c,a), P(a/bc) W' = P(c/ab) W, and P(k/ij) W' = 3 W', so
+//     Y(abc,ijk) += 1/3 sum_de X4(b,c)(d,e) t3(dea,ijk);
+//   P(i/jk) P(a/bc) sum_ld X6(a,l)(i,d) t3(dbc,ljk): W is antisymmetric in bc and jk; with
+//     W'(ijk) = W(kij), P(k/ij) W' = P(i/jk) W, so Y(abc,ijk) += sum_ld X6(a,l)(k,d) t3(dbc,lij).
+void Engine::triples_m5_terms() {
+    const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
+    const int64_t OV = O * V, O2V = O2 * V, V2 = V * V;
+    const uint32_t uO = (uint32_t)O, uV = (uint32_t)V;
+    const int iO = (int)O, iV = (int)V;
+    const double *t3 = t3_.p;
+    // X4: M = (b,c), N = (a, ijk), K = (d,e)
+    gemm((int)V2, (int)(V * O3), (int)V2, 0.5 / 3.0, mv(so_vvvv_.p, ix1(V2), ix1(1)), mv(t3, ix1(1), ix1(VO3)), 1.0,
+         ovw(y3_.p, ix1(O3), ix2((uint32_t)O3, V2O3, 1)), 0, 0, "T3_X4t3");
+    // X3: M = (abc, k), N = (i,j), K = (l,m)
+    gemm((int)(V * V2 * O), (int)O2, (int)O2, 0.5 / 3.0, mv(t3, ix2(uO, O3, 1), ix1(O)),
+         mv(so_oooo_.p, ix1(O2), ix1(1)), 1.0, ovw(y3_.p, ix2(uO, O3, 1), ix1(O)), 0, 0, "T3_X3t3");
+    // X6: M = (a,k), N = (bc, ij), K = (l,d)
+    gemm(iV * iO, (int)(V2 * O2), iO * iV, 1.0, mv(so_voov_.p, ix2(uO, O2V, V), ix2(uV, OV, 1)),
+         mv(t3, ix2((uint32_t)O2, O3, 1), ix2(uV, O2, V2O3)), 1.0,
+         ovw(y3_.p, ix2(uO, V2O3, 1), ix2((uint32_t)O2, O3, O)), 0, 0, "T3_X6t3");
+}
+
 void Engine::triples_step() {
     const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
     const int io = (int)o, iv = (int)v;
@@ -419,6 +447,10 @@ void Engine::triples_step() {
     }
     // integral operands are split once (positive keys) unless they change every update
     const int ksign = m3 ? -1 : 1;
+    // The Y blocks below write only their 18 spin blocks and leave the rest of Y at zero;
+    // the CCSDT-4 terms add to all of Y (also to spin-allowed elements outside those
+    // blocks), so Y starts from zero each update there
+    if (opt_.method >= CCSD_METHOD_CCSDT4) y3_.zero(st_);
 
     // ---- T3 from the previous T2 (ccsdt.cpp:1016-1058, 1235-1238), by spin blocks.
     // Spin orbital X = 2x + s, so a block of fixed spins is a stride-2 view of
@@ -469,6 +501,7 @@ void Engine::triples_step() {
                     }
             }
     if (m3) triples_m3_products();
+    if (opt_.method >= CCSD_METHOD_CCSDT4) triples_m5_terms();  // the previous t3 into Y
 
     cudaEvent_t ea = nullptr, eb = nullptr, ec = nullptr;
     if (opt_.profile) {  // a site of its own in the contraction profile (no flops)

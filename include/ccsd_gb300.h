@@ -118,6 +118,9 @@ typedef struct ccsd_options {
  * 2321-2383).  Also keeps the spin-orbital <ab||cd> block ((2 nvir)^4 doubles);
  * the method must be set at ccsd_create. */
 #define CCSD_METHOD_CCSDT3 4
+/* CCSDT-4, CCSDT::Calc_Energy(toler, 5) (initializer.cpp:128-132): CCSDT-3 with the
+ * X3/X4/X6 terms of the previous T3 in T3 (ccsdt.cpp:1134-1180); same memory as CCSDT-3. */
+#define CCSD_METHOD_CCSDT4 5
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */

@@ -1,8 +1,7 @@
-"""CCSDT-1a, -1b, -2 and -3 on the GPU engine (the reference's
-CCSDT::Calc_Energy(toler, 1 | 2 | 3 | 4), ccsdt.cpp:255-271) against the
+"""CCSDT-1a, -1b, -2, -3 and -4 on the GPU engine (the reference's
+CCSDT::Calc_Energy(toler, Method_Nr 1-5), ccsdt.cpp:255-271) against the
 spin-orbital oracle and the reference's own runs (tests/golden/
-reference_ccsdt1a.json, reference_ccsdt1b.json, reference_ccsdt2.json,
-reference_ccsdt3.json): FP64
+reference_ccsdt{1a,1b,2,3,4}.json): FP64
 energies to 1e-11 with the reference's iteration counter, amplitudes to 1e-12
 after a fixed number of updates, split precision within 1e-8."""
 import json
@@ -22,8 +21,9 @@ GOLD = Path(__file__).parent / "golden"
 CCSDT1A = json.loads((GOLD / "reference_ccsdt1a.json").read_text())
 GOLDEN = {"ccsdt-1a": CCSDT1A, "ccsdt-1b": json.loads((GOLD / "reference_ccsdt1b.json").read_text()),
           "ccsdt-2": json.loads((GOLD / "reference_ccsdt2.json").read_text()),
-          "ccsdt-3": json.loads((GOLD / "reference_ccsdt3.json").read_text())}
-METHOD_NR = {"ccsdt-1a": 1, "ccsdt-1b": 2, "ccsdt-2": 3, "ccsdt-3": 4}
+          "ccsdt-3": json.loads((GOLD / "reference_ccsdt3.json").read_text()),
+          "ccsdt-4": json.loads((GOLD / "reference_ccsdt4.json").read_text())}
+METHOD_NR = {"ccsdt-1a": 1, "ccsdt-1b": 2, "ccsdt-2": 3, "ccsdt-3": 4, "ccsdt-4": 5}
 
 
 def _case(c):
