@@ -30,6 +30,8 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
   terms of T3 (``triples``).
 * CCSDT-4 (``Method_Nr == 5``): CCSDT-3 with the X3/X4/X6 terms of the previous T3
   in T3 (``triples``).
+* CCSDT (``Method_Nr == 6``): CCSDT-4 with T3 terms in X1/X2, dressed X3/X4/X6 and
+  the X7/X8 terms (``triples``), including the reference's X3 loop as written.
 
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
@@ -76,9 +78,9 @@ class SpinOrbitalCCSD:
     def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
         method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3,
-        5 = CCSDT-4 (the reference's Method_Nr)."""
-        if method not in (-1, 1, 2, 3, 4, 5):
-            raise ValueError("method must be -1 (CCSD1) or 1-5 (CCSDT-1a, -1b, -2, -3, -4)")
+        5 = CCSDT-4, 6 = CCSDT (the reference's Method_Nr)."""
+        if method not in (-1, 1, 2, 3, 4, 5, 6):
+            raise ValueError("method must be -1 (CCSD1) or 1-6 (CCSDT-1a, -1b, -2, -3, -4, CCSDT)")
         self.method = method
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
@@ -160,11 +162,17 @@ class SpinOrbitalCCSD:
         bare X3(i,j)(l,m) = 1/2 <ij||lm>, X4(a,b)(d,e) = 1/2 <ab||de>, X6(a,l)(i,d) = <al||id>
         (``ccsdt.cpp:2185-2300``):
           P(c/ab) sum_de X4(a,b)(d,e) t3(dec,ijk) + P(k/ij) sum_lm X3(i,j)(l,m) t3(abc,lmk)
-          + P(i/jk) P(a/bc) sum_ld X6(a,l)(i,d) t3(dbc,ljk)"""
+          + P(i/jk) P(a/bc) sum_ld X6(a,l)(i,d) t3(dbc,ljk)
+        CCSDT (Method_Nr 6) dresses X1, X2 with T3 and X3, X4, X6 with T1/T2, and adds
+        P(a/bc) sum_d X8(a,d) t3(dbc,ijk) + P(i/jk) sum_m X7(i,m) t3(abc,mjk)
+                                                        ``ccsdt.cpp:1183-1200, 1960-2040, 2128-2300``"""
         X1, X2 = self.gvvvo, self.govoo  # X1 at [b,c,e,k], X2 at [m,c,j,k]
         if self.method >= 3:
             X1 = X1 + 0.5 * np.einsum("lmek,bclm->bcek", self.goovo, t2, **ES)
             X2 = X2 + 0.5 * np.einsum("dejk,mcde->mcjk", t2, self.govvv, **ES)
+        if self.method >= 6 and t3 is not None:  # ccsdt.cpp:1982-1988, 2020-2030
+            X1 = X1 - 0.5 * np.einsum("lmde,beclmk->bcdk", self.goovv, t3, **ES)
+            X2 = X2 + 0.5 * np.einsum("lmde,decjmk->lcjk", self.goovv, t3, **ES)
         A = np.einsum("bcek,aeij->abcijk", X1, t2, **ES)
         B = np.einsum("mcjk,abim->abcijk", X2, t2, **ES)
         if self.method >= 4:
@@ -206,11 +214,35 @@ class SpinOrbitalCCSD:
                  + S.transpose(0, 1, 2, 4, 5, 3) + S.transpose(0, 1, 2, 5, 3, 4))
             num = num + Q + S
         if self.method >= 5 and t3 is not None:
-            W = 0.5 * np.einsum("abde,decijk->abcijk", self.gvvvv, t3, **ES)
+            X3, X4, X6 = 0.5 * self.goooo, 0.5 * self.gvvvv, self.gvoov
+            if self.method >= 6:  # ccsdt.cpp:2128-2300
+                tau = self.tau(t1, t2)
+                # X3: the reference's tau loop runs "for (e = n_Electrons; d < Matrix_Size; d++)",
+                # so e stays at the first virtual and d runs over all virtuals once
+                X3 = (X3 + 0.5 * np.einsum("lmd,dij->ijlm", self.goovv[:, :, :, 0], tau[:, 0], **ES)
+                      + np.einsum("lmdj,di->ijlm", self.goovo, t1, **ES)
+                      - np.einsum("lmdi,dj->ijlm", self.goovo, t1, **ES))
+                X4 = (X4 + 0.5 * np.einsum("lmde,ablm->abde", self.goovv, tau, **ES)
+                      + np.einsum("lbde,al->abde", self.govvv, t1, **ES)
+                      - np.einsum("lade,bl->abde", self.govvv, t1, **ES))
+                X6 = (X6 + np.einsum("mled,aeim->alid", self.goovv, t2, **ES)
+                      - np.einsum("mled,ei,am->alid", self.goovv, t1, t1, **ES)
+                      + np.einsum("aled,ei->alid", self.gvovv, t1, **ES)
+                      - np.einsum("mlid,am->alid", self.gooov, t1, **ES))
+                X7 = (-0.5 * np.einsum("lmde,deli->im", self.goovv, tau, **ES)
+                      - np.einsum("lmdi,dl->im", self.goovo, t1, **ES))
+                X8 = (np.einsum("lade,dl->ae", self.govvv, t1, **ES)
+                      - 0.5 * np.einsum("lmde,dalm->ae", self.goovv, tau, **ES)
+                      - np.einsum("le,al->ae", self.fs[:self.O, self.O:], t1, **ES))
+                W = np.einsum("ad,dbcijk->abcijk", X8, t3, **ES)
+                num = num + W - W.transpose(1, 0, 2, 3, 4, 5) - W.transpose(2, 1, 0, 3, 4, 5)  # P(a/bc)
+                W = np.einsum("im,abcmjk->abcijk", X7, t3, **ES)
+                num = num + W - W.transpose(0, 1, 2, 4, 3, 5) - W.transpose(0, 1, 2, 5, 4, 3)  # P(i/jk)
+            W = np.einsum("abde,decijk->abcijk", X4, t3, **ES)
             num = num + W - W.transpose(2, 1, 0, 3, 4, 5) - W.transpose(0, 2, 1, 3, 4, 5)      # P(c/ab)
-            W = 0.5 * np.einsum("ijlm,abclmk->abcijk", self.goooo, t3, **ES)
+            W = np.einsum("ijlm,abclmk->abcijk", X3, t3, **ES)
             num = num + W - W.transpose(0, 1, 2, 5, 4, 3) - W.transpose(0, 1, 2, 3, 5, 4)      # P(k/ij)
-            W = np.einsum("alid,dbcljk->abcijk", self.gvoov, t3, **ES)
+            W = np.einsum("alid,dbcljk->abcijk", X6, t3, **ES)
             W = W - W.transpose(1, 0, 2, 3, 4, 5) - W.transpose(2, 1, 0, 3, 4, 5)              # P(a/bc)
             num = num + W - W.transpose(0, 1, 2, 4, 3, 5) - W.transpose(0, 1, 2, 5, 4, 3)      # P(i/jk)
         d = self.den

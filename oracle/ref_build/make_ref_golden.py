@@ -112,13 +112,13 @@ CCSDT1A_SYNTHETIC = [  # (nocc, nvir, naux, seed, sigma); sigma 0.2-0.3 gives vi
 
 CCSDT_METHODS = {"ccsdt-1a": (1, "reference_ccsdt1a.json"), "ccsdt-1b": (2, "reference_ccsdt1b.json"),
                  "ccsdt-2": (3, "reference_ccsdt2.json"), "ccsdt-3": (4, "reference_ccsdt3.json"),
-                 "ccsdt-4": (5, "reference_ccsdt4.json")}
+                 "ccsdt-4": (5, "reference_ccsdt4.json"), "ccsdt": (6, "reference_ccsdt.json")}
 
 
 def main_ccsdt(name="ccsdt-1a"):
     """The reference's CCSDT::Calc_Energy(toler, Method_Nr) on the synthetic
     systems and on H2O; Method_Nr 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3,
-    5 = CCSDT-4."""
+    5 = CCSDT-4, 6 = CCSDT."""
     method, out = CCSDT_METHODS[name]
     mode = f"ccsdt-{method}"
     runs = {"synthetic": {}, "h2o": {}}

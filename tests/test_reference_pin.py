@@ -105,14 +105,15 @@ CCSDT = {1: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1a.js
          2: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt1b.json").read_text()),
          3: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt2.json").read_text()),
          4: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt3.json").read_text()),
-         5: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt4.json").read_text())}
-CCSDT_IDS = ["ccsdt1a", "ccsdt1b", "ccsdt2", "ccsdt3", "ccsdt4"]
+         5: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt4.json").read_text()),
+         6: json.loads((Path(__file__).parent / "golden" / "reference_ccsdt.json").read_text())}
+CCSDT_IDS = ["ccsdt1a", "ccsdt1b", "ccsdt2", "ccsdt3", "ccsdt4", "ccsdt"]
 
 
-@pytest.mark.parametrize("method", [1, 2, 3, 4, 5], ids=CCSDT_IDS)
+@pytest.mark.parametrize("method", [1, 2, 3, 4, 5, 6], ids=CCSDT_IDS)
 @pytest.mark.parametrize("key", sorted(CCSDT[1]["synthetic"]))
 def test_oracle_ccsdt_matches_reference_synthetic(method, key):
-    """The spin-orbital oracle's CCSDT-1a / -1b / -2 / -3 / -4 against the reference's own
+    """The spin-orbital oracle's CCSDT-1a / -1b / -2 / -3 / -4 / CCSDT against the reference's own
     CCSDT::Calc_Energy(toler, Method_Nr), compiled unchanged: same iteration
     counter, energies to 1e-13."""
     c = CCSDT[method]["synthetic"][key]
@@ -123,7 +124,7 @@ def test_oracle_ccsdt_matches_reference_synthetic(method, key):
     assert abs(r["e_corr"] - c["e_corr"]) < 1e-13
 
 
-@pytest.mark.parametrize("method", [1, 2, 3, 4, 5], ids=CCSDT_IDS)
+@pytest.mark.parametrize("method", [1, 2, 3, 4, 5, 6], ids=CCSDT_IDS)
 @pytest.mark.parametrize("name", sorted(CCSDT[1]["h2o"]))
 def test_oracle_ccsdt_matches_reference_h2o(method, name):
     d, fock, mo = _h2o(Path(__file__).parent / "golden" / name)
@@ -138,5 +139,5 @@ def test_ccsdt_methods_are_distinct():
     1e-10 (the smallest step, CCSDT-2 -> -3 at o4v6, is 8.8e-10), far above the
     1e-13 pin tolerance, so the pins above distinguish the methods."""
     for key in CCSDT[1]["synthetic"]:
-        e = [CCSDT[m]["synthetic"][key]["e_corr"] for m in (1, 2, 3, 4, 5)]
-        assert all(abs(e[m] - e[m + 1]) > 1e-10 for m in range(4))
+        e = [CCSDT[m]["synthetic"][key]["e_corr"] for m in (1, 2, 3, 4, 5, 6)]
+        assert all(abs(e[m] - e[m + 1]) > 1e-10 for m in range(5))
