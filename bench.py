@@ -294,11 +294,20 @@ def measure_ccsdt1a(cg, precision, pk):
     out["abs_dE_split_vs_fp64"] = abs(e[precision] - e["fp64"])
     # CCSDT-1b (Method_Nr 2: + the T3 T1 term of T2), CCSDT-2 (Method_Nr 3: + dressed
     # X1/X2 and the X12/X13 terms of T3) and CCSDT-3 (Method_Nr 4: + T1 terms and X14/X15)
-    for meth in ("ccsdt-1b", "ccsdt-2", "ccsdt-3"):
-        ms = {}
+    # on the same system; CCSDT-4 (Method_Nr 5: + X3/X4/X6 terms of T3) and CCSDT (Method_Nr 6:
+    # + T3 in X1/X2, dressed X3/X4/X6, X7/X8), whose X4 term is O(V^5 O^3), on a smaller one
+    mo, mv_ = 4, 24
+    f_m, b_m = cg.make_synthetic(mo, mv_, 3 * (mo + mv_) // 2, 79)
+    for meth in ("ccsdt-1b", "ccsdt-2", "ccsdt-3", "ccsdt-4", "ccsdt"):
+        small = meth in ("ccsdt-4", "ccsdt")
+        ms = {"workload": f"synthetic nocc={mo} nvir={mv_} (seed 79)"} if small else {}
         for prec in ("fp64", precision):
-            with cg.Solver(fock, o, df=b, precision=prec, method=meth, fixed_iterations=5) as s:
+            with cg.Solver(*((f_m, mo) if small else (fock, o)), df=b_m if small else b, precision=prec,
+                           method=meth, fixed_iterations=5, profile=small) as s:
                 r = s.solve(amplitudes=False)
+                if small:
+                    top = sorted(s.profile()["sites"], key=lambda x: -x["ms"])[:6]
+                    ms[prec + "_top_sites_ms"] = {x["site"]: x["ms"] / x["calls"] for x in top}
             ms[prec + "_update_ms"] = float(np.median(r["update_ms"][1:]))
             ms[prec + "_e_corr"] = r["e_corr"]
         out[meth.replace("-", "")] = ms

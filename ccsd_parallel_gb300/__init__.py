@@ -51,7 +51,8 @@ def flops_per_update(nocc: int, nvir: int) -> float:
 
 METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A,
            "ccsdt-1b": _abi.CCSD_METHOD_CCSDT1B, "ccsdt-2": _abi.CCSD_METHOD_CCSDT2,
-           "ccsdt-3": _abi.CCSD_METHOD_CCSDT3, "ccsdt-4": _abi.CCSD_METHOD_CCSDT4}
+           "ccsdt-3": _abi.CCSD_METHOD_CCSDT3, "ccsdt-4": _abi.CCSD_METHOD_CCSDT4,
+           "ccsdt": _abi.CCSD_METHOD_CCSDT}
 
 
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,

@@ -32,6 +32,7 @@ CCSD_METHOD_CCSDT1B = 2
 CCSD_METHOD_CCSDT2 = 3
 CCSD_METHOD_CCSDT3 = 4
 CCSD_METHOD_CCSDT4 = 5
+CCSD_METHOD_CCSDT = 6
 
 CCSD_PREC_FP64 = 0
 CCSD_PREC_SPLIT2 = 2

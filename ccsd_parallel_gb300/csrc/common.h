@@ -125,6 +125,8 @@ void k_theta(int o, int v, const double *t1, const double *t2, double *th1, doub
              cudaStream_t st);
 // t2_new = (R + Rp + Rp^T) / D2, returns into t2_new; also writes the per-block
 // partial sums of |t2_new - t2_old|^2 into `partials` (length >= grid).
+// R[i][j][a][b] = R[j][i][b][a] = their mean (o o v v, in place)
+void k_pair_mean(int o, int v, double *R, cudaStream_t st);
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
                  const double *ev, const double *t2_old, double *t2_new, double *partials,
                  int nblocks, cudaStream_t st);

@@ -168,7 +168,7 @@ void Engine::set_options(const ccsd_options &opts) {
         throw Error(CCSD_ERR_INVALID_ARG, "diis_size must be in [0, 16]");
     if (opts.max_iter < 0 || opts.fixed_iterations < 0)
         throw Error(CCSD_ERR_INVALID_ARG, "iteration counts must be >= 0");
-    if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT4)
+    if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT)
         throw Error(CCSD_ERR_INVALID_ARG, "unknown method");
     if (opts.stream) {
         if (own_stream_ && st_) cudaStreamDestroy(st_);

@@ -115,6 +115,7 @@ class Engine {
     DBuf x1d_, x2d_, x12_, x13_, q12_, q13_;         // CCSDT-2: dressed X1/X2, X12/X13 and their products
     DBuf so_voov_, so_oooo_, so_vvvv_, tauso_;       // CCSDT-3
     DBuf p1_, p2_, p3_, p4_, a1_, d14_, e15_, g15_, x14_, x15_;
+    DBuf x3_, x4_, x6_, x7_, x8_, fsoT_;             // CCSDT: dressed X3/X4/X6, X7, X8
     void triples_m4_terms();
     void triples_m5_terms();
     void triples_1b_terms();

@@ -6,6 +6,7 @@
 // this path is DFMA on the CUDA cores: a 64x64 block tile, 16-deep K step,
 // 4x4 register micro-tile per thread.  Skinny shapes are split over K into a
 // scratch buffer and summed in a fixed order (deterministic results).
+#include "../../include/ccsd_gb300.h"
 #include "common.h"
 
 namespace ccsd {
@@ -264,6 +265,59 @@ __global__ void __launch_bounds__(256) gemm_skinny_f64_kernel(int M, int N, int 
     }
 }
 
+// Thin form (N <= 16 columns, K <= 64, many rows): the product streams A and C
+// once, with about 2 N flops per byte.  One thread per row of A; the N x K block
+// of B and the column offsets of A and C sit in shared memory, so a warp reads 32
+// rows at each k and writes its rows' N outputs with no reduction.
+constexpr int TH_KMAX = 64;
+
+template <int NN>
+__global__ void __launch_bounds__(256) gemm_thin_f64_kernel(int M, int N, int K, double alpha, MatView A,
+                                                            MatView B, double beta, OutView C) {
+    __shared__ double bs[TH_KMAX][NN];
+    __shared__ int64_t ak[TH_KMAX];
+    __shared__ int64_t cn[NN];
+    for (int e = threadIdx.x; e < K * NN; e += blockDim.x) {
+        const int k = e / NN, n = e % NN;
+        bs[k][n] = n < N ? B.p[dim_off(B.row, n) + dim_off(B.col, k)] : 0.0;
+    }
+    for (int k = threadIdx.x; k < K; k += blockDim.x) ak[k] = dim_off(A.col, k);
+    for (int n = threadIdx.x; n < NN; n += blockDim.x) cn[n] = n < N ? dim_off(C.col, n) : 0;
+    __syncthreads();
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+        const double *a = A.p + dim_off(A.row, m);
+        double acc[NN];
+#pragma unroll
+        for (int n = 0; n < NN; ++n) acc[n] = 0.0;
+        for (int k = 0; k < K; ++k) {
+            const double x = a[ak[k]];
+#pragma unroll
+            for (int n = 0; n < NN; ++n) acc[n] = fma(x, bs[k][n], acc[n]);
+        }
+        double *c = C.p + dim_off(C.row, m);
+#pragma unroll
+        for (int n = 0; n < NN; ++n) {
+            if (n >= N) break;
+            double v = alpha * acc[n];
+            if (beta != 0.0) v = fma(beta, c[cn[n]], v);
+            c[cn[n]] = v;
+        }
+    }
+}
+
+bool thin_shape(int M, int N, int K) {
+    const int lo = M < N ? M : N, hi = M < N ? N : M;
+    return lo <= 16 && hi >= 256 && K <= TH_KMAX;
+}
+
+template <int NN>
+void launch_thin(int M, int N, int K, double alpha, const MatView &A, const MatView &B, double beta,
+                 const OutView &C, cudaStream_t st) {
+    const int blocks = (int)std::min<long>((M + 255) / 256, 152L * 8);
+    gemm_thin_f64_kernel<NN><<<blocks, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C);
+    CCSD_LAUNCH_CHECK();
+}
+
 constexpr int kTargetBlocks = 2 * 152;
 constexpr int kSkinnyMaxN = 16;
 
@@ -298,6 +352,7 @@ int choose_splits(int M, int N, int K) {
 }  // namespace
 
 size_t gemm_f64_ws_elems(int M, int N, int K) {
+    if (M > 1 && N > 1 && thin_shape(M, N, K)) return 0;
     if (skinny_shape(M, N, K)) {
         const int Ml = M < N ? N : M;
         int s = choose_skinny_splits(Ml, K);
@@ -354,6 +409,17 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         CCSD_LAUNCH_CHECK();
         return;
     }
+    if (thin_shape(M, N, K)) {
+        if (M < N) {  // the short side goes to the columns
+            gemm_f64(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, ws, ws_elems, st);
+            return;
+        }
+        if (N <= 2) launch_thin<2>(M, N, K, alpha, A, B, beta, C, st);
+        else if (N <= 4) launch_thin<4>(M, N, K, alpha, A, B, beta, C, st);
+        else if (N <= 8) launch_thin<8>(M, N, K, alpha, A, B, beta, C, st);
+        else launch_thin<16>(M, N, K, alpha, A, B, beta, C, st);
+        return;
+    }
     if (skinny_shape(M, N, K)) {
         if (M < N) {  // the short side goes to the columns
             gemm_f64(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, ws, ws_elems, st);
@@ -363,6 +429,11 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         else if (N <= 4) launch_skinny<4>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
         else if (N <= 8) launch_skinny<8>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
         else launch_skinny<16>(M, N, K, alpha, A, B, beta, C, ws, ws_elems, st);
+        return;
+    }
+    if ((N + BN - 1) / BN > 65535) {  // grid.y limit: the long side goes to grid.x
+        if ((M + BN - 1) / BN > 65535) throw Error(CCSD_ERR_INVALID_ARG, "FP64 GEMM beyond the launch grid");
+        gemm_f64(N, M, K, alpha, B, A, beta, OutView{C.p, C.col, C.row}, ws, ws_elems, st);
         return;
     }
     int splits = choose_splits(M, N, K);

@@ -183,6 +183,25 @@ __global__ void update_t2_kernel(int o, int v, const double *R, const double *Rp
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// R[i][j][a][b] and R[j][i][b][a] both become their mean; the thread at the
+// smaller index of a pair does both writes
+__global__ void pair_mean_kernel(int o, int v, double *R) {
+    const size_t total = (size_t)o * o * v * v, v2 = (size_t)v * v, ov2 = (size_t)o * v2;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(idx % v);
+        size_t r = idx / v;
+        const int a = (int)(r % v);
+        r /= v;
+        const int j = (int)(r % o), i = (int)(r / o);
+        const size_t p = (size_t)j * ov2 + (size_t)i * v2 + (size_t)b * v + a;
+        if (p <= idx) continue;
+        const double m = 0.5 * (R[idx] + R[p]);
+        R[idx] = m;
+        R[p] = m;
+    }
+}
+
 __global__ void update_t1_kernel(int o, int v, const double *R1, const double *eo,
                                  const double *ev, const double *t1_old, double *t1_new,
                                  double *partials) {
@@ -327,6 +346,13 @@ void k_update_t2(int o, int v, const double *R, const double *Rp, const double *
                  int nblocks, cudaStream_t st) {
     update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new,
                                                          partials);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_pair_mean(int o, int v, double *R, cudaStream_t st) {
+    const size_t n = (size_t)o * o * v * v;
+    if (n == 0) return;
+    pair_mean_kernel<<<grid_for(n), 256, 0, st>>>(o, v, R);
     CCSD_LAUNCH_CHECK();
 }
 

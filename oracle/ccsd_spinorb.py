@@ -75,13 +75,16 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 
 
 class SpinOrbitalCCSD:
-    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1):
+    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1, x3_as_written: bool = True):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
         method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3,
         5 = CCSDT-4, 6 = CCSDT (the reference's Method_Nr)."""
         if method not in (-1, 1, 2, 3, 4, 5, 6):
             raise ValueError("method must be -1 (CCSD1) or 1-6 (CCSDT-1a, -1b, -2, -3, -4, CCSDT)")
         self.method = method
+        # CCSDT's X3 tau term: the reference's loop (e fixed at the first virtual) or the
+        # sum over all (d, e) that the equations state
+        self.x3_as_written = x3_as_written
         self.fs = spin_orbital_fock(fock)
         self.g = spin_orbital_integrals(eri)
         self.O = 2 * nocc
@@ -219,7 +222,9 @@ class SpinOrbitalCCSD:
                 tau = self.tau(t1, t2)
                 # X3: the reference's tau loop runs "for (e = n_Electrons; d < Matrix_Size; d++)",
                 # so e stays at the first virtual and d runs over all virtuals once
-                X3 = (X3 + 0.5 * np.einsum("lmd,dij->ijlm", self.goovv[:, :, :, 0], tau[:, 0], **ES)
+                x3tau = (np.einsum("lmd,dij->ijlm", self.goovv[:, :, :, 0], tau[:, 0], **ES) if self.x3_as_written
+                         else np.einsum("lmde,deij->ijlm", self.goovv, tau, **ES))
+                X3 = (X3 + 0.5 * x3tau
                       + np.einsum("lmdj,di->ijlm", self.goovo, t1, **ES)
                       - np.einsum("lmdi,dj->ijlm", self.goovo, t1, **ES))
                 X4 = (X4 + 0.5 * np.einsum("lmde,ablm->abde", self.goovv, tau, **ES)
@@ -327,9 +332,36 @@ class SpinOrbitalCCSD:
             return t1_new, t2_new, self.triples(t2, t1, t3)
         return t1_new, t2_new
 
-    def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None):
+    def closed_shell(self, t1, t2):
+        """The spin-orbital t1, t2 a closed-shell engine works from: only the
+        closed-shell amplitudes t1[i,a] = t1(2a,2i) and t2[i,j,a,b] =
+        (t2(2a,2b+1,2i,2j+1) + t2(2b,2a+1,2j,2i+1)) / 2 (one amplitude for the pair
+        t2[i,j,a,b] = t2[j,i,b,a]; the two differ only where the reference's X3 loop,
+        ccsdt.cpp:2199-2206, breaks the alpha/beta symmetry) are kept, and expanded back as
+        t1(A,I) = t1[I',A'] d(sA,sI),
+        t2(A,B,I,J) = t2[I',J',A',B'] d(sA,sI) d(sB,sJ) - t2[J',I',A',B'] d(sA,sJ) d(sB,sI)."""
+        t1s = np.zeros_like(t1)
+        t1s[0::2, 0::2] = t1[0::2, 0::2]
+        t1s[1::2, 1::2] = t1[0::2, 0::2]
+        sp = t2[0::2, 1::2, 0::2, 1::2].transpose(2, 3, 0, 1)      # t2[i, j, a, b]
+        sp = 0.5 * (sp + sp.transpose(1, 0, 3, 2))
+        V, O = t2.shape[0], t2.shape[2]
+        sa = np.arange(V) % 2
+        si = np.arange(O) % 2
+        A = np.arange(V) // 2
+        I = np.arange(O) // 2
+        direct = sp[I[None, None, :, None], I[None, None, None, :], A[:, None, None, None], A[None, :, None, None]]
+        swapped = sp[I[None, None, None, :], I[None, None, :, None], A[:, None, None, None], A[None, :, None, None]]
+        d1 = (sa[:, None, None, None] == si[None, None, :, None]) & (sa[None, :, None, None] == si[None, None, None, :])
+        d2 = (sa[:, None, None, None] == si[None, None, None, :]) & (sa[None, :, None, None] == si[None, None, :, None])
+        return t1s, np.where(d1, direct, 0.0) - np.where(d2, swapped, 0.0)
+
+    def run(self, toler: float = 1e-10, itermax: int = 1000, max_passes: int | None = None,
+            closed_shell: bool = False):
         """Reference driver loop. Returns dict with e_corr, energies (per
-        ``iter``), iter (reference counter), t1, t2."""
+        ``iter``), iter (reference counter), t1, t2.  closed_shell: after every
+        pass keep only the closed-shell amplitudes of T1/T2 (as a spin-adapted
+        engine does, ``closed_shell()``), T3 as formed."""
         t1, t2 = self.mp2_guess()
         t3 = np.zeros((self.V,) * 3 + (self.O,) * 3) if self.method >= 0 else None
         e_new = self.energy(t1, t2)
@@ -342,6 +374,8 @@ class SpinOrbitalCCSD:
                 t1, t2, t3 = self.update(t1, t2, t3)
             else:
                 t1, t2 = self.update(t1, t2)
+            if closed_shell:
+                t1, t2 = self.closed_shell(t1, t2)
             e_new = self.energy(t1, t2)
             it += 1
             passes += 1

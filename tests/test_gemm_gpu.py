@@ -47,9 +47,28 @@ SKINNY = [(2000, 6, 3000), (7, 900, 1200), (240, 1, 100000), (3000, 16, 257), (1
           (33, 2, 70000)]
 
 
-@pytest.mark.parametrize("M,N,K", SHAPES + SKINNY)
+# short side <= 16 with K <= 64 over many rows: the thin form (one thread per row,
+# B in shared memory), short side in N or in M
+THIN = [(5000, 8, 8), (7, 3000, 64), (300, 16, 1), (100000, 3, 33), (2000, 2, 64)]
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES + SKINNY + THIN)
 def test_fp64_kernel(M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 13 + K)
+    A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
+    C0 = torch.randn(M, N, dtype=torch.float64, device="cuda", generator=g)
+    out = run_gemm("fp64", A, B, C0, alpha=0.7, beta=-1.3)
+    ref = 0.7 * (A @ B.T) - 1.3 * C0
+    scale = 0.7 * (A.abs() @ B.abs().T) + 1.3 * C0.abs()
+    assert ((out - ref).abs() <= 1e-13 * scale + 1e-300).all()
+
+
+def test_fp64_kernel_beyond_grid_y():
+    """N over 65535 column tiles (the CCSDT X3 term's V^3 O columns at nocc=6,
+    nvir=40 are 6.1M) runs with the long side in the grid's x dimension."""
+    M, N, K = 24, 64 * 65535 + 100, 8
+    g = torch.Generator(device="cuda").manual_seed(5)
     A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
     B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
     C0 = torch.randn(M, N, dtype=torch.float64, device="cuda", generator=g)
