@@ -24,8 +24,8 @@ from ._abi import (CCSD_INTS_AO_DENSE, CCSD_INTS_DF, CCSD_INTS_MO_DENSE, CCSD_IN
 PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD_PREC_SPLIT3,
               "split4": CCSD_PREC_SPLIT4}
 
-__all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "CCSD_Memory_optimized",
-           "CCSDError", "PRECISIONS"]
+__all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "frozen_core_count",
+           "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
 
 
 def _ptr(a):
@@ -74,16 +74,27 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     return o
 
 
-def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None):
+def frozen_core_count(Z) -> int:
+    """Frozen core orbitals by the reference's rule (one per atom with 2 < Z < 11;
+    ``ccsd_frozen_core_count``) for the nuclear charges Z."""
+    z = np.ascontiguousarray(Z, dtype=np.float64).ravel()
+    rc = _abi.lib().ccsd_frozen_core_count(_ptr(z), z.size)
+    _abi.check(min(rc, 0))
+    return int(rc)
+
+
+def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, nfrozen=0):
     """ccsd_problem over host arrays; returns (problem, arrays to keep alive).
 
     Integrals: ``eri`` spatial (pq|rs) [n]^4, ``df`` factors B[Q][p][q],
     ``ao_eri`` + ``mo_coeff``, or ``so_eri`` = <PQ||RS> over 2n interleaved
-    spin orbitals (the reference's antisymmetrised integrals)."""
+    spin orbitals (the reference's antisymmetrised integrals).  ``nocc`` counts
+    the occupied orbitals of these arrays; ``nfrozen`` of them (the lowest) are
+    frozen core, so the amplitudes cover nocc - nfrozen occupied orbitals."""
     fock = _f64(fock)
     n = fock.shape[0]
     p = _abi.Problem()
-    p.nocc, p.nvir = nocc, n - nocc
+    p.nocc, p.nvir, p.nfrozen = nocc - nfrozen, n - nocc, nfrozen
     keep = [fock]
     p.fock = _ptr(fock)
     if df is not None:
@@ -113,10 +124,11 @@ def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=N
 class Solver:
     """One device-resident system (integrals uploaded/transformed once)."""
 
-    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, **opts):
-        p, self._keep = _problem(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri)
-        n = p.nocc + p.nvir
-        self.nocc, self.nvir = nocc, n - nocc
+    def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, nfrozen=0, **opts):
+        p, self._keep = _problem(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri,
+                                 nfrozen=nfrozen)
+        n = p.nfrozen + p.nocc + p.nvir
+        self.nocc, self.nvir = p.nocc, p.nvir  # active orbitals (the amplitudes' shape)
         self._opts = _options(**opts)
         h = C.c_void_p()
         _abi.check(_abi.lib().ccsd_create(C.byref(p), C.byref(self._opts), C.byref(h)))
@@ -196,8 +208,10 @@ class Solver:
         self.close()
 
 
-def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, amplitudes=True, **opts):
-    with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri, **opts) as s:
+def solve(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, amplitudes=True, nfrozen=0,
+          **opts):
+    with Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri, nfrozen=nfrozen,
+                **opts) as s:
         return s.solve(amplitudes=amplitudes)
 
 
@@ -289,21 +303,24 @@ class CCSD_Memory_optimized:
     reference (ccsd_memory_optimized.h)        here
     ------------------------------------------------------------------
     CCSD_Memory_optimized(n_N, Z, R, basis,     CCSD_Memory_optimized(fock, nocc, eri=|df=|ao_eri=,
-      n_Elec, rank, size, HartFock*, frozen)      mo_coeff=, E_HF=) -- the integrals that
-                                                  Prepear_AOs would build are passed in
+      n_Elec, rank, size, HartFock*, frozen)      mo_coeff=, E_HF=, nfrozen=) -- the integrals that
+                                                  Prepear_AOs would build are passed in; frozen=true
+                                                  is nfrozen=frozen_core_count(Z)
     double CCSD(double toler, bool print)      CCSD(toler, print_stuff) -> E_HF + E_corr
-    E_new, T_1, t2                             E_new, t1 (o x v), t2 (o,o,v,v)
-    n_Electrons, unocc_orb (spin orbitals)     n_Electrons = 2 nocc, unocc_orb = 2 nvir
+    E_new, T_1, t2                             E_new, t1 (o x v), t2 (o,o,v,v) over active orbitals
+    n_Electrons, unocc_orb (spin orbitals)     n_Electrons = 2 (nocc - nfrozen), unocc_orb = 2 nvir
+                                                  (the reference subtracts the frozen electrons,
+                                                  ccsd_memory_optimized.cpp:3520)
 
     Like the reference, CCSD() runs plain Jacobi updates from the MP2 guess
     until |E_new - E_old| < toler or 999 updates (iter reaching 1000).
     """
 
     def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, E_HF=0.0,
-                 precision="fp64", so_eri=None):
+                 precision="fp64", so_eri=None, nfrozen=0):
         self._solver = Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri,
-                              precision=precision)
-        self.n_Electrons = 2 * nocc
+                              precision=precision, nfrozen=nfrozen)
+        self.n_Electrons = 2 * (nocc - nfrozen)
         self.unocc_orb = 2 * (np.asarray(fock).shape[0] - nocc)
         self.E_HF = E_HF
         self.E_new = 0.0

@@ -46,7 +46,7 @@ class Problem(C.Structure):
     _fields_ = [
         ("nocc", C.c_int32), ("nvir", C.c_int32), ("integral_kind", C.c_int32),
         ("naux", C.c_int32), ("nao", C.c_int32), ("device_inputs", C.c_int32),
-        ("fock", _dp), ("eri", _dp), ("df", _dp), ("mo_coeff", _dp),
+        ("fock", _dp), ("eri", _dp), ("df", _dp), ("mo_coeff", _dp), ("nfrozen", C.c_int32),
     ]
 
 
@@ -87,6 +87,7 @@ SIGNATURES = {
     "ccsd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "ccsd_profile_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
+    "ccsd_frozen_core_count": (C.c_int, [_dp, C.c_int32]),
     "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),
     "ccsd_gemm": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                             C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,

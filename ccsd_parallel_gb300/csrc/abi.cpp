@@ -236,4 +236,13 @@ double ccsd_flops_per_update(int32_t nocc, int32_t nvir) {
     return 2.0 * o * o * v * v * v * v + 4.0 * o * o * o * o * v * v + 8.0 * o * o * o * v * v * v;
 }
 
+int ccsd_frozen_core_count(const double *Z, int32_t n_atoms) {
+    if (n_atoms < 0 || (n_atoms > 0 && !Z)) return fail(CCSD_ERR_INVALID_ARG, "ccsd_frozen_core_count: n_atoms < 0 or Z is NULL");
+    g_last_error.clear();
+    int count = 0;
+    for (int32_t a = 0; a < n_atoms; ++a)
+        if (Z[a] > 2.0 && Z[a] < 11.0) ++count;
+    return count;
+}
+
 }  // extern "C"

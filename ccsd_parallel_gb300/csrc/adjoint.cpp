@@ -283,10 +283,12 @@ void Engine::reverse(const std::vector<TapeOp> &tape) {
 // their adjoints (v^4 each) are formed.  Lh and P tau are split once per call
 // (per-update cache keys, dropped at the next residual).
 void Engine::ladder_df_grad(const double *lam2, int naux) {
-    const int64_t o = o_, v = v_, n = n_, o2 = o * o, v2 = v * v, nn = n * n;
+    // B[Q][p][q] over the nt_ input orbitals, the active ones from nf_ on
+    const int64_t o = o_, v = v_, n = nt_, o2 = o * o, v2 = v * v, nn = n * n, f0 = (int64_t)nf_ * n + nf_;
     double *Bb = adj_of(input_df_ ? input_df_->p : nullptr);
     if (!Bb) return;
-    const double *B = input_df_->p;
+    Bb += f0;
+    const double *B = input_df_->p + f0;
     DBuf lh((size_t)(o2 * v2)), pt((size_t)(o2 * v2));
     // element (i,j | x,b) of a [j][i][b][x] read: row (i,j) strides (v2, o v2), column (x,b) strides (1, v)
     const MatView lt = mv(lam2, ix2((uint32_t)o, v2, o * v2), ix2((uint32_t)v, 1, v));
@@ -319,7 +321,8 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     if (!solved_) throw Error(CCSD_ERR_INVALID_ARG, "ccsd_lambda_grad needs a completed ccsd_solve first");
     if (opt_.method != CCSD_METHOD_CCSD)
         throw Error(CCSD_ERR_UNSUPPORTED, "ccsd_lambda_grad is built for CCSD (method CCSD_METHOD_CCSD)");
-    if (prob.nocc != o_ || prob.nvir != v_) throw Error(CCSD_ERR_INVALID_ARG, "problem shape differs from the handle's");
+    if (prob.nocc != o_ || prob.nvir != v_ || prob.nfrozen != nf_)
+        throw Error(CCSD_ERR_INVALID_ARG, "problem shape differs from the handle's");
     const int o = o_, v = v_;
     const int64_t ov = (int64_t)o * v, v2 = (int64_t)v * v, ov2 = (int64_t)o * v2, o2 = (int64_t)o * o;
     const size_t nT1 = (size_t)ov, nT2 = (size_t)(o2 * v2);
@@ -432,7 +435,7 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     CCSD_CUDA(cudaMemcpy(hl2.data(), l2.p, nT2 * sizeof(double), cudaMemcpyDeviceToHost));
     CCSD_CUDA(cudaMemcpy(ht1.data(), t1_.p, nT1 * sizeof(double), cudaMemcpyDeviceToHost));
     CCSD_CUDA(cudaMemcpy(ht2.data(), t2_.p, nT2 * sizeof(double), cudaMemcpyDeviceToHost));
-    const int n = o + v;
+    const int n = nt_, nf = nf_;  // d_fock covers the input's nt_ orbitals; frozen rows stay 0
     if (out->d_fock) {
         std::vector<double> deo(o, 0.0), dev(v, 0.0);
         for (int i = 0; i < o; ++i)
@@ -458,12 +461,13 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
         CCSD_CUDA(cudaMemcpy(fov.data(), adj_of(f_ov_.p), fov.size() * sizeof(double), cudaMemcpyDeviceToHost));
         double *F = out->d_fock;
         std::memset(F, 0, sizeof(double) * n * n);
+        auto at = [&](int p, int q) -> double & { return F[(size_t)(nf + p) * n + nf + q]; };
         for (int i = 0; i < o; ++i)
-            for (int j = 0; j < o; ++j) F[(size_t)i * n + j] = i == j ? deo[i] : foo[i * o + j];
+            for (int j = 0; j < o; ++j) at(i, j) = i == j ? deo[i] : foo[i * o + j];
         for (int a = 0; a < v; ++a)
-            for (int b = 0; b < v; ++b) F[(size_t)(o + a) * n + o + b] = a == b ? dev[a] : fvv[a * v + b];
+            for (int b = 0; b < v; ++b) at(o + a, o + b) = a == b ? dev[a] : fvv[a * v + b];
         for (int i = 0; i < o; ++i)
-            for (int a = 0; a < v; ++a) F[(size_t)i * n + o + a] = fov[i * v + a];
+            for (int a = 0; a < v; ++a) at(i, o + a) = fov[i * v + a];
     }
     auto fetch = [&](double *dst, DBuf *src) {
         if (!dst) return;

@@ -95,9 +95,12 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     if (prob.nocc <= 0 || prob.nvir <= 0)
         throw Error(CCSD_ERR_INVALID_ARG, "nocc and nvir must be positive");
     if (!prob.fock) throw Error(CCSD_ERR_INVALID_ARG, "fock is NULL");
+    if (prob.nfrozen < 0) throw Error(CCSD_ERR_INVALID_ARG, "nfrozen must be >= 0");
     o_ = prob.nocc;
     v_ = prob.nvir;
     n_ = o_ + v_;
+    nf_ = prob.nfrozen;
+    nt_ = nf_ + n_;
     const double ov2 = (double)o_ * o_ * v_ * v_;
     if (ov2 > 2.0e9 || (double)v_ * v_ >= 2.0e9)
         throw Error(CCSD_ERR_UNSUPPORTED, "shape too large for 32-bit tile indices");
@@ -188,25 +191,27 @@ void Engine::set_options(const ccsd_options &opts) {
 // ---------------------------------------------------------------------------
 // Integral set-up (the reference's Prepear_AOs + Fill_FS, ccsd_memory_optimized.cpp:71-74)
 void Engine::build_integrals(const ccsd_problem &prob) {
-    const int n = n_, o = o_, v = v_;
+    const int n = n_, o = o_, v = v_, nt = nt_, nf = nf_;
     // Fock, on the host: the diagonal goes to the denominators; the
     // off-diagonal blocks enter the intermediates (the reference only supports
-    // a diagonal matrix, Fill_FS :3560).
+    // a diagonal matrix, Fill_FS :3560).  Frozen core orbitals (the first nf of
+    // the nt input orbitals) are left out: the active block starts at nf.
     {
-        std::vector<double> hf((size_t)n * n);
+        std::vector<double> hf((size_t)nt * nt);
         if (prob.device_inputs)
-            CCSD_CUDA(cudaMemcpy(hf.data(), prob.fock, sizeof(double) * n * n, cudaMemcpyDeviceToHost));
+            CCSD_CUDA(cudaMemcpy(hf.data(), prob.fock, sizeof(double) * nt * nt, cudaMemcpyDeviceToHost));
         else
-            std::memcpy(hf.data(), prob.fock, sizeof(double) * n * n);
+            std::memcpy(hf.data(), prob.fock, sizeof(double) * nt * nt);
+        auto F = [&](int p, int q) { return hf[(size_t)(nf + p) * nt + nf + q]; };
         std::vector<double> eo(o), ev(v), oo((size_t)o * o), vv((size_t)v * v), ov((size_t)o * v);
-        for (int i = 0; i < o; ++i) eo[i] = hf[(size_t)i * n + i];
-        for (int a = 0; a < v; ++a) ev[a] = hf[(size_t)(o + a) * n + o + a];
+        for (int i = 0; i < o; ++i) eo[i] = F(i, i);
+        for (int a = 0; a < v; ++a) ev[a] = F(o + a, o + a);
         for (int i = 0; i < o; ++i)
-            for (int j = 0; j < o; ++j) oo[i * o + j] = i == j ? 0.0 : hf[(size_t)i * n + j];
+            for (int j = 0; j < o; ++j) oo[i * o + j] = i == j ? 0.0 : F(i, j);
         for (int a = 0; a < v; ++a)
-            for (int b = 0; b < v; ++b) vv[a * v + b] = a == b ? 0.0 : hf[(size_t)(o + a) * n + o + b];
+            for (int b = 0; b < v; ++b) vv[a * v + b] = a == b ? 0.0 : F(o + a, o + b);
         for (int i = 0; i < o; ++i)
-            for (int a = 0; a < v; ++a) ov[i * v + a] = hf[(size_t)i * n + o + a];
+            for (int a = 0; a < v; ++a) ov[i * v + a] = F(i, o + a);
         eo_.ensure(o);
         ev_.ensure(v);
         f_oo_off_.ensure((size_t)o * o);
@@ -229,30 +234,30 @@ void Engine::build_integrals(const ccsd_problem &prob) {
     const cudaMemcpyKind kind = prob.device_inputs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (prob.integral_kind == CCSD_INTS_MO_DENSE) {
         if (!prob.eri) throw Error(CCSD_ERR_INVALID_ARG, "eri is NULL");
-        std::unique_ptr<DBuf> eri(new DBuf((size_t)n * n * n * n));
+        std::unique_ptr<DBuf> eri(new DBuf((size_t)nt * nt * nt * nt));
         CCSD_CUDA(cudaMemcpyAsync(eri->p, prob.eri, sizeof(double) * eri->n, kind, st_));
-        build_from_mo_dense(eri->p);
+        build_from_mo_dense(eri->p, nt, nf);
         CCSD_CUDA(cudaStreamSynchronize(st_));
         input_eri_ = eri.get();
         keep(std::move(eri));
     } else if (prob.integral_kind == CCSD_INTS_DF) {
         if (!prob.df || prob.naux <= 0) throw Error(CCSD_ERR_INVALID_ARG, "df factors missing");
-        std::unique_ptr<DBuf> b(new DBuf((size_t)prob.naux * n * n));
+        std::unique_ptr<DBuf> b(new DBuf((size_t)prob.naux * nt * nt));
         CCSD_CUDA(cudaMemcpyAsync(b->p, prob.df, sizeof(double) * b->n, kind, st_));
         build_from_df(b->p, prob.naux);
         CCSD_CUDA(cudaStreamSynchronize(st_));
         input_df_ = b.get();
         keep(std::move(b));
     } else if (prob.integral_kind == CCSD_INTS_AO_DENSE) {
-        if (!prob.eri || !prob.mo_coeff || prob.nao < n)
+        if (!prob.eri || !prob.mo_coeff || prob.nao < nt)
             throw Error(CCSD_ERR_INVALID_ARG, "AO integrals / mo_coeff missing or nao < n");
         const size_t nao = prob.nao;
-        std::unique_ptr<DBuf> ao(new DBuf(nao * nao * nao * nao)), c(new DBuf(nao * n));
+        std::unique_ptr<DBuf> ao(new DBuf(nao * nao * nao * nao)), c(new DBuf(nao * nt));
         CCSD_CUDA(cudaMemcpyAsync(ao->p, prob.eri, sizeof(double) * ao->n, kind, st_));
         CCSD_CUDA(cudaMemcpyAsync(c->p, prob.mo_coeff, sizeof(double) * c->n, kind, st_));
         std::unique_ptr<DBuf> mo(new DBuf());
         ao_to_mo(ao->p, c->p, (int)nao, *mo);
-        build_from_mo_dense(mo->p);
+        build_from_mo_dense(mo->p, n, 0);
         CCSD_CUDA(cudaStreamSynchronize(st_));
         input_eri_ = ao.get();
         input_c_ = c.get();
@@ -265,14 +270,16 @@ void Engine::build_integrals(const ccsd_problem &prob) {
         // = so[2p][2r+1][2q][2s+1]: one strided copy (recorded, so the gradient
         // lands on these elements of the input).
         if (!prob.eri) throw Error(CCSD_ERR_INVALID_ARG, "eri is NULL");
-        const int64_t N = 2 * (int64_t)n, nn = n;
-        if (!prob.device_inputs) check_closed_shell_so(prob.eri, n);
+        const int64_t N = 2 * (int64_t)nt, nn = n, f2 = 2 * (int64_t)nf;
+        if (!prob.device_inputs) check_closed_shell_so(prob.eri, nt);
         std::unique_ptr<DBuf> so(new DBuf((size_t)(N * N * N * N))), mo(new DBuf((size_t)(nn * nn * nn * nn)));
         CCSD_CUDA(cudaMemcpyAsync(so->p, prob.eri, sizeof(double) * so->n, kind, st_));
+        // active block: spin orbitals from 2 nf on
         axpby((int)(nn * nn), (int)(nn * nn), 1.0,
-              mv(so->p + N * N + 1, ix2((uint32_t)n, 2 * N * N * N, 2 * N), ix2((uint32_t)n, 2 * N * N, 2)), 0.0,
-              ovw(mo->p, ix1(nn * nn), ix1(1)));
-        build_from_mo_dense(mo->p);
+              mv(so->p + f2 * (N * N * N + N * N + N + 1) + N * N + 1, ix2((uint32_t)n, 2 * N * N * N, 2 * N),
+                 ix2((uint32_t)n, 2 * N * N, 2)),
+              0.0, ovw(mo->p, ix1(nn * nn), ix1(1)));
+        build_from_mo_dense(mo->p, n, 0);
         CCSD_CUDA(cudaStreamSynchronize(st_));
         input_eri_ = so.get();
         keep(std::move(so));
@@ -315,8 +322,9 @@ void Engine::check_closed_shell_so(const double *so, int n) {
 }
 
 // Y[p'][q'][r'][s'] = eri[p0+p'][q0+q'][r0+r'][s0+s'] for every block.
-void Engine::build_from_mo_dense(const double *eri) {
-    const int64_t n = n_, o = o_, v = v_;
+void Engine::build_from_mo_dense(const double *eri, int64_t ld, int64_t off) {
+    const int64_t n = ld, o = o_, v = v_;
+    eri += ((off * n + off) * n + off) * n + off;
     auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
                    int64_t er, int64_t s0, int64_t es) {
         dst.ensure((size_t)(ep * eq * er * es));
@@ -340,7 +348,9 @@ void Engine::build_from_mo_dense(const double *eri) {
 
 // (pq|rs) = sum_Q B[Q][p][q] B[Q][r][s] as contractions over Q.
 void Engine::build_from_df(const double *B, int naux) {
-    const int64_t n = n_, o = o_, v = v_, nn = n * n;
+    // B[Q][p][q] over the nt_ input orbitals; the active ones start at nf_
+    const int64_t n = nt_, o = o_, v = v_, nn = n * n;
+    B += (int64_t)nf_ * n + nf_;
     auto blk = [&](DBuf &dst, int64_t p0, int64_t ep, int64_t q0, int64_t eq, int64_t r0,
                    int64_t er, int64_t s0, int64_t es) {
         dst.ensure((size_t)(ep * eq * er * es));
@@ -367,24 +377,26 @@ void Engine::build_from_df(const double *B, int naux) {
 
 // Four quarter transforms (mu nu|la si) -> (pq|rs) with C[mu][p]
 // (the reference's Prepear_AOs quarter matvecs, ccsd_memory_optimized.cpp:2990-3037).
-void Engine::ao_to_mo(const double *ao, const double *c, int nao_i, DBuf &mo) {
-    const int64_t N = nao_i, n = n_;
+void Engine::ao_to_mo(const double *ao, const double *c_in, int nao_i, DBuf &mo) {
+    // C[mu][p] over the nt_ input orbitals (row stride nt_); the active columns start at nf_
+    const int64_t N = nao_i, n = n_, ldc = nt_;
+    const double *c = c_in + nf_;
     std::unique_ptr<DBuf> x1(new DBuf((size_t)(n * N * N * N))), x2(new DBuf((size_t)(n * n * N * N))),
         x3(new DBuf((size_t)(n * n * n * N)));
     mo.ensure((size_t)(n * n * n * n));
     // x1[p][nu][la][si] = sum_mu C[mu][p] ao[mu][nu la si]
-    gemm((int)n, (int)(N * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+    gemm((int)n, (int)(N * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(ldc)),
          mv(ao, ix1(1), ix1(N * N * N)), 0.0, ovw(x1->p, ix1(N * N * N), ix1(1)));
     // x2[p][q][la si] = sum_nu C[nu][q] x1[p][nu][la si]; M = q, N = (p, lasi)
-    gemm((int)n, (int)(n * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+    gemm((int)n, (int)(n * N * N), (int)N, 1.0, mv(c, ix1(1), ix1(ldc)),
          mv(x1->p, ix2((uint32_t)(N * N), N * N * N, 1), ix1(N * N)), 0.0,
          ovw(x2->p, ix1(N * N), ix2((uint32_t)(N * N), n * N * N, 1)));
     // x3[pq][r][si] = sum_la C[la][r] x2[pq][la][si]; M = r, N = (pq, si)
-    gemm((int)n, (int)(n * n * N), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+    gemm((int)n, (int)(n * n * N), (int)N, 1.0, mv(c, ix1(1), ix1(ldc)),
          mv(x2->p, ix2((uint32_t)N, N * N, 1), ix1(N)), 0.0,
          ovw(x3->p, ix1(N), ix2((uint32_t)N, n * N, 1)));
     // mo[pqr][s] = sum_si C[si][s] x3[pqr][si]; M = s, N = pqr
-    gemm((int)n, (int)(n * n * n), (int)N, 1.0, mv(c, ix1(1), ix1(n)),
+    gemm((int)n, (int)(n * n * n), (int)N, 1.0, mv(c, ix1(1), ix1(ldc)),
          mv(x3->p, ix1(N), ix1(1)), 0.0, ovw(mo.p, ix1(1), ix1(n)));
     CCSD_CUDA(cudaStreamSynchronize(st_));
     if (tape_) {

@@ -66,7 +66,8 @@ class Engine {
   private:
     // set-up
     void build_integrals(const ccsd_problem &prob);
-    void build_from_mo_dense(const double *eri_dev);
+    // (pq|rs) with leading dimension ld, active orbitals from orbital `off` on
+    void build_from_mo_dense(const double *eri_dev, int64_t ld, int64_t off);
     void build_from_df(const double *b_dev, int naux);
     void ao_to_mo(const double *ao_dev, const double *c_dev, int nao, DBuf &mo_out);
     void build_derived();
@@ -159,6 +160,7 @@ class Engine {
     void diis_step(int update_index);
 
     int o_ = 0, v_ = 0, n_ = 0;
+    int nf_ = 0, nt_ = 0;  // frozen core orbitals; orbitals of the input arrays (nf_ + n_)
     ccsd_options opt_{};
     cudaStream_t st_ = nullptr;
     bool own_stream_ = false;

@@ -80,6 +80,13 @@ typedef struct ccsd_problem {
     const double *eri;     /* MO_DENSE: n^4; AO_DENSE: nao^4; SO_ANTISYM: (2n)^4 */
     const double *df;      /* DF: naux * n * n                                 */
     const double *mo_coeff;/* AO_DENSE: nao x n, row-major C[mu][p]            */
+    int32_t nfrozen;       /* frozen core: the first nfrozen spatial orbitals of
+                              the inputs stay doubly occupied and out of the
+                              correlation treatment (the reference's Freeze_Core,
+                              Prepear_AOs(nr_freeze), ccsd_memory_optimized.cpp:
+                              2698-2709, 3520-3521).  The arrays above then cover
+                              n = nfrozen + nocc + nvir orbitals; nocc counts the
+                              active occupied ones.  0 = all electrons.          */
 } ccsd_problem;
 
 typedef struct ccsd_options {
@@ -230,6 +237,15 @@ int ccsd_last_error(char *buf, size_t len);
 
 /* Algorithmic FLOP of one update: 2 o^2 v^4 + 4 o^4 v^2 + 8 o^3 v^3. */
 double ccsd_flops_per_update(int32_t nocc, int32_t nvir);
+
+/* Frozen core orbitals for ccsd_problem.nfrozen by the reference's rule
+ * (CCSD_Memory_optimized::Freeze_How_Meny_Orbitals, ccsd_memory_optimized.cpp:
+ * 5203-5231): one spatial orbital per atom with 2 < Z < 11 (Li-Ne), none for H
+ * and He or beyond Ne.  The reference's loop runs over the electrons and reads
+ * the nuclear charge Z(i) at the electron index; this counts per atom, as its
+ * comments state.  Z holds the n_atoms nuclear charges (the reference's vec Z).
+ * Returns the count, or CCSD_ERR_INVALID_ARG for n_atoms < 0 or a NULL Z. */
+int ccsd_frozen_core_count(const double *Z, int32_t n_atoms);
 
 /* One contraction on the engine's kernels, for row-major FP64 device matrices:
  *   C[M][N] = alpha * A[M][K] * B[N][K]^T + beta * C     (leading dims lda/ldb/ldc)

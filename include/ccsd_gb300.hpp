@@ -7,7 +7,10 @@
 //   -------------------------------------------------------------------------
 //   CCSD_Memory_optimized(n_N, Z, R, basis,      CCSD_Memory_optimized(Problem, E_HF)
 //     n_Elec, rank, size, HartFock*, frozen)      -- the inputs Prepear_AOs and
-//                                                    Fill_FS produce are passed in
+//                                                    Fill_FS produce are passed in;
+//                                                    frozen = true is Problem.nfrozen =
+//                                                    ccsd_frozen_core_count(Z, n_N)
+//   n_Electrons (less 2 nr_freeze, .cpp:3520)    n_Electrons = 2 Problem.nocc (active)
 //   double CCSD(double toler, bool print_stuff)  double CCSD(double toler, bool print_stuff)
 //     returns E_HF + E_corr                        returns E_HF + E_corr
 //   E_new, iter                                  E_new, iter (counter starts at 1)

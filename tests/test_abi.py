@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_struct_layouts_match_header_sizes():
-    assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8
+    assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8 + 8  # nfrozen (int32) padded to 8
     assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8
     assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
 
@@ -80,6 +80,20 @@ def test_flop_count_formula():
     o, v = 24.0, 300.0
     assert f == pytest.approx(2 * o**2 * v**4 + 4 * o**4 * v**2 + 8 * o**3 * v**3)
     assert f == pytest.approx(1.24e13, rel=0.02)
+
+
+def test_frozen_core_count_follows_reference_rule():
+    """One frozen spatial orbital per atom with 2 < Z < 11, none for H, He or
+    beyond Ne (Freeze_How_Meny_Orbitals, ccsd_memory_optimized.cpp:5203-5231),
+    counted per atom."""
+    import ccsd_parallel_gb300 as cg
+    assert cg.frozen_core_count([8.0, 1.0, 1.0]) == 1
+    assert cg.frozen_core_count([6.0, 8.0, 8.0]) == 3
+    assert cg.frozen_core_count([1.0, 2.0, 11.0, 17.0]) == 0
+    assert cg.frozen_core_count([3.0, 10.0]) == 2
+    assert cg.frozen_core_count([]) == 0
+    assert _abi.lib().ccsd_frozen_core_count(None, -1) == _abi.CCSD_ERR_INVALID_ARG
+    assert _abi.lib().ccsd_frozen_core_count(None, 2) == _abi.CCSD_ERR_INVALID_ARG
 
 
 def test_library_generator_matches_oracle_generator():
