@@ -25,7 +25,7 @@ PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD
               "split4": CCSD_PREC_SPLIT4}
 
 __all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "frozen_core_count",
-           "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
+           "ao_integrals", "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
 
 
 def _ptr(a):
@@ -81,6 +81,39 @@ def frozen_core_count(Z) -> int:
     rc = _abi.lib().ccsd_frozen_core_count(_ptr(z), z.size)
     _abi.check(min(rc, 0))
     return int(rc)
+
+
+def _basis(basis, accurate_boys=False):
+    """ccsd_basis over host arrays from a dict with the keys Z, R, atom, powers,
+    nprim, alpha, coef (the reference's Set_Input description); returns
+    (struct, arrays to keep alive)."""
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    Z, R = _f64(np.ravel(basis["Z"])), _f64(np.reshape(basis["R"], (-1, 3)))
+    atom, powers, nprim = i32(basis["atom"]), i32(np.reshape(basis["powers"], (-1, 3))), i32(basis["nprim"])
+    alpha, coef = _f64(np.atleast_2d(basis["alpha"])), _f64(np.atleast_2d(basis["coef"]))
+    b = _abi.Basis()
+    b.natoms, b.nbf, b.maxprim = Z.size, atom.size, alpha.shape[1]
+    b.flags = _abi.CCSD_BASIS_ACCURATE_BOYS if accurate_boys else 0
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+    b.Z, b.R, b.alpha, b.coef = _ptr(Z), _ptr(R), _ptr(alpha), _ptr(coef)
+    b.atom, b.powers, b.nprim = ip(atom), ip(powers), ip(nprim)
+    return b, [Z, R, atom, powers, nprim, alpha, coef]
+
+
+def ao_integrals(basis, eri: bool = True, accurate_boys: bool = False) -> dict:
+    """S, T, V (= -sum_C Z_C <mu|1/r_C|nu>), the ERIs (mu nu|la si) and E_nuc of a
+    contracted Cartesian Gaussian basis, computed on the GPU (ccsd_ao_integrals).
+    accurate_boys: CCSD_BASIS_ACCURATE_BOYS (the reference's Boys function is
+    reproduced by default)."""
+    b, keep = _basis(basis, accurate_boys)
+    n = b.nbf
+    S, T, V = np.empty((n, n)), np.empty((n, n)), np.empty((n, n))
+    G = np.empty((n, n, n, n)) if eri else None
+    e_nuc = C.c_double()
+    _abi.check(_abi.lib().ccsd_ao_integrals(C.byref(b), S.ctypes.data, T.ctypes.data, V.ctypes.data,
+                                            None if G is None else G.ctypes.data, C.byref(e_nuc), 0, None))
+    del keep
+    return dict(S=S, T=T, V=V, eri=G, e_nuc=e_nuc.value)
 
 
 def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, nfrozen=0):

@@ -17,6 +17,7 @@ CCSD_ERR_CUDA = -2
 CCSD_ERR_OUT_OF_MEMORY = -3
 CCSD_ERR_DIVERGED = -4
 CCSD_ERR_NO_DEVICE = -5
+CCSD_BASIS_ACCURATE_BOYS = 1
 CCSD_ERR_TIMEOUT = -6
 CCSD_ERR_UNSUPPORTED = -7
 CCSD_ERR_NOT_CONVERGED = -8
@@ -47,6 +48,14 @@ class Problem(C.Structure):
         ("nocc", C.c_int32), ("nvir", C.c_int32), ("integral_kind", C.c_int32),
         ("naux", C.c_int32), ("nao", C.c_int32), ("device_inputs", C.c_int32),
         ("fock", _dp), ("eri", _dp), ("df", _dp), ("mo_coeff", _dp), ("nfrozen", C.c_int32),
+    ]
+
+
+class Basis(C.Structure):
+    _fields_ = [
+        ("natoms", C.c_int32), ("nbf", C.c_int32), ("maxprim", C.c_int32), ("flags", C.c_int32),
+        ("Z", _dp), ("R", _dp), ("atom", C.POINTER(C.c_int32)), ("powers", C.POINTER(C.c_int32)),
+        ("nprim", C.POINTER(C.c_int32)), ("alpha", _dp), ("coef", _dp),
     ]
 
 
@@ -88,6 +97,8 @@ SIGNATURES = {
     "ccsd_profile_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
     "ccsd_frozen_core_count": (C.c_int, [_dp, C.c_int32]),
+    "ccsd_ao_integrals": (C.c_int, [C.POINTER(Basis), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_double), C.c_int32, C.c_void_p]),
     "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),
     "ccsd_gemm": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                             C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,

@@ -247,6 +247,48 @@ double ccsd_flops_per_update(int32_t nocc, int32_t nvir);
  * Returns the count, or CCSD_ERR_INVALID_ARG for n_atoms < 0 or a NULL Z. */
 int ccsd_frozen_core_count(const double *Z, int32_t n_atoms);
 
+/* ---- Gaussian integrals (the producer of the CCSD inputs) -------------- */
+/* A contracted Cartesian Gaussian basis as the reference's integral engine
+ * receives it (Hartree_Integrals::Set_Input, hartree_integrals.cpp:8-21): per
+ * basis function its atom, Cartesian powers (l, m, n), primitive count,
+ * exponents and contraction coefficients normalised as Normalize_small_c
+ * leaves them (hartree_fock_solver.cpp:236-462).  Host arrays. */
+typedef struct ccsd_basis {
+    int32_t natoms;
+    int32_t nbf;
+    int32_t maxprim;        /* row length of alpha / coef                       */
+    int32_t flags;          /* CCSD_BASIS_* bits; 0 = the reference's arithmetic */
+    const double *Z;        /* [natoms] nuclear charges                        */
+    const double *R;        /* [natoms][3] positions (bohr)                    */
+    const int32_t *atom;    /* [nbf] atom of each basis function               */
+    const int32_t *powers;  /* [nbf][3] Cartesian powers, l + m + n <= 3        */
+    const int32_t *nprim;   /* [nbf] primitives (<= maxprim)                   */
+    const double *alpha;    /* [nbf][maxprim] exponents                        */
+    const double *coef;     /* [nbf][maxprim] normalised coefficients          */
+} ccsd_basis;
+
+/* The reference's Boys function takes x > 50 from an asymptotic form of F_30
+ * (hartree_integrals.cpp:656-666) that is off by up to 1.2e-3 (relative) for
+ * 50 < x < 80 and gives 0 above x = 1.1e5 (x^61 overflows); by default the
+ * engine reproduces it, so its integrals equal the reference's.  This flag takes
+ * x > 50 from F_0 = sqrt(pi/x)/2 instead, accurate to e^{-x}. */
+#define CCSD_BASIS_ACCURATE_BOYS 1
+
+/* Overlap, kinetic, nuclear-attraction and electron-repulsion integrals on the
+ * GPU (McMurchie-Davidson, FP64), replacing Hartree_Integrals::Overlap_Matrix,
+ * Kinetic_Energy, Nuclei_Electron_Interaction, Nuclei_Nuclei_Interaction
+ * (hartree_integrals.cpp:293-718) and the (mu nu|la si) loop of
+ * Hartree_Fock_Solver::get_Energy (hartree_fock_solver.cpp:714-817):
+ *   S[mu][nu], T = -1/2 <mu|nabla^2|nu> (the reference's Kinetic_Energy is the
+ *   nabla^2 matrix), V = -sum_C Z_C <mu|1/r_C|nu> (its Nuclei_Electron_Interaction
+ *   is + the sum), so T + V is its EK; eri = (mu nu|la si), nbf^4 row-major;
+ *   e_nuc = sum_{A<B} Z_A Z_B / R_AB.
+ * Each output is optional (NULL).  device_outputs = 1: S/T/V/eri are device
+ * pointers (e_nuc stays host).  stream may be NULL.  Returns after the work is
+ * done.  CCSD_ERR_UNSUPPORTED above f functions. */
+int ccsd_ao_integrals(const ccsd_basis *basis, double *S, double *T, double *V, double *eri, double *e_nuc,
+                      int32_t device_outputs, void *stream);
+
 /* One contraction on the engine's kernels, for row-major FP64 device matrices:
  *   C[M][N] = alpha * A[M][K] * B[N][K]^T + beta * C     (leading dims lda/ldb/ldc)
  * precision CCSD_PREC_FP64 runs the DFMA kernel, CCSD_PREC_SPLIT* the

@@ -11,7 +11,7 @@ directory shim/x/y.  Flags: -O2 and -ftrivial-auto-var-init=zero, which gives
 the uninitialised `double temp` read in the reference's W_4 build
 (ccsd_memory_optimized.cpp:4789,4837) the value 0 it has on the even path.
 
-    python -m oracle.ref_build.build_ref        # builds ref_synthetic and ref_h2o
+    python -m oracle.ref_build.build_ref        # builds ref_synthetic, ref_h2o and ref_ints
 """
 from __future__ import annotations
 
@@ -47,18 +47,20 @@ def build(quiet: bool = False) -> bool:
         return False
     OUT.mkdir(exist_ok=True)
     jobs = [(REFERENCE / f"{s}.cpp", OUT / f"{s}.o") for s in COMMON + SCF]
-    jobs += [(HERE / "ref_synthetic.cpp", OUT / "ref_synthetic.o"), (HERE / "ref_h2o.cpp", OUT / "ref_h2o.o")]
+    jobs += [(HERE / "ref_synthetic.cpp", OUT / "ref_synthetic.o"), (HERE / "ref_h2o.cpp", OUT / "ref_h2o.o"),
+             (HERE / "ref_ints.cpp", OUT / "ref_ints.o")]
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(lambda a: _compile(*a), jobs))
     common = [str(OUT / f"{s}.o") for s in COMMON]
     for exe, extra in (("ref_synthetic", ["ref_synthetic.o"]),
-                       ("ref_h2o", ["ref_h2o.o"] + [f"{s}.o" for s in SCF])):
+                       ("ref_h2o", ["ref_h2o.o"] + [f"{s}.o" for s in SCF]),
+                       ("ref_ints", ["ref_ints.o"] + [f"{s}.o" for s in SCF])):
         r = subprocess.run(["g++", "-o", str(OUT / exe), *[str(OUT / e) for e in extra], *common],
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"linking {exe} failed:\n{r.stderr[-4000:]}")
     if not quiet:
-        print(f"built {OUT / 'ref_synthetic'} and {OUT / 'ref_h2o'}")
+        print(f"built {OUT / 'ref_synthetic'}, {OUT / 'ref_h2o'} and {OUT / 'ref_ints'}")
     return True
 
 

@@ -136,3 +136,15 @@ def test_no_cpu_path_when_no_device():
     rc = _abi.lib().ccsd_create(C.byref(p), None, C.byref(h))
     assert rc == _abi.CCSD_ERR_NO_DEVICE
     assert "no CPU path" in _abi.last_error()
+
+
+def test_integrals_have_no_cpu_path():
+    """ccsd_ao_integrals refuses without a GPU as well."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    import ccsd_parallel_gb300 as cg
+    d = np.load(ROOT / "tests" / "golden" / "ints_h2o_sto3g.npz")
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.ao_integrals(d)
+    assert ei.value.code == _abi.CCSD_ERR_NO_DEVICE
