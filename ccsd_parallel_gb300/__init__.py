@@ -25,7 +25,7 @@ PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD
               "split4": CCSD_PREC_SPLIT4}
 
 __all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "frozen_core_count",
-           "ao_integrals", "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
+           "ao_integrals", "rhf", "ccsd_inputs", "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
 
 
 def _ptr(a):
@@ -114,6 +114,29 @@ def ao_integrals(basis, eri: bool = True, accurate_boys: bool = False) -> dict:
                                             None if G is None else G.ctypes.data, C.byref(e_nuc), 0, None))
     del keep
     return dict(S=S, T=T, V=V, eri=G, e_nuc=e_nuc.value)
+
+
+def rhf(basis, n_electrons: int, tol: float = 1e-10, max_iter: int = 0, eri: bool = True,
+        accurate_boys: bool = False) -> dict:
+    """Closed-shell Hartree-Fock on the GPU integrals (ccsd_rhf), step for step as
+    the reference's Hartree_Fock_Solver::get_Energy: e_hf, e_nuc, eps, C[mu][p],
+    the AO integrals and the SCF step count.  ``ccsd_inputs(r)`` turns the result
+    into the keyword arguments of :func:`solve` (AO input)."""
+    b, keep = _basis(basis, accurate_boys)
+    n = b.nbf
+    r = _abi.ScfResult()
+    eps, Cm = np.empty(n), np.empty((n, n))
+    G = np.empty((n, n, n, n)) if eri else None
+    r.eps, r.C, r.eri = _ptr(eps), _ptr(Cm), _ptr(G)
+    _abi.check(_abi.lib().ccsd_rhf(C.byref(b), n_electrons, tol, max_iter, C.byref(r)))
+    del keep
+    return dict(e_hf=r.e_hf, e_nuc=r.e_nuc, iterations=r.iterations, converged=bool(r.converged), eps=eps,
+                C=Cm, eri=G, nocc=n_electrons // 2)
+
+
+def ccsd_inputs(scf: dict) -> dict:
+    """fock / nocc / ao_eri / mo_coeff for :func:`solve` from an :func:`rhf` result."""
+    return dict(fock=np.diag(scf["eps"]), nocc=scf["nocc"], ao_eri=scf["eri"], mo_coeff=scf["C"])
 
 
 def _problem(fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, so_eri=None, nfrozen=0):

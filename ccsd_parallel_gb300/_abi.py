@@ -59,6 +59,13 @@ class Basis(C.Structure):
     ]
 
 
+class ScfResult(C.Structure):
+    _fields_ = [
+        ("e_hf", C.c_double), ("e_nuc", C.c_double), ("iterations", C.c_int32), ("converged", C.c_int32),
+        ("eps", _dp), ("C", _dp), ("eri", _dp), ("stream", C.c_void_p),
+    ]
+
+
 class Options(C.Structure):
     _fields_ = [
         ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
@@ -97,6 +104,7 @@ SIGNATURES = {
     "ccsd_profile_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
     "ccsd_frozen_core_count": (C.c_int, [_dp, C.c_int32]),
+    "ccsd_rhf": (C.c_int, [C.POINTER(Basis), C.c_int32, C.c_double, C.c_int32, C.POINTER(ScfResult)]),
     "ccsd_ao_integrals": (C.c_int, [C.POINTER(Basis), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double), C.c_int32, C.c_void_p]),
     "ccsd_make_synthetic": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _dp, _dp]),

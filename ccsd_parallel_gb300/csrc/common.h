@@ -7,6 +7,8 @@
 #include <stdexcept>
 #include <string>
 
+struct ccsd_basis;  // include/ccsd_gb300.h
+
 namespace ccsd {
 
 // Status carried through the engine as an exception internally; converted to
@@ -125,6 +127,9 @@ void k_theta(int o, int v, const double *t1, const double *t2, double *th1, doub
              cudaStream_t st);
 // t2_new = (R + Rp + Rp^T) / D2, returns into t2_new; also writes the per-block
 // partial sums of |t2_new - t2_old|^2 into `partials` (length >= grid).
+// Gaussian integrals of a basis (gto_ints.cu); device_out: S/T/V/eri are device pointers
+void ao_integrals(const ::ccsd_basis &bs, double *S, double *T, double *V, double *eri, double *e_nuc,
+                  bool device_out, cudaStream_t st);
 // R[i][j][a][b] = R[j][i][b][a] = their mean (o o v v, in place)
 void k_pair_mean(int o, int v, double *R, cudaStream_t st);
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,

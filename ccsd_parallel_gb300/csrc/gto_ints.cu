@@ -320,6 +320,8 @@ void set_constants() {
     done = true;
 }
 
+}  // namespace
+
 void ao_integrals(const ccsd_basis &bs, double *S, double *T, double *V, double *eri, double *e_nuc,
                   bool device_out, cudaStream_t st) {
     const int n = bs.nbf, na = bs.natoms, mp = bs.maxprim;
@@ -419,7 +421,6 @@ void ao_integrals(const ccsd_basis &bs, double *S, double *T, double *V, double 
     CCSD_CUDA(cudaStreamSynchronize(st));
 }
 
-}  // namespace
 }  // namespace ccsd
 
 extern "C" int ccsd_ao_integrals(const ccsd_basis *basis, double *S, double *T, double *V, double *eri,

@@ -1,0 +1,273 @@
+// Closed-shell Hartree-Fock (the reference's Hartree_Fock_Solver::get_Energy with
+// do_uhf = 0, hartree_fock_solver.cpp:578-1229): the producer of the CCSD inputs.
+//
+// The integrals come from the GPU engine (ao_integrals) and stay on the device;
+// each iteration's two O(n^4) contractions run there as matrix-vector products
+// over views of the ERI tensor:
+//   J[i][j] = sum_kl (ij|kl) P[l][k],   K[i][j] = sum_kl (il|kj) P[l][k]
+//   F = h + J - K / 2                   (Make_Fock_Matrix, :490-569)
+// The n x n algebra stays on the host in FP64, step for step as the reference:
+//   - canonical orthogonalisation X = U diag(lambda^-1/2) from S (:686-690);
+//   - P = 0 at the start, so the first F is h;
+//   - DIIS over the last 3 Fock matrices with error F P S - S P F, from the second
+//     Fock matrix on, extrapolating once 4 have been seen (DIIS, :1252-1311);
+//   - eigenpairs of X^T F X ascending, C = X W, each column scaled to
+//     c^T S c = 1 (Normalize, :1230-1245), P = 2 C_occ C_occ^T (Calc_Density);
+//   - stop when |sum of occupied eps - previous sum| < tol or after 300 steps;
+//   - E_HF = sum h*P + 1/2 sum F_prev*P - 1/2 sum h*P + E_nuc (Calc_Energy,
+//     :482-488), F_prev the Fock matrix before DIIS and before the last step.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ccsd_gb300.h"
+#include "common.h"
+
+namespace ccsd {
+void set_last_error(const std::string &msg);
+
+namespace {
+
+using Mat = std::vector<double>;  // row-major n x n
+
+// Eigenpairs of a symmetric matrix by cyclic Jacobi rotations (the rotation that
+// zeroes a[p][q], applied to rows/columns p, q and accumulated into V), sorted
+// ascending; V holds the eigenvectors as columns.
+void jacobi_eigh(int n, Mat a, std::vector<double> &w, Mat &V) {
+    V.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+    auto A = [&](int i, int j) -> double & { return a[(size_t)i * n + j]; };
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int i = 0; i < n; ++i) {
+            diag += A(i, i) * A(i, i);
+            for (int j = i + 1; j < n; ++j) off += A(i, j) * A(i, j);
+        }
+        if (off <= 1e-34 * std::max(diag, 1e-300)) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A(p, q);
+                if (apq == 0.0) continue;
+                const double theta = (A(q, q) - A(p, p)) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {  // columns p, q
+                    const double akp = A(k, p), akq = A(k, q);
+                    A(k, p) = c * akp - s * akq;
+                    A(k, q) = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {  // rows p, q
+                    const double apk = A(p, k), aqk = A(q, k);
+                    A(p, k) = c * apk - s * aqk;
+                    A(q, k) = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+                    V[(size_t)k * n + p] = c * vkp - s * vkq;
+                    V[(size_t)k * n + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A(x, x) < A(y, y); });
+    w.resize(n);
+    Mat Vs((size_t)n * n);
+    for (int c = 0; c < n; ++c) {
+        w[c] = A(ord[c], ord[c]);
+        for (int r = 0; r < n; ++r) Vs[(size_t)r * n + c] = V[(size_t)r * n + ord[c]];
+    }
+    V.swap(Vs);
+}
+
+Mat matmul(int n, const Mat &a, const Mat &b, bool ta = false) {
+    Mat c((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < n; ++k) {
+            const double x = ta ? a[(size_t)k * n + i] : a[(size_t)i * n + k];
+            if (x == 0.0) continue;
+            for (int j = 0; j < n; ++j) c[(size_t)i * n + j] += x * b[(size_t)k * n + j];
+        }
+    return c;
+}
+
+// solve A x = b (m x m) by Gaussian elimination with partial pivoting
+std::vector<double> solve_small(int m, Mat A, std::vector<double> b) {
+    for (int c = 0; c < m; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < m; ++r)
+            if (std::fabs(A[(size_t)r * m + c]) > std::fabs(A[(size_t)piv * m + c])) piv = r;
+        if (A[(size_t)piv * m + c] == 0.0) throw Error(CCSD_ERR_DIVERGED, "RHF: singular DIIS system");
+        if (piv != c) {
+            for (int k = 0; k < m; ++k) std::swap(A[(size_t)c * m + k], A[(size_t)piv * m + k]);
+            std::swap(b[c], b[piv]);
+        }
+        for (int r = c + 1; r < m; ++r) {
+            const double f = A[(size_t)r * m + c] / A[(size_t)c * m + c];
+            for (int k = c; k < m; ++k) A[(size_t)r * m + k] -= f * A[(size_t)c * m + k];
+            b[r] -= f * b[c];
+        }
+    }
+    std::vector<double> x(m);
+    for (int r = m - 1; r >= 0; --r) {
+        double s = b[r];
+        for (int k = r + 1; k < m; ++k) s -= A[(size_t)r * m + k] * x[k];
+        x[r] = s / A[(size_t)r * m + r];
+    }
+    return x;
+}
+
+struct Dev {
+    double *p = nullptr;
+    ~Dev() {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t n) { CCSD_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
+};
+
+void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_result &res, cudaStream_t st) {
+    const int n = bs.nbf;
+    if (nelec <= 0 || nelec % 2 || nelec / 2 > n)
+        throw Error(CCSD_ERR_INVALID_ARG, "RHF: n_electrons must be even, positive and at most 2 nbf");
+    const int nocc = nelec / 2;
+    const size_t nn = (size_t)n * n;
+    Mat S(nn), T(nn), Vn(nn);
+    Dev eri, P_d, G_d, ws;
+    eri.alloc(nn * nn);
+    double e_nuc = 0.0;
+    ao_integrals(bs, S.data(), T.data(), Vn.data(), nullptr, &e_nuc, false, st);
+    ao_integrals(bs, nullptr, nullptr, nullptr, eri.p, nullptr, true, st);
+    Mat h(nn);
+    for (size_t k = 0; k < nn; ++k) h[k] = T[k] + Vn[k];
+    P_d.alloc(nn);
+    G_d.alloc(nn);
+    const int M = (int)nn;
+    const size_t ws_n = std::max(gemm_f64_ws_elems(M, 1, M), (size_t)1);
+    ws.alloc(ws_n);
+
+    // X = U diag(lambda^-1/2)
+    std::vector<double> lam;
+    Mat U, X(nn);
+    jacobi_eigh(n, S, lam, U);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) X[(size_t)i * n + j] = U[(size_t)i * n + j] / std::sqrt(lam[j]);
+
+    Mat P(nn, 0.0), F(nn), Fprev(nn), C(nn);
+    std::vector<double> eps;
+    std::vector<Mat> errs, focks;
+    const int ndiis = 3;
+    double hf_new = 0.0, hf_old = 0.0;
+    int step = 0;
+    const int limit = max_iter > 0 ? max_iter : 300;
+    bool converged = false;
+    while (true) {
+        hf_old = hf_new;
+        // F = h + J - K/2 on the device
+        CCSD_CUDA(cudaMemcpyAsync(P_d.p, P.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+        const int64_t N = n, N2 = N * N, N3 = N2 * N;
+        MatView Pv{P_d.p, ix1(0), ix1(1)};
+        OutView Gv{G_d.p, ix1(1), ix1(0)};
+        gemm_f64(M, 1, M, 1.0, MatView{eri.p, ix1(N2), ix1(1)}, Pv, 0.0, Gv, ws.p, ws_n, st);
+        gemm_f64(M, 1, M, -0.5, MatView{eri.p, ix2((uint32_t)n, N3, 1), ix2((uint32_t)n, N2, N)}, Pv, 1.0, Gv, ws.p,
+                 ws_n, st);
+        CCSD_CUDA(cudaMemcpyAsync(F.data(), G_d.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, st));
+        CCSD_CUDA(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < nn; ++k) F[k] += h[k];
+        Fprev = F;
+        // DIIS (the reference's, with 3 vectors)
+        if (step > 0) {
+            Mat e = matmul(n, matmul(n, F, P), S);
+            const Mat SPF = matmul(n, S, matmul(n, P, F));
+            for (size_t k = 0; k < nn; ++k) e[k] -= SPF[k];
+            errs.push_back(e);
+            focks.push_back(F);
+            if (step > ndiis) {
+                errs.erase(errs.begin());
+                focks.erase(focks.begin());
+                Mat B((size_t)(ndiis + 1) * (ndiis + 1), 0.0);
+                for (int i = 0; i < ndiis; ++i) {
+                    for (int j = 0; j < ndiis; ++j) {
+                        double tr = 0.0;
+                        for (size_t k = 0; k < nn; ++k) tr += errs[i][k] * errs[j][k];
+                        B[(size_t)i * (ndiis + 1) + j] = tr;
+                    }
+                    B[(size_t)i * (ndiis + 1) + ndiis] = B[(size_t)ndiis * (ndiis + 1) + i] = -1.0;
+                }
+                std::vector<double> z(ndiis + 1, 0.0);
+                z[ndiis] = -1.0;
+                const std::vector<double> c = solve_small(ndiis + 1, B, z);
+                for (size_t k = 0; k < nn; ++k) {
+                    double f = 0.0;
+                    for (int i = 0; i < ndiis; ++i) f += c[i] * focks[i][k];
+                    F[k] = f;
+                }
+            }
+        }
+        // X^T F X, eigenpairs, C = X W with c^T S c = 1
+        const Mat Fo = matmul(n, X, matmul(n, F, X), true);
+        Mat W;
+        jacobi_eigh(n, Fo, eps, W);
+        C = matmul(n, X, W);
+        for (int c = 0; c < n; ++c) {
+            double s = 0.0;
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) s += C[(size_t)i * n + c] * S[(size_t)i * n + j] * C[(size_t)j * n + c];
+            const double f = 1.0 / std::sqrt(s);
+            for (int i = 0; i < n; ++i) C[(size_t)i * n + c] *= f;
+        }
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < nocc; ++k) s += 2.0 * C[(size_t)i * n + k] * C[(size_t)j * n + k];
+                P[(size_t)i * n + j] = s;
+            }
+        hf_new = 0.0;
+        for (int i = 0; i < nocc; ++i) hf_new += eps[i];
+        ++step;
+        if (!std::isfinite(hf_new)) throw Error(CCSD_ERR_DIVERGED, "RHF diverged (NaN/Inf)");
+        if (std::fabs(hf_new - hf_old) < tol) {
+            converged = true;
+            break;
+        }
+        if (step > limit) break;
+    }
+    double e1 = 0.0, e2 = 0.0;
+    for (size_t k = 0; k < nn; ++k) {
+        e1 += h[k] * P[k];
+        e2 += Fprev[k] * P[k];
+    }
+    res.e_hf = e1 + 0.5 * e2 - 0.5 * e1 + e_nuc;
+    res.e_nuc = e_nuc;
+    res.iterations = step;
+    res.converged = converged ? 1 : 0;
+    if (res.eps) std::memcpy(res.eps, eps.data(), sizeof(double) * n);
+    if (res.C) std::memcpy(res.C, C.data(), sizeof(double) * nn);
+    if (res.eri) CCSD_CUDA(cudaMemcpy(res.eri, eri.p, sizeof(double) * nn * nn, cudaMemcpyDeviceToHost));
+}
+
+}  // namespace
+}  // namespace ccsd
+
+extern "C" int ccsd_rhf(const ccsd_basis *basis, int32_t n_electrons, double tol, int32_t max_iter,
+                        ccsd_scf_result *res) {
+    try {
+        ccsd::set_last_error("");
+        if (!basis || !res) throw ccsd::Error(CCSD_ERR_INVALID_ARG, "ccsd_rhf: basis or result is NULL");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw ccsd::Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
+        }
+        cudaStream_t st = (cudaStream_t)res->stream;
+        ccsd::rhf(*basis, n_electrons, tol > 0.0 ? tol : 1e-10, max_iter, *res, st);
+        return CCSD_OK;
+    } catch (const ccsd::Error &e) {
+        ccsd::set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        ccsd::set_last_error(e.what());
+        return CCSD_ERR_CUDA;
+    }
+}

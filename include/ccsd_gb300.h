@@ -289,6 +289,27 @@ typedef struct ccsd_basis {
 int ccsd_ao_integrals(const ccsd_basis *basis, double *S, double *T, double *V, double *eri, double *e_nuc,
                       int32_t device_outputs, void *stream);
 
+typedef struct ccsd_scf_result {
+    double e_hf;            /* out: E_HF with E_nuc (what get_Energy returns)   */
+    double e_nuc;           /* out: nuclear repulsion                           */
+    int32_t iterations;     /* out: SCF steps (the reference's steppp)          */
+    int32_t converged;      /* out: 1 when the stopping rule was met            */
+    double *eps;            /* optional out: nbf orbital energies, ascending    */
+    double *C;              /* optional out: nbf x nbf MO coefficients C[mu][p] */
+    double *eri;            /* optional out: nbf^4 AO integrals (mu nu|la si)   */
+    void *stream;           /* in: cudaStream_t, or NULL                        */
+} ccsd_scf_result;
+
+/* Closed-shell Hartree-Fock on the GPU integrals, step for step as
+ * Hartree_Fock_Solver::get_Energy(toler, 0) (hartree_fock_solver.cpp:578-1229):
+ * canonical orthogonalisation, zero-density start, DIIS over 3 Fock matrices,
+ * stop when the sum of occupied orbital energies moves by less than tol
+ * (0: 1e-10) or after max_iter (0: the reference's 300) steps.  J and K are
+ * contractions over the device-resident ERI tensor; the n x n algebra runs on
+ * the host in FP64.  Its eps, C and eri are the CCSD inputs (ccsd_problem with
+ * CCSD_INTS_AO_DENSE and fock = diag(eps)). */
+int ccsd_rhf(const ccsd_basis *basis, int32_t n_electrons, double tol, int32_t max_iter, ccsd_scf_result *res);
+
 /* One contraction on the engine's kernels, for row-major FP64 device matrices:
  *   C[M][N] = alpha * A[M][K] * B[N][K]^T + beta * C     (leading dims lda/ldb/ldc)
  * precision CCSD_PREC_FP64 runs the DFMA kernel, CCSD_PREC_SPLIT* the

@@ -8,7 +8,8 @@ Each tests/golden/ints_<name>.npz holds:
   - S, lap (<mu|nabla^2|nu>) and nuc (sum_C Z_C <mu|1/r_C|nu>) as the reference returns them;
   - the AO integrals (mu nu|la si): the whole tensor ("eri") up to 13 functions, else
     the values at a seeded sample of unique quartets ("eri_idx" [k, 4], "eri_val" [k]);
-  - E_nuc, E_HF, the orbital energies eps and C[mu][p] of its SCF.
+  - E_nuc, E_HF, the orbital energies eps and C[mu][p] of its SCF (run to
+    tolerance 10^log10_tol).
 
     python tests/golden/make_ints_golden.py      # needs the reference sources
 """
@@ -94,6 +95,7 @@ def main():
                 d["eri_idx"] = q[sel]
                 d["eri_val"] = G[tuple(q[sel].T)]
             d["basis_name"] = np.array(basis)
+            d["log10_tol"] = np.array(tol)
             np.savez_compressed(HERE / f"ints_{name}.npz", **d)
             print(f"ints_{name}.npz: nbf {n}, E_HF {d['e_hf']:.12f}")
 
