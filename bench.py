@@ -41,6 +41,9 @@ SLICES_PLANES = {"split2": 2, "split3": 3, "split4": 4}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--only", default="", choices=["", "scf"],
+                    help="scf: only the integrals + RHF measurement (a water cluster), one JSON line")
+    ap.add_argument("--waters", type=int, default=6, help="cluster size for --only scf")
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -329,6 +332,68 @@ def measure_ccsdt1a(cg, precision, pk):
     return out
 
 
+def water_cluster(d, k: int, spacing: float = 5.6) -> dict:
+    """k copies of a one-water basis description (the reference's own exponents and
+    normalised coefficients, tests/golden/ints_*.npz) on a cubic grid of the given
+    spacing (bohr)."""
+    side = int(np.ceil(k ** (1.0 / 3.0) - 1e-9))
+    shifts = [np.array([x, y, z]) * spacing for x in range(side) for y in range(side) for z in range(side)][:k]
+    na = len(d["Z"])
+    return dict(Z=np.tile(d["Z"], k), R=np.concatenate([d["R"] + s for s in shifts]),
+                atom=np.concatenate([d["atom"] + na * w for w in range(k)]), powers=np.tile(d["powers"], (k, 1)),
+                nprim=np.tile(d["nprim"], k), alpha=np.tile(d["alpha"], (k, 1)), coef=np.tile(d["coef"], (k, 1)))
+
+
+def measure_scf(cg, k: int = 6) -> dict:
+    """The CCSD inputs' producer on a water cluster in cc-pVDZ (the reference's H2O
+    basis description tiled k times): the GPU integrals alone (device outputs; unique
+    quartets (ij|kl), ij >= kl, and their primitive quartets per second), the whole
+    RHF, and the integral oracle's quartet rate on the host for comparison."""
+    import ctypes as C
+    import torch
+    from ccsd_parallel_gb300 import _abi
+    from oracle.gto_ints import Basis, Integrals
+    d = np.load(Path(__file__).parent / "tests" / "golden" / "ints_h2o_ccpvdz.npz")
+    bas = water_cluster(d, k)
+    n = len(bas["atom"])
+    pp = np.array([bas["nprim"][i] * bas["nprim"][j] for i in range(n) for j in range(i + 1)], dtype=np.float64)
+    npair = len(pp)
+    quartets = npair * (npair + 1) // 2
+    prim_quartets = (pp.sum() ** 2 + (pp ** 2).sum()) / 2
+    b, keep = cg._basis(bas)
+    G = torch.empty(n ** 4, dtype=torch.float64, device="cuda")
+    S = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    e_nuc = C.c_double()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _abi.check(_abi.lib().ccsd_ao_integrals(C.byref(b), S.data_ptr(), None, None, G.data_ptr(), C.byref(e_nuc),
+                                                1, None))
+        times.append(time.perf_counter() - t0)
+    t_int = float(np.median(times))
+    del G, S
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    scf = cg.rhf(bas, 10 * k, tol=1e-10, eri=False)
+    t_scf = time.perf_counter() - t0
+    # the oracle on a few quartets of the same basis
+    I = Integrals(Basis.from_dict(bas))
+    rng = np.random.default_rng(0)
+    sample = rng.integers(0, n, size=(12, 4))
+    t0 = time.perf_counter()
+    for q in sample:
+        I.eri(*map(int, q))
+    cpu_q_per_s = len(sample) / (time.perf_counter() - t0)
+    return dict(workload=f"(H2O)_{k} cc-pVDZ, {n} Cartesian basis functions, grid spacing 5.6 bohr",
+                nbf=n, unique_quartets=quartets, primitive_quartets=prim_quartets,
+                integrals_s=t_int, quartets_per_s=quartets / t_int, primitive_quartets_per_s=prim_quartets / t_int,
+                eri_gb=n ** 4 * 8 / 1e9,
+                rhf_s=t_scf, rhf_iterations=scf["iterations"], e_hf=scf["e_hf"],
+                cpu_port_quartets_per_s=cpu_q_per_s,
+                cpu_port_note="the numpy integral oracle (oracle/gto_ints.py), one thread, on 12 sampled quartets")
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -336,6 +401,10 @@ def main():
         run_reference(args, rank, world)
         return
     import ccsd_parallel_gb300 as cg
+    if args.only == "scf":
+        if rank == 0:
+            print(json.dumps(measure_scf(cg, args.waters)), flush=True)
+        return
     o, v, q = args.nocc, args.nvir, args.naux
     W, K = max(args.warmup, 3), args.steps
     U = W + K
@@ -402,6 +471,7 @@ def main():
     if args.extras and rank == 0:
         extras = measure_extras(cg, fock, df, o, args.precision)
         extras["ccsdt1a"] = measure_ccsdt1a(cg, args.precision, pk)
+        extras["scf"] = measure_scf(cg)
 
     if rank != 0:
         return
