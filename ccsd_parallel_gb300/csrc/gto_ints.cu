@@ -16,6 +16,7 @@
 //     in a local buffer, and the E (-1)^{t'+u'+v'} E R contraction (:720-796); the
 //     value lands in its 8 symmetric places.
 // FP64 throughout: the outputs feed an FP64 SCF and CCSD.
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -41,6 +42,11 @@ __constant__ double c_inv_series[100];    // 1 / (2 kBoysN + 1 + 2 j)
 __constant__ double c_inv_odd[kBoysN + 1];  // 1 / (2 i - 1)
 __constant__ double c_boys_start;         // (2 kBoysN - 1)!! / 2^(kBoysN + 1), as Set_Boys_Start
 
+// F_m(x_k) for x_k = k h, k <= kTabN - 1 (x <= 50), m < kTabM, from the series below
+constexpr int kTabN = 1001, kTabM = 4 * kLMax + 7;
+constexpr double kTabH = 0.05;
+__constant__ const double *c_boys_tab;
+
 __device__ __forceinline__ int tri_row(long long q) {
     // largest r with r (r + 1) / 2 <= q
     long long r = (long long)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
@@ -56,6 +62,22 @@ __device__ __forceinline__ int tri_row(long long q) {
 // by 1.2e-3 (relative), 1e-5 at 60, 1e-11 at 80, and x^61 overflows to F = 0 above
 // x = 1.1e5.  accurate = true takes x > 50 from F_0 = sqrt(pi/x)/2 upward instead
 // (F_{n+1} = (2n+1)/(2x) F_n, accurate to e^{-x}).
+//
+// Below x = 50 the values come from a table of the same series on a grid of step
+// h = 0.05: F_nmax(x) = sum_{j<7} F_{nmax+j}(x_k) (x_k - x)^j / j! about the nearest
+// x_k (truncation below (h/2)^7/7! = 1.2e-15 relative), then the same downward
+// recursion.  The table is built once by the series (boys_table_kernel).
+__device__ double boys_series30(double x, double ex) {
+    double term = c_inv_series[0], sum = term;
+    const double tx = 2.0 * x;
+    for (int j = 1; j < 100; ++j) {
+        term *= tx * c_inv_series[j];
+        sum += term;
+        if (term < 1e-17 * sum) break;
+    }
+    return sum * ex;
+}
+
 __device__ void boys(int nmax, double x, double *F, bool accurate) {
     if (x > 50.0 && accurate) {
         F[0] = 0.5 * sqrt(M_PI / x);
@@ -64,18 +86,26 @@ __device__ void boys(int nmax, double x, double *F, bool accurate) {
         return;
     }
     const double ex = exp(-x);
+    if (x <= 50.0 && c_boys_tab && nmax + 6 < kTabM) {
+        const int k = (int)(x * (1.0 / kTabH) + 0.5);
+        const double d = k * kTabH - x;  // x_k - x
+        const double *T = c_boys_tab + (size_t)k * kTabM + nmax;
+        double f = T[6];
+        f = T[5] + f * d * (1.0 / 6.0);
+        f = T[4] + f * d * (1.0 / 5.0);
+        f = T[3] + f * d * (1.0 / 4.0);
+        f = T[2] + f * d * (1.0 / 3.0);
+        f = T[1] + f * d * (1.0 / 2.0);
+        f = T[0] + f * d;
+        F[nmax] = f;
+        for (int i = nmax; i > 0; --i) F[i - 1] = (2.0 * x * F[i] + ex) * c_inv_odd[i];
+        return;
+    }
     double f;
     if (x > 50.0) {
         f = c_boys_start * sqrt(M_PI / pow(x, 2.0 * kBoysN + 1.0));
     } else {
-        double term = c_inv_series[0], sum = term;
-        const double tx = 2.0 * x;
-        for (int j = 1; j < 100; ++j) {
-            term *= tx * c_inv_series[j];
-            sum += term;
-            if (term < 1e-17 * sum) break;
-        }
-        f = sum * ex;
+        f = boys_series30(x, ex);
     }
     for (int i = kBoysN; i > 0; --i) {
         if (i <= nmax) F[i] = f;
@@ -147,6 +177,18 @@ __device__ void hermite_R(double alpha, double X, double Y, double Zc, int T, in
         cu = tmp;
     }
     for (int i = 0; i < (T + 1) * st; ++i) R[i] = nx[i];
+}
+
+__global__ void boys_table_kernel(double *tab) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kTabN) return;
+    const double x = k * kTabH, ex = exp(-x);
+    double f = boys_series30(x, ex);
+    for (int i = kBoysN; i > 0; --i) {
+        if (i < kTabM) tab[(size_t)k * kTabM + i] = f;
+        f = (2.0 * x * f + ex) * c_inv_odd[i];
+    }
+    tab[(size_t)k * kTabM] = f;
 }
 
 struct BasisDev {
@@ -231,14 +273,17 @@ __global__ void one_electron_kernel(BasisDev b, double *S, double *lap, double *
     }
 }
 
-// (ij|kl) for each unique quartet, pair(ij) >= pair(kl); RB bounds (Tx+1)(Uy+1)(Wz+1)
+// (ij|kl) for each unique quartet: q enumerates (a >= b) over the function pairs in
+// `order` (sorted by angular momentum and primitive count, so that the threads of a
+// warp do alike work); RB bounds (Tx+1)(Uy+1)(Wz+1)
 template <int RB>
 __global__ void __launch_bounds__(128) eri_kernel(int n, long long nquart, const int *pw, const long long *pp_off,
-                                                  const PrimPair *pp, double *eri, bool accurate) {
+                                                  const PrimPair *pp, const int *order, double *eri, bool accurate) {
     const double pref = 2.0 * pow(M_PI, 2.5);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nquart;
          q += (long long)gridDim.x * blockDim.x) {
-        const int P1 = tri_row(q), P2 = (int)(q - (long long)P1 * (P1 + 1) / 2);
+        const int a = tri_row(q), b = (int)(q - (long long)a * (a + 1) / 2);
+        const int P1 = order[a], P2 = order[b];
         const int i = tri_row(P1), j = P1 - i * (i + 1) / 2;
         const int k = tri_row(P2), l = P2 - k * (k + 1) / 2;
         int Lb[3], Lk[3];
@@ -317,6 +362,16 @@ void set_constants() {
     CCSD_CUDA(cudaMemcpyToSymbol(c_inv_series, inv_series, sizeof inv_series));
     CCSD_CUDA(cudaMemcpyToSymbol(c_inv_odd, inv_odd, sizeof inv_odd));
     CCSD_CUDA(cudaMemcpyToSymbol(c_boys_start, &start, sizeof start));
+    // the Boys table, built once per process by the series (it lives as long as the process)
+    double *tab = nullptr;
+    CCSD_CUDA(cudaMalloc(&tab, sizeof(double) * kTabN * kTabM));
+    const double *null_tab = nullptr;
+    CCSD_CUDA(cudaMemcpyToSymbol(c_boys_tab, &null_tab, sizeof null_tab));
+    boys_table_kernel<<<(kTabN + 127) / 128, 128>>>(tab);
+    CCSD_LAUNCH_CHECK();
+    CCSD_CUDA(cudaDeviceSynchronize());
+    const double *ctab = tab;
+    CCSD_CUDA(cudaMemcpyToSymbol(c_boys_tab, &ctab, sizeof ctab));
     done = true;
 }
 
@@ -358,7 +413,7 @@ void ao_integrals(const ccsd_basis &bs, double *S, double *T, double *V, double 
         *e_nuc = e;
     }
     set_constants();
-    DevBuf d_atom, d_pw, d_np, d_al, d_co, d_R, d_Z, d_off, d_pp, d_S, d_L, d_N, d_eri;
+    DevBuf d_atom, d_pw, d_np, d_al, d_co, d_R, d_Z, d_off, d_pp, d_S, d_L, d_N, d_eri, d_ord;
     int *atom = d_atom.alloc<int>(n), *pw = d_pw.alloc<int>(3 * n), *np_ = d_np.alloc<int>(n);
     double *al = d_al.alloc<double>((size_t)n * mp), *co = d_co.alloc<double>((size_t)n * mp);
     double *R = d_R.alloc<double>(3 * na), *Z = d_Z.alloc<double>(na);
@@ -400,15 +455,27 @@ void ao_integrals(const ccsd_basis &bs, double *S, double *T, double *V, double 
     }
     if (eri) {
         const long long np = npair, nquart = np * (np + 1) / 2;
+        // pairs by (l_i + l_j, primitive pairs): neighbouring quartets then cost alike
+        std::vector<int> ord(npair), key(npair);
+        for (int i = 0, P = 0; i < n; ++i)
+            for (int j = 0; j <= i; ++j, ++P) {
+                const int L = bs.powers[3 * i] + bs.powers[3 * i + 1] + bs.powers[3 * i + 2] + bs.powers[3 * j] +
+                              bs.powers[3 * j + 1] + bs.powers[3 * j + 2];
+                key[P] = L * 100000 + bs.nprim[i] * bs.nprim[j];
+                ord[P] = P;
+            }
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key[x] < key[y]; });
+        int *dord = d_ord.alloc<int>(npair);
+        up(dord, ord.data(), sizeof(int) * npair);
         double *dE = device_out ? eri : d_eri.alloc<double>(nn * nn);
         const int L = 4 * lmax;
         const int blocks = (int)std::min<long long>((nquart + 127) / 128, 152LL * 64);
         if (L <= 4)
-            eri_kernel<12><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dE, accurate);
+            eri_kernel<12><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dord, dE, accurate);
         else if (L <= 8)
-            eri_kernel<48><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dE, accurate);
+            eri_kernel<48><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dord, dE, accurate);
         else
-            eri_kernel<125><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dE, accurate);
+            eri_kernel<125><<<blocks, 128, 0, st>>>(n, nquart, pw, poff, pp, dord, dE, accurate);
         CCSD_LAUNCH_CHECK();
         if (!device_out)
             CCSD_CUDA(cudaMemcpyAsync(eri, dE, sizeof(double) * nn * nn, cudaMemcpyDeviceToHost, st));
