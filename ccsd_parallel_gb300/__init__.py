@@ -25,7 +25,8 @@ PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD
               "split4": CCSD_PREC_SPLIT4}
 
 __all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "frozen_core_count",
-           "ao_integrals", "rhf", "ccsd_inputs", "CCSD_Memory_optimized", "CCSDError", "PRECISIONS"]
+           "ao_integrals", "rhf", "ccsd_inputs", "parse_incar", "run_incar", "CCSD_Memory_optimized", "CCSDError",
+           "PRECISIONS"]
 
 
 def _ptr(a):
@@ -132,6 +133,37 @@ def rhf(basis, n_electrons: int, tol: float = 1e-10, max_iter: int = 0, eri: boo
     del keep
     return dict(e_hf=r.e_hf, e_nuc=r.e_nuc, iterations=r.iterations, converged=bool(r.converged), eps=eps,
                 C=Cm, eri=G, nocc=n_electrons // 2)
+
+
+def parse_incar(incar_text: str, basis_text: str) -> dict:
+    """The reference's INCAR keywords and atoms with a Gaussian94 basis, expanded to
+    the ccsd_basis arrays (ccsd_incar_parse; host only)."""
+    inc = _abi.Incar()
+    lib = _abi.lib()
+    a, b = incar_text.encode(), basis_text.encode()
+    _abi.check(lib.ccsd_incar_parse(a, b, C.byref(inc)))
+    na, n, mp = inc.natoms, inc.nbf, inc.maxprim
+    out = dict(Z=np.empty(na), R=np.empty((na, 3)), atom=np.empty(n, np.int32), powers=np.empty((n, 3), np.int32),
+               nprim=np.empty(n, np.int32), alpha=np.empty((n, mp)), coef=np.empty((n, mp)))
+    inc.capacity_atoms, inc.capacity_bf, inc.capacity_prim = na, n, mp
+    inc.Z, inc.R, inc.alpha, inc.coef = _ptr(out["Z"]), _ptr(out["R"]), _ptr(out["alpha"]), _ptr(out["coef"])
+    ip = lambda x: x.ctypes.data_as(C.POINTER(C.c_int32))
+    inc.atom, inc.powers, inc.nprim = ip(out["atom"]), ip(out["powers"]), ip(out["nprim"])
+    _abi.check(lib.ccsd_incar_parse(a, b, C.byref(inc)))
+    out.update(basis_set=inc.basis_set.decode(), method=inc.method.decode(), tol=inc.convergance_criteria,
+               freeze_core=bool(inc.freeze_core), relax_pos=bool(inc.relax_pos), use_angstrom=bool(inc.use_angstrom),
+               print_stuffies=bool(inc.print_stuffies), n_electrons=inc.n_electrons, nfrozen=inc.nfrozen)
+    return out
+
+
+def run_incar(incar_text: str, basis_text: str, precision="fp64") -> dict:
+    """The reference's Initializer::Go on the engine (ccsd_incar_run): returns the
+    energy it would print (E_HF for HF, E_HF + E_corr otherwise) and its parts."""
+    r = _abi.IncarResult()
+    prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    _abi.check(_abi.lib().ccsd_incar_run(incar_text.encode(), basis_text.encode(), prec, C.byref(r)))
+    return dict(energy=r.energy, e_hf=r.e_hf, e_corr=r.e_corr, scf_iterations=r.scf_iterations, cc_iter=r.cc_iter,
+                method=r.method, nbf=r.nbf)
 
 
 def ccsd_inputs(scf: dict) -> dict:

@@ -66,6 +66,25 @@ class ScfResult(C.Structure):
     ]
 
 
+class Incar(C.Structure):
+    _fields_ = [
+        ("basis_set", C.c_char * 64), ("method", C.c_char * 32), ("convergance_criteria", C.c_double),
+        ("freeze_core", C.c_int32), ("relax_pos", C.c_int32), ("use_angstrom", C.c_int32),
+        ("print_stuffies", C.c_int32), ("natoms", C.c_int32), ("nbf", C.c_int32), ("maxprim", C.c_int32),
+        ("n_electrons", C.c_int32), ("nfrozen", C.c_int32), ("capacity_atoms", C.c_int32),
+        ("capacity_bf", C.c_int32), ("capacity_prim", C.c_int32), ("Z", _dp), ("R", _dp),
+        ("atom", C.POINTER(C.c_int32)), ("powers", C.POINTER(C.c_int32)), ("nprim", C.POINTER(C.c_int32)),
+        ("alpha", _dp), ("coef", _dp),
+    ]
+
+
+class IncarResult(C.Structure):
+    _fields_ = [
+        ("energy", C.c_double), ("e_hf", C.c_double), ("e_corr", C.c_double), ("scf_iterations", C.c_int32),
+        ("cc_iter", C.c_int32), ("method", C.c_int32), ("nbf", C.c_int32),
+    ]
+
+
 class Options(C.Structure):
     _fields_ = [
         ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
@@ -104,6 +123,8 @@ SIGNATURES = {
     "ccsd_profile_report": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "ccsd_flops_per_update": (C.c_double, [C.c_int32, C.c_int32]),
     "ccsd_frozen_core_count": (C.c_int, [_dp, C.c_int32]),
+    "ccsd_incar_parse": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(Incar)]),
+    "ccsd_incar_run": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.POINTER(IncarResult)]),
     "ccsd_rhf": (C.c_int, [C.POINTER(Basis), C.c_int32, C.c_double, C.c_int32, C.POINTER(ScfResult)]),
     "ccsd_ao_integrals": (C.c_int, [C.POINTER(Basis), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double), C.c_int32, C.c_void_p]),

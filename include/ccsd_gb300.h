@@ -310,6 +310,50 @@ typedef struct ccsd_scf_result {
  * CCSD_INTS_AO_DENSE and fock = diag(eps)). */
 int ccsd_rhf(const ccsd_basis *basis, int32_t n_electrons, double tol, int32_t max_iter, ccsd_scf_result *res);
 
+/* ---- INCAR front end (main.cpp:83-298, initializer.cpp:17-210) ----------- */
+/* The reference's INCAR keywords (Basis_Set, Method, convergance_criteria as
+ * log10, Freeze_Core, Relax_Pos, use_angstrom, print_stuffies) and its atom
+ * lines "<element> x y z" (optionally between "#ATOMS START" and a '#' line),
+ * read line by line: a keyword counts only at the start of a line, a missing
+ * Method or an empty atom list is CCSD_ERR_INVALID_ARG, blanks of any length
+ * separate values.  The basis is Gaussian94 text (S, P, D, F, SP shells per
+ * element), expanded to Cartesian functions in the reference's order with its
+ * primitive normalisation; the reference's own basis tables are not included. */
+typedef struct ccsd_incar {
+    char basis_set[64];            /* out: the Basis_Set value (a name only)      */
+    char method[32];               /* out: the Method value                       */
+    double convergance_criteria;   /* out: 10^value (default 1e-8)                */
+    int32_t freeze_core, relax_pos, use_angstrom, print_stuffies;  /* out: flags */
+    int32_t natoms, nbf, maxprim;  /* out: sizes                                  */
+    int32_t n_electrons;           /* out: sum of the nuclear charges             */
+    int32_t nfrozen;               /* out: ccsd_frozen_core_count when Freeze_Core */
+    int32_t capacity_atoms;        /* in: rows of Z / R (0: sizes only)           */
+    int32_t capacity_bf;           /* in: rows of atom / powers / nprim / alpha / coef */
+    int32_t capacity_prim;         /* in: row length of alpha / coef              */
+    double *Z, *R;                 /* out: [natoms], [natoms][3] in bohr          */
+    int32_t *atom, *powers, *nprim;/* out: the ccsd_basis arrays                  */
+    double *alpha, *coef;          /* out: [nbf][capacity_prim]                   */
+} ccsd_incar;
+
+/* Parse only (no GPU): call once with capacities 0 for the sizes, then with arrays. */
+int ccsd_incar_parse(const char *incar_text, const char *basis_text, ccsd_incar *inc);
+
+typedef struct ccsd_incar_result {
+    double energy;          /* what Initializer::Go returns: E_HF (HF) or E_HF + E_corr */
+    double e_hf, e_corr;
+    int32_t scf_iterations; /* SCF steps                                           */
+    int32_t cc_iter;        /* the reference's counter (updates + 1); 0 for HF     */
+    int32_t method;         /* CCSD_METHOD_* that ran; -1 for HF                   */
+    int32_t nbf;
+} ccsd_incar_result;
+
+/* Initializer::Go on the engine: the molecule and method of incar_text with the
+ * basis of basis_text, n_electrons = sum Z, the SCF and the amplitudes both to
+ * convergance_criteria; HF, CCSD / CCSD1 (one engine), CCSDT-1a ... CCSDT;
+ * Freeze_Core freezes ccsd_frozen_core_count(Z) orbitals; other methods (UHF,
+ * UCCSDT) are CCSD_ERR_UNSUPPORTED.  precision: CCSD_PREC_* of the amplitudes. */
+int ccsd_incar_run(const char *incar_text, const char *basis_text, int32_t precision, ccsd_incar_result *res);
+
 /* One contraction on the engine's kernels, for row-major FP64 device matrices:
  *   C[M][N] = alpha * A[M][K] * B[N][K]^T + beta * C     (leading dims lda/ldb/ldc)
  * precision CCSD_PREC_FP64 runs the DFMA kernel, CCSD_PREC_SPLIT* the

@@ -1,0 +1,60 @@
+"""The INCAR front end's parsing (ccsd_incar_parse, host only): the reference's
+INCAR keywords and atom lines (main.cpp:83-298) and a Gaussian94 basis expanded
+to the arrays the reference's integral engine receives (Cartesian order and
+primitive normalisation of Normalize_small_c), checked against the reference's
+own arrays in tests/golden/ints_*.npz; the reader's hazards fixed."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ccsd_parallel_gb300 as cg
+from ccsd_parallel_gb300 import _abi
+from incar_util import g94_from_fixture, incar_text
+
+GOLD = Path(__file__).parent / "golden"
+CASES = ["h2o_sto3g", "nh3_sto3g", "h2o_631g", "h2o_ccpvdz", "o_ccpvtz"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_basis_expansion_matches_reference(name):
+    d = np.load(GOLD / f"ints_{name}.npz")
+    p = cg.parse_incar(incar_text(d, "CCSD", -10), g94_from_fixture(d))
+    np.testing.assert_array_equal(p["atom"], d["atom"])
+    np.testing.assert_array_equal(p["powers"], d["powers"])
+    np.testing.assert_array_equal(p["nprim"], d["nprim"])
+    mp = p["alpha"].shape[1]
+    np.testing.assert_array_equal(p["alpha"], d["alpha"][:, :mp])
+    np.testing.assert_allclose(p["coef"], d["coef"][:, :mp], rtol=1e-14, atol=0)
+    np.testing.assert_array_equal(p["Z"], d["Z"])
+    np.testing.assert_array_equal(p["R"], d["R"])
+    assert p["n_electrons"] == int(np.sum(d["Z"]))
+    assert p["method"] == "CCSD" and p["tol"] == pytest.approx(1e-10, rel=1e-15)
+
+
+def test_incar_reader_hazards():
+    d = np.load(GOLD / "ints_h2o_sto3g.npz")
+    basis = g94_from_fixture(d)
+    # a keyword inside a comment or another value does not count; blanks of any length
+    text = ("# Method HF would be taken by strstr\nBasis_Set STO-3G\nMethod   CCSDT-1a  \n"
+            "convergance_criteria -9\nFreeze_Core true\nuse_angstrom true\n"
+            "O   0.0   0.0    0.0\nH 0   1.079252   1.474611\nH\t0 1.079252 -1.47611\n")
+    p = cg.parse_incar(text, basis)  # no "#ATOMS START": the atom lines are still read
+    assert p["method"] == "CCSDT-1a" and p["tol"] == pytest.approx(1e-9)
+    assert p["freeze_core"] and p["nfrozen"] == 1  # the O 1s
+    np.testing.assert_allclose(p["R"][1], np.array([0, 1.079252, 1.474611]) * 1.889725989, rtol=1e-15)
+    for bad, code in (("Basis_Set STO-3G\nO 0 0 0\n", _abi.CCSD_ERR_INVALID_ARG),  # no Method
+                      ("Method HF\n", _abi.CCSD_ERR_INVALID_ARG),  # no atoms
+                      ("Method HF\n#ATOMS START\nO 0 0\n#\n", _abi.CCSD_ERR_INVALID_ARG),  # short atom line
+                      ("Method HF\nNe 0 0 0\n", _abi.CCSD_ERR_INVALID_ARG)):  # element missing from the basis
+        with pytest.raises(cg.CCSDError) as ei:
+            cg.parse_incar(bad, basis)
+        assert ei.value.code == code
+
+
+def test_unbuilt_methods_are_refused_before_any_compute():
+    d = np.load(GOLD / "ints_h2o_sto3g.npz")
+    for m in ("UHF", "UCCSDT", "CCSDT--Q"):
+        with pytest.raises(cg.CCSDError) as ei:
+            cg.run_incar(incar_text(d, m, -8), g94_from_fixture(d))
+        assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
