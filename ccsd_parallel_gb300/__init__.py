@@ -25,7 +25,7 @@ PRECISIONS = {"fp64": CCSD_PREC_FP64, "split2": CCSD_PREC_SPLIT2, "split3": CCSD
               "split4": CCSD_PREC_SPLIT4}
 
 __all__ = ["Solver", "solve", "Batch", "solve_batched", "make_synthetic", "flops_per_update", "frozen_core_count",
-           "ao_integrals", "rhf", "ccsd_inputs", "parse_incar", "run_incar", "CCSD_Memory_optimized", "CCSDError",
+           "ao_integrals", "rhf", "uhf", "ccsd_inputs", "parse_incar", "run_incar", "CCSD_Memory_optimized", "CCSDError",
            "PRECISIONS"]
 
 
@@ -164,6 +164,22 @@ def run_incar(incar_text: str, basis_text: str, precision="fp64") -> dict:
     _abi.check(_abi.lib().ccsd_incar_run(incar_text.encode(), basis_text.encode(), prec, C.byref(r)))
     return dict(energy=r.energy, e_hf=r.e_hf, e_corr=r.e_corr, scf_iterations=r.scf_iterations, cc_iter=r.cc_iter,
                 method=r.method, nbf=r.nbf)
+
+
+def uhf(basis, n_up: int, n_down: int, tol: float = 1e-10, max_iter: int = 0, seed: int = 0,
+        accurate_boys: bool = False) -> dict:
+    """Unrestricted Hartree-Fock on the GPU integrals (ccsd_uhf), step for step as the
+    reference's get_Energy(toler, 1), from a seeded random start."""
+    b, keep = _basis(basis, accurate_boys)
+    n = b.nbf
+    r = _abi.UhfResult()
+    out = dict(eps_up=np.empty(n), eps_down=np.empty(n), C_up=np.empty((n, n)), C_down=np.empty((n, n)))
+    r.eps_up, r.eps_down, r.C_up, r.C_down = (_ptr(out[k]) for k in ("eps_up", "eps_down", "C_up", "C_down"))
+    r.seed = seed
+    _abi.check(_abi.lib().ccsd_uhf(C.byref(b), n_up, n_down, tol, max_iter, C.byref(r)))
+    del keep
+    out.update(e_uhf=r.e_uhf, e_nuc=r.e_nuc, iterations=r.iterations, converged=bool(r.converged))
+    return out
 
 
 def ccsd_inputs(scf: dict) -> dict:

@@ -66,6 +66,14 @@ class ScfResult(C.Structure):
     ]
 
 
+class UhfResult(C.Structure):
+    _fields_ = [
+        ("e_uhf", C.c_double), ("e_nuc", C.c_double), ("iterations", C.c_int32), ("converged", C.c_int32),
+        ("eps_up", _dp), ("eps_down", _dp), ("C_up", _dp), ("C_down", _dp), ("seed", C.c_uint64),
+        ("stream", C.c_void_p),
+    ]
+
+
 class Incar(C.Structure):
     _fields_ = [
         ("basis_set", C.c_char * 64), ("method", C.c_char * 32), ("convergance_criteria", C.c_double),
@@ -125,6 +133,7 @@ SIGNATURES = {
     "ccsd_frozen_core_count": (C.c_int, [_dp, C.c_int32]),
     "ccsd_incar_parse": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(Incar)]),
     "ccsd_incar_run": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.POINTER(IncarResult)]),
+    "ccsd_uhf": (C.c_int, [C.POINTER(Basis), C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(UhfResult)]),
     "ccsd_rhf": (C.c_int, [C.POINTER(Basis), C.c_int32, C.c_double, C.c_int32, C.POINTER(ScfResult)]),
     "ccsd_ao_integrals": (C.c_int, [C.POINTER(Basis), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double), C.c_int32, C.c_void_p]),

@@ -1,7 +1,7 @@
 // INCAR front end: the reference's input reader (main.cpp:83-298: find_and_write,
 // find_start_of_atoms, Fill_One_Atom, return_charge) and Initializer::Go's dispatch
-// (initializer.cpp:17-210) onto the engine: HF -> ccsd_rhf; CCSD / CCSD1 -> RHF +
-// ccsd_solve; CCSDT-1a ... CCSDT -> RHF + the triples methods.
+// (initializer.cpp:17-210) onto the engine: HF -> ccsd_rhf; UHF -> ccsd_uhf; CCSD /
+// CCSD1 -> RHF + ccsd_solve; CCSDT-1a ... CCSDT -> RHF + the triples methods.
 //
 // Differences from the reference's reader (its parsing hazards):
 //   - a keyword counts only at the start of a line (the reference takes the first
@@ -272,6 +272,7 @@ void copy_name(char *dst, size_t cap, const std::string &s) {
 
 int method_of(const std::string &m) {
     if (m == "HF") return -1;
+    if (m == "UHF") return -2;
     if (m == "CCSD" || m == "CCSD1") return CCSD_METHOD_CCSD;
     if (m == "CCSDT-1a") return CCSD_METHOD_CCSDT1A;
     if (m == "CCSDT-1b") return CCSD_METHOD_CCSDT1B;
@@ -279,7 +280,7 @@ int method_of(const std::string &m) {
     if (m == "CCSDT-3") return CCSD_METHOD_CCSDT3;
     if (m == "CCSDT-4") return CCSD_METHOD_CCSDT4;
     if (m == "CCSDT") return CCSD_METHOD_CCSDT;
-    throw Error(CCSD_ERR_UNSUPPORTED, "Method '" + m + "' is not built (HF, CCSD, CCSD1, CCSDT-1a ... CCSDT are)");
+    throw Error(CCSD_ERR_UNSUPPORTED, "Method '" + m + "' is not built (HF, UHF, CCSD, CCSD1, CCSDT-1a ... CCSDT are)");
 }
 
 }  // namespace
@@ -354,6 +355,23 @@ extern "C" int ccsd_incar_run(const char *incar_text, const char *basis_text, in
         for (double z : p.Z) ne += (int)z;
         const int n = b.nbf;
         res->nbf = n;
+        if (method == -2) {  // UHF as Initializer::Go (initializer.cpp:163-185)
+            const int half = ne / 2;
+            ccsd_uhf_result u{};
+            int rc = CCSD_OK;
+            if (ne % 2) {
+                rc = ccsd_uhf(&b, half + 1, half, p.tol, 0, &u);
+            } else {
+                rc = ccsd_uhf(&b, half, half, p.tol, 0, &u);  // the singlet, which Go prints
+                if (rc == CCSD_OK && p.print) std::printf("Energy = %.12f (UHF singlet)\n", u.e_uhf);
+                if (rc == CCSD_OK) rc = ccsd_uhf(&b, half + 1, half - 1, p.tol, 0, &u);
+            }
+            if (rc != CCSD_OK) return rc;
+            res->e_hf = res->energy = u.e_uhf;
+            res->scf_iterations = u.iterations;
+            if (p.print) std::printf("Energy = %.12f (UHF)\n", u.e_uhf);
+            return CCSD_OK;
+        }
         std::vector<double> eps(n), C((size_t)n * n), eri(method >= 0 ? (size_t)n * n * n * n : 0);
         ccsd_scf_result scf{};
         scf.eps = eps.data();

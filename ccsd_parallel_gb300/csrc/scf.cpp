@@ -127,32 +127,90 @@ struct Dev {
     void alloc(size_t n) { CCSD_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
 };
 
+// What both SCF forms share: S, h = T + V and X = U diag(lambda^-1/2) on the host,
+// the ERI tensor on the device, and the device contractions
+//   G = aj J(Pj) + ak K(Pk),  J[i][j] = sum_kl (ij|kl) P[k][l],  K[i][j] = sum_kl (il|kj) P[l][k]
+struct ScfSystem {
+    int n;
+    size_t nn;
+    Mat S, h, X;
+    double e_nuc = 0.0;
+    Dev eri, P_d, G_d, ws;
+    size_t ws_n = 1;
+    cudaStream_t st;
+
+    ScfSystem(const ccsd_basis &bs, cudaStream_t s) : n(bs.nbf), nn((size_t)bs.nbf * bs.nbf), st(s) {
+        S.resize(nn);
+        Mat T(nn), Vn(nn);
+        eri.alloc(nn * nn);
+        ao_integrals(bs, S.data(), T.data(), Vn.data(), nullptr, &e_nuc, false, st);
+        ao_integrals(bs, nullptr, nullptr, nullptr, eri.p, nullptr, true, st);
+        h.resize(nn);
+        for (size_t k = 0; k < nn; ++k) h[k] = T[k] + Vn[k];
+        P_d.alloc(2 * nn);
+        G_d.alloc(nn);
+        ws_n = std::max(gemm_f64_ws_elems((int)nn, 1, (int)nn), (size_t)1);
+        ws.alloc(ws_n);
+        std::vector<double> lam;
+        Mat U;
+        jacobi_eigh(n, S, lam, U);
+        X.resize(nn);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) X[(size_t)i * n + j] = U[(size_t)i * n + j] / std::sqrt(lam[j]);
+    }
+
+    void two_electron(const Mat &Pj, double aj, const Mat &Pk, double ak, Mat &G) {
+        const int M = (int)nn;
+        const int64_t N = n, N2 = N * N, N3 = N2 * N;
+        CCSD_CUDA(cudaMemcpyAsync(P_d.p, Pj.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+        CCSD_CUDA(cudaMemcpyAsync(P_d.p + nn, Pk.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+        const OutView Gv{G_d.p, ix1(1), ix1(0)};
+        gemm_f64(M, 1, M, aj, MatView{eri.p, ix1(N2), ix1(1)}, MatView{P_d.p, ix1(0), ix1(1)}, 0.0, Gv, ws.p,
+                 ws_n, st);
+        gemm_f64(M, 1, M, ak, MatView{eri.p, ix2((uint32_t)n, N3, 1), ix2((uint32_t)n, N2, N)},
+                 MatView{P_d.p + nn, ix1(0), ix1(1)}, 1.0, Gv, ws.p, ws_n, st);
+        G.resize(nn);
+        CCSD_CUDA(cudaMemcpyAsync(G.data(), G_d.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, st));
+        CCSD_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // eigenpairs of X^T F X ascending, C = X W with every column at c^T S c = 1 (Normalize)
+    void orbitals(const Mat &F, std::vector<double> &eps, Mat &C) const {
+        const Mat Fo = matmul(n, X, matmul(n, F, X), true);
+        Mat W;
+        jacobi_eigh(n, Fo, eps, W);
+        C = matmul(n, X, W);
+        for (int c = 0; c < n; ++c) {
+            double s = 0.0;
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) s += C[(size_t)i * n + c] * S[(size_t)i * n + j] * C[(size_t)j * n + c];
+            const double f = 1.0 / std::sqrt(s);
+            for (int i = 0; i < n; ++i) C[(size_t)i * n + c] *= f;
+        }
+    }
+
+    // P = w C_occ C_occ^T over the first k columns
+    Mat density(const Mat &C, int k, double w) const {
+        Mat P(nn);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                double s = 0.0;
+                for (int c = 0; c < k; ++c) s += C[(size_t)i * n + c] * C[(size_t)j * n + c];
+                P[(size_t)i * n + j] = w * s;
+            }
+        return P;
+    }
+};
+
 void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_result &res, cudaStream_t st) {
     const int n = bs.nbf;
     if (nelec <= 0 || nelec % 2 || nelec / 2 > n)
         throw Error(CCSD_ERR_INVALID_ARG, "RHF: n_electrons must be even, positive and at most 2 nbf");
     const int nocc = nelec / 2;
     const size_t nn = (size_t)n * n;
-    Mat S(nn), T(nn), Vn(nn);
-    Dev eri, P_d, G_d, ws;
-    eri.alloc(nn * nn);
-    double e_nuc = 0.0;
-    ao_integrals(bs, S.data(), T.data(), Vn.data(), nullptr, &e_nuc, false, st);
-    ao_integrals(bs, nullptr, nullptr, nullptr, eri.p, nullptr, true, st);
-    Mat h(nn);
-    for (size_t k = 0; k < nn; ++k) h[k] = T[k] + Vn[k];
-    P_d.alloc(nn);
-    G_d.alloc(nn);
-    const int M = (int)nn;
-    const size_t ws_n = std::max(gemm_f64_ws_elems(M, 1, M), (size_t)1);
-    ws.alloc(ws_n);
-
-    // X = U diag(lambda^-1/2)
-    std::vector<double> lam;
-    Mat U, X(nn);
-    jacobi_eigh(n, S, lam, U);
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) X[(size_t)i * n + j] = U[(size_t)i * n + j] / std::sqrt(lam[j]);
+    ScfSystem sys(bs, st);
+    const Mat &S = sys.S, &h = sys.h;
+    const double e_nuc = sys.e_nuc;
 
     Mat P(nn, 0.0), F(nn), Fprev(nn), C(nn);
     std::vector<double> eps;
@@ -165,15 +223,7 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
     while (true) {
         hf_old = hf_new;
         // F = h + J - K/2 on the device
-        CCSD_CUDA(cudaMemcpyAsync(P_d.p, P.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
-        const int64_t N = n, N2 = N * N, N3 = N2 * N;
-        MatView Pv{P_d.p, ix1(0), ix1(1)};
-        OutView Gv{G_d.p, ix1(1), ix1(0)};
-        gemm_f64(M, 1, M, 1.0, MatView{eri.p, ix1(N2), ix1(1)}, Pv, 0.0, Gv, ws.p, ws_n, st);
-        gemm_f64(M, 1, M, -0.5, MatView{eri.p, ix2((uint32_t)n, N3, 1), ix2((uint32_t)n, N2, N)}, Pv, 1.0, Gv, ws.p,
-                 ws_n, st);
-        CCSD_CUDA(cudaMemcpyAsync(F.data(), G_d.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, st));
-        CCSD_CUDA(cudaStreamSynchronize(st));
+        sys.two_electron(P, 1.0, P, -0.5, F);
         for (size_t k = 0; k < nn; ++k) F[k] += h[k];
         Fprev = F;
         // DIIS (the reference's, with 3 vectors)
@@ -205,24 +255,8 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
                 }
             }
         }
-        // X^T F X, eigenpairs, C = X W with c^T S c = 1
-        const Mat Fo = matmul(n, X, matmul(n, F, X), true);
-        Mat W;
-        jacobi_eigh(n, Fo, eps, W);
-        C = matmul(n, X, W);
-        for (int c = 0; c < n; ++c) {
-            double s = 0.0;
-            for (int i = 0; i < n; ++i)
-                for (int j = 0; j < n; ++j) s += C[(size_t)i * n + c] * S[(size_t)i * n + j] * C[(size_t)j * n + c];
-            const double f = 1.0 / std::sqrt(s);
-            for (int i = 0; i < n; ++i) C[(size_t)i * n + c] *= f;
-        }
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < nocc; ++k) s += 2.0 * C[(size_t)i * n + k] * C[(size_t)j * n + k];
-                P[(size_t)i * n + j] = s;
-            }
+        sys.orbitals(F, eps, C);
+        P = sys.density(C, nocc, 2.0);
         hf_new = 0.0;
         for (int i = 0; i < nocc; ++i) hf_new += eps[i];
         ++step;
@@ -244,7 +278,85 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
     res.converged = converged ? 1 : 0;
     if (res.eps) std::memcpy(res.eps, eps.data(), sizeof(double) * n);
     if (res.C) std::memcpy(res.C, C.data(), sizeof(double) * nn);
-    if (res.eri) CCSD_CUDA(cudaMemcpy(res.eri, eri.p, sizeof(double) * nn * nn, cudaMemcpyDeviceToHost));
+    if (res.eri) CCSD_CUDA(cudaMemcpy(res.eri, sys.eri.p, sizeof(double) * nn * nn, cudaMemcpyDeviceToHost));
+}
+
+// Unrestricted Hartree-Fock, step for step as get_Energy(toler, 1) (hartree_fock_solver.cpp:
+// 959-1025, Unrestricted_Fock_Matrix :1359-1503, Unrestricted_P_Matrix :1505-1529,
+// Unrestricted_Energy :1531-1537): F_up = h + J(P_up + P_down) - K(P_up), F_down likewise;
+// no DIIS; stop when |eps_up[0] - previous| + |eps_down[0] - previous| < tol or after 300
+// steps.  The reference starts from Armadillo's randn densities (Initialize_UHF); this
+// starts from normal deviates of a seeded generator (symmetrised), so a run is repeatable.
+void uhf(const ccsd_basis &bs, int n_up, int n_down, double tol, int max_iter, ccsd_uhf_result &res,
+         cudaStream_t st) {
+    const int n = bs.nbf;
+    if (n_up < 0 || n_down < 0 || n_up + n_down == 0 || n_up > n || n_down > n)
+        throw Error(CCSD_ERR_INVALID_ARG, "UHF: electron counts must be >= 0, not both 0, at most nbf each");
+    const size_t nn = (size_t)n * n;
+    ScfSystem sys(bs, st);
+    // seeded normal deviates (xorshift64* and Box-Muller)
+    uint64_t state = res.seed ? res.seed : 2024;
+    auto uniform = [&]() {
+        state ^= state >> 12;
+        state ^= state << 25;
+        state ^= state >> 27;
+        return ((state * 2685821657736338717ull) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto normal = [&]() {
+        const double u1 = std::max(uniform(), 1e-300), u2 = uniform();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+    };
+    Mat Pu(nn), Pd(nn);
+    for (Mat *P : {&Pu, &Pd}) {
+        for (size_t k = 0; k < nn; ++k) (*P)[k] = normal();
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < i; ++j) {
+                const double m = 0.5 * ((*P)[(size_t)i * n + j] + (*P)[(size_t)j * n + i]);
+                (*P)[(size_t)i * n + j] = (*P)[(size_t)j * n + i] = m;
+            }
+    }
+    Mat Pt(nn), Fu, Fd, Cu, Cd;
+    std::vector<double> eu, ed;
+    double eu_old = 0.0, ed_old = 0.0;
+    int step = 0;
+    const int limit = max_iter > 0 ? max_iter : 300;
+    bool converged = false;
+    while (true) {
+        for (size_t k = 0; k < nn; ++k) Pt[k] = Pu[k] + Pd[k];
+        sys.two_electron(Pt, 1.0, Pu, -1.0, Fu);
+        sys.two_electron(Pt, 1.0, Pd, -1.0, Fd);
+        for (size_t k = 0; k < nn; ++k) {
+            Fu[k] += sys.h[k];
+            Fd[k] += sys.h[k];
+        }
+        sys.orbitals(Fu, eu, Cu);
+        sys.orbitals(Fd, ed, Cd);
+        Pu = sys.density(Cu, n_up, 1.0);
+        Pd = sys.density(Cd, n_down, 1.0);
+        const double check = std::fabs(eu[0] - eu_old) + std::fabs(ed[0] - ed_old);
+        eu_old = eu[0];
+        ed_old = ed[0];
+        ++step;
+        if (!std::isfinite(check)) throw Error(CCSD_ERR_DIVERGED, "UHF diverged (NaN/Inf)");
+        if (check < tol) {
+            converged = true;
+            break;
+        }
+        if (step > limit) break;
+    }
+    double e1 = 0.0, e2 = 0.0;
+    for (size_t k = 0; k < nn; ++k) {
+        e1 += (Pu[k] + Pd[k]) * sys.h[k];
+        e2 += Fu[k] * Pu[k] + Fd[k] * Pd[k];
+    }
+    res.e_uhf = e1 + 0.5 * e2 - 0.5 * e1 + sys.e_nuc;
+    res.e_nuc = sys.e_nuc;
+    res.iterations = step;
+    res.converged = converged ? 1 : 0;
+    if (res.eps_up) std::memcpy(res.eps_up, eu.data(), sizeof(double) * n);
+    if (res.eps_down) std::memcpy(res.eps_down, ed.data(), sizeof(double) * n);
+    if (res.C_up) std::memcpy(res.C_up, Cu.data(), sizeof(double) * nn);
+    if (res.C_down) std::memcpy(res.C_down, Cd.data(), sizeof(double) * nn);
 }
 
 }  // namespace
@@ -262,6 +374,27 @@ extern "C" int ccsd_rhf(const ccsd_basis *basis, int32_t n_electrons, double tol
         }
         cudaStream_t st = (cudaStream_t)res->stream;
         ccsd::rhf(*basis, n_electrons, tol > 0.0 ? tol : 1e-10, max_iter, *res, st);
+        return CCSD_OK;
+    } catch (const ccsd::Error &e) {
+        ccsd::set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        ccsd::set_last_error(e.what());
+        return CCSD_ERR_CUDA;
+    }
+}
+
+extern "C" int ccsd_uhf(const ccsd_basis *basis, int32_t n_up, int32_t n_down, double tol, int32_t max_iter,
+                        ccsd_uhf_result *res) {
+    try {
+        ccsd::set_last_error("");
+        if (!basis || !res) throw ccsd::Error(CCSD_ERR_INVALID_ARG, "ccsd_uhf: basis or result is NULL");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw ccsd::Error(CCSD_ERR_NO_DEVICE, "no CUDA device: this engine has no CPU path");
+        }
+        ccsd::uhf(*basis, n_up, n_down, tol > 0.0 ? tol : 1e-10, max_iter, *res, (cudaStream_t)res->stream);
         return CCSD_OK;
     } catch (const ccsd::Error &e) {
         ccsd::set_last_error(e.what());

@@ -310,6 +310,28 @@ typedef struct ccsd_scf_result {
  * CCSD_INTS_AO_DENSE and fock = diag(eps)). */
 int ccsd_rhf(const ccsd_basis *basis, int32_t n_electrons, double tol, int32_t max_iter, ccsd_scf_result *res);
 
+typedef struct ccsd_uhf_result {
+    double e_uhf;           /* out: E_UHF with E_nuc                           */
+    double e_nuc;           /* out                                             */
+    int32_t iterations;     /* out: SCF steps                                  */
+    int32_t converged;      /* out                                             */
+    double *eps_up, *eps_down;  /* optional out: nbf orbital energies each     */
+    double *C_up, *C_down;      /* optional out: nbf x nbf, C[mu][p]           */
+    uint64_t seed;          /* in: seed of the random start (0: 2024)          */
+    void *stream;           /* in: cudaStream_t, or NULL                       */
+} ccsd_uhf_result;
+
+/* Unrestricted Hartree-Fock with n_up / n_down electrons, step for step as
+ * get_Energy(toler, 1) (hartree_fock_solver.cpp:959-1025): F_up = h + J(P_up +
+ * P_down) - K(P_up), F_down likewise, no DIIS, stop when the lowest orbital energy
+ * of each spin moves by less than tol in sum (0: 1e-10) or after max_iter (0: 300)
+ * steps, the reference's energy expression.  The reference starts from random
+ * densities (Armadillo randn, Initialize_UHF); this starts from a seeded generator,
+ * so a run is repeatable and, like the reference, can reach a lower state than a
+ * core-Hamiltonian start. */
+int ccsd_uhf(const ccsd_basis *basis, int32_t n_up, int32_t n_down, double tol, int32_t max_iter,
+             ccsd_uhf_result *res);
+
 /* ---- INCAR front end (main.cpp:83-298, initializer.cpp:17-210) ----------- */
 /* The reference's INCAR keywords (Basis_Set, Method, convergance_criteria as
  * log10, Freeze_Core, Relax_Pos, use_angstrom, print_stuffies) and its atom
@@ -343,15 +365,17 @@ typedef struct ccsd_incar_result {
     double e_hf, e_corr;
     int32_t scf_iterations; /* SCF steps                                           */
     int32_t cc_iter;        /* the reference's counter (updates + 1); 0 for HF     */
-    int32_t method;         /* CCSD_METHOD_* that ran; -1 for HF                   */
+    int32_t method;         /* CCSD_METHOD_* that ran; -1 for HF, -2 for UHF       */
     int32_t nbf;
 } ccsd_incar_result;
 
 /* Initializer::Go on the engine: the molecule and method of incar_text with the
  * basis of basis_text, n_electrons = sum Z, the SCF and the amplitudes both to
- * convergance_criteria; HF, CCSD / CCSD1 (one engine), CCSDT-1a ... CCSDT;
- * Freeze_Core freezes ccsd_frozen_core_count(Z) orbitals; other methods (UHF,
- * UCCSDT) are CCSD_ERR_UNSUPPORTED.  precision: CCSD_PREC_* of the amplitudes. */
+ * convergance_criteria; HF, UHF (odd: n/2 + 1 up, n/2 down; even: the singlet, then
+ * the triplet n/2 + 1, n/2 - 1, whose energy is returned, as Go does), CCSD / CCSD1
+ * (one engine), CCSDT-1a ... CCSDT; Freeze_Core freezes ccsd_frozen_core_count(Z)
+ * orbitals; UCCSDT and CCSDT--Q (not working in the reference) are
+ * CCSD_ERR_UNSUPPORTED.  precision: CCSD_PREC_* of the amplitudes. */
 int ccsd_incar_run(const char *incar_text, const char *basis_text, int32_t precision, ccsd_incar_result *res);
 
 /* One contraction on the engine's kernels, for row-major FP64 device matrices:

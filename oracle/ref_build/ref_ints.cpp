@@ -5,6 +5,7 @@
 // (TEST INFRASTRUCTURE ONLY).
 //
 //   usage: ref_ints <basis> <atoms "Z,x,y,z;Z,x,y,z;..." (bohr)> <n_electrons> <log10 tol> <dump.bin>
+//          [uhf <n_up> <n_down>]   (then only "uhf <E_UHF> <steps>" is printed, nothing dumped)
 //   dump (native endian):
 //     int32 natoms, nbf, maxprim, nelec
 //     float64 Z[natoms], R[natoms][3]
@@ -50,6 +51,14 @@ int main(int argc, char **argv) {
     for (int a = 0; a < na; ++a) {
         Z(a) = zs[a];
         for (int d = 0; d < 3; ++d) R(a, d) = xyz[3 * a + d];
+    }
+    if (argc > 8 && std::string(argv[6]) == "uhf") {
+        Hartree_Fock_Solver uhf(na, Z, R, basis, n_elec, false, 0, 1, false);
+        uhf.Set_UP_DOWN(std::atoi(argv[7]), std::atoi(argv[8]));
+        const double e = uhf.get_Energy(toler, 1);
+        std::printf("uhf %.17e %d\n", e, uhf.steppp);
+        MPI_Finalize();
+        return 0;
     }
     Hartree_Fock_Solver hf(na, Z, R, basis, n_elec, false, 0, 1, false);
     const double ehf = hf.get_Energy(toler, 0);

@@ -9,7 +9,9 @@ Each tests/golden/ints_<name>.npz holds:
   - the AO integrals (mu nu|la si): the whole tensor ("eri") up to 13 functions, else
     the values at a seeded sample of unique quartets ("eri_idx" [k, 4], "eri_val" [k]);
   - E_nuc, E_HF, the orbital energies eps and C[mu][p] of its SCF (run to
-    tolerance 10^log10_tol).
+    tolerance 10^log10_tol; OH, with 9 electrons, is there for its basis only).
+tests/golden/reference_uhf.json holds the reference's UHF energies (get_Energy(toler, 1)
+after Set_UP_DOWN) on open shells of those molecules.
 
     python tests/golden/make_ints_golden.py      # needs the reference sources
 """
@@ -32,6 +34,10 @@ AMMONIA = "7,0,0,0.2;1,1.77,0,-0.48;1,-0.885,1.533,-0.48;1,-0.885,-1.533,-0.48"
 CASES = [("h2o_sto3g", "STO-3G", WATER, 10, -10), ("nh3_sto3g", "STO-3G", AMMONIA, 10, -10),
          ("h2o_631g", "6-31G", WATER, 10, -10), ("h2o_ccpvdz", "cc-pVDZ", WATER, 10, -10),
          ("o_ccpvtz", "cc-pVTZ", "8,0,0,0", 8, -6)]
+HYDROXYL = "8,0,0,0;1,1.8,0,0"
+# the reference's UHF (get_Energy(toler, 1)) on open shells: basis fixture, n_up, n_down
+UHF_CASES = [("oh_sto3g", 5, 4), ("h2o_sto3g", 5, 4), ("oh_631g", 5, 4), ("h2o_sto3g", 6, 4)]
+CASES += [("oh_sto3g", "STO-3G", HYDROXYL, 9, -10), ("oh_631g", "6-31G", HYDROXYL, 9, -10)]
 FULL_MAX = 13
 SAMPLE = 3000
 
@@ -98,6 +104,17 @@ def main():
             d["log10_tol"] = np.array(tol)
             np.savez_compressed(HERE / f"ints_{name}.npz", **d)
             print(f"ints_{name}.npz: nbf {n}, E_HF {d['e_hf']:.12f}")
+        spec = {name: (basis, atoms, ne) for name, basis, atoms, ne, _ in CASES}
+        uhf = []
+        for name, nu, nd in UHF_CASES:
+            basis, atoms, ne = spec[name]
+            out = subprocess.run([str(exe), basis, atoms, str(ne), "-10", str(Path(tmp) / "u.bin"), "uhf", str(nu),
+                                  str(nd)], check=True, cwd=tmp, capture_output=True, text=True).stdout.split()
+            uhf.append(dict(basis_fixture=f"ints_{name}.npz", n_up=nu, n_down=nd, log10_tol=-10,
+                            e_uhf=float(out[-2]), steps=int(out[-1])))
+            print(f"UHF {name} ({nu}, {nd}): {uhf[-1]['e_uhf']:.12f}")
+        import json
+        (HERE / "reference_uhf.json").write_text(json.dumps(uhf, indent=1) + "\n")
 
 
 if __name__ == "__main__":

@@ -54,7 +54,7 @@ def test_incar_reader_hazards():
 
 def test_unbuilt_methods_are_refused_before_any_compute():
     d = np.load(GOLD / "ints_h2o_sto3g.npz")
-    for m in ("UHF", "UCCSDT", "CCSDT--Q"):
+    for m in ("UCCSDT", "CCSDT--Q"):
         with pytest.raises(cg.CCSDError) as ei:
             cg.run_incar(incar_text(d, m, -8), g94_from_fixture(d))
         assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED

@@ -46,3 +46,14 @@ def test_incar_ccsdt1a():
     assert r["cc_iter"] == ref["iter"]
     assert abs(r["e_corr"] - ref["e_corr"]) < 1e-9
     assert abs(r["energy"] - (float(h["e_hf"]) + ref["e_corr"])) < 1e-9
+
+
+def test_incar_uhf_triplet():
+    """Method UHF with 10 electrons: Go runs the singlet, then returns the triplet
+    (6 up, 4 down); the reference's triplet H2O STO-3G energy."""
+    d = np.load(GOLD / "ints_h2o_sto3g.npz")
+    ref = [c for c in json.loads((GOLD / "reference_uhf.json").read_text())
+           if c["basis_fixture"] == "ints_h2o_sto3g.npz" and c["n_up"] == 6][0]
+    r = cg.run_incar(incar_text(d, "UHF", -10), g94_from_fixture(d))
+    assert r["method"] == -2
+    assert abs(r["energy"] - ref["e_uhf"]) < 1e-9

@@ -8,6 +8,7 @@ and the stopping step agree; what is left is rounding); the density
 P = 2 C_occ C_occ^T and the occupied orbital energies 1e-8 (the reference stops
 on the orbital-energy sum at 1e-10, so the last step moves these by about its
 square root); CCSD energies 1e-9 with the reference's iteration counter."""
+import json
 from pathlib import Path
 
 import numpy as np
@@ -64,3 +65,19 @@ def test_rhf_rejects_bad_electron_counts():
         with pytest.raises(cg.CCSDError) as ei:
             cg.rhf(d, ne)
         assert ei.value.code == _abi.CCSD_ERR_INVALID_ARG
+
+
+UHF = json.loads((GOLD / "reference_uhf.json").read_text())
+
+
+@pytest.mark.parametrize("case", UHF, ids=[f"{c['basis_fixture'][5:-4]}_{c['n_up']}{c['n_down']}" for c in UHF])
+def test_uhf_matches_reference(case):
+    """The reference's UHF (get_Energy(toler, 1)) on open shells: OH doublets, H2O+
+    and the H2O triplet.  Its stopping rule (the lowest orbital energy of each spin
+    settles to 1e-10) leaves the energy good to about 1e-10, and it starts from
+    random densities; energies within 1e-9, for two seeds of the engine's start."""
+    d = np.load(GOLD / case["basis_fixture"])
+    for seed in (0, 7):
+        r = cg.uhf(d, case["n_up"], case["n_down"], tol=10.0 ** case["log10_tol"], seed=seed)
+        assert r["converged"]
+        assert abs(r["e_uhf"] - case["e_uhf"]) < 1e-9
