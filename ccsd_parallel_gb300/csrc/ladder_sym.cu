@@ -125,6 +125,50 @@ __global__ void w_sym_kernel(int v, const double *__restrict__ W, double *__rest
     }
 }
 
+// The same by tiles: a block takes one pair a >= b and one 32 x 32 tile (C, D), C >= D, of
+// (c, d); it reads W[a][b] and W[b][a] at tiles (C, D) and (D, C) along their rows into
+// shared memory, so the transposed reads W[..][d][c] come from there, and writes W+/W-
+// rows of consecutive d.  Each W element is read once.
+constexpr int WT = 32;
+__global__ void __launch_bounds__(256) w_sym_tiled_kernel(int v, const double *__restrict__ W,
+                                                          double *__restrict__ wp, double *__restrict__ wm) {
+    __shared__ double t_ab_cd[WT][WT + 1], t_ba_cd[WT][WT + 1], t_ab_dc[WT][WT + 1], t_ba_dc[WT][WT + 1];
+    const int nt = (v + WT - 1) / WT;
+    const int64_t ntt = (int64_t)nt * (nt + 1) / 2;
+    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2, v2 = (int64_t)v * v;
+    const int64_t P = blockIdx.x / ntt;
+    int a, b, C, D;
+    untri(P, a, b);
+    untri(blockIdx.x % ntt, C, D);
+    const int64_t ab = ((int64_t)a * v + b) * v2, ba = ((int64_t)b * v + a) * v2;
+    const int tx = threadIdx.x % WT, ty = threadIdx.x / WT;  // 32 x 8
+    for (int r = ty; r < WT; r += 8) {
+        const int c = C * WT + r, d = D * WT + tx;  // rows c of tile (C, D)
+        const bool in = c < v && d < v;
+        t_ab_cd[r][tx] = in ? W[ab + (int64_t)c * v + d] : 0.0;
+        t_ba_cd[r][tx] = in ? W[ba + (int64_t)c * v + d] : 0.0;
+        const int dr = D * WT + r, cc = C * WT + tx;  // rows d of tile (D, C)
+        const bool in2 = dr < v && cc < v;
+        t_ab_dc[r][tx] = in2 ? W[ab + (int64_t)dr * v + cc] : 0.0;
+        t_ba_dc[r][tx] = in2 ? W[ba + (int64_t)dr * v + cc] : 0.0;
+    }
+    __syncthreads();
+    for (int r = ty; r < WT; r += 8) {
+        const int c = C * WT + r, d = D * WT + tx;
+        if (c >= v || d >= v || d > c) continue;
+        // W[ab][c][d], W[ba][d][c], W[ab][d][c], W[ba][c][d]
+        const double fcd = 0.5 * (t_ab_cd[r][tx] + t_ba_dc[tx][r]);
+        const int64_t out = P * Tv + tri(c, d);
+        if (c == d) {
+            wp[out] = fcd;
+        } else {
+            const double fdc = 0.5 * (t_ab_dc[tx][r] + t_ba_cd[r][tx]);
+            wp[out] = fcd + fdc;
+            if (a > b) wm[stri(a, b) * Tmv + stri(c, d)] = fcd - fdc;
+        }
+    }
+}
+
 // transpose of w_sym: Wbar[a,b,c,d] += cw W+bar[..] + s/2 W-bar[..]
 __global__ void w_sym_adj_kernel(int v, const double *__restrict__ wpb, const double *__restrict__ wmb,
                                  double *__restrict__ Wb) {
@@ -171,8 +215,13 @@ void k_ladder_unpack_adj(int o, int v, const double *Rb, double *spb, double *sm
 }
 
 void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st) {
-    const size_t n = ((size_t)v * (v + 1) / 2) * ((size_t)v * (v + 1) / 2);
-    w_sym_kernel<<<blocks_for(n), 256, 0, st>>>(v, W, wp, wm);
+    const int64_t nt = (v + WT - 1) / WT, blocks = (int64_t)v * (v + 1) / 2 * (nt * (nt + 1) / 2);
+    if (blocks <= 0x7fffffffLL) {
+        w_sym_tiled_kernel<<<(unsigned)blocks, 256, 0, st>>>(v, W, wp, wm);
+    } else {
+        const size_t n = ((size_t)v * (v + 1) / 2) * ((size_t)v * (v + 1) / 2);
+        w_sym_kernel<<<blocks_for(n), 256, 0, st>>>(v, W, wp, wm);
+    }
     CCSD_LAUNCH_CHECK();
 }
 
