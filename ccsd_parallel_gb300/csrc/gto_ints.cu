@@ -18,6 +18,7 @@
 // FP64 throughout: the outputs feed an FP64 SCF and CCSD.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -346,9 +347,14 @@ struct DevBuf {
     }
 };
 
+// __constant__ memory and the table belong to the current device: set up once per device
 void set_constants() {
-    static bool done = false;
-    if (done) return;
+    static std::mutex mu;
+    static std::vector<bool> done;
+    int dev = 0;
+    CCSD_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() > dev && done[dev]) return;
     double inv_series[100], inv_odd[kBoysN + 1];
     for (int j = 0; j < 100; ++j) inv_series[j] = 1.0 / (2.0 * kBoysN + 1.0 + 2.0 * j);
     inv_odd[0] = 0.0;
@@ -372,7 +378,8 @@ void set_constants() {
     CCSD_CUDA(cudaDeviceSynchronize());
     const double *ctab = tab;
     CCSD_CUDA(cudaMemcpyToSymbol(c_boys_tab, &ctab, sizeof ctab));
-    done = true;
+    if ((int)done.size() <= dev) done.resize(dev + 1, false);
+    done[dev] = true;
 }
 
 }  // namespace
