@@ -2,8 +2,9 @@
 
 Nothing in the product path imports this package.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
-legs of ``bench.py`` may use it, and only as the checker or as the timed CPU
-baseline -- never as the thing that is measured or shipped.
+legs of ``bench.py`` may use it, and only as the reference the GPU results are
+compared with or as the timed CPU baseline -- never as the thing that is
+measured or shipped.
 
 Contents
 --------

@@ -1,6 +1,6 @@
 """FP64 restatement of the reference's Gaussian integral engine
-(hartree_integrals.cpp), TEST INFRASTRUCTURE ONLY: the checker for the GPU
-integral kernels (ccsd_ao_integrals), never on the product path.
+(hartree_integrals.cpp), TEST INFRASTRUCTURE ONLY: what the GPU integral
+kernels (ccsd_ao_integrals) are compared with, never on the product path.
 
 McMurchie-Davidson over contracted Cartesian Gaussians, as the reference does it:
   - Hermite expansion coefficients E_t^{ij} of a product of two 1-D Gaussians
