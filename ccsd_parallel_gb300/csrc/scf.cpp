@@ -174,11 +174,20 @@ struct ScfSystem {
         CCSD_CUDA(cudaStreamSynchronize(st));
     }
 
-    // eigenpairs of X^T F X ascending, C = X W with every column at c^T S c = 1 (Normalize)
-    void orbitals(const Mat &F, std::vector<double> &eps, Mat &C) const {
+    // eigenpairs of X^T F X ascending, C = X W with every column at c^T S c = 1 (Normalize).
+    // warm: the previous step's W of this spin; X^T F X is rotated into it first, where it
+    // is nearly diagonal, so the Jacobi sweeps start close to the answer (then warm = W)
+    void orbitals(const Mat &F, std::vector<double> &eps, Mat &C, Mat &warm) const {
         const Mat Fo = matmul(n, X, matmul(n, F, X), true);
         Mat W;
-        jacobi_eigh(n, Fo, eps, W);
+        if (warm.size() == nn) {
+            Mat V;
+            jacobi_eigh(n, matmul(n, warm, matmul(n, Fo, warm), true), eps, V);
+            W = matmul(n, warm, V);
+        } else {
+            jacobi_eigh(n, Fo, eps, W);
+        }
+        warm = W;
         C = matmul(n, X, W);
         for (int c = 0; c < n; ++c) {
             double s = 0.0;
@@ -212,7 +221,7 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
     const Mat &S = sys.S, &h = sys.h;
     const double e_nuc = sys.e_nuc;
 
-    Mat P(nn, 0.0), F(nn), Fprev(nn), C(nn);
+    Mat P(nn, 0.0), F(nn), Fprev(nn), C(nn), warm;
     std::vector<double> eps;
     std::vector<Mat> errs, focks;
     const int ndiis = 3;
@@ -255,7 +264,7 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
                 }
             }
         }
-        sys.orbitals(F, eps, C);
+        sys.orbitals(F, eps, C, warm);
         P = sys.density(C, nocc, 2.0);
         hf_new = 0.0;
         for (int i = 0; i < nocc; ++i) hf_new += eps[i];
@@ -315,7 +324,7 @@ void uhf(const ccsd_basis &bs, int n_up, int n_down, double tol, int max_iter, c
                 (*P)[(size_t)i * n + j] = (*P)[(size_t)j * n + i] = m;
             }
     }
-    Mat Pt(nn), Fu, Fd, Cu, Cd;
+    Mat Pt(nn), Fu, Fd, Cu, Cd, warm_u, warm_d;
     std::vector<double> eu, ed;
     double eu_old = 0.0, ed_old = 0.0;
     int step = 0;
@@ -329,8 +338,8 @@ void uhf(const ccsd_basis &bs, int n_up, int n_down, double tol, int max_iter, c
             Fu[k] += sys.h[k];
             Fd[k] += sys.h[k];
         }
-        sys.orbitals(Fu, eu, Cu);
-        sys.orbitals(Fd, ed, Cd);
+        sys.orbitals(Fu, eu, Cu, warm_u);
+        sys.orbitals(Fd, ed, Cd, warm_d);
         Pu = sys.density(Cu, n_up, 1.0);
         Pd = sys.density(Cd, n_down, 1.0);
         const double check = std::fabs(eu[0] - eu_old) + std::fabs(ed[0] - ed_old);
