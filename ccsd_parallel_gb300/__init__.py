@@ -135,9 +135,9 @@ def rhf(basis, n_electrons: int, tol: float = 1e-10, max_iter: int = 0, eri: boo
                 C=Cm, eri=G, nocc=n_electrons // 2)
 
 
-def parse_incar(incar_text: str, basis_text: str) -> dict:
-    """The reference's INCAR keywords and atoms with a Gaussian94 basis, expanded to
-    the ccsd_basis arrays (ccsd_incar_parse; host only)."""
+def parse_incar(incar_text: str, basis_text: str = "") -> dict:
+    """The reference's INCAR keywords and atoms with a Gaussian94 basis (or the
+    INCAR's Basis_File), expanded to the ccsd_basis arrays (ccsd_incar_parse; host only)."""
     inc = _abi.Incar()
     lib = _abi.lib()
     a, b = incar_text.encode(), basis_text.encode()
@@ -156,7 +156,7 @@ def parse_incar(incar_text: str, basis_text: str) -> dict:
     return out
 
 
-def run_incar(incar_text: str, basis_text: str, precision="fp64") -> dict:
+def run_incar(incar_text: str, basis_text: str = "", precision="fp64") -> dict:
     """The reference's Initializer::Go on the engine (ccsd_incar_run): returns the
     energy it would print (E_HF for HF, E_HF + E_corr otherwise) and its parts."""
     r = _abi.IncarResult()

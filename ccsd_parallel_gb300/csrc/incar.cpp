@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <sstream>
 #include <string>
@@ -139,7 +140,7 @@ struct Input {
 
 Input parse_incar(const std::string &text) {
     static const char *const keys[] = {"Basis_Set", "Method", "convergance_criteria", "Freeze_Core",
-                                       "Relax_Pos", "use_angstrom", "print_stuffies"};
+                                       "Relax_Pos", "use_angstrom", "print_stuffies", "Basis_File"};
     Input in;
     std::istringstream is(text);
     std::string line;
@@ -238,7 +239,17 @@ Parsed parse_all(const char *incar_text, const char *basis_text) {
     p.R = in.R;
     if (p.angstrom)
         for (double &x : p.R) x *= kBohrPerAngstrom;
-    if (!basis_text) throw Error(CCSD_ERR_INVALID_ARG, "no basis text (Gaussian94 format)");
+    std::string file_text;
+    if (!basis_text || !*basis_text) {  // the INCAR's own Basis_File line (this engine's keyword)
+        if (!get("Basis_File"))
+            throw Error(CCSD_ERR_INVALID_ARG, "no basis: pass Gaussian94 text or give a Basis_File line");
+        std::ifstream f(*get("Basis_File"));
+        if (!f) throw Error(CCSD_ERR_INVALID_ARG, "cannot read Basis_File '" + *get("Basis_File") + "'");
+        std::stringstream ss;
+        ss << f.rdbuf();
+        file_text = ss.str();
+        basis_text = file_text.c_str();
+    }
     const Library lib = parse_g94(basis_text);
     for (size_t a = 0; a < p.Z.size(); ++a) {
         auto it = lib.find((int)p.Z[a]);

@@ -3,7 +3,7 @@
 //
 //   g++ -std=c++17 -O2 -I include ccsd_parallel_gb300/examples/ccsd_incar.cpp \
 //       -L ccsd_parallel_gb300/_lib -lccsd_gb300 -Wl,-rpath,<that directory> -o ccsd_incar
-//   ./ccsd_incar INCAR basis.g94 [split3]
+//   ./ccsd_incar INCAR [basis.g94] [split3]     (no basis file: the INCAR's Basis_File line)
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -22,19 +22,24 @@ static bool slurp(const char *path, std::string &out) {
 }
 
 int main(int argc, char **argv) {
-    if (argc < 3) {
-        std::fprintf(stderr, "usage: %s INCAR basis.g94 [fp64|split2|split3|split4]\n", argv[0]);
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s INCAR [basis.g94] [fp64|split2|split3|split4]\n", argv[0]);
         return 2;
+    }
+    int prec = CCSD_PREC_FP64, nargs = argc;
+    const char *last = argv[argc - 1];
+    if (argc > 2 && std::strncmp(last, "split", 5) == 0) {
+        prec = std::strcmp(last, "split2") == 0 ? CCSD_PREC_SPLIT2
+               : std::strcmp(last, "split4") == 0 ? CCSD_PREC_SPLIT4 : CCSD_PREC_SPLIT3;
+        --nargs;
+    } else if (argc > 2 && std::strcmp(last, "fp64") == 0) {
+        --nargs;
     }
     std::string incar, basis;
-    if (!slurp(argv[1], incar) || !slurp(argv[2], basis)) {
-        std::fprintf(stderr, "cannot read %s or %s\n", argv[1], argv[2]);
+    if (!slurp(argv[1], incar) || (nargs > 2 && !slurp(argv[2], basis))) {
+        std::fprintf(stderr, "cannot read the INCAR or the basis file\n");
         return 2;
     }
-    int prec = CCSD_PREC_FP64;
-    if (argc > 3 && std::strcmp(argv[3], "split2") == 0) prec = CCSD_PREC_SPLIT2;
-    if (argc > 3 && std::strcmp(argv[3], "split3") == 0) prec = CCSD_PREC_SPLIT3;
-    if (argc > 3 && std::strcmp(argv[3], "split4") == 0) prec = CCSD_PREC_SPLIT4;
     ccsd_incar_result r{};
     const int rc = ccsd_incar_run(incar.c_str(), basis.c_str(), prec, &r);
     if (rc != CCSD_OK) {

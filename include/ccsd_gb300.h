@@ -357,7 +357,9 @@ typedef struct ccsd_incar {
     double *alpha, *coef;          /* out: [nbf][capacity_prim]                   */
 } ccsd_incar;
 
-/* Parse only (no GPU): call once with capacities 0 for the sizes, then with arrays. */
+/* Parse only (no GPU): call once with capacities 0 for the sizes, then with arrays.
+ * basis_text NULL or empty: the basis file named by an INCAR line "Basis_File <path>"
+ * (this engine's keyword; the reference selects built-in tables by Basis_Set). */
 int ccsd_incar_parse(const char *incar_text, const char *basis_text, ccsd_incar *inc);
 
 typedef struct ccsd_incar_result {

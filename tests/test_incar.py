@@ -58,3 +58,15 @@ def test_unbuilt_methods_are_refused_before_any_compute():
         with pytest.raises(cg.CCSDError) as ei:
             cg.run_incar(incar_text(d, m, -8), g94_from_fixture(d))
         assert ei.value.code == _abi.CCSD_ERR_UNSUPPORTED
+
+
+def test_basis_file_keyword(tmp_path):
+    """With no basis text the INCAR's Basis_File line names the Gaussian94 file."""
+    d = np.load(GOLD / "ints_h2o_631g.npz")
+    path = tmp_path / "water.g94"
+    path.write_text(g94_from_fixture(d))
+    p = cg.parse_incar(incar_text(d, "HF", -10, extra=f"Basis_File {path}"))
+    np.testing.assert_allclose(p["coef"], d["coef"][:, :p["coef"].shape[1]], rtol=1e-14, atol=0)
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.parse_incar(incar_text(d, "HF", -10))
+    assert ei.value.code == _abi.CCSD_ERR_INVALID_ARG
