@@ -70,3 +70,23 @@ def test_basis_file_keyword(tmp_path):
     with pytest.raises(cg.CCSDError) as ei:
         cg.parse_incar(incar_text(d, "HF", -10))
     assert ei.value.code == _abi.CCSD_ERR_INVALID_ARG
+
+
+def test_gaussian94_forms():
+    """SP (and its synonym L) shells give S then P from one exponent list; Fortran
+    D exponents; '!' comments and blank lines are skipped."""
+    incar = "Method HF\nH 0 0 0\nLi 0 0 3.0\n"
+    basis = ("! a hand-written basis\n\nH 0\nS 2 1.00\n  3.0D+00  0.5\n  0.5D0 0.6\n****\n"
+             "Li 0\nS 1 1.00\n 16.0 1.0\nSP 2 1.00\n 1.5 0.3 0.2\n 0.2 0.7 0.8\n"
+             "L 1 1.00\n 0.05 1.0 1.0\n****\n")
+    p = cg.parse_incar(incar, basis)
+    assert p["n_electrons"] == 4
+    # H: 1 s; Li: s, (s, p x3) from SP, (s, p x3) from L
+    np.testing.assert_array_equal(p["atom"], [0] + [1] * 9)
+    np.testing.assert_array_equal(p["powers"].sum(axis=1), [0, 0, 0, 1, 1, 1, 0, 1, 1, 1])
+    np.testing.assert_array_equal(p["nprim"], [2, 1, 2, 2, 2, 2, 1, 1, 1, 1])
+    assert p["alpha"][0, 0] == 3.0 and p["alpha"][0, 1] == 0.5
+    # an s primitive carries (2a/pi)^{3/4}, a p_x primitive (2a/pi)^{3/4} (4a)^{1/2}
+    a = 1.5
+    assert p["coef"][2, 0] == pytest.approx(0.3 * (2 * a / np.pi) ** 0.75, rel=1e-15)
+    assert p["coef"][3, 0] == pytest.approx(0.2 * (2 * a / np.pi) ** 0.75 * np.sqrt(4 * a), rel=1e-15)
