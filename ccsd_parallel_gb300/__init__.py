@@ -58,7 +58,7 @@ METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A,
 
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
              fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, profile=False,
-             stream=None, method="ccsd"):
+             stream=None, method="ccsd", t1_start=None, t2_start=None):
     o = _abi.Options()
     _abi.check(_abi.lib().ccsd_default_options(C.byref(o)))
     o.energy_tol = energy_tol
@@ -72,6 +72,8 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     o.profile = int(bool(profile))
     o.method = METHODS[method] if isinstance(method, str) else int(method)
     o.stream = stream
+    # restart amplitudes: the arrays must outlive the solve, so the caller keeps them (Solver does)
+    o.t1_start, o.t2_start = _ptr(t1_start), _ptr(t2_start)
     return o
 
 
@@ -233,15 +235,24 @@ class Solver:
                                  nfrozen=nfrozen)
         n = p.nfrozen + p.nocc + p.nvir
         self.nocc, self.nvir = p.nocc, p.nvir  # active orbitals (the amplitudes' shape)
-        self._opts = _options(**opts)
+        self._opts = _options(**self._restart(opts))
         h = C.c_void_p()
         _abi.check(_abi.lib().ccsd_create(C.byref(p), C.byref(self._opts), C.byref(h)))
         self._h = h
         self._problem = p  # re-read by lambda_grad (the arrays in _keep stay referenced)
         self._n = n
 
+    def _restart(self, opts):
+        """t1_start / t2_start (a restart) as contiguous FP64 arrays kept alive here."""
+        self._restart_keep = []
+        for k in ("t1_start", "t2_start"):
+            if opts.get(k) is not None:
+                opts[k] = _f64(opts[k])
+                self._restart_keep.append(opts[k])
+        return opts
+
     def set_options(self, **opts):
-        self._opts = _options(**opts)
+        self._opts = _options(**self._restart(opts))
         _abi.check(_abi.lib().ccsd_set_options(self._h, C.byref(self._opts)))
 
     def solve(self, amplitudes: bool = True, history: int = 1001) -> dict:

@@ -98,7 +98,7 @@ class Options(C.Structure):
         ("energy_tol", C.c_double), ("residual_tol", C.c_double), ("max_iter", C.c_int32),
         ("fixed_iterations", C.c_int32), ("diis_size", C.c_int32), ("diis_start", C.c_int32),
         ("precision", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
-        ("method", C.c_int32), ("stream", C.c_void_p),
+        ("method", C.c_int32), ("stream", C.c_void_p), ("t1_start", _dp), ("t2_start", _dp),
     ]
 
 

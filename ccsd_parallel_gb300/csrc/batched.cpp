@@ -72,6 +72,8 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
     if (n <= 0 || !problems) throw Error(CCSD_ERR_INVALID_ARG, "batched solve needs n >= 1 problems");
     for (int i = 0; i < n; ++i)
         if (!problems[i]) throw Error(CCSD_ERR_INVALID_ARG, "problem " + std::to_string(i) + " is NULL");
+    if (opts.t1_start || opts.t2_start)
+        throw Error(CCSD_ERR_INVALID_ARG, "restart amplitudes (t1_start / t2_start) are for single solves");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();

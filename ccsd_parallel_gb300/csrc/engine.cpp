@@ -890,9 +890,18 @@ void Engine::solve(ccsd_result *res) {
     prof_update_ms_ = 0.0;
     prof_updates_ = 0;
     prof_launches_ = 0;
-    // T1 = 0, T2 = MP2 (ccsd_memory_optimized.cpp:473-490)
-    t1_.zero(st_);
-    k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
+    // T1 = 0, T2 = MP2 (ccsd_memory_optimized.cpp:473-490), or the caller's amplitudes (a restart)
+    if (opt_.t2_start) {
+        CCSD_CUDA(cudaMemcpyAsync(t2_.p, opt_.t2_start, sizeof(double) * nT2, cudaMemcpyHostToDevice, st_));
+        if (opt_.t1_start)
+            CCSD_CUDA(cudaMemcpyAsync(t1_.p, opt_.t1_start, sizeof(double) * nT1, cudaMemcpyHostToDevice, st_));
+        else
+            t1_.zero(st_);
+        CCSD_CUDA(cudaStreamSynchronize(st_));  // the host arrays may go away after the call
+    } else {
+        t1_.zero(st_);
+        k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
+    }
     if (opt_.method != CCSD_METHOD_CCSD) triples_setup();  // T3 = 0
     double e_new = energy_of(t1_.p, t2_.p);
     int hist = 0;

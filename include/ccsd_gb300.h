@@ -102,6 +102,12 @@ typedef struct ccsd_options {
     int32_t profile;           /* 1: time every contraction with CUDA events   */
     int32_t method;            /* CCSD_METHOD_*                                 */
     void *stream;              /* cudaStream_t, or NULL for a private stream   */
+    const double *t1_start;    /* restart: ccsd_solve starts from these host   */
+    const double *t2_start;    /*   amplitudes ([i][a], [i][j][a][b]) instead of
+                                    T1 = 0, T2 = MP2 when t2_start is set (t1_start
+                                    NULL: T1 = 0); single solves only; the DIIS
+                                    history and T3 start afresh.  A checkpoint is
+                                    ccsd_result.t1 / t2 of an earlier solve.    */
 } ccsd_options;
 
 /* ---- coupled-cluster method (ccsd_options.method) ------------------------ */

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8 + 8  # nfrozen (int32) padded to 8
-    assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8
+    assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8 + 2 * 8  # + t1_start, t2_start
     assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
 
 
@@ -148,3 +148,23 @@ def test_integrals_have_no_cpu_path():
     with pytest.raises(cg.CCSDError) as ei:
         cg.ao_integrals(d)
     assert ei.value.code == _abi.CCSD_ERR_NO_DEVICE
+
+
+def test_batched_solve_refuses_restart_amplitudes():
+    """t1_start / t2_start belong to single solves; the batched entry refuses them
+    before touching a device."""
+    p = _abi.Problem()
+    p.nocc, p.nvir, p.integral_kind, p.naux = 2, 4, _abi.CCSD_INTS_DF, 5
+    fock, b = syn.make_system(2, 4, 5, 1)
+    fock, b = np.ascontiguousarray(fock), np.ascontiguousarray(b)
+    p.fock = fock.ctypes.data_as(C.POINTER(C.c_double))
+    p.df = b.ctypes.data_as(C.POINTER(C.c_double))
+    o = _abi.Options()
+    _abi.lib().ccsd_default_options(C.byref(o))
+    t2 = np.zeros(2 * 2 * 4 * 4)
+    o.t2_start = t2.ctypes.data_as(C.POINTER(C.c_double))
+    probs = (C.POINTER(_abi.Problem) * 1)(C.pointer(p))
+    res = (_abi.Result * 1)()
+    rc = _abi.lib().ccsd_solve_batched(probs, 1, C.byref(o), res)
+    assert rc == _abi.CCSD_ERR_INVALID_ARG
+    assert "single solves" in _abi.last_error()

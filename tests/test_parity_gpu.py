@@ -196,3 +196,15 @@ def test_spin_orbital_input_rejects_open_shell_integrals():
     with pytest.raises(cg.CCSDError) as ei:
         cg.solve(np.diag(syn.orbital_energies(o, v, 9)), o, so_eri=g)
     assert ei.value.code == -1 and "closed-shell" in str(ei.value)
+
+
+def test_restart_from_saved_amplitudes_continues_the_iteration():
+    """A checkpoint: 3 updates, then a new solve started from their T1/T2
+    (t1_start / t2_start) for 3 more gives the energies of 6 updates in a row
+    (plain Jacobi, so no history is lost)."""
+    fock, b = cg.make_synthetic(4, 16, 30, 5)
+    full = cg.solve(fock, 4, df=b, fixed_iterations=6)
+    first = cg.solve(fock, 4, df=b, fixed_iterations=3)
+    second = cg.solve(fock, 4, df=b, fixed_iterations=3, t1_start=first["t1"], t2_start=first["t2"])
+    np.testing.assert_allclose(second["energies"], full["energies"][3:], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(second["t2"], full["t2"], rtol=0, atol=1e-13)
