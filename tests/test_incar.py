@@ -90,3 +90,17 @@ def test_gaussian94_forms():
     a = 1.5
     assert p["coef"][2, 0] == pytest.approx(0.3 * (2 * a / np.pi) ** 0.75, rel=1e-15)
     assert p["coef"][3, 0] == pytest.approx(0.2 * (2 * a / np.pi) ** 0.75 * np.sqrt(4 * a), rel=1e-15)
+
+
+@pytest.mark.parametrize("basis,msg", [
+    ("H 0\nS 2 1.00\n 3.0 0.5\n****\n", "missing primitive lines"),
+    ("H 0\nS 1 1.00\n -3.0 0.5\n****\n", "bad exponent"),
+    ("H 0\nG 1 1.00\n 3.0 0.5\n****\n", "shell type"),
+    ("H 0\nSP 1 1.00\n 3.0 0.5\n****\n", "coefficient"),
+    ("Xx 0\nS 1 1.00\n 3.0 0.5\n****\n", "unknown element"),
+])
+def test_gaussian94_errors_name_the_line(basis, msg):
+    with pytest.raises(cg.CCSDError) as ei:
+        cg.parse_incar("Method HF\nH 0 0 0\nH 0 0 1.4\n", basis)
+    assert ei.value.code == _abi.CCSD_ERR_INVALID_ARG
+    assert msg in str(ei.value) and "line" in str(ei.value)
