@@ -93,7 +93,8 @@ def test_gaussian94_forms():
 
 
 @pytest.mark.parametrize("basis,msg", [
-    ("H 0\nS 2 1.00\n 3.0 0.5\n****\n", "missing primitive lines"),
+    ("H 0\nS 2 1.00\n 3.0 0.5\n****\n", "expected an exponent"),  # '****' read as the 2nd primitive
+    ("H 0\nS 2 1.00\n 3.0 0.5\n", "missing primitive lines"),
     ("H 0\nS 1 1.00\n -3.0 0.5\n****\n", "bad exponent"),
     ("H 0\nG 1 1.00\n 3.0 0.5\n****\n", "shell type"),
     ("H 0\nSP 1 1.00\n 3.0 0.5\n****\n", "coefficient"),
