@@ -54,11 +54,16 @@ METHODS = {"ccsd": _abi.CCSD_METHOD_CCSD, "ccsdt-1a": _abi.CCSD_METHOD_CCSDT1A,
            "ccsdt-1b": _abi.CCSD_METHOD_CCSDT1B, "ccsdt-2": _abi.CCSD_METHOD_CCSDT2,
            "ccsdt-3": _abi.CCSD_METHOD_CCSDT3, "ccsdt-4": _abi.CCSD_METHOD_CCSDT4,
            "ccsdt": _abi.CCSD_METHOD_CCSDT}
+# the reference's two CCSD maps: "ccsd" = the CCSD equations of its dense CCSD1
+# (ccsdt.cpp:625-727); "memory_optimized" = CCSD_Memory_optimized as written,
+# F_mi contracted transposed in T2 (ccsd_memory_optimized.cpp:2085-2086 and its
+# five other spin cases)
+VARIANTS = {"ccsd": _abi.CCSD_VARIANT_CCSD, "memory_optimized": _abi.CCSD_VARIANT_MEMORY_OPTIMIZED}
 
 
 def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
              fixed_iterations=0, diis_size=0, diis_start=0, verbose=False, profile=False,
-             stream=None, method="ccsd", t1_start=None, t2_start=None):
+             stream=None, method="ccsd", t1_start=None, t2_start=None, variant="ccsd"):
     o = _abi.Options()
     _abi.check(_abi.lib().ccsd_default_options(C.byref(o)))
     o.energy_tol = energy_tol
@@ -74,6 +79,7 @@ def _options(precision="fp64", energy_tol=1e-10, residual_tol=0.0, max_iter=999,
     o.stream = stream
     # restart amplitudes: the arrays must outlive the solve, so the caller keeps them (Solver does)
     o.t1_start, o.t2_start = _ptr(t1_start), _ptr(t2_start)
+    o.variant = VARIANTS[variant] if isinstance(variant, str) else int(variant)
     return o
 
 
@@ -243,12 +249,19 @@ class Solver:
         self._n = n
 
     def _restart(self, opts):
-        """t1_start / t2_start (a restart) as contiguous FP64 arrays kept alive here."""
+        """t1_start / t2_start (a restart) as contiguous FP64 arrays kept alive here.
+        Their shapes are checked against this system's (o, v) and (o, o, v, v):
+        the library copies exactly that many doubles from the pointers."""
         self._restart_keep = []
-        for k in ("t1_start", "t2_start"):
+        o, v = self.nocc, self.nvir
+        for k, shape in (("t1_start", (o, v)), ("t2_start", (o, o, v, v))):
             if opts.get(k) is not None:
-                opts[k] = _f64(opts[k])
-                self._restart_keep.append(opts[k])
+                a = _f64(opts[k])
+                if a.shape != shape:
+                    raise CCSDError(_abi.CCSD_ERR_INVALID_ARG,
+                                    f"{k} has shape {a.shape}; this system's amplitudes are {shape}")
+                opts[k] = a
+                self._restart_keep.append(a)
         return opts
 
     def set_options(self, **opts):
@@ -428,13 +441,19 @@ class CCSD_Memory_optimized:
                                                   ccsd_memory_optimized.cpp:3520)
 
     Like the reference, CCSD() runs plain Jacobi updates from the MP2 guess
-    until |E_new - E_old| < toler or 999 updates (iter reaching 1000).
+    until |E_new - E_old| < toler or 999 updates (iter reaching 1000).  It
+    iterates the reference class's own map by default (variant
+    "memory_optimized": F_mi contracted transposed in T2,
+    ccsd_memory_optimized.cpp:2085-2086), so energies and counters are the
+    class's; variant="ccsd" iterates the CCSD equations of the reference's
+    dense CCSD1 instead.
     """
 
     def __init__(self, fock, nocc, eri=None, df=None, ao_eri=None, mo_coeff=None, E_HF=0.0,
-                 precision="fp64", so_eri=None, nfrozen=0):
+                 precision="fp64", so_eri=None, nfrozen=0, variant="memory_optimized"):
+        self._variant = variant
         self._solver = Solver(fock, nocc, eri=eri, df=df, ao_eri=ao_eri, mo_coeff=mo_coeff, so_eri=so_eri,
-                              precision=precision, nfrozen=nfrozen)
+                              precision=precision, nfrozen=nfrozen, variant=variant)
         self.n_Electrons = 2 * (nocc - nfrozen)
         self.unocc_orb = 2 * (np.asarray(fock).shape[0] - nocc)
         self.E_HF = E_HF
@@ -444,7 +463,7 @@ class CCSD_Memory_optimized:
 
     def CCSD(self, toler: float, print_stuff: bool = False) -> float:
         self._solver.set_options(precision=self._solver._opts.precision, energy_tol=toler,
-                                 max_iter=999, verbose=print_stuff)
+                                 max_iter=999, verbose=print_stuff, variant=self._variant)
         r = self._solver.solve()
         self.E_new, self.t1, self.t2 = r["e_corr"], r["t1"], r["t2"]
         self.iter = r["iterations"] + 1  # the reference counter starts at 1

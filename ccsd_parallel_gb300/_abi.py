@@ -34,6 +34,8 @@ CCSD_METHOD_CCSDT2 = 3
 CCSD_METHOD_CCSDT3 = 4
 CCSD_METHOD_CCSDT4 = 5
 CCSD_METHOD_CCSDT = 6
+CCSD_VARIANT_CCSD = 0
+CCSD_VARIANT_MEMORY_OPTIMIZED = 1
 
 CCSD_PREC_FP64 = 0
 CCSD_PREC_SPLIT2 = 2
@@ -99,6 +101,7 @@ class Options(C.Structure):
         ("fixed_iterations", C.c_int32), ("diis_size", C.c_int32), ("diis_start", C.c_int32),
         ("precision", C.c_int32), ("verbose", C.c_int32), ("profile", C.c_int32),
         ("method", C.c_int32), ("stream", C.c_void_p), ("t1_start", _dp), ("t2_start", _dp),
+        ("variant", C.c_int32),
     ]
 
 

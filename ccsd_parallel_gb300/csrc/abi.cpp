@@ -213,6 +213,17 @@ int ccsd_gemm(int32_t precision, int32_t M, int32_t N, int32_t K, double alpha, 
         c.row.s2 = ldc;
         c.col.s2 = 1;
         if (M == 0 || N == 0) return;
+        if (K == 0) {  // C = beta C, nothing to contract (alpha is not applied, as in BLAS)
+            if (beta != 1.0) {
+                ccsd::MatView cv;
+                cv.p = C;
+                cv.row = c.row;
+                cv.col = c.col;
+                ccsd::axpby_view(M, N, 0.0, cv, beta, c, st);
+                CCSD_CUDA(cudaStreamSynchronize(st));
+            }
+            return;
+        }
         if (precision == CCSD_PREC_FP64) {
             size_t ws_n = ccsd::gemm_f64_ws_elems(M, N, K);
             double *ws = nullptr;

@@ -173,6 +173,13 @@ void Engine::set_options(const ccsd_options &opts) {
         throw Error(CCSD_ERR_INVALID_ARG, "iteration counts must be >= 0");
     if (opts.method < CCSD_METHOD_CCSD || opts.method > CCSD_METHOD_CCSDT)
         throw Error(CCSD_ERR_INVALID_ARG, "unknown method");
+    if (opts.variant != CCSD_VARIANT_CCSD && opts.variant != CCSD_VARIANT_MEMORY_OPTIMIZED)
+        throw Error(CCSD_ERR_INVALID_ARG, "unknown CCSD variant");
+    if (opts.variant == CCSD_VARIANT_MEMORY_OPTIMIZED && opts.method != CCSD_METHOD_CCSD)
+        throw Error(CCSD_ERR_INVALID_ARG,
+                    "the memory-optimised CCSD map is a CCSD method; the triples methods iterate the CCSD1 equations");
+    if (opts.t1_start && !opts.t2_start)
+        throw Error(CCSD_ERR_INVALID_ARG, "t1_start needs t2_start (a restart sets both, or T2 alone)");
     if (opts.stream) {
         if (own_stream_ && st_) cudaStreamDestroy(st_);
         st_ = (cudaStream_t)opts.stream;
@@ -753,9 +760,11 @@ void Engine::residual() {
     // + sum_c Lvv'[a,c] t2[i,j,c,b]: M = a, N = (i,j,b), K = c
     gemm(iv, (int)(o2 * v), iv, 1.0, mv(Lvv_.p, ix1(v), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, 1), ix1(v)), 1.0, ovw(Rp_.p, ix1(v), ix2((uint32_t)v, v2, 1)), 0, 0, "Rp_Lvv");
-    // - sum_k Loo'[k,i] t2[k,j,a,b]: M = i, N = (j,a,b), K = k
-    gemm(io, (int)ov2, io, -1.0, mv(Loo_.p, ix1(1), ix1(o)), mv(t2, ix1(1), ix1(ov2)), 1.0,
-         ovw(Rp_.p, ix1(ov2), ix1(1)), 0, 0, "Rp_Loo");
+    // - sum_k Loo'[k,i] t2[k,j,a,b]: M = i, N = (j,a,b), K = k.  The memory-optimised
+    // map reads Loo' transposed here, Loo'[i,k] (ccsd_memory_optimized.cpp:2085-2086)
+    const bool fik = opt_.variant == CCSD_VARIANT_MEMORY_OPTIMIZED;
+    gemm(io, (int)ov2, io, -1.0, fik ? mv(Loo_.p, ix1(o), ix1(1)) : mv(Loo_.p, ix1(1), ix1(o)),
+         mv(t2, ix1(1), ix1(ov2)), 1.0, ovw(Rp_.p, ix1(ov2), ix1(1)), 0, 0, "Rp_Loo");
     // rings, M = (i,a), N = (j,b), K = (k,c)
     // + sum_kc Wa[i,a,k,c] t2[k,j,c,b]
     gemm((int)ov, (int)ov, (int)ov, 1.0, mv(Wa_.p, ix1(ov), ix1(1)),

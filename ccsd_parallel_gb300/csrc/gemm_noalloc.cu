@@ -113,8 +113,20 @@ extern "C" int ccsd_gemm_noalloc(int32_t precision, int32_t M, int32_t N, int32_
         c.p = C;
         c.row.s2 = ldc;
         c.col.s2 = 1;
-        // same operand roles as ccsd_gemm: keep the long side in the 128-row tile
-        if (SplitEngine::prefer_swap(M, N)) {
+        if (K == 0) {  // C = beta C, nothing to contract (alpha is not applied, as in BLAS)
+            if (beta != 1.0) {
+                MatView cv;
+                cv.p = C;
+                cv.row = c.row;
+                cv.col = c.col;
+                axpby_view(M, N, 0.0, cv, beta, c, st);
+                CCSD_CUDA(cudaStreamSynchronize(st));
+            }
+            return CCSD_OK;
+        }
+        // the same operand roles as ccsd_gemm (SplitEngine::gemm): the long side in the
+        // 128-row tile, and C's index with the smaller stride in the TMEM lanes
+        if (SplitEngine::prefer_swap(M, N, c)) {
             std::swap(a, b);
             std::swap(M, N);
             std::swap(c.row, c.col);

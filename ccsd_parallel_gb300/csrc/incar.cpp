@@ -1,7 +1,10 @@
 // INCAR front end: the reference's input reader (main.cpp:83-298: find_and_write,
 // find_start_of_atoms, Fill_One_Atom, return_charge) and Initializer::Go's dispatch
-// (initializer.cpp:17-210) onto the engine: HF -> ccsd_rhf; UHF -> ccsd_uhf; CCSD /
-// CCSD1 -> RHF + ccsd_solve; CCSDT-1a ... CCSDT -> RHF + the triples methods.
+// (initializer.cpp:17-210) onto the engine: HF -> ccsd_rhf; UHF -> ccsd_uhf; CCSD ->
+// RHF + ccsd_solve of the memory-optimised map (the reference's "CCSD" runs the class
+// CCSD_Memory_optimized, initializer.cpp:191-195); CCSD1 -> RHF + ccsd_solve of the
+// CCSD equations (the reference's dense CCSDT::Calc_Energy(toler, -1)); CCSDT-1a ...
+// CCSDT -> RHF + the triples methods.
 //
 // Differences from the reference's reader (its parsing hazards):
 //   - a keyword counts only at the start of a line (the reference takes the first
@@ -413,6 +416,7 @@ extern "C" int ccsd_incar_run(const char *incar_text, const char *basis_text, in
         opt.energy_tol = p.tol;
         opt.precision = precision;
         opt.method = method;
+        opt.variant = p.method == "CCSD" ? CCSD_VARIANT_MEMORY_OPTIMIZED : CCSD_VARIANT_CCSD;
         opt.verbose = p.print ? 1 : 0;
         ccsd_handle *h = nullptr;
         rc = ccsd_create(&prob, &opt, &h);

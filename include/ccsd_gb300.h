@@ -105,10 +105,31 @@ typedef struct ccsd_options {
     const double *t1_start;    /* restart: ccsd_solve starts from these host   */
     const double *t2_start;    /*   amplitudes ([i][a], [i][j][a][b]) instead of
                                     T1 = 0, T2 = MP2 when t2_start is set (t1_start
-                                    NULL: T1 = 0); single solves only; the DIIS
-                                    history and T3 start afresh.  A checkpoint is
-                                    ccsd_result.t1 / t2 of an earlier solve.    */
+                                    NULL: T1 = 0); t1_start without t2_start is
+                                    rejected (CCSD_ERR_INVALID_ARG); single solves
+                                    only; the DIIS history and T3 start afresh.  A
+                                    checkpoint is ccsd_result.t1 / t2 of an earlier
+                                    solve.                                       */
+    int32_t variant;           /* CCSD_VARIANT_*: which of the reference's two
+                                  CCSD maps is iterated (method CCSD only)      */
 } ccsd_options;
+
+/* ---- CCSD map (ccsd_options.variant) --------------------------------------
+ * The reference holds two CCSD codes that iterate different maps.
+ * CCSD_VARIANT_CCSD is the CCSD equations as its dense spin-orbital CCSD
+ * ("CCSD1", CCSDT::Calc_Energy(toler, -1), ccsdt.cpp:625-727) states them:
+ *   R_ij^ab += sum_k t_jk^ab F_ki - sum_k t_ik^ab F_kj.
+ * CCSD_VARIANT_MEMORY_OPTIMIZED is CCSD_Memory_optimized::CCSD as written (the
+ * INCAR method "CCSD", initializer.cpp:191-195): its Fill_t2_new contracts the
+ * occupied Fock intermediate transposed, in every spin case,
+ *   R_ij^ab += sum_k t_jk^ab F_ik - sum_k t_ik^ab F_jk
+ * (D2.row(i/2), ccsd_memory_optimized.cpp:2085-2086, 2143-2144, 2193-2194,
+ * 2269-2270, 2324-2325, 2375-2376, where D2(k,i) = F_ki), while its T1 equation
+ * uses F_ki (:2444).  F_ki is not symmetric once T1/T2 are non-zero, so the
+ * two maps reach fixed points ~1e-8 Eh apart on molecules (H2O/6-31G:
+ * 1.9e-8).  The default is CCSD_VARIANT_CCSD. */
+#define CCSD_VARIANT_CCSD 0
+#define CCSD_VARIANT_MEMORY_OPTIMIZED 1
 
 /* ---- coupled-cluster method (ccsd_options.method) ------------------------ */
 #define CCSD_METHOD_CCSD 0     /* CCSD (the reference's CCSD / CCSD1)            */

@@ -17,7 +17,11 @@
 //   T_1 (compact, V x o), t2 (compact field)     t1 [i][a], t2 [i][j][a][b] (spatial)
 //
 // As in the reference, CCSD() iterates plain Jacobi updates from the MP2
-// guess until |E_new - E_old| < toler or iter reaches 1000.  Failures are
+// guess until |E_new - E_old| < toler or iter reaches 1000.  By default it
+// iterates the reference class's own map (CCSD_VARIANT_MEMORY_OPTIMIZED: F_mi
+// contracted transposed in T2, ccsd_memory_optimized.cpp:2085-2086), so the
+// energies and counters are the class's; CCSD_VARIANT_CCSD gives the CCSD
+// equations of the reference's dense CCSD1.  Failures are
 // reported with ccsd_gb300::Error (status code + message); the reference
 // prints and keeps going instead.
 #ifndef CCSD_GB300_HPP
@@ -50,10 +54,12 @@ class CCSD_Memory_optimized {
     // `problem` pointers must stay valid for the constructor only: the
     // integrals are copied to the device here.
     explicit CCSD_Memory_optimized(const ccsd_problem &problem, double E_HF = 0.0,
-                                   int precision = CCSD_PREC_FP64)
+                                   int precision = CCSD_PREC_FP64,
+                                   int variant = CCSD_VARIANT_MEMORY_OPTIMIZED)
         : E_HF_(E_HF), nocc_(problem.nocc), nvir_(problem.nvir) {
         ccsd_default_options(&opts_);
         opts_.precision = precision;
+        opts_.variant = variant;
         check(ccsd_create(&problem, &opts_, &h_));
         n_Electrons = 2 * nocc_;
         unocc_orb = 2 * nvir_;

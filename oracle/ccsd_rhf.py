@@ -19,6 +19,15 @@ Off-diagonal Fock blocks are treated exactly here; the reference adds
 matrix is a parity case.  As in the reference driver the energy omits the
 f_ia t_i^a term (``ccsd_memory_optimized.cpp:646``).
 
+variant="memory_optimized" iterates the map of the reference's class
+CCSD_Memory_optimized as written instead of the CCSD equations: its
+Fill_t2_new contracts the occupied Fock intermediate transposed,
+R_ij^ab += sum_k t_jk^ab F_ik - sum_k t_ik^ab F_jk, in all six spin cases
+(``ccsd_memory_optimized.cpp:2085-2086, 2143-2144, 2193-2194, 2269-2270,
+2324-2325, 2375-2376``: ``D2.row(i/2)`` where ``D2(k, i)`` holds F_ki), while
+its T1 equation keeps F_ki (``:2444``).  In the closed-shell form this is
+Loo'[i,k] in place of Loo'[k,i] in the T2 residual.
+
 Index conventions: t1[i, a], t2[i, j, a, b] with t2[i,j,a,b] = t2[j,i,b,a];
 integral blocks in chemist notation, e.g. ovov[i,a,j,b] = (ia|jb).
 """
@@ -65,7 +74,10 @@ class Blocks:
 
 
 class RHFCCSD:
-    def __init__(self, fock: np.ndarray, nocc: int, eri=None, df=None, with_vvvv=True):
+    def __init__(self, fock: np.ndarray, nocc: int, eri=None, df=None, with_vvvv=True, variant="ccsd"):
+        if variant not in ("ccsd", "memory_optimized"):
+            raise ValueError("variant must be 'ccsd' or 'memory_optimized'")
+        self.variant = variant
         self.o = nocc
         self.n = fock.shape[0]
         self.v = self.n - nocc
@@ -172,7 +184,10 @@ class RHFCCSD:
         Z = np.einsum("kdac,ijcd->ijka", ovvv, tau, **ES)           # sum_cd (ac|kd) tau_ij^cd
         R2 -= P(np.einsum("ijka,kb->ijab", Z, t1, **ES))
         R2 += P(np.einsum("ac,ijcb->ijab", Lvv_p, t2, **ES))
-        R2 -= P(np.einsum("ki,kjab->ijab", Loo_p, t2, **ES))
+        if self.variant == "memory_optimized":  # F_ik, ccsd_memory_optimized.cpp:2085-2086
+            R2 -= P(np.einsum("ik,kjab->ijab", Loo_p, t2, **ES))
+        else:
+            R2 -= P(np.einsum("ki,kjab->ijab", Loo_p, t2, **ES))
         R2 += P(np.einsum("akic,kjcb->ijab", 2.0 * Wvoov - Wvovo.transpose(0, 1, 3, 2), t2, **ES))
         R2 -= P(np.einsum("akic,kjbc->ijab", Wvoov, t2, **ES))
         R2 -= P(np.einsum("bkci,kjac->ijab", Wvovo, t2, **ES))

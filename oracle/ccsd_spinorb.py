@@ -33,6 +33,13 @@ Equations: the reference's dense spin-orbital CCSD, ``CCSDT::Calc_Energy`` with
 * CCSDT (``Method_Nr == 6``): CCSDT-4 with T3 terms in X1/X2, dressed X3/X4/X6 and
   the X7/X8 terms (``triples``), including the reference's X3 loop as written.
 
+variant="memory_optimized" (CCSD only) is the map of the reference's class
+CCSD_Memory_optimized as written: its Fill_t2_new contracts the F_mi
+intermediate transposed, + sum_k t_jk^ab F_ik - sum_k t_ik^ab F_jk, in all six
+spin cases (``ccsd_memory_optimized.cpp:2085-2086, 2143-2144, 2193-2194,
+2269-2270, 2324-2325, 2375-2376``: ``D2.row(i/2)`` with ``D2(k, i)`` = F_ki);
+its T1 equation keeps F_ki (``:2444``).
+
 Driver semantics follow ``CCSD_Memory_optimized::CCSD``
 (``ccsd_memory_optimized.cpp:473-557``): E = 1/4 sum <ij||ab> tau_ij^ab with
 the f_ia t_i^a term dropped (``:646``); ``iter`` starts at 1, each pass adds 1,
@@ -75,12 +82,16 @@ def spin_orbital_fock(fock: np.ndarray) -> np.ndarray:
 
 
 class SpinOrbitalCCSD:
-    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1, x3_as_written: bool = True):
+    def __init__(self, fock: np.ndarray, eri: np.ndarray, nocc: int, method: int = -1, x3_as_written: bool = True,
+                 variant: str = "ccsd"):
         """fock: spatial n x n; eri: spatial chemist (pq|rs); nocc spatial;
         method: -1 = CCSD ("CCSD1"), 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2, 4 = CCSDT-3,
         5 = CCSDT-4, 6 = CCSDT (the reference's Method_Nr)."""
         if method not in (-1, 1, 2, 3, 4, 5, 6):
             raise ValueError("method must be -1 (CCSD1) or 1-6 (CCSDT-1a, -1b, -2, -3, -4, CCSDT)")
+        if variant not in ("ccsd", "memory_optimized") or (variant != "ccsd" and method != -1):
+            raise ValueError("variant must be 'ccsd', or 'memory_optimized' with method -1")
+        self.variant = variant
         self.method = method
         # CCSDT's X3 tau term: the reference's loop (e fixed at the first virtual) or the
         # sum over all (d, e) that the equations state
@@ -303,8 +314,8 @@ class SpinOrbitalCCSD:
               + 0.5 * np.einsum("abkl,ijkl->abij", tau, W1, **ES)
               - np.einsum("bk,akij->abij", t1, W2, **ES)
               + np.einsum("ak,bkij->abij", t1, W2, **ES)
-              + np.einsum("abjk,ki->abij", t2, D2, **ES)
-              - np.einsum("abik,kj->abij", t2, D2, **ES)
+              + np.einsum("abjk,ki->abij", t2, D2 if self.variant == "ccsd" else D2.T, **ES)
+              - np.einsum("abik,kj->abij", t2, D2 if self.variant == "ccsd" else D2.T, **ES)
               + ring - ring.transpose(1, 0, 2, 3) - ring.transpose(0, 1, 3, 2)
               + ring.transpose(1, 0, 3, 2)
               - np.einsum("bcij,ac->abij", t2, D3, **ES)

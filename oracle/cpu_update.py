@@ -1,0 +1,257 @@
+"""Complete FP64 amplitude updates on the host cores (TEST INFRASTRUCTURE ONLY).
+
+The timed CPU implementation of ``bench.py`` (its ``cpu_baseline`` object and
+the ``--impl reference`` arm).  The reference's own CCSD keeps spin-orbital
+arrays that cannot hold the nocc = 24 / nvir = 300 benchmark system (the v^4
+spin-orbital block alone would be ~1 TB) and it cannot be compiled on the GPU
+host (its sources are not there), so the timed implementation is this
+repository's FP64 closed-shell restatement of the same map
+(``oracle.ccsd_rhf.RHFCCSD.residual``, the Jacobi map of
+``ccsd_memory_optimized.cpp:513-557`` over spatial orbitals), written for the
+host's BLAS:
+
+* every step is one whole update -- residual, denominators, DIIS extrapolation
+  and energy -- with no term sampled or skipped;
+* every o^3 v^3 and o^2 v^4 term is a matrix product on numpy's BLAS, all host
+  threads; the particle-particle ladder runs in the same pair form as the GPU
+  engine (S+ = tau+ W+^T over c >= d, S- = tau- W-^T over c > d: a quarter of
+  2 o^2 v^4), on W+/W- built once from the DF factors;
+* the integral blocks and W+/W- are built once, outside the timed steps, as the
+  GPU engine builds them in ccsd_create.
+
+``residual`` equals ``RHFCCSD.residual`` to rounding (tests/test_oracle.py).
+"""
+from __future__ import annotations
+
+import os
+import time
+
+import numpy as np
+
+
+def cores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+class FullUpdate:
+    """Closed-shell CCSD from a diagonal-or-not Fock matrix and DF factors
+    B[Q][p][q]; t1[i,a], t2[i,j,a,b] as in ``oracle.ccsd_rhf``."""
+
+    def __init__(self, fock: np.ndarray, nocc: int, df: np.ndarray, diis_size: int = 6, diis_start: int = 2):
+        o = nocc
+        n = fock.shape[0]
+        v = n - o
+        self.o, self.v = o, v
+        self.f_oo = np.ascontiguousarray(fock[:o, :o])
+        self.f_vv = np.ascontiguousarray(fock[o:, o:])
+        self.f_ov = np.ascontiguousarray(fock[:o, o:])
+        self.eo, self.ev = np.diag(fock)[:o].copy(), np.diag(fock)[o:].copy()
+        self.d1 = self.eo[:, None] - self.ev[None, :]
+        self.d2 = self.d1[:, None, :, None] + self.d1[None, :, None, :]
+        naux = df.shape[0]
+        bo = np.ascontiguousarray(df[:, :o, :o]).reshape(naux, o * o)
+        bov = np.ascontiguousarray(df[:, :o, o:]).reshape(naux, o * v)
+        bvv = np.ascontiguousarray(df[:, o:, o:])
+        bvv2 = bvv.reshape(naux, v * v)
+        self.ovov = (bov.T @ bov).reshape(o, v, o, v)
+        self.oovv = (bo.T @ bvv2).reshape(o, o, v, v)
+        self.ovoo = (bov.T @ bo).reshape(o, v, o, o)
+        self.oooo = (bo.T @ bo).reshape(o, o, o, o)
+        self.ovvv = (bov.T @ bvv2).reshape(o, v, v, v)
+        ovov = self.ovov
+        self.Lovov = 2.0 * ovov - ovov.transpose(0, 3, 2, 1)                    # [k,c,l,d]
+        self.LovovT = np.ascontiguousarray(self.Lovov.transpose(0, 2, 1, 3))      # [k,l,c,d]
+        self.LovovC = np.ascontiguousarray(self.Lovov.transpose(1, 0, 2, 3))      # [c,k,l,d]
+        self.ovovT = np.ascontiguousarray(ovov.transpose(0, 2, 1, 3))             # [i,j,a,b] = (ia|jb)
+        self.ovovX = np.ascontiguousarray(ovov.transpose(0, 3, 2, 1))             # [l,d,k,c] = (lc|kd)
+        self.Lovoo = 2.0 * self.ovoo - self.ovoo.transpose(2, 1, 0, 3)           # [l,c,k,i]
+        self._build_pairs(bvv)
+        self.diis_size, self.diis_start = diis_size, diis_start
+        self.t1 = np.zeros((o, v))
+        self.t2 = self.ovovT / self.d2
+        self.updates = 0
+        self._hist = []
+
+    # ---- particle-particle ladder in pair form --------------------------------
+    def _build_pairs(self, bvv):
+        """W+[ab,cd] = (ac|bd) + (ad|bc) (c > d), (ac|bc) (c = d) over a >= b, c >= d;
+        W-[ab,cd] = (ac|bd) - (ad|bc) over a > b, c > d; rows built a at a time."""
+        v = self.v
+        naux = bvv.shape[0]
+        tc, td = np.tril_indices(v)
+        sc, sd = np.tril_indices(v, -1)
+        Tv, Tmv = tc.size, sc.size
+        self.Wp = np.empty((Tv, Tv))
+        self.Wm = np.empty((Tmv, Tmv))
+        diag = tc == td
+        bflat = bvv.reshape(naux, v * v)
+        for a in range(v):
+            # G[b, c, d] = (ac|bd) for b <= a
+            g = (bvv[:, a, :].T @ bflat[:, :(a + 1) * v]).reshape(v, a + 1, v).transpose(1, 0, 2)
+            s = g + g.transpose(0, 2, 1)
+            rows = s[:, tc, td]
+            rows[:, diag] *= 0.5
+            r0 = a * (a + 1) // 2
+            self.Wp[r0:r0 + a + 1] = rows
+            if a > 0:
+                m0 = a * (a - 1) // 2
+                self.Wm[m0:m0 + a] = (g[:a] - g[:a].transpose(0, 2, 1))[:, sc, sd]
+        o = self.o
+        self._otri = np.tril_indices(o)
+        self._ostr = np.tril_indices(o, -1)
+        self._vtri = (tc, td)
+        self._vstr = (sc, sd)
+        # unpack maps: tri(max, min) / stri(max, min) and the sign of the antisymmetric half
+        def maps(m):
+            p = np.arange(m)
+            hi, lo = np.maximum(p[:, None], p[None, :]), np.minimum(p[:, None], p[None, :])
+            tri = hi * (hi + 1) // 2 + lo
+            stri = np.where(hi > lo, hi * (hi - 1) // 2 + lo, 0)
+            sgn = np.sign(p[:, None] - p[None, :]).astype(np.float64)
+            return tri, stri, sgn
+        self._otri_map, self._ostr_map, self._osgn = maps(o)
+        self._vtri_map, self._vstr_map, self._vsgn = maps(v)
+
+    def ladder(self, tau):
+        """sum_cd (ac|bd) tau[i,j,c,d] through the pair forms."""
+        tsw = tau.transpose(0, 1, 3, 2)
+        tji = tau.transpose(1, 0, 3, 2)
+        plus = 0.25 * (tau + tsw + tji + tji.transpose(0, 1, 3, 2))
+        minus = 0.25 * (tau - tsw + tji - tji.transpose(0, 1, 3, 2))
+        oi, oj = self._otri
+        si, sj = self._ostr
+        tc, td = self._vtri
+        sc, sd = self._vstr
+        taup = plus[oi, oj][:, tc, td]
+        taum = minus[si, sj][:, sc, sd]
+        Sp = taup @ self.Wp.T
+        Sm = taum @ self.Wm.T
+        R = Sp[self._otri_map[:, :, None, None], self._vtri_map[None, None, :, :]]
+        if Sm.size:
+            R += (self._osgn[:, :, None, None] * self._vsgn[None, None, :, :]
+                  * Sm[self._ostr_map[:, :, None, None], self._vstr_map[None, None, :, :]])
+        return R
+
+    # ---- the residual numerators (diagonal Fock moved to the denominators) -----
+    def residual(self, t1, t2):
+        o, v = self.o, self.v
+        ov = o * v
+        ovov, oovv, ovoo, oooo, ovvv = self.ovov, self.oovv, self.ovoo, self.oooo, self.ovvv
+        fov = self.f_ov
+        tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+        tau_r = tau.reshape(o * o, v * v)
+
+        Foo = self.f_oo + self.LovovT.reshape(o, -1) @ tau.reshape(o, -1).T
+        Fvv = self.f_vv - np.ascontiguousarray(tau.transpose(2, 0, 1, 3)).reshape(v, -1) @ \
+            self.LovovC.reshape(v, -1).T
+        Fov = fov + (self.Lovov.reshape(ov, ov) @ t1.ravel()).reshape(o, v)
+        Loo = (Foo + fov @ t1.T + np.einsum("lcki,lc->ki", self.Lovoo, t1, optimize=True))
+        # sum_kd (2 (kd|ac) - (kc|ad)) t1[k,d]
+        Lvv = Fvv - t1.T @ fov
+        Lvv += (t1.ravel() @ ovvv.reshape(ov, v * v)).reshape(v, v) * 2.0
+        for k in range(o):                                   # (kc|ad) t1[k,d] -> [c, a]
+            Lvv -= (ovvv[k].reshape(v * v, v) @ t1[k]).reshape(v, v).T
+        Foo_p = Foo - np.diag(self.eo)
+        Fvv_p = Fvv - np.diag(self.ev)
+        Loo_p = Loo - np.diag(self.eo)
+        Lvv_p = Lvv - np.diag(self.ev)
+
+        # ---- T1 --------------------------------------------------------------
+        R1 = (fov - 2.0 * (t1 @ fov.T) @ t1 + t1 @ Fvv_p.T - Foo_p.T @ t1
+              + np.einsum("kc,kica->ia", Fov, 2.0 * t2 - t2.transpose(1, 0, 2, 3), optimize=True)
+              + (t1 @ Fov.T) @ t1
+              + 2.0 * np.einsum("kcia,kc->ia", ovov, t1, optimize=True) - np.einsum("kiac,kc->ia", oovv, t1, optimize=True))
+        # + sum_kcd (2 (kd|ac) - (kc|ad)) tau[i,k,c,d]
+        for k in range(o):
+            g = ovvv[k]                                            # g[d, a, c] = (kd|ac)
+            L = 2.0 * g.transpose(2, 0, 1) - g.transpose(0, 2, 1)  # L[c, d, a] = 2 (kd|ac) - (kc|ad)
+            R1 += tau[:, k].reshape(o, v * v) @ L.reshape(v * v, v)
+        R1 -= np.einsum("lcki,klac->ia", self.Lovoo, tau, optimize=True)
+
+        # ---- intermediates ---------------------------------------------------
+        Woooo = (oooo.transpose(0, 2, 1, 3) + np.einsum("lcki,jc->klij", ovoo, t1, optimize=True)
+                 + np.einsum("kclj,ic->klij", ovoo, t1, optimize=True)
+                 + (self.ovovT.reshape(o * o, v * v) @ tau_r.T).reshape(o, o, o, o))
+        # Wvoov and Wvovo stored as [i, a, k, c] (W_akic, W_akci)
+        t2_iald = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)   # [(i,a),(l,d)] = t2[i,l,a,d]
+        t2_ilda = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)   # [(i,a),(l,d)] = t2[i,l,d,a]
+        t1t1 = (t1[:, None, None, :] * t1.T[None, :, :, None]).reshape(ov, ov)      # t1[i,d] t1[l,a]
+        th1 = t2_iald - 0.5 * t2_ilda - t1t1
+        th2 = 0.5 * t2_ilda + t1t1
+        Wvoov = ovov.reshape(ov, ov).copy()                                         # (ia|kc) = (ai|kc)
+        Wvoov += (ovvv.reshape(o * v * v, v) @ t1.T).reshape(o, v, v, o).transpose(3, 2, 0, 1).reshape(ov, ov)
+        Wvoov -= np.einsum("kcli,la->iakc", ovoo, t1, optimize=True).reshape(ov, ov)
+        Wvoov += th1 @ ovov.reshape(ov, ov)
+        Wvoov -= 0.5 * (t2_iald @ self.ovovX.reshape(ov, ov))
+        Wvovo = oovv.transpose(1, 2, 0, 3).reshape(ov, ov).copy()                  # (ki|ac)
+        for k in range(o):                                                         # sum_d (kd|ac) t1[i,d]
+            Wvovo.reshape(o, v, o, v)[:, :, k, :] += (t1 @ ovvv[k].reshape(v, v * v)).reshape(o, v, v)
+        Wvovo -= np.einsum("lcki,la->iakc", ovoo, t1, optimize=True).reshape(ov, ov)
+        Wvovo -= th2 @ self.ovovX.reshape(ov, ov)
+
+        # ---- T2 --------------------------------------------------------------
+        def P(x):
+            return x + x.transpose(1, 0, 3, 2)
+
+        X = (ovvv.reshape(o * v * v, v) @ t1.T).reshape(o, v, v, o).transpose(0, 3, 1, 2)
+        Vk = (oovv.reshape(o * o * v, v) @ t1.T).reshape(o, o, v, o)               # [k,i,b,j]
+        X = X - (t1.T @ Vk.reshape(o, -1)).reshape(v, o, v, o).transpose(1, 3, 0, 2)
+        tmpB = (np.einsum("kcia,jc->akij", ovov, t1, optimize=True) + ovoo.transpose(1, 3, 0, 2))   # [a,k,i,j]
+        Y = np.einsum("akij,kb->ijab", tmpB, t1, optimize=True)
+        R2 = self.ovovT.copy()
+        R2 += P(X - Y)
+        R2 += (Woooo.reshape(o * o, o * o).T @ tau_r).reshape(o, o, v, v)
+        R2 += self.ladder(tau)
+        Z = np.empty((o * o, o, v))                                                # [(i,j), k, a]
+        for k in range(o):
+            Z[:, k, :] = tau_r @ np.ascontiguousarray(ovvv[k].transpose(1, 2, 0)).reshape(v, v * v).T
+        R2 -= P((Z.transpose(0, 2, 1).reshape(o * o * v, o) @ t1).reshape(o, o, v, v))
+        R2 += P(np.matmul(Lvv_p, t2))
+        R2 -= P((Loo_p.T @ t2.reshape(o, -1)).reshape(o, o, v, v))
+        Wa = 2.0 * Wvoov - Wvovo
+        t2_kcjb = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)   # t2[k,j,c,b]
+        t2_kcjb2 = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)  # t2[k,j,b,c]
+        ring = (Wa @ t2_kcjb - Wvoov @ t2_kcjb2).reshape(o, v, o, v).transpose(0, 2, 1, 3)
+        ring = ring - (Wvovo @ t2_kcjb2).reshape(o, v, o, v).transpose(0, 2, 3, 1)
+        R2 += P(ring)
+        return R1, R2
+
+    def energy(self, t1, t2):
+        tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+        L = 2.0 * self.ovovT - self.ovovT.transpose(0, 1, 3, 2)
+        return float(np.vdot(L, tau))
+
+    def _diis(self, t1, t2, t1_old, t2_old):
+        """Pulay extrapolation over the last diis_size (T, T - T_old) pairs."""
+        if not self.diis_size:
+            return t1, t2
+        self._hist.append((t1.copy(), t2.copy(), t1 - t1_old, t2 - t2_old))
+        if len(self._hist) > self.diis_size:
+            self._hist.pop(0)
+        if self.updates < self.diis_start or len(self._hist) < 2:
+            return t1, t2
+        m = len(self._hist)
+        B = -np.ones((m + 1, m + 1))
+        B[m, m] = 0.0
+        for i in range(m):
+            for j in range(i, m):
+                B[i, j] = B[j, i] = (np.vdot(self._hist[i][2], self._hist[j][2])
+                                     + np.vdot(self._hist[i][3], self._hist[j][3]))
+        rhs = np.zeros(m + 1)
+        rhs[m] = -1.0
+        try:
+            c = np.linalg.solve(B, rhs)[:m]
+        except np.linalg.LinAlgError:
+            return t1, t2
+        return (sum(ci * h[0] for ci, h in zip(c, self._hist)), sum(ci * h[1] for ci, h in zip(c, self._hist)))
+
+    def step(self) -> dict:
+        """One whole update; returns its wall-clock seconds and the new energy."""
+        t0 = time.perf_counter()
+        R1, R2 = self.residual(self.t1, self.t2)
+        t1n, t2n = R1 / self.d1, R2 / self.d2
+        self.updates += 1
+        t1n, t2n = self._diis(t1n, t2n, self.t1, self.t2)
+        self.t1, self.t2 = t1n, t2n
+        e = self.energy(t1n, t2n)
+        return dict(seconds=time.perf_counter() - t0, e_corr=e)

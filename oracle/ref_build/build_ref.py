@@ -11,18 +11,21 @@ directory shim/x/y.  Flags: -O2 and -ftrivial-auto-var-init=zero, which gives
 the uninitialised `double temp` read in the reference's W_4 build
 (ccsd_memory_optimized.cpp:4789,4837) the value 0 it has on the even path.
 
-    python -m oracle.ref_build.build_ref        # builds ref_synthetic, ref_h2o and ref_ints
+    python -m oracle.ref_build.build_ref        # builds ref_synthetic, ref_probe, ref_h2o and ref_ints
+
+The reference tree is read from $CCSD_REFERENCE_DIR, default /root/reference.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
+import os
 import subprocess
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-REFERENCE = Path("/root/reference")
+REFERENCE = Path(os.environ.get("CCSD_REFERENCE_DIR", "/root/reference"))
 SHIM = HERE / "shim"
 FLAGS = ["-std=c++17", "-O2", "-ftrivial-auto-var-init=zero", "-w",
          "-I", str(SHIM / "x" / "y"), "-I", str(SHIM), "-I", str(REFERENCE)]
@@ -47,12 +50,11 @@ def build(quiet: bool = False) -> bool:
         return False
     OUT.mkdir(exist_ok=True)
     jobs = [(REFERENCE / f"{s}.cpp", OUT / f"{s}.o") for s in COMMON + SCF]
-    jobs += [(HERE / "ref_synthetic.cpp", OUT / "ref_synthetic.o"), (HERE / "ref_h2o.cpp", OUT / "ref_h2o.o"),
-             (HERE / "ref_ints.cpp", OUT / "ref_ints.o")]
+    jobs += [(HERE / f"{d}.cpp", OUT / f"{d}.o") for d in ("ref_synthetic", "ref_probe", "ref_h2o", "ref_ints")]
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(lambda a: _compile(*a), jobs))
     common = [str(OUT / f"{s}.o") for s in COMMON]
-    for exe, extra in (("ref_synthetic", ["ref_synthetic.o"]),
+    for exe, extra in (("ref_synthetic", ["ref_synthetic.o"]), ("ref_probe", ["ref_probe.o"]),
                        ("ref_h2o", ["ref_h2o.o"] + [f"{s}.o" for s in SCF]),
                        ("ref_ints", ["ref_ints.o"] + [f"{s}.o" for s in SCF])):
         r = subprocess.run(["g++", "-o", str(OUT / exe), *[str(OUT / e) for e in extra], *common],
@@ -60,7 +62,7 @@ def build(quiet: bool = False) -> bool:
         if r.returncode != 0:
             raise RuntimeError(f"linking {exe} failed:\n{r.stderr[-4000:]}")
     if not quiet:
-        print(f"built {OUT / 'ref_synthetic'}, {OUT / 'ref_h2o'} and {OUT / 'ref_ints'}")
+        print(f"built ref_synthetic, ref_probe, ref_h2o and ref_ints in {OUT}")
     return True
 
 

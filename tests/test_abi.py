@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_abi.Problem) == 6 * 4 + 4 * 8 + 8  # nfrozen (int32) padded to 8
-    assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8 + 2 * 8  # + t1_start, t2_start
+    assert C.sizeof(_abi.Options) == 2 * 8 + 8 * 4 + 8 + 2 * 8 + 8  # + t1_start, t2_start, variant (padded)
     assert C.sizeof(_abi.Result) == 2 * 8 + 2 * 4 + 4 * 8 + 2 * 4 + 8
 
 

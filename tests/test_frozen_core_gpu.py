@@ -72,7 +72,7 @@ def test_frozen_core_h2o_matches_oracle():
     assert cg.frozen_core_count([8.0, 1.0, 1.0]) == 1
     mo = np.einsum("pqrs,pi,qj,rk,sl->ijkl", ao, c, c, c, c, optimize=True)
     ref = RHFCCSD(fock[1:, 1:], nocc - 1, eri=mo[1:, 1:, 1:, 1:]).run(toler=1e-10)
-    cc = cg.CCSD_Memory_optimized(fock, nocc, ao_eri=ao, mo_coeff=c, nfrozen=1)
+    cc = cg.CCSD_Memory_optimized(fock, nocc, ao_eri=ao, mo_coeff=c, nfrozen=1, variant="ccsd")
     cc.CCSD(1e-10, False)
     assert cc.n_Electrons == 2 * (nocc - 1)
     assert cc.iter == ref["iter"]

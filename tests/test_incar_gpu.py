@@ -31,9 +31,14 @@ def test_incar_hf():
 def test_incar_ccsd_and_units():
     d, h = _inputs()
     basis = g94_from_fixture(d)
+    # "CCSD" runs the memory-optimised class in the reference (initializer.cpp:191-195)
     r = cg.run_incar(incar_text(d, "CCSD", -10), basis)
-    assert r["cc_iter"] == int(h["ref_ccsd1_iter"])
-    assert abs(r["energy"] - (float(h["e_hf"]) + float(h["ref_ccsd1_e_corr"]))) < 1e-9
+    assert r["cc_iter"] == int(h["ref_iter"])
+    assert abs(r["energy"] - float(h["ref_e_total"])) < 1e-9
+    # "CCSD1" runs its dense spin-orbital CCSD (initializer.cpp:98-103)
+    r1 = cg.run_incar(incar_text(d, "CCSD1", -10), basis)
+    assert r1["cc_iter"] == int(h["ref_ccsd1_iter"])
+    assert abs(r1["energy"] - (float(h["e_hf"]) + float(h["ref_ccsd1_e_corr"]))) < 1e-9
     # the same molecule in angstrom
     ra = cg.run_incar(incar_text(d, "CCSD", -10, angstrom=True), basis)
     assert abs(ra["energy"] - r["energy"]) < 1e-9

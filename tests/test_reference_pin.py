@@ -7,11 +7,14 @@ reference sources compiled unchanged):
 
 The reference has two CCSD implementations.  Its dense spin-orbital CCSD
 (CCSDT::Calc_Energy with method -1, "CCSD1") agrees with the oracle to
-rounding on every case.  Its memory-optimised class (the "CCSD" method) agrees
-to rounding on weakly correlated systems but converges to a slightly
-different point once correlation is strong (|dE| up to 7.6e-9 on the sigma =
-0.3 synthetics, 5.2e-8 on H2O/STO-3G): its amplitudes already differ from the
-CCSD map after the first update, in directions the energy does not see."""
+rounding on every case.  Its memory-optimised class (the "CCSD" method)
+iterates a different map: Fill_t2_new contracts the occupied Fock
+intermediate transposed, sum_k t_jk^ab F_ik in place of sum_k t_jk^ab F_ki
+(ccsd_memory_optimized.cpp:2085-2086 and the five other spin cases).  The
+oracle's variant="memory_optimized" carries that one change and reproduces the
+class's map at arbitrary amplitudes (ref_probe), its energies and its counters;
+the CCSD map itself converges to points up to 7.6e-9 (sigma = 0.3 synthetics)
+and 5.2e-8 (H2O/STO-3G) away."""
 import json
 import subprocess
 from pathlib import Path
@@ -27,6 +30,7 @@ GOLD = Path(__file__).parent / "golden"
 RUNS = json.loads((GOLD / "reference_runs.json").read_text())
 H2O = sorted(GOLD.glob("h2o_*.npz"))
 REF_BIN = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_synthetic"
+PROBE_BIN = REF_BIN.parent / "ref_probe"
 
 
 def _system(c):
@@ -52,6 +56,72 @@ def test_oracle_vs_reference_memory_optimized(key):
     assert r["iter"] == c["mo"]["iter"]
     bound = 1e-13 if c["sigma"] <= 0.05 else 1e-8
     assert abs(r["e_corr"] - c["mo"]["e_corr"]) < bound
+
+
+@pytest.mark.parametrize("key", sorted(RUNS))
+def test_memory_optimized_variant_matches_reference_class(key):
+    """The located departure, on every synthetic fixture: the oracle with F_mi
+    transposed in T2 gives the class's energies and counters to 1e-12."""
+    c = RUNS[key]
+    fock, b = _system(c)
+    r = RHFCCSD(fock, c["nocc"], df=b, variant="memory_optimized").run(toler=10.0 ** c["log10_tol"])
+    assert r["iter"] == c["mo"]["iter"]
+    assert abs(r["e_corr"] - c["mo"]["e_corr"]) < 1e-12
+
+
+@pytest.mark.parametrize("path", H2O, ids=[p.stem for p in H2O])
+def test_memory_optimized_variant_matches_reference_class_on_h2o(path):
+    d, fock, mo = _h2o(path)
+    tol = 10.0 ** float(d["log10_tol"])
+    r = RHFCCSD(fock, int(d["nocc"]), eri=mo, variant="memory_optimized").run(toler=tol)
+    assert r["iter"] == int(d["ref_iter"])
+    assert abs(r["e_corr"] - float(d["ref_e_corr"])) < 1e-12
+    s = SpinOrbitalCCSD(fock, mo, int(d["nocc"]), variant="memory_optimized").run(toler=tol)
+    assert abs(s["e_corr"] - r["e_corr"]) < 1e-13
+
+
+def _so_amplitudes(t1s, t2s):
+    """Closed-shell t1[i,a], t2[i,j,a,b] as spin-orbital t1[A,I], t2[A,B,I,J]
+    (alpha/beta interleaved): t(AB,IJ) = d(sA,sI) d(sB,sJ) t2[i,j,a,b] - d(sA,sJ) d(sB,sI) t2[j,i,a,b]."""
+    o, v = t1s.shape
+    sa, si = np.arange(2 * v) % 2, np.arange(2 * o) % 2
+    pa, pi = np.arange(2 * v) // 2, np.arange(2 * o) // 2
+    t1 = t1s[np.ix_(pi, pa)].T * (sa[:, None] == si[None, :])
+    d = t2s[np.ix_(pi, pi, pa, pa)].transpose(2, 3, 0, 1)
+    m1 = (sa[:, None, None, None] == si[None, None, :, None]) & (sa[None, :, None, None] == si[None, None, None, :])
+    m2 = (sa[:, None, None, None] == si[None, None, None, :]) & (sa[None, :, None, None] == si[None, None, :, None])
+    return t1, d * m1 - d.transpose(0, 1, 3, 2) * m2
+
+
+@pytest.mark.skipif(not PROBE_BIN.exists(), reason="reference not built here (oracle/_ref)")
+@pytest.mark.parametrize("o,v,seed", [(3, 3, 5), (2, 4, 6), (3, 4, 7), (4, 3, 8)])
+def test_reference_class_map_at_arbitrary_amplitudes(tmp_path, o, v, seed):
+    """ref_probe runs one loop body of the reference class (its member functions,
+    compiled unchanged) at chosen T1/T2.  Its T1/T2 equal the oracle's
+    memory-optimised map to 1e-15 in every spin block, while the CCSD map is
+    off by > 1e-5: the transposed F_mi is the whole departure."""
+    eps = syn.orbital_energies(o, v, seed)
+    eri = syn.eri_from_df(syn.df_factors(o + v, 4 * (o + v), seed, sigma=0.3))
+    rng = np.random.default_rng(seed)
+    x = 0.05 * rng.standard_normal((o, o, v, v))
+    t1, t2 = _so_amplitudes(0.05 * rng.standard_normal((o, v)), x + x.transpose(1, 0, 3, 2))
+    pin, pamp, pout = tmp_path / "in.bin", tmp_path / "amps.bin", tmp_path / "out.bin"
+    with open(pin, "wb") as f:
+        np.array([o + v, o], dtype=np.int32).tofile(f)
+        eps.tofile(f)
+        np.ascontiguousarray(eri).tofile(f)
+    with open(pamp, "wb") as f:
+        np.array([2 * o, 2 * v], dtype=np.int32).tofile(f)
+        t1.tofile(f)
+        t2.tofile(f)
+    subprocess.run([str(PROBE_BIN), str(pin), str(pamp), str(pout)], capture_output=True, check=True)
+    V, O = 2 * v, 2 * o
+    raw = np.fromfile(pout, dtype=np.float64, offset=8, count=V * O + V * V * O * O)
+    r1, r2 = raw[:V * O].reshape(V, O), raw[V * O:].reshape(V, V, O, O)
+    mo1, mo2 = SpinOrbitalCCSD(np.diag(eps), eri, o, variant="memory_optimized").update(t1, t2)
+    c1, c2 = SpinOrbitalCCSD(np.diag(eps), eri, o).update(t1, t2)
+    assert np.abs(r1 - mo1).max() < 1e-15 and np.abs(r2 - mo2).max() < 1e-15
+    assert np.abs(r2 - c2).max() > 1e-5
 
 
 def _h2o(path):

@@ -62,3 +62,21 @@ def test_noalloc_rejects_oversized_operands():
     assert "64 MiB" in _abi.last_error()
     rc = _call("ccsd_gemm_noalloc", 0, A[:8, :8], B[:8, :8], out[:8, :8])
     assert rc == _abi.CCSD_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("name,prec", [("ccsd_gemm", 0), ("ccsd_gemm", 3), ("ccsd_gemm_noalloc", 3)])
+def test_empty_contraction_scales_c(name, prec):
+    """K = 0: nothing is contracted and C becomes beta * C (beta = 0 clears C,
+    NaN included; beta = 1 leaves it untouched)."""
+    dummy = torch.zeros(1, dtype=torch.float64, device="cuda")  # A and B are never read
+    for beta in (0.0, 1.0, -2.5):
+        C0 = torch.randn(40, 30, dtype=torch.float64, device="cuda")
+        C0[0, 0] = float("nan") if beta == 0.0 else C0[0, 0]
+        out = C0.clone()
+        M, N = 40, 30
+        torch.cuda.synchronize()
+        rc = getattr(_abi.lib(), name)(prec, M, N, 0, 0.7, C.c_void_p(dummy.data_ptr()), 0,
+                                       C.c_void_p(dummy.data_ptr()), 0, beta, C.c_void_p(out.data_ptr()), N, None)
+        assert rc == 0, _abi.last_error()
+        expect = torch.zeros_like(C0) if beta == 0.0 else beta * C0
+        assert torch.equal(out, expect)
