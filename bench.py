@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -104,11 +105,10 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"ccsd_bench_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -176,37 +176,65 @@ def ladder_traffic(nocc, nvir):
     return d["dram_bytes_per_ladder"] * (nvir / d["nvir"]) ** 4, d
 
 
-def cpu_sample(fock, df, nocc, steps=1):
-    from oracle.cpu_baseline import SampledUpdate, cores
-    s = SampledUpdate(fock, nocc, df, ladder_rows=3)
+def workload_config(args, world=1):
+    """The `config` object of both arms (the same workload, so the same dict)."""
+    o, v, q = args.nocc, args.nvir, args.naux
+    return dict(workload=f"synthetic closed-shell {args.method.upper()} nocc={o} nvir={v} naux={q} (seed "
+                         f"{WORKLOAD['seed']}), DIIS({WORKLOAD['diis']}), 1 step = 1 amplitude update",
+                precision=args.precision, l2="inputs larger than L2: split W+/W- planes "
+                f"{SLICES_PLANES.get(args.precision, 0) * 2 * (v * (v + 1) // 2) ** 2 * 2 / 1e9:.0f} GB "
+                "resident in HBM",
+                parallelism="replicas" if world > 1 else "single GPU")
+
+
+CPU_SAMPLE = ("complete FP64 amplitude updates (residual, denominators, DIIS(6), energy; no term sampled) of "
+              "the closed-shell restatement of the reference's CCSD map (oracle.cpu_update, numpy + OpenBLAS on "
+              "all host threads, pp ladder in the engine's pair form); integral blocks and W+/W- built once "
+              "outside the timed steps")
+
+
+def cpu_full_update(o, v, q, steps=1):
+    """Seconds of `steps` complete CPU updates at this workload (after one untimed set-up)."""
+    from oracle import synthetic as syn
+    from oracle.cpu_update import FullUpdate, cores
+    fock, df = syn.make_system(o, v, q, WORKLOAD["seed"])
+    t0 = time.perf_counter()
+    s = FullUpdate(fock, o, df, diis_size=WORKLOAD["diis"], diis_start=2)
+    setup = time.perf_counter() - t0
     res = [s.step() for _ in range(steps)]
-    return res, cores()
+    return res, setup, cores()
 
 
 def run_reference(args, rank, world):
-    import ccsd_parallel_gb300 as cg
+    """The CPU implementation of the path on the host cores: the oracle port (the
+    reference's sources are not on this host), on this arm's workload, every step
+    one complete update.  It maps none of this repository's libraries."""
     if rank != 0:
         return
-    fock, df = cg.make_synthetic(args.nocc, args.nvir, args.naux, WORKLOAD["seed"])
-    from oracle.cpu_baseline import SampledUpdate, cores
-    s = SampledUpdate(fock, args.nocc, df, ladder_rows=3)
+    from oracle import synthetic as syn
+    from oracle.cpu_update import FullUpdate, cores
+    fock, df = syn.make_system(args.nocc, args.nvir, args.naux, WORKLOAD["seed"])
+    t0 = time.perf_counter()
+    s = FullUpdate(fock, args.nocc, df, diis_size=WORKLOAD["diis"], diis_start=2)
+    setup = time.perf_counter() - t0
     for _ in range(args.warmup):
         s.step()
     times = [s.step()["seconds"] for _ in range(args.steps)]
     v = float(np.mean(times))
-    sample = (f"numpy FP64 closed-shell restatement of the reference update (oracle.ccsd_rhf); per step all "
-              f"residual terms except the pp ladder in full + the pp ladder on 3 of {args.nvir} virtual rows "
-              f"scaled x{args.nvir / 3:.0f}; integral blocks built once outside the timed region")
+    sample = f"{CPU_SAMPLE}; set-up {setup:.1f} s; {args.warmup} untimed + {args.steps} timed updates"
     line = dict(impl="reference", metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=v * 1e3, higher_is_better=False, scaling="weak",
-                vs_baseline=None, dtype="f64", data="synthetic",
-                config=dict(workload=f"synthetic closed-shell CCSD nocc={args.nocc} nvir={args.nvir} "
-                                     f"naux={args.naux}, 1 step = 1 amplitude update",
-                            note="the reference's spin-orbital arrays cannot hold this system; its CPU "
-                                 "update is timed through the FP64 restatement"),
+                vs_baseline=None, dtype="f64", data="synthetic", config=workload_config(args, world),
                 cpu_baseline=dict(value=v, unit=UNIT, cores=cores(), kind="port", sample=sample),
-                e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+                e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                tflops_alg=flops_per_update(args.nocc, args.nvir) / v / 1e12, e_corr=s.energy(s.t1, s.t2))
     print(json.dumps(line), flush=True)
+
+
+def flops_per_update(o, v):
+    """The fixed algorithmic count 2 o^2 v^4 + 4 o^4 v^2 + 8 o^3 v^3 (ccsd_flops_per_update)."""
+    o, v = float(o), float(v)
+    return 2 * o ** 2 * v ** 4 + 4 * o ** 4 * v ** 2 + 8 * o ** 3 * v ** 3
 
 
 def measure_extras(cg, fock, df, o, precision):
@@ -268,7 +296,7 @@ def measure_ccsdt1a(cg, precision, pk):
     size (nocc=4, nvir=16) the update time of the spin-orbital oracle on the
     host beside the GPU's."""
     from oracle.ccsd_spinorb import SpinOrbitalCCSD
-    from oracle.cpu_baseline import cores
+    from oracle.cpu_update import cores
     o, v = 6, 40
     O, V = 2 * o, 2 * v
     n3 = V ** 3 * O ** 3
@@ -461,12 +489,9 @@ def main():
 
     cpu = None
     if args.cpu_baseline and rank == 0:
-        res, ncores = cpu_sample(fock, df, o, steps=1)
+        res, setup, ncores = cpu_full_update(o, v, q, steps=1)
         cpu = dict(value=res[0]["seconds"], unit=UNIT, cores=ncores, kind="port",
-                   sample=(f"one update of the numpy FP64 restatement (oracle.ccsd_rhf) at this workload: "
-                           f"all terms except the pp ladder in full ({res[0]['rest_s']:.1f} s), the pp ladder "
-                           f"on 3 of {v} virtual rows ({res[0]['ladder_sample_s']:.1f} s, scaled "
-                           f"x{res[0]['ladder_scale']:.0f})"))
+                   sample=f"one {CPU_SAMPLE.replace('updates', 'update', 1)}; set-up {setup:.1f} s")
 
     extras = {}
     if args.extras and rank == 0:
@@ -482,12 +507,7 @@ def main():
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=K, warmup=W,
         ms_per_step=value * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
         dtype=f"bf16x{nprod}-products/fp32-acc + f64 ({args.precision})", data="synthetic",
-        config=dict(workload=f"synthetic closed-shell {args.method.upper()} nocc={o} nvir={v} naux={q} (seed "
-                             f"{WORKLOAD['seed']}), DIIS({WORKLOAD['diis']}), 1 step = 1 amplitude update",
-                    precision=args.precision, l2="inputs larger than L2: split W+/W- planes "
-                    f"{SLICES_PLANES.get(args.precision, 0) * 2 * (v * (v + 1) // 2) ** 2 * 2 / 1e9:.0f} GB "
-                    "resident in HBM",
-                    parallelism="replicas" if world > 1 else "single GPU"),
+        config=workload_config(args, world),
         tflops_alg=flops_upd / value / 1e12,
         e_corr=r["energies"][U], abs_dE_corr_vs_fp64=fp64.get("abs_dE_corr_vs_fp64"),
         **{k: val for k, val in fp64.items() if k != "abs_dE_corr_vs_fp64"},

@@ -154,6 +154,7 @@ SIGNATURES = {
     "ccsd_gemm_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p,
                                     C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,
                                     C.c_void_p]),
+    "ccsd_debug_stall_split_mma": (C.c_int, [C.c_uint64]),
 }
 
 _lib = None

@@ -366,6 +366,8 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
     grad_lean_vvvv_ = false;
     tape_ = nullptr;
     CCSD_CUDA(cudaStreamSynchronize(st_));
+    if (build_split_ && build_split_->error_status())
+        throw Error(CCSD_ERR_TIMEOUT, "split-precision kernel of the integral build reported a bounded-wait timeout");
     build_split_.reset();
     for (auto &b : keep_) reg(*b, false);
     tape_ = &res_tape;
@@ -475,6 +477,8 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
         double *a = adj_of(src->p);
         CCSD_CUDA(cudaMemcpy(dst, a, src->n * sizeof(double), cudaMemcpyDeviceToHost));
     };
+    if (split_ && split_->error_status())
+        throw Error(CCSD_ERR_TIMEOUT, "split-precision kernel of the Lambda sweep reported a bounded-wait timeout");
     fetch(out->d_eri, input_eri_);
     fetch(out->d_df, input_df_);
     fetch(out->d_mo_coeff, input_c_);

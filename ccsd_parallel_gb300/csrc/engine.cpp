@@ -109,6 +109,8 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     build_integrals(prob);
     build_derived();
     CCSD_CUDA(cudaStreamSynchronize(st_));
+    if (build_split_ && build_split_->error_status())
+        throw Error(CCSD_ERR_TIMEOUT, "split-precision kernel of the integral build reported a bounded-wait timeout");
     build_split_.reset();
     // the ladder reads W+ and W- (a gradient rebuilds (ac|bd) from the inputs); CCSDT-3
     // builds its spin-orbital <ab||cd> block from (ac|bd) and keeps it
@@ -894,6 +896,7 @@ void Engine::solve(ccsd_result *res) {
     // cudaMallocs cost tens of ms at the bench size); only the history restarts
     diis_count_ = diis_next_ = 0;
     std::fill(diis_b_.begin(), diis_b_.end(), 0.0);
+    if (split_) split_->clear_error();  // a time-out of an earlier solve does not carry over
     prof_.clear();
     prof_pending_.clear();
     prof_update_ms_ = 0.0;

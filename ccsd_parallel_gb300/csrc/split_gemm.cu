@@ -20,7 +20,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <string>
 
+#include "../../include/ccsd_gb300.h"
 #include "ptx.cuh"
 #include "split_gemm.h"
 
@@ -54,13 +56,36 @@ struct alignas(8) Bars {
     uint32_t tmem_base;
     int abort;
     int never;  // stays 0: a wait that must not be cut short by another role
+    int eb_min, eb_max;  // range of the tile's column-scale exponents (FP32 epilogue check)
 };
 
 // Behind the barriers: the tile's output column offsets and column scales, set
 // once by the epilogue warps instead of per element (a 3-level column view costs
 // tens of integer instructions per offset).
 __host__ __device__ constexpr size_t epi_offset() { return (sizeof(Bars) + 15) / 16 * 16; }
-__host__ __device__ constexpr size_t epi_bytes(int BN) { return (size_t)BN * (sizeof(int64_t) + sizeof(double)); }
+__host__ __device__ constexpr size_t epi_bytes(int BN) {
+    return (size_t)BN * (sizeof(int64_t) + sizeof(double) + sizeof(float));
+}
+
+// Binary exponent of a normal double (|x| in [2^e, 2^(e+1))); zero gives -1023.
+__device__ __forceinline__ int exp2_of(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7FF) - 1023;
+}
+
+// The FP32 epilogue (S <= 3) forms (I0 + F) * sA * sB * alpha in FP32 and
+// leaves one conversion and one FMA per element on the FP64 pipe, which runs
+// at 1/64 of the FP32 rate on this part.  Rounding the sum to FP32 adds at most
+// 2^-23 of |C_mn|, below split3's bound 2^-21 max|A_m| max|B_n| K.  A warp
+// whose scale products could leave [2^-100, 2^90] (so that a sum below 2^32
+// might overflow or a result become subnormal) keeps the FP64 epilogue.
+constexpr int kEpi32Lo = -100, kEpi32Hi = 90;
+
+// Failure injection (ccsd_debug_stall_split_mma): while non-zero, the MMA
+// thread of every CTA first waits on an mbarrier that no role arrives at before
+// its main loop (the drain barrier, whose first arrival is the final commit),
+// bounded by this many nanoseconds.  The wait gives up and the CTA leaves
+// through the time-out path of a real stall.
+__device__ unsigned long long g_stall_mma_ns = 0;
 
 }  // namespace
 
@@ -195,6 +220,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
         ptx::mbar_init(&bars->drain, 1);
         bars->abort = 0;
         bars->never = 0;
+        bars->eb_min = 1 << 20;
+        bars->eb_max = -(1 << 20);
         ptx::fence_barrier_init();
         ptx::prefetch_tmap(&tmA);
         ptx::prefetch_tmap(&tmB);
@@ -233,8 +260,10 @@ __global__ void __launch_bounds__(kThreads, MINB)
         }
     } else if (warp == 1) {
         if (lane == 0 && nkb > 0) {
+            const unsigned long long stall = g_stall_mma_ns;
+            const bool go = stall == 0 || ptx::mbar_wait(&bars->drain, 0, abort, gerr, 128, stall);
             bool first_rest = true;
-            for (int l = 0; l < nkb; ++l) {
+            for (int l = 0; go && l < nkb; ++l) {
                 const int st = l % NST, round = l / NST;
                 const int c = l / CHUNK_KB, b = c & 1;
                 const bool chunk_start = (l % CHUNK_KB) == 0;
@@ -276,10 +305,21 @@ __global__ void __launch_bounds__(kThreads, MINB)
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         int64_t *s_coff = (int64_t *)((unsigned char *)bars + epi_offset());
         double *s_sb = (double *)(s_coff + BN);
+        float *s_fsb = (float *)(s_sb + BN);
+        constexpr bool kEpi32 = S <= 3;
         for (int j = threadIdx.x - 64; j < BN; j += 128) {
             const int n = n0 + j;
+            const double sbn = n < N ? scaleB[n] : 0.0;
             s_coff[j] = n < N ? dim_off(C.col, (uint32_t)n) : -1;
-            s_sb[j] = n < N ? scaleB[n] : 0.0;
+            s_sb[j] = sbn;
+            if (kEpi32) {
+                s_fsb[j] = (float)sbn;
+                if (n < N) {
+                    const int e = exp2_of(sbn);
+                    atomicMin(&bars->eb_min, e);
+                    atomicMax(&bars->eb_max, e);
+                }
+            }
         }
         asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps only
         int32_t iacc[BN];
@@ -315,6 +355,14 @@ __global__ void __launch_bounds__(kThreads, MINB)
             const int64_t crow = mval ? dim_off(C.row, (uint32_t)m) : 0;
             const bool direct = J.wsz == nullptr;
             double *wsz = J.wsz;
+            // FP32 epilogue: the row factor sa (times alpha when writing C) as a float, if
+            // every scale product of this warp's rows stays in range
+            const double sa_out = direct ? sa * alpha : sa;
+            const int ea = exp2_of(sa_out);
+            const bool in_range = !mval || sa_out == 0.0 ||
+                                  (ea + bars->eb_min >= kEpi32Lo && ea + bars->eb_max <= kEpi32Hi);
+            const bool epi32 = kEpi32 && __all_sync(0xffffffffu, in_range);
+            const float fsa = (float)sa_out;
 #pragma unroll
             for (int g = 0; g < BN / 32; ++g) {
                 uint32_t r[32];
@@ -342,8 +390,18 @@ __global__ void __launch_bounds__(kThreads, MINB)
                     for (int j = 0; j < kCB; ++j) {
                         if (off[j] < 0) continue;
                         const int n = n0 + g * 32 + j0 + j;
-                        const double val = sa * s_sb[g * 32 + j0 + j] *
-                                           ((double)iacc[g * 32 + j0 + j] + (double)__uint_as_float(r[j0 + j]));
+                        const int jj = g * 32 + j0 + j;
+                        if (kEpi32 && epi32) {
+                            const float f = (__int2float_rn(iacc[jj]) + __uint_as_float(r[j0 + j])) * fsa *
+                                            s_fsb[jj];
+                            const double val = (double)f;
+                            if (direct)
+                                C.p[off[j]] = beta != 0.0 ? fma(beta, cold[j], val) : val;
+                            else
+                                wsz[(size_t)m * N + n] = val;
+                            continue;
+                        }
+                        const double val = sa * s_sb[jj] * ((double)iacc[jj] + (double)__uint_as_float(r[j0 + j]));
                         if (direct) {
                             double out = alpha * val;
                             if (beta != 0.0) out = fma(beta, cold[j], out);
@@ -947,6 +1005,8 @@ void SplitEngine::run(const SplitOperand &a, const SplitOperand &b, int M, int N
     split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
 }
 
+void SplitEngine::clear_error() { CCSD_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), st_)); }
+
 int SplitEngine::error_status() {
     int h = 0;
     CCSD_CUDA(cudaMemcpyAsync(&h, d_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -961,3 +1021,18 @@ size_t SplitEngine::cached_bytes() const {
 }
 
 }  // namespace ccsd
+
+namespace ccsd {
+void set_last_error(const std::string &msg);
+}
+
+extern "C" int ccsd_debug_stall_split_mma(uint64_t stall_ns) {
+    const unsigned long long v = stall_ns;
+    const cudaError_t e = cudaMemcpyToSymbol(ccsd::g_stall_mma_ns, &v, sizeof v);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ccsd::set_last_error(std::string("ccsd_debug_stall_split_mma: ") + cudaGetErrorString(e));
+        return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? CCSD_ERR_NO_DEVICE : CCSD_ERR_CUDA;
+    }
+    return CCSD_OK;
+}

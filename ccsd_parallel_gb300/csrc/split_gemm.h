@@ -69,6 +69,7 @@ class SplitEngine {
     }
     // Device error word (bounded waits that gave up); 0 when clean.
     int error_status();
+    void clear_error();
     size_t cached_bytes() const;
 
   private:

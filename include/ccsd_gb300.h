@@ -442,6 +442,18 @@ int ccsd_gemm_noalloc(int32_t precision, int32_t M, int32_t N, int32_t K, double
                       const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                       double *C, int64_t ldc, void *stream);
 
+/* Failure injection for tests; no counterpart in the reference, whose only
+ * failure handling is its 1000-iteration cap (ccsd_memory_optimized.cpp:42,553).
+ * While stall_ns > 0, the MMA thread of every split-precision contraction
+ * launched afterwards on the current device first waits on an mbarrier that
+ * nothing arrives at, for at most stall_ns nanoseconds.  The wait gives up and
+ * the kernel leaves through the path of a real device-side stall: the error
+ * word is set, the other roles stop, in-flight TMA loads are awaited and TMEM
+ * is freed, so the context stays usable.  ccsd_gemm and ccsd_solve then return
+ * CCSD_ERR_TIMEOUT.  ccsd_debug_stall_split_mma(0) restores normal operation;
+ * a later ccsd_solve on the same handle starts with a clean error word. */
+int ccsd_debug_stall_split_mma(uint64_t stall_ns);
+
 /* Seeded synthetic closed-shell system (host only, no GPU needed): diagonal
  * fock (n x n) with occupied U[-2,-0.3] / virtual U[0.1,3] energies, and
  * DF factors B[Q][p][q] = 0.05 z / sqrt(naux), z ~ N(0,1), symmetric in p,q.

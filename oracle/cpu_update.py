@@ -65,6 +65,14 @@ class FullUpdate:
         self.ovovT = np.ascontiguousarray(ovov.transpose(0, 2, 1, 3))             # [i,j,a,b] = (ia|jb)
         self.ovovX = np.ascontiguousarray(ovov.transpose(0, 3, 2, 1))             # [l,d,k,c] = (lc|kd)
         self.Lovoo = 2.0 * self.ovoo - self.ovoo.transpose(2, 1, 0, 3)           # [l,c,k,i]
+        # (k,l,c) x i layout of Lovoo for sum_klc Lovoo[l,c,k,i] tau[k,l,a,c]
+        self.LovooK = np.ascontiguousarray(self.Lovoo.transpose(2, 0, 1, 3)).reshape(o * o * v, o)
+        self.ovooA = np.ascontiguousarray(self.ovoo.transpose(0, 1, 3, 2)).reshape(o * v * o, o)  # [(k,c,i), l]
+        self.ovooB = np.ascontiguousarray(self.ovoo.transpose(1, 2, 3, 0)).reshape(v * o * o, o)  # [(c,k,i), l]
+        ovvv = self.ovvv
+        # [(k,c,d), a] = 2 (kd|ac) - (kc|ad); [(k,a), (c,d)] = (kd|ac)
+        self.LovvvR = (2.0 * ovvv.transpose(0, 3, 1, 2) - ovvv.transpose(0, 1, 3, 2)).reshape(o * v * v, v)
+        self.ovvvZ = np.ascontiguousarray(ovvv.transpose(0, 2, 3, 1)).reshape(o * v, v * v)
         self._build_pairs(bvv)
         self.diis_size, self.diis_start = diis_size, diis_start
         self.t1 = np.zeros((o, v))
@@ -99,6 +107,8 @@ class FullUpdate:
         o = self.o
         self._otri = np.tril_indices(o)
         self._ostr = np.tril_indices(o, -1)
+        # position of each strict pair i > j in the list of pairs i >= j (both row-major)
+        self._ostr_in_tri = np.searchsorted(self._otri[0] * o + self._otri[1], self._ostr[0] * o + self._ostr[1])
         self._vtri = (tc, td)
         self._vstr = (sc, sd)
         # unpack maps: tri(max, min) / stri(max, min) and the sign of the antisymmetric half
@@ -114,22 +124,22 @@ class FullUpdate:
 
     def ladder(self, tau):
         """sum_cd (ac|bd) tau[i,j,c,d] through the pair forms."""
+        o, v = self.o, self.v
         tsw = tau.transpose(0, 1, 3, 2)
         tji = tau.transpose(1, 0, 3, 2)
-        plus = 0.25 * (tau + tsw + tji + tji.transpose(0, 1, 3, 2))
-        minus = 0.25 * (tau - tsw + tji - tji.transpose(0, 1, 3, 2))
         oi, oj = self._otri
-        si, sj = self._ostr
         tc, td = self._vtri
         sc, sd = self._vstr
-        taup = plus[oi, oj][:, tc, td]
-        taum = minus[si, sj][:, sc, sd]
-        Sp = taup @ self.Wp.T
-        Sm = taum @ self.Wm.T
-        R = Sp[self._otri_map[:, :, None, None], self._vtri_map[None, None, :, :]]
-        if Sm.size:
-            R += (self._osgn[:, :, None, None] * self._vsgn[None, None, :, :]
-                  * Sm[self._ostr_map[:, :, None, None], self._vstr_map[None, None, :, :]])
+        a, b = tau[oi, oj], tsw[oi, oj]                    # [ij pair, c, d]: tau[ijcd], tau[ijdc]
+        c_, d_ = tji[oi, oj], tji.transpose(0, 1, 3, 2)[oi, oj]  # tau[jidc], tau[jicd]
+        taup = (0.25 * (a + b + c_ + d_))[:, tc, td]
+        taum = (0.25 * (a - b + c_ - d_))[self._ostr_in_tri][:, sc, sd]   # strict pairs i > j
+        Sp = taup @ self.Wp.T                              # [ij pair, ab pair]
+        R = Sp[:, self._vtri_map.ravel()].reshape(-1, v, v)[self._otri_map.ravel()].reshape(o, o, v, v)
+        if taum.size and sc.size:
+            Sm = taum @ self.Wm.T
+            U = (Sm[:, self._vstr_map.ravel()].reshape(-1, v, v) * self._vsgn)[self._ostr_map.ravel()]
+            R += U.reshape(o, o, v, v) * self._osgn[:, :, None, None]
         return R
 
     # ---- the residual numerators (diagonal Fock moved to the denominators) -----
@@ -140,15 +150,17 @@ class FullUpdate:
         fov = self.f_ov
         tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
         tau_r = tau.reshape(o * o, v * v)
+        # t2 as [(i,a),(l,d)]: t2[i,l,a,d] and t2[i,l,d,a]
+        t2_iald = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)
+        t2_ilda = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)
 
         Foo = self.f_oo + self.LovovT.reshape(o, -1) @ tau.reshape(o, -1).T
         Fvv = self.f_vv - np.ascontiguousarray(tau.transpose(2, 0, 1, 3)).reshape(v, -1) @ \
             self.LovovC.reshape(v, -1).T
         Fov = fov + (self.Lovov.reshape(ov, ov) @ t1.ravel()).reshape(o, v)
-        Loo = (Foo + fov @ t1.T + np.einsum("lcki,lc->ki", self.Lovoo, t1, optimize=True))
-        # sum_kd (2 (kd|ac) - (kc|ad)) t1[k,d]
-        Lvv = Fvv - t1.T @ fov
-        Lvv += (t1.ravel() @ ovvv.reshape(ov, v * v)).reshape(v, v) * 2.0
+        Loo = Foo + fov @ t1.T + np.einsum("lcki,lc->ki", self.Lovoo, t1, optimize=True)
+        # Lvv = Fvv - t1^T f + sum_kd (2 (kd|ac) - (kc|ad)) t1[k,d]
+        Lvv = Fvv - t1.T @ fov + 2.0 * (t1.ravel() @ ovvv.reshape(ov, v * v)).reshape(v, v)
         for k in range(o):                                   # (kc|ad) t1[k,d] -> [c, a]
             Lvv -= (ovvv[k].reshape(v * v, v) @ t1[k]).reshape(v, v).T
         Foo_p = Foo - np.diag(self.eo)
@@ -157,63 +169,55 @@ class FullUpdate:
         Lvv_p = Lvv - np.diag(self.ev)
 
         # ---- T1 --------------------------------------------------------------
+        t2_kica = t2_iald.reshape(o, v, o, v)                # [k,c,i,a] = t2[k,i,c,a]
         R1 = (fov - 2.0 * (t1 @ fov.T) @ t1 + t1 @ Fvv_p.T - Foo_p.T @ t1
-              + np.einsum("kc,kica->ia", Fov, 2.0 * t2 - t2.transpose(1, 0, 2, 3), optimize=True)
+              + 2.0 * (Fov.ravel() @ t2_kica.reshape(ov, ov)).reshape(o, v)
+              - (Fov.ravel() @ t2_kica.transpose(2, 1, 0, 3).reshape(ov, ov)).reshape(o, v)   # t2[i,k,c,a]
               + (t1 @ Fov.T) @ t1
-              + 2.0 * np.einsum("kcia,kc->ia", ovov, t1, optimize=True) - np.einsum("kiac,kc->ia", oovv, t1, optimize=True))
-        # + sum_kcd (2 (kd|ac) - (kc|ad)) tau[i,k,c,d]
-        for k in range(o):
-            g = ovvv[k]                                            # g[d, a, c] = (kd|ac)
-            L = 2.0 * g.transpose(2, 0, 1) - g.transpose(0, 2, 1)  # L[c, d, a] = 2 (kd|ac) - (kc|ad)
-            R1 += tau[:, k].reshape(o, v * v) @ L.reshape(v * v, v)
-        R1 -= np.einsum("lcki,klac->ia", self.Lovoo, tau, optimize=True)
+              + 2.0 * (t1.ravel() @ ovov.reshape(ov, ov)).reshape(o, v)
+              - np.einsum("kiac,kc->ia", oovv, t1, optimize=True))
+        R1 += tau.reshape(o, o * v * v) @ self.LovvvR       # sum_kcd (2 (kd|ac) - (kc|ad)) tau[i,k,c,d]
+        R1 -= (np.ascontiguousarray(tau.transpose(0, 1, 3, 2)).reshape(o * o * v, v).T @ self.LovooK).T
 
         # ---- intermediates ---------------------------------------------------
         Woooo = (oooo.transpose(0, 2, 1, 3) + np.einsum("lcki,jc->klij", ovoo, t1, optimize=True)
                  + np.einsum("kclj,ic->klij", ovoo, t1, optimize=True)
                  + (self.ovovT.reshape(o * o, v * v) @ tau_r.T).reshape(o, o, o, o))
-        # Wvoov and Wvovo stored as [i, a, k, c] (W_akic, W_akci)
-        t2_iald = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)   # [(i,a),(l,d)] = t2[i,l,a,d]
-        t2_ilda = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)   # [(i,a),(l,d)] = t2[i,l,d,a]
+        # Wvoov and Wvovo stored as [(i,a), (k,c)] (W_akic, W_akci)
         t1t1 = (t1[:, None, None, :] * t1.T[None, :, :, None]).reshape(ov, ov)      # t1[i,d] t1[l,a]
         th1 = t2_iald - 0.5 * t2_ilda - t1t1
         th2 = 0.5 * t2_ilda + t1t1
         Wvoov = ovov.reshape(ov, ov).copy()                                         # (ia|kc) = (ai|kc)
         Wvoov += (ovvv.reshape(o * v * v, v) @ t1.T).reshape(o, v, v, o).transpose(3, 2, 0, 1).reshape(ov, ov)
-        Wvoov -= np.einsum("kcli,la->iakc", ovoo, t1, optimize=True).reshape(ov, ov)
+        Wvoov -= (self.ovooA @ t1).reshape(o, v, o, v).transpose(2, 3, 0, 1).reshape(ov, ov)
         Wvoov += th1 @ ovov.reshape(ov, ov)
         Wvoov -= 0.5 * (t2_iald @ self.ovovX.reshape(ov, ov))
         Wvovo = oovv.transpose(1, 2, 0, 3).reshape(ov, ov).copy()                  # (ki|ac)
+        W4 = Wvovo.reshape(o, v, o, v)
         for k in range(o):                                                         # sum_d (kd|ac) t1[i,d]
-            Wvovo.reshape(o, v, o, v)[:, :, k, :] += (t1 @ ovvv[k].reshape(v, v * v)).reshape(o, v, v)
-        Wvovo -= np.einsum("lcki,la->iakc", ovoo, t1, optimize=True).reshape(ov, ov)
+            W4[:, :, k, :] += (t1 @ ovvv[k].reshape(v, v * v)).reshape(o, v, v)
+        Wvovo -= (self.ovooB @ t1).reshape(v, o, o, v).transpose(2, 3, 1, 0).reshape(ov, ov)
         Wvovo -= th2 @ self.ovovX.reshape(ov, ov)
 
-        # ---- T2 --------------------------------------------------------------
-        def P(x):
-            return x + x.transpose(1, 0, 3, 2)
-
-        X = (ovvv.reshape(o * v * v, v) @ t1.T).reshape(o, v, v, o).transpose(0, 3, 1, 2)
+        # ---- T2: R2 = (ia|jb) + Woooo tau + ladder + Rp + Rp^T (Rp^T[ijab] = Rp[jiba]) ----
+        Rp = (ovvv.reshape(o * v * v, v) @ t1.T).reshape(o, v, v, o).transpose(0, 3, 1, 2).copy()  # (ia|bc) t1[j,c]
         Vk = (oovv.reshape(o * o * v, v) @ t1.T).reshape(o, o, v, o)               # [k,i,b,j]
-        X = X - (t1.T @ Vk.reshape(o, -1)).reshape(v, o, v, o).transpose(1, 3, 0, 2)
+        Rp -= (t1.T @ Vk.reshape(o, -1)).reshape(v, o, v, o).transpose(1, 3, 0, 2)
         tmpB = (np.einsum("kcia,jc->akij", ovov, t1, optimize=True) + ovoo.transpose(1, 3, 0, 2))   # [a,k,i,j]
-        Y = np.einsum("akij,kb->ijab", tmpB, t1, optimize=True)
-        R2 = self.ovovT.copy()
-        R2 += P(X - Y)
-        R2 += (Woooo.reshape(o * o, o * o).T @ tau_r).reshape(o, o, v, v)
-        R2 += self.ladder(tau)
-        Z = np.empty((o * o, o, v))                                                # [(i,j), k, a]
-        for k in range(o):
-            Z[:, k, :] = tau_r @ np.ascontiguousarray(ovvv[k].transpose(1, 2, 0)).reshape(v, v * v).T
-        R2 -= P((Z.transpose(0, 2, 1).reshape(o * o * v, o) @ t1).reshape(o, o, v, v))
-        R2 += P(np.matmul(Lvv_p, t2))
-        R2 -= P((Loo_p.T @ t2.reshape(o, -1)).reshape(o, o, v, v))
+        Rp -= np.einsum("akij,kb->ijab", tmpB, t1, optimize=True)
+        Z = tau_r @ self.ovvvZ.T                                                    # [(i,j), (k,a)]
+        Rp -= (Z.reshape(o * o, o, v).transpose(0, 2, 1).reshape(o * o * v, o) @ t1).reshape(o, o, v, v)
+        Rp += np.matmul(Lvv_p, t2)
+        Rp -= (Loo_p.T @ t2.reshape(o, -1)).reshape(o, o, v, v)
         Wa = 2.0 * Wvoov - Wvovo
-        t2_kcjb = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)   # t2[k,j,c,b]
-        t2_kcjb2 = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)  # t2[k,j,b,c]
-        ring = (Wa @ t2_kcjb - Wvoov @ t2_kcjb2).reshape(o, v, o, v).transpose(0, 2, 1, 3)
-        ring = ring - (Wvovo @ t2_kcjb2).reshape(o, v, o, v).transpose(0, 2, 3, 1)
-        R2 += P(ring)
+        ring = Wa @ t2_iald                                                         # t2_iald = t2[k,j,c,b]
+        ring -= Wvoov @ t2_ilda                                                     # t2_ilda = t2[k,j,b,c]
+        Rp += ring.reshape(o, v, o, v).transpose(0, 2, 1, 3)
+        Rp -= (Wvovo @ t2_ilda).reshape(o, v, o, v).transpose(0, 2, 3, 1)
+        R2 = self.ovovT + (Woooo.reshape(o * o, o * o).T @ tau_r).reshape(o, o, v, v)
+        R2 += self.ladder(tau)
+        R2 += Rp
+        R2 += Rp.transpose(1, 0, 3, 2)
         return R1, R2
 
     def energy(self, t1, t2):
