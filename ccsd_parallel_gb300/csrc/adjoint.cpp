@@ -408,7 +408,7 @@ void Engine::lambda_grad(const ccsd_problem &prob, ccsd_grad *out) {
         CCSD_CUDA(cudaMemcpyAsync(r2.p, e2.p, nT2 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
         axpby_view(1, (int)nT1, 1.0, mv(t1b, ix1(0), ix1(1)), 1.0, ovw(r1.p, ix1(0), ix1(1)), st_);
         axpby_view(1, (int)nT2, 1.0, mv(t2b, ix1(0), ix1(1)), 1.0, ovw(r2.p, ix1(0), ix1(1)), st_);
-        k_update_t2(o, v, r2.p, zero2.p, eo_.p, ev_.p, l2.p, l2n.p, partials_.p, reduce_blocks(), st_);
+        k_update_t2(o, v, r2.p, zero2.p, eo_.p, ev_.p, dinv2_.p, l2.p, l2n.p, partials_.p, reduce_blocks(), st_);
         // r2 alone (Rp = 0, so Rp^T adds 0): l2n = r2 / D2
         k_update_t1(o, v, r1.p, eo_.p, ev_.p, l1.p, l1n.p, partials_.p + reduce_blocks(), st_);
         resid = std::sqrt(std::max(reduce_sum(reduce_blocks() + 1), 0.0));

@@ -132,9 +132,23 @@ void ao_integrals(const ::ccsd_basis &bs, double *S, double *T, double *V, doubl
                   bool device_out, cudaStream_t st);
 // R[i][j][a][b] = R[j][i][b][a] = their mean (o o v v, in place)
 void k_pair_mean(int o, int v, double *R, cudaStream_t st);
+// dinv2 (o o v v: 1 / D_ij^ab, from k_dinv2) may be NULL: then D is formed and divided per element
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
-                 const double *ev, const double *t2_old, double *t2_new, double *partials,
-                 int nblocks, cudaStream_t st);
+                 const double *ev, const double *dinv2, const double *t2_old, double *t2_new,
+                 double *partials, int nblocks, cudaStream_t st);
+void k_dinv2(int o, int v, const double *eo, const double *ev, double *dinv, cudaStream_t st);
+// DIIS: one pass stores T_s = x_new and E_s = x_new - x_old (x = t1 then t2, lengths n1 + n2) and
+// writes the block partials of <E_s, others[q]> (others[q] NULL: E_s itself) at partials[q * nblocks]
+void k_diis_store(size_t n1, size_t n2, const double *x1n, const double *x2n, const double *x1o,
+                  const double *x2o, double *Ts, double *Es, const double *const *others, int nothers,
+                  double *partials, int nblocks, cudaStream_t st);
+// (y1, y2) = sum_q coef[q] vecs[q] in one pass (n <= 16)
+void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const double *coef, int n, double *y1,
+                    double *y2, cudaStream_t st);
+// R1[i][a] += sum_k (2 Z[i][k][k][a] - Z[k][i][k][a]) for Z[i][j][k][a] (o o o v)
+void k_r1_from_z(int o, int v, const double *Z, double *R1, cudaStream_t st);
+// out[q] = sum of partials[q * nparts .. q * nparts + nparts) for q < nq
+void k_multi_sum(int nq, int nparts, const double *partials, double *out, cudaStream_t st);
 void k_update_t1(int o, int v, const double *R1, const double *eo, const double *ev,
                  const double *t1_old, double *t1_new, double *partials, cudaStream_t st);
 // E = sum_{ijab} L[i,j,a,b] * tau[i,j,a,b]; block partial sums into `partials`.

@@ -231,6 +231,10 @@ void Engine::build_integrals(const ccsd_problem &prob) {
         CCSD_CUDA(cudaMemcpyAsync(f_oo_off_.p, oo.data(), sizeof(double) * o * o, cudaMemcpyHostToDevice, st_));
         CCSD_CUDA(cudaMemcpyAsync(f_vv_off_.p, vv.data(), sizeof(double) * v * v, cudaMemcpyHostToDevice, st_));
         CCSD_CUDA(cudaMemcpyAsync(f_ov_.p, ov.data(), sizeof(double) * o * v, cudaMemcpyHostToDevice, st_));
+        if (!tape_) {  // the update's reciprocal denominators (not part of a recorded build)
+            dinv2_.ensure((size_t)o * o * v * v);
+            k_dinv2(o, v, eo_.p, ev_.p, dinv2_.p, st_);
+        }
         CCSD_CUDA(cudaStreamSynchronize(st_));
     }
 
@@ -250,6 +254,7 @@ void Engine::build_integrals(const ccsd_problem &prob) {
         input_eri_ = eri.get();
         keep(std::move(eri));
     } else if (prob.integral_kind == CCSD_INTS_DF) {
+        df_input_ = true;
         if (!prob.df || prob.naux <= 0) throw Error(CCSD_ERR_INVALID_ARG, "df factors missing");
         std::unique_ptr<DBuf> b(new DBuf((size_t)prob.naux * nt * nt));
         CCSD_CUDA(cudaMemcpyAsync(b->p, prob.df, sizeof(double) * b->n, kind, st_));
@@ -647,7 +652,15 @@ void Engine::residual() {
     // + sum_kc LT1[i,a,k,c] t1[k,c]
     gemm((int)ov, 1, (int)ov, 1.0, mv(LT1_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
          ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_LT1");
-    // + sum_kcd Lovvv[k,d,a,c] tau[i,k,c,d]
+    // + sum_kcd Lovvv[k,d,a,c] tau[i,k,c,d].  With tau[i,k,d,c] = tau[k,i,c,d] this equals
+    // sum_k (2 Z[i,k,k,a] - Z[k,i,k,a]) with Z of Rp_Z below, so the o v^3 block need not
+    // be read a second time (r1_from_z).  The amplitudes keep that symmetry whenever
+    // (pq|rs) = (rs|pq), which DF factors guarantee for any B; dense inputs may break it
+    // (one perturbed element, as a finite-difference check does), and a recorded
+    // residual (gradient, batched solve) follows the contraction's per-element
+    // derivative convention, so both keep the contraction.
+    const bool r1_from_z = tape_ == nullptr && df_input_;
+    if (!r1_from_z)
     gemm(io, iv, (int)(o * v2), 1.0, mv(tau, ix1(ov2), ix1(1)),
          mv(Lovvv_.p, ix1(v), ix3((uint32_t)v, (uint32_t)v, v * v2, 1, v2)), 1.0,
          ovw(R1_.p, ix1(v), ix1(1)), -5, 3, "R1_ovvv_tau");
@@ -757,6 +770,7 @@ void Engine::residual() {
     gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
          mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
          ovw(Z_.p, ix1(ov), ix1(1)), -1, 12, "Rp_Z");
+    if (r1_from_z) k_r1_from_z(io, iv, Z_.p, R1_.p, st_);
     gemm((int)(o2 * v), iv, io, -1.0, mv(Z_.p, ix2((uint32_t)v, ov, 1), ix1(v)), mv(t1, ix1(1), ix1(v)),
          1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_Z_t1");
     // + sum_c Lvv'[a,c] t2[i,j,c,b]: M = a, N = (i,j,b), K = c
@@ -820,22 +834,27 @@ void Engine::diis_step(int update_index) {
     }
     const int slot = diis_next_;
     DBuf &T = diis_t_[slot], &E = diis_e_[slot];
-    CCSD_CUDA(cudaMemcpyAsync(T.p, t1n_.p, nT1 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
-    CCSD_CUDA(cudaMemcpyAsync(T.p + nT1, t2n_.p, nT2 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
-    CCSD_CUDA(cudaMemcpyAsync(E.p, t1n_.p, nT1 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
-    CCSD_CUDA(cudaMemcpyAsync(E.p + nT1, t2n_.p, nT2 * sizeof(double), cudaMemcpyDeviceToDevice, st_));
-    axpby_view(1, (int)nT1, -1.0, mv(t1_.p, ix1(0), ix1(1)), 1.0, ovw(E.p, ix1(0), ix1(1)), st_);
-    axpby_view(1, (int)nT2, -1.0, mv(t2_.p, ix1(0), ix1(1)), 1.0, ovw(E.p + nT1, ix1(0), ix1(1)), st_);
     diis_next_ = (diis_next_ + 1) % m;
     diis_count_ = std::min(diis_count_ + 1, m);
-    for (int j = 0; j < m; ++j) {
-        if (j != slot && j >= diis_count_ && diis_count_ < m) continue;
-        if (j >= (int)diis_e_.size()) continue;
-        if (diis_count_ < m && j >= diis_count_) continue;
-        k_dot(len, E.p, diis_e_[j].p, partials_.p, reduce_blocks(), st_);
-        double d = reduce_sum(reduce_blocks());
-        diis_b_[(size_t)slot * m + j] = d;
-        diis_b_[(size_t)j * m + slot] = d;
+    // one pass: T = x_new, E = x_new - x_old and <E, E_j> for every stored slot j (E itself as NULL)
+    std::vector<int> js;
+    std::vector<const double *> others;
+    for (int j = 0; j < diis_count_; ++j) {
+        js.push_back(j);
+        others.push_back(j == slot ? nullptr : diis_e_[j].p);
+    }
+    const int nb = reduce_blocks();
+    diis_partials_.ensure((size_t)m * nb);
+    if (scalars_.n < (size_t)m) scalars_.alloc(std::max<size_t>(m, 8));
+    k_diis_store(nT1, nT2, t1n_.p, t2n_.p, t1_.p, t2_.p, T.p, E.p, others.data(), (int)others.size(),
+                 diis_partials_.p, nb, st_);
+    k_multi_sum((int)others.size(), nb, diis_partials_.p, scalars_.p, st_);
+    std::vector<double> dots(others.size());
+    CCSD_CUDA(cudaMemcpyAsync(dots.data(), scalars_.p, sizeof(double) * dots.size(), cudaMemcpyDeviceToHost, st_));
+    CCSD_CUDA(cudaStreamSynchronize(st_));
+    for (size_t q = 0; q < js.size(); ++q) {
+        diis_b_[(size_t)slot * m + js[q]] = dots[q];
+        diis_b_[(size_t)js[q] * m + slot] = dots[q];
     }
     if (diis_count_ < 2 || update_index < opt_.diis_start) return;
     // bordered system [B -1; -1 0] [c; lam] = [0; -1], scaled for conditioning
@@ -877,15 +896,10 @@ void Engine::diis_step(int update_index) {
     }
     for (int a = 0; a < k; ++a)
         if (!std::isfinite(x[a])) return;
-    // T_new = sum_a c_a T_a
-    k_fill(nT1, 0.0, t1n_.p, st_);
-    k_fill(nT2, 0.0, t2n_.p, st_);
-    for (int a = 0; a < k; ++a) {
-        const DBuf &Ta = diis_t_[idx[a]];
-        axpby_view(1, (int)nT1, x[a], mv(Ta.p, ix1(0), ix1(1)), 1.0, ovw(t1n_.p, ix1(0), ix1(1)), st_);
-        axpby_view(1, (int)nT2, x[a], mv(Ta.p + nT1, ix1(0), ix1(1)), 1.0, ovw(t2n_.p, ix1(0), ix1(1)),
-                   st_);
-    }
+    // T_new = sum_a c_a T_a, one pass over the stored vectors
+    std::vector<const double *> vecs(k);
+    for (int a = 0; a < k; ++a) vecs[a] = diis_t_[idx[a]].p;
+    k_diis_combine(nT1, nT2, vecs.data(), x.data(), k, t1n_.p, t2n_.p, st_);
 }
 
 // ---------------------------------------------------------------------------
@@ -933,7 +947,7 @@ void Engine::solve(ccsd_result *res) {
             CCSD_CUDA(cudaEventRecord(ev0, st_));
             residual();
             if (opt_.method != CCSD_METHOD_CCSD) triples_step();  // T3 terms, then T3 from this T2
-            k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
+            k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, dinv2_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
             k_update_t1(o, v, R1_.p, eo_.p, ev_.p, t1_.p, t1n_.p, partials_.p + reduce_blocks(), st_);
             const double rn2 = reduce_sum(reduce_blocks() + 1);
             last_resid_ = std::sqrt(std::max(rn2, 0.0));

@@ -180,6 +180,9 @@ class Engine {
     DBuf Foo_, Fvv_, Fov_, Loo_, Lvv_, tmpo_, tmpo2_;
     DBuf Woooo_, Wvoov_, Wvovo_, Wa_, Z_, tmpB_, Vk_;
     DBuf ws_, partials_, scalars_;
+    DBuf dinv2_;          // 1 / D_ij^ab, [i][j][a][b] (the update multiplies by it)
+    bool df_input_ = false;  // integrals from DF factors: (pq|rs) = (rs|pq) for any input
+    DBuf diis_partials_;  // DIIS overlaps: block partials per stored vector
     // DIIS storage: vectors (T) and errors (T_new - T_old), each o*v + o^2 v^2
     std::vector<DBuf> diis_t_, diis_e_;
     int diis_count_ = 0, diis_next_ = 0;

@@ -180,6 +180,48 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int M, int K, double alph
     }
 }
 
+// ROWC matrix-vector form with K split: a block covers 128 consecutive rows (1 KB
+// per k along the contiguous index, so every k touches whole DRAM bursts) and 2
+// k-slices; grid.y splits K so that few rows still fill the GPU.  With grid.y > 1
+// each block writes its partial sums to ws[y][m], added by splitk_reduce_kernel
+// in a fixed order.
+constexpr int GV_RW = 128;
+__global__ void __launch_bounds__(256) gemv_rowc_split_kernel(int M, int K, int kchunk, double alpha, MatView A,
+                                                              MatView X, double beta, OutView Y, double *ws) {
+    constexpr int KS = 256 / GV_RW;
+    __shared__ double part[KS][GV_RW + 1];
+    const int tr = threadIdx.x % GV_RW, ts = threadIdx.x / GV_RW;
+    const int m = blockIdx.x * GV_RW + tr;
+    const int kbeg = blockIdx.y * kchunk, kend = min(K, kbeg + kchunk);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (m < M) {
+        const int64_t ro = dim_off(A.row, m);
+        int k = kbeg + ts;
+        for (; k + 3 * KS < kend; k += 4 * KS) {
+            a0 = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], a0);
+            a1 = fma(A.p[ro + dim_off(A.col, k + KS)], X.p[dim_off(X.col, k + KS)], a1);
+            a2 = fma(A.p[ro + dim_off(A.col, k + 2 * KS)], X.p[dim_off(X.col, k + 2 * KS)], a2);
+            a3 = fma(A.p[ro + dim_off(A.col, k + 3 * KS)], X.p[dim_off(X.col, k + 3 * KS)], a3);
+        }
+        for (; k < kend; k += KS) a0 = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], a0);
+    }
+    part[ts][tr] = (a0 + a1) + (a2 + a3);
+    __syncthreads();
+    if (ts == 0 && m < M) {
+        double sum = 0.0;
+#pragma unroll
+        for (int q = 0; q < KS; ++q) sum += part[q][tr];
+        if (gridDim.y == 1) {
+            double *y = Y.p + dim_off(Y.row, m) + dim_off(Y.col, 0);
+            double v = alpha * sum;
+            if (beta != 0.0) v = fma(beta, *y, v);
+            *y = v;
+        } else {
+            ws[(size_t)blockIdx.y * M + m] = sum;
+        }
+    }
+}
+
 // Skinny form (N <= 16 columns, long K): the contraction streams A once and is
 // memory-bound.  A block covers 32 rows (4 per warp) and one K range; for each
 // 128-wide k chunk it stages B(0..N-1, k) in shared memory, and every lane
@@ -358,7 +400,7 @@ size_t gemm_f64_ws_elems(int M, int N, int K) {
         int s = choose_skinny_splits(Ml, K);
         return s > 1 ? (size_t)s * M * N : 0;
     }
-    if (M == 1 || N == 1) return 0;
+    if (M == 1 || N == 1) return (size_t)std::max(M, N) * 64;  // the K-split matrix-vector form
     int s = choose_splits(M, N, K);
     return s > 1 ? (size_t)s * M * N : 0;
 }
@@ -398,7 +440,19 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         const OutView Y = N == 1 ? C : OutView{C.p, C.col, C.row};
         const int R = N == 1 ? M : N;
         if (Am.row.s2 == 1 && Am.col.s2 != 1) {
-            gemv_f64_kernel<true><<<(R + 31) / 32, 256, 0, st>>>(R, K, alpha, Am, Xv, beta, Y);
+            // K split until the grid holds about 4 blocks per SM (deterministic partials in ws)
+            const int gx = (R + GV_RW - 1) / GV_RW;
+            int splits = std::max(1, std::min((4 * 152 + gx - 1) / gx, K / 256));
+            while (splits > 1 && (size_t)splits * R > ws_elems) --splits;
+            const int kchunk = (K + splits - 1) / splits;
+            splits = (K + kchunk - 1) / kchunk;
+            gemv_rowc_split_kernel<<<dim3(gx, splits), 256, 0, st>>>(R, K, kchunk, alpha, Am, Xv, beta, Y, ws);
+            CCSD_LAUNCH_CHECK();
+            if (splits > 1) {
+                splitk_reduce_kernel<<<(R + 255) / 256, 256, 0, st>>>(R, 1, splits, alpha, ws, beta, Y);
+                CCSD_LAUNCH_CHECK();
+            }
+            return;
         } else if (skinny_shape(R, 1, K) && R < 8 * 152 * 8) {
             // few rows of a long K: the K-split skinny form keeps every SM busy
             launch_skinny<1>(R, 1, K, alpha, Am, Xv, beta, Y, ws, ws_elems, st);

@@ -508,6 +508,29 @@ __device__ __forceinline__ void load_tile(double (&t)[32][33], int rows, int K, 
     }
 }
 
+// The S plane values of x for a row whose maximum has biased exponent emax
+// (0 for a zero row): Y = round(x 2^(7 - e + 8(S-1))) as an integer, peeled into
+// balanced base-256 digits from the bottom; plane p holds d_p 2^(-8p).
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int emax, float (&out)[S]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    long long Y = 0;
+    const int rs = emax - e + 54 - 8 * S;  // right shift that puts x on the 2^-(8(S-1)) grid
+    if (emax && e && rs < 63) {
+        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
+        if (bits >> 63) Y = -Y;
+    }
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+        const long long d = ((Y + 128) & 255) - 128;
+        Y = (Y - d) >> 8;
+        out[p] = (float)d * exp2f(-8.0f * p);
+    }
+    out[0] = (float)Y;
+}
+
 // Digits of one 32 x 32 block from row r0 and column k0.  Rows below rows_pad
 // and columns below kpad are written (zeros past rows / K); row r of plane p
 // sits at planes + p * plane + r * pitch.
@@ -545,6 +568,46 @@ __device__ void planes_block(int rows, int rows_pad, int K, int kpad, int64_t pi
         dst[0] = __float2bfloat16_rn((float)Y);
     }
     __syncthreads();  // t is reused by the next block of a looping caller
+}
+
+// One pass for operands read along k: a warp owns a row, takes its maximum, then
+// reads it again (from L2: one row at a time per warp) and writes its digits, two
+// consecutive k per lane.  Rows past `rows` are not written: TMA boxes that run
+// into them only feed output rows or columns the epilogue discards.  The K padding
+// up to kpad is written as zeros (it enters every output).
+template <int S>
+__global__ void __launch_bounds__(256) split_rows_kernel(int rows, int K, int kpad, MatView v,
+                                                         __nv_bfloat16 *__restrict__ planes, size_t plane,
+                                                         double *__restrict__ scale) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)(((size_t)gridDim.x * blockDim.x) >> 5);
+    const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
+    for (int r = warp; r < rows; r += nwarps) {
+        const int64_t ro = dim_off(v.row, (uint32_t)r);
+        unsigned long long m = 0;
+        for (int k = lane; k < K; k += 32) {
+            const unsigned long long b =
+                (unsigned long long)__double_as_longlong(v.p[ro + dim_off(v.col, (uint32_t)k)]) & absmask;
+            m = b > m ? b : m;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long o2 = __shfl_xor_sync(0xffffffffu, m, off);
+            m = o2 > m ? o2 : m;
+        }
+        const int emax = (int)((m >> 52) & 0x7FF);  // 0: zero (or denormal) row
+        if (lane == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
+        __nv_bfloat16 *dst = planes + (size_t)r * kpad;
+        for (int k = 2 * lane; k < kpad; k += 64) {
+            float d0[S], d1[S];
+            split_digits<S>(k < K ? v.p[ro + dim_off(v.col, (uint32_t)k)] : 0.0, emax, d0);
+            split_digits<S>(k + 1 < K ? v.p[ro + dim_off(v.col, (uint32_t)(k + 1))] : 0.0, emax, d1);
+#pragma unroll
+            for (int p = 0; p < S; ++p)
+                *reinterpret_cast<__nv_bfloat162 *>(dst + p * plane + k) = __floats2bfloat162_rn(d0[p], d1[p]);
+        }
+    }
 }
 
 template <int S, bool ROWC>
@@ -838,6 +901,19 @@ void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatVie
     const dim3 thr(32, 8);
     // read along rows when the row index is the contiguous one
     const bool rowc = v.row.s2 == 1 && v.col.s2 != 1;
+    __nv_bfloat16 *pl0 = (__nv_bfloat16 *)op.planes;
+    if (!rowc && K <= 32768 && rows >= 8 * 152) {  // one pass, a warp per row
+        const size_t plane = (size_t)op.rows_pad * op.kpad;
+        const int grid = (int)std::min<long long>((rows + 7) / 8, 152LL * 8);
+        switch (op.nslices) {
+            case 2: split_rows_kernel<2><<<grid, 256, 0, st>>>(rows, K, op.kpad, v, pl0, plane, op.scale); break;
+            case 3: split_rows_kernel<3><<<grid, 256, 0, st>>>(rows, K, op.kpad, v, pl0, plane, op.scale); break;
+            case 4: split_rows_kernel<4><<<grid, 256, 0, st>>>(rows, K, op.kpad, v, pl0, plane, op.scale); break;
+            default: throw Error(-1, "nslices must be 2, 3 or 4");
+        }
+        CCSD_LAUNCH_CHECK();
+        return;
+    }
     const long long nkg = (op.kpad + 32 * kRowmaxKT - 1) / (32 * kRowmaxKT);
     CCSD_CUDA(cudaMemsetAsync(op.rmax, 0, sizeof(unsigned long long) * op.rows_pad, st));
     __nv_bfloat16 *pl = (__nv_bfloat16 *)op.planes;

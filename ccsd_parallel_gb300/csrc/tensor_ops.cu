@@ -4,6 +4,7 @@
 // is HBM bandwidth.
 //
 // Index conventions (closed-shell spatial): t1[i][a], t2[i][j][a][b].
+#include <algorithm>
 #include <atomic>
 
 #include "common.h"
@@ -202,6 +203,200 @@ __global__ void pair_mean_kernel(int o, int v, double *R) {
     }
 }
 
+// ---- 32 x 32 tiles over the (a, b) indices of an o x o x v x v array ---------
+// A block (32 x 8 threads) walks tiles t = ((i o + j) nt + A) nt + B, nt = ceil(v/32);
+// tile indices are decoded once per tile, never per element.  Element (a, b) of a
+// tile is a = 32 A + q (q = ty, ty + 8, ...), b = 32 B + tx, so global loads and
+// stores along b are coalesced; a partner read with a and b exchanged goes through
+// a shared-memory tile loaded along its own contiguous index.
+struct Tile4 {
+    int i, j, A, B;
+};
+__device__ __forceinline__ Tile4 tile_of(int t, int o, int nt) {
+    Tile4 T;
+    T.B = t % nt;
+    t /= nt;
+    T.A = t % nt;
+    t /= nt;
+    T.j = t % o;
+    T.i = t / o;
+    return T;
+}
+
+// 1 / (eo[i] + eo[j] - ev[a] - ev[b]) over [i][j][a][b] (fixed for a solve)
+__global__ void dinv2_kernel(int o, int v, const double *eo, const double *ev, double *dinv) {
+    const int rows = o * o * v;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int a = r % v, ij = r / v, j = ij % o, i = ij / o;
+        const double dij = eo[i] + eo[j] - ev[a];
+        for (int b = threadIdx.x; b < v; b += blockDim.x) dinv[(size_t)r * v + b] = 1.0 / (dij - ev[b]);
+    }
+}
+
+// t2_new = (R + Rp + Rp^T) * dinv with Rp^T[i][j][a][b] = Rp[j][i][b][a]; per-block
+// partial sums of |t2_new - t2_old|^2 (a fixed tile order per block: deterministic)
+__global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, const double *__restrict__ R,
+                                                              const double *__restrict__ Rp,
+                                                              const double *__restrict__ dinv,
+                                                              const double *__restrict__ t2o,
+                                                              double *__restrict__ t2n, double *partials) {
+    __shared__ double s[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int nt = (v + 31) / 32, ntiles = o * o * nt * nt;
+    const size_t v2 = (size_t)v * v;
+    double acc = 0.0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile4 T = tile_of(t, o, nt);
+        const double *rpt = Rp + ((size_t)T.j * o + T.i) * v2;  // Rp[j][i][b][a], read along a
+        for (int q = ty; q < 32; q += 8) {
+            const int b = T.B * 32 + q, a = T.A * 32 + tx;
+            s[q][tx] = (b < v && a < v) ? rpt[(size_t)b * v + a] : 0.0;
+        }
+        __syncthreads();
+        const size_t base = ((size_t)T.i * o + T.j) * v2;
+        const int b = T.B * 32 + tx;
+        for (int q = ty; q < 32; q += 8) {
+            const int a = T.A * 32 + q;
+            if (a < v && b < v) {
+                const size_t idx = base + (size_t)a * v + b;
+                const double tn = (R[idx] + Rp[idx] + s[tx][q]) * dinv[idx];
+                const double d = tn - t2o[idx];
+                acc = fma(d, d, acc);
+                t2n[idx] = tn;
+            }
+        }
+        __syncthreads();
+    }
+    const double sum = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = sum;
+}
+
+// th1[i,a,l,d] = t2[i,l,a,d] - t2[i,l,d,a]/2 - t1[i,d] t1[l,a]; th2[i,a,l,d] = t2[i,l,d,a]/2 + t1[i,d] t1[l,a]
+// (tiles over (a, d) for each (i, l))
+__global__ void __launch_bounds__(256) theta_tiled_kernel(int o, int v, const double *__restrict__ t1,
+                                                          const double *__restrict__ t2, double *__restrict__ th1,
+                                                          double *__restrict__ th2) {
+    __shared__ double s[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int nt = (v + 31) / 32, ntiles = o * o * nt * nt;
+    const size_t v2 = (size_t)v * v;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile4 T = tile_of(t, o, nt);  // (i, l, A, D)
+        const int i = T.i, l = T.j;
+        const double *t2il = t2 + ((size_t)i * o + l) * v2;
+        for (int q = ty; q < 32; q += 8) {  // s[d][a] = t2[i,l,d,a]
+            const int d = T.B * 32 + q, a = T.A * 32 + tx;
+            s[q][tx] = (d < v && a < v) ? t2il[(size_t)d * v + a] : 0.0;
+        }
+        __syncthreads();
+        const int d = T.B * 32 + tx;
+        for (int q = ty; q < 32; q += 8) {
+            const int a = T.A * 32 + q;
+            if (a < v && d < v) {
+                const double tad = t2il[(size_t)a * v + d];
+                const double tda = s[tx][q];
+                const double tt = t1[i * v + d] * t1[l * v + a];
+                const size_t out = (((size_t)i * v + a) * o + l) * v + d;
+                th1[out] = tad - 0.5 * tda - tt;
+                th2[out] = 0.5 * tda + tt;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// tau[i][j][a][b] = t2 + t1[i][a] t1[j][b], one row (i, j, a) at a time
+__global__ void tau_rows_kernel(int o, int v, const double *__restrict__ t1, const double *__restrict__ t2,
+                                double *__restrict__ tau) {
+    const int rows = o * o * v;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int a = r % v, ij = r / v, j = ij % o, i = ij / o;
+        const double ta = t1[i * v + a];
+        const double *t1j = t1 + (size_t)j * v;
+        const size_t base = (size_t)r * v;
+        for (int b = threadIdx.x; b < v; b += blockDim.x) tau[base + b] = t2[base + b] + ta * t1j[b];
+    }
+}
+
+// ---- DIIS on the amplitude vector x = (t1, t2) ---------------------------------
+// store: T_s = x_new, E_s = x_new - x_old, and the block partials of <E_s, E_j>
+// for the listed slots j (E_s itself included), all in one pass.
+constexpr int kDiisMax = 16;
+struct DiisVecs {
+    const double *p[kDiisMax];
+    double c[kDiisMax];
+    int n;
+};
+
+__global__ void __launch_bounds__(256) diis_store_kernel(size_t n1, size_t n2, const double *__restrict__ x1n,
+                                                         const double *__restrict__ x2n,
+                                                         const double *__restrict__ x1o,
+                                                         const double *__restrict__ x2o, double *__restrict__ Ts,
+                                                         double *__restrict__ Es, DiisVecs others,
+                                                         double *partials) {
+    double acc[kDiisMax];
+#pragma unroll
+    for (int q = 0; q < kDiisMax; ++q) acc[q] = 0.0;
+    const size_t n = n1 + n2;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const double xn = idx < n1 ? x1n[idx] : x2n[idx - n1];
+        const double xo = idx < n1 ? x1o[idx] : x2o[idx - n1];
+        const double e = xn - xo;
+        Ts[idx] = xn;
+        Es[idx] = e;
+#pragma unroll
+        for (int q = 0; q < kDiisMax; ++q)
+            if (q < others.n) acc[q] = fma(e, others.p[q] ? others.p[q][idx] : e, acc[q]);
+    }
+    for (int q = 0; q < others.n; ++q) {
+        const double sum = block_sum(acc[q]);
+        if (threadIdx.x == 0) partials[(size_t)q * gridDim.x + blockIdx.x] = sum;
+    }
+}
+
+// extrapolate: (y1, y2) = sum_q c_q V_q, V_q = (t1 part of length n1, t2 part)
+__global__ void __launch_bounds__(256) diis_combine_kernel(size_t n1, size_t n2, DiisVecs vecs,
+                                                           double *__restrict__ y1, double *__restrict__ y2) {
+    const size_t n = n1 + n2;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kDiisMax; ++q)
+            if (q < vecs.n) s = fma(vecs.c[q], vecs.p[q][idx], s);
+        if (idx < n1)
+            y1[idx] = s;
+        else
+            y2[idx - n1] = s;
+    }
+}
+
+// R1[i][a] += sum_k (2 Z[i][k][k][a] - Z[k][i][k][a]),  Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d]
+__global__ void r1_from_z_kernel(int o, int v, const double *__restrict__ Z, double *__restrict__ R1) {
+    const int n = o * v;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int i = idx / v, a = idx % v;
+        double s = 0.0;
+        for (int k = 0; k < o; ++k) {
+            const double zd = Z[(((size_t)i * o + k) * o + k) * v + a];
+            const double zx = Z[(((size_t)k * o + i) * o + k) * v + a];
+            s += 2.0 * zd - zx;
+        }
+        R1[idx] += s;
+    }
+}
+
+// sums of `nq` groups of `nparts` partials: out[q] = sum_b partials[q * nparts + b]
+__global__ void multi_sum_kernel(int nq, int nparts, const double *partials, double *out) {
+    for (int q = 0; q < nq; ++q) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partials[(size_t)q * nparts + i];
+        const double s = block_sum(acc);
+        if (threadIdx.x == 0) out[q] = s;
+    }
+}
+
 __global__ void update_t1_kernel(int o, int v, const double *R1, const double *eo,
                                  const double *ev, const double *t1_old, double *t1_new,
                                  double *partials) {
@@ -324,14 +519,68 @@ void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const
     CCSD_LAUNCH_CHECK();
 }
 
+// grids of the row and tile kernels: whole waves of 152 SMs
+inline int rows_grid(long rows) { return (int)std::max(1L, std::min(rows, 152L * 16)); }
+inline int tiles_grid(int o, int v) {
+    const long nt = (v + 31) / 32, tiles = (long)o * o * nt * nt;
+    return (int)std::max(1L, std::min(tiles, 152L * 8));
+}
+
 void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st) {
-    tau_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, tau);
+    if ((size_t)o * o * v * v >= ((size_t)1 << 31)) {  // row indices stay 32-bit in the row kernel
+        tau_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, tau);
+    } else {
+        tau_rows_kernel<<<rows_grid((long)o * o * v), v <= 128 ? 128 : 320, 0, st>>>(o, v, t1, t2, tau);
+    }
     CCSD_LAUNCH_CHECK();
 }
 
 void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
              cudaStream_t st) {
-    theta_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
+    if ((size_t)o * o * v * v >= ((size_t)1 << 31)) {
+        theta_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
+    } else {
+        theta_tiled_kernel<<<tiles_grid(o, v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
+    }
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_dinv2(int o, int v, const double *eo, const double *ev, double *dinv, cudaStream_t st) {
+    dinv2_kernel<<<rows_grid((long)o * o * v), v <= 128 ? 128 : 320, 0, st>>>(o, v, eo, ev, dinv);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_diis_store(size_t n1, size_t n2, const double *x1n, const double *x2n, const double *x1o,
+                  const double *x2o, double *Ts, double *Es, const double *const *others, int nothers,
+                  double *partials, int nblocks, cudaStream_t st) {
+    if (nothers > kDiisMax) throw Error(-1, "DIIS: at most 16 vectors");
+    DiisVecs d{};
+    for (int q = 0; q < nothers; ++q) d.p[q] = others[q];
+    d.n = nothers;
+    diis_store_kernel<<<nblocks, 256, 0, st>>>(n1, n2, x1n, x2n, x1o, x2o, Ts, Es, d, partials);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const double *coef, int n, double *y1,
+                    double *y2, cudaStream_t st) {
+    if (n > kDiisMax || n < 1) throw Error(-1, "DIIS: 1 to 16 vectors");
+    DiisVecs d{};
+    for (int q = 0; q < n; ++q) {
+        d.p[q] = vecs[q];
+        d.c[q] = coef[q];
+    }
+    d.n = n;
+    diis_combine_kernel<<<grid_for(n1 + n2), 256, 0, st>>>(n1, n2, d, y1, y2);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_r1_from_z(int o, int v, const double *Z, double *R1, cudaStream_t st) {
+    r1_from_z_kernel<<<(o * v + 255) / 256, 256, 0, st>>>(o, v, Z, R1);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_multi_sum(int nq, int nparts, const double *partials, double *out, cudaStream_t st) {
+    multi_sum_kernel<<<1, 1024, 0, st>>>(nq, nparts, partials, out);
     CCSD_LAUNCH_CHECK();
 }
 
@@ -342,10 +591,12 @@ void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const doubl
 }
 
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
-                 const double *ev, const double *t2_old, double *t2_new, double *partials,
-                 int nblocks, cudaStream_t st) {
-    update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new,
-                                                         partials);
+                 const double *ev, const double *dinv2, const double *t2_old, double *t2_new,
+                 double *partials, int nblocks, cudaStream_t st) {
+    if (dinv2 && (size_t)o * o * v * v < ((size_t)1 << 31))
+        update_t2_tiled_kernel<<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
+    else
+        update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new, partials);
     CCSD_LAUNCH_CHECK();
 }
 
