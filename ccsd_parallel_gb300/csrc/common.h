@@ -145,6 +145,8 @@ void k_diis_store(size_t n1, size_t n2, const double *x1n, const double *x2n, co
 // (y1, y2) = sum_q coef[q] vecs[q] in one pass (n <= 16)
 void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const double *coef, int n, double *y1,
                     double *y2, cudaStream_t st);
+// y = a x1 + b x2 over n contiguous elements (16-byte aligned arrays)
+void k_lincomb2(size_t n, double a, const double *x1, double b, const double *x2, double *y, cudaStream_t st);
 // R1[i][a] += sum_k (2 Z[i][k][k][a] - Z[k][i][k][a]) for Z[i][j][k][a] (o o o v)
 void k_r1_from_z(int o, int v, const double *Z, double *R1, cudaStream_t st);
 // out[q] = sum of partials[q * nparts .. q * nparts + nparts) for q < nq

@@ -723,9 +723,13 @@ void Engine::residual() {
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(th2_.p, ix1(ov), ix1(1)),
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
          ovw(Wvovo_.p, ix1(ov), ix1(1)), 0, 8, "Wvovo_th2");
-    // Wa = 2 Wvoov - Wvovo
-    axpby((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)));
-    axpby((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)));
+    // Wa = 2 Wvoov - Wvovo (one pass unless a tape records the two steps)
+    if (tape_) {
+        axpby((int)ov, (int)ov, -1.0, mv(Wvovo_.p, ix1(ov), ix1(1)), 0.0, ovw(Wa_.p, ix1(ov), ix1(1)));
+        axpby((int)ov, (int)ov, 2.0, mv(Wvoov_.p, ix1(ov), ix1(1)), 1.0, ovw(Wa_.p, ix1(ov), ix1(1)));
+    } else {
+        k_lincomb2((size_t)(ov * ov), 2.0, Wvoov_.p, -1.0, Wvovo_.p, Wa_.p, st_);
+    }
 
     // ---- R (symmetric terms) ---------------------------------------------
     // (ia|jb)

@@ -180,37 +180,52 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(int M, int K, double alph
     }
 }
 
-// ROWC matrix-vector form with K split: a block covers 128 consecutive rows (1 KB
-// per k along the contiguous index, so every k touches whole DRAM bursts) and 2
-// k-slices; grid.y splits K so that few rows still fill the GPU.  With grid.y > 1
-// each block writes its partial sums to ws[y][m], added by splitk_reduce_kernel
-// in a fixed order.
-constexpr int GV_RW = 128;
+// ROWC matrix-vector form with K split: a block covers 1024 consecutive rows (each
+// thread 4 rows, 256 apart), so every k reads 8 KB of A contiguously; grid.y splits
+// K so that the grid holds several blocks per SM.  With grid.y > 1 each block
+// writes its partial sums to ws[y][m], added by splitk_reduce_kernel in a fixed
+// order.
+constexpr int GV_RW = 1024;
 __global__ void __launch_bounds__(256) gemv_rowc_split_kernel(int M, int K, int kchunk, double alpha, MatView A,
                                                               MatView X, double beta, OutView Y, double *ws) {
-    constexpr int KS = 256 / GV_RW;
-    __shared__ double part[KS][GV_RW + 1];
-    const int tr = threadIdx.x % GV_RW, ts = threadIdx.x / GV_RW;
-    const int m = blockIdx.x * GV_RW + tr;
+    const int m0 = blockIdx.x * GV_RW + threadIdx.x;
     const int kbeg = blockIdx.y * kchunk, kend = min(K, kbeg + kchunk);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    if (m < M) {
-        const int64_t ro = dim_off(A.row, m);
-        int k = kbeg + ts;
-        for (; k + 3 * KS < kend; k += 4 * KS) {
-            a0 = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], a0);
-            a1 = fma(A.p[ro + dim_off(A.col, k + KS)], X.p[dim_off(X.col, k + KS)], a1);
-            a2 = fma(A.p[ro + dim_off(A.col, k + 2 * KS)], X.p[dim_off(X.col, k + 2 * KS)], a2);
-            a3 = fma(A.p[ro + dim_off(A.col, k + 3 * KS)], X.p[dim_off(X.col, k + 3 * KS)], a3);
-        }
-        for (; k < kend; k += KS) a0 = fma(A.p[ro + dim_off(A.col, k)], X.p[dim_off(X.col, k)], a0);
-    }
-    part[ts][tr] = (a0 + a1) + (a2 + a3);
-    __syncthreads();
-    if (ts == 0 && m < M) {
-        double sum = 0.0;
+    int64_t ro[4];
+    bool ok[4];
 #pragma unroll
-        for (int q = 0; q < KS; ++q) sum += part[q][tr];
+    for (int q = 0; q < 4; ++q) {
+        ok[q] = m0 + 256 * q < M;
+        ro[q] = ok[q] ? dim_off(A.row, m0 + 256 * q) : 0;
+    }
+    double acc[4] = {0.0, 0.0, 0.0, 0.0}, acc2[4] = {0.0, 0.0, 0.0, 0.0};
+    int k = kbeg;
+    for (; k + 1 < kend; k += 2) {
+        const int64_t c0 = dim_off(A.col, k), c1 = dim_off(A.col, k + 1);
+        const double x0 = X.p[dim_off(X.col, k)], x1 = X.p[dim_off(X.col, k + 1)];
+        double a0[4], a1[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            a0[q] = ok[q] ? A.p[ro[q] + c0] : 0.0;
+            a1[q] = ok[q] ? A.p[ro[q] + c1] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            acc[q] = fma(a0[q], x0, acc[q]);
+            acc2[q] = fma(a1[q], x1, acc2[q]);
+        }
+    }
+    if (k < kend) {
+        const int64_t c0 = dim_off(A.col, k);
+        const double x0 = X.p[dim_off(X.col, k)];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (ok[q]) acc[q] = fma(A.p[ro[q] + c0], x0, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (!ok[q]) continue;
+        const int m = m0 + 256 * q;
+        const double sum = acc[q] + acc2[q];
         if (gridDim.y == 1) {
             double *y = Y.p + dim_off(Y.row, m) + dim_off(Y.col, 0);
             double v = alpha * sum;
@@ -440,9 +455,10 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
         const OutView Y = N == 1 ? C : OutView{C.p, C.col, C.row};
         const int R = N == 1 ? M : N;
         if (Am.row.s2 == 1 && Am.col.s2 != 1) {
-            // K split until the grid holds about 4 blocks per SM (deterministic partials in ws)
+            // K split until the grid holds about 8 blocks per SM, the loads in flight that
+            // HBM latency needs (deterministic partials in ws)
             const int gx = (R + GV_RW - 1) / GV_RW;
-            int splits = std::max(1, std::min((4 * 152 + gx - 1) / gx, K / 256));
+            int splits = std::max(1, std::min((8 * 152 + gx - 1) / gx, K / 64));
             while (splits > 1 && (size_t)splits * R > ws_elems) --splits;
             const int kchunk = (K + splits - 1) / splits;
             splits = (K + kchunk - 1) / kchunk;

@@ -105,16 +105,21 @@ struct TileJob {
 
 // One contraction over the whole grid (grouped rasterisation, split-K over z).
 struct SingleJobs {
-    int M, N, tiles_m, tiles_n, nkb_total, kb_per_split;
+    int M, N, tiles_m, tiles_n, nkb_total, kb_per_split, splits;
     const double *scaleA, *scaleB;
     double alpha, beta;
     OutView C;
     double *ws;
-    __device__ TileJob job() const {
+    __device__ TileJob job() const { return at(blockIdx.x, blockIdx.z); }
+    // Work item w of the persistent kernel: split-K slice z = w / tiles, tile w % tiles.
+    __device__ TileJob job_at(int w) const {
+        const int tiles = tiles_m * tiles_n, z = w / tiles;
+        return at(w - z * tiles, z);
+    }
+    __device__ TileJob at(int t, int z) const {
         TileJob J;
         // Grouped rasterisation: consecutive CTAs walk kGroupM row tiles across
         // all column tiles, so the CTAs resident together share A and B tiles in L2.
-        const int t = blockIdx.x;
         const int group = kGroupM * tiles_n;
         const int g = t / group, first_m = g * kGroupM;
         const int gm = min(tiles_m - first_m, kGroupM);
@@ -124,14 +129,14 @@ struct SingleJobs {
         J.rowA0 = J.rowB0 = 0;
         J.M = M;
         J.N = N;
-        J.kb0 = blockIdx.z * kb_per_split;
+        J.kb0 = z * kb_per_split;
         J.nkb = min(nkb_total, J.kb0 + kb_per_split) - J.kb0;
         J.scaleA = scaleA;
         J.scaleB = scaleB;
         J.alpha = alpha;
         J.beta = beta;
         J.C = C;
-        J.wsz = gridDim.z == 1 ? nullptr : ws + (size_t)blockIdx.z * M * N;
+        J.wsz = splits == 1 ? nullptr : ws + (size_t)z * M * N;
         J.run = true;
         return J;
     }
@@ -412,6 +417,300 @@ __global__ void __launch_bounds__(kThreads, MINB)
                     }
                 }
             }
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, NCOLS);
+    }
+}
+
+// ---- persistent form of one contraction ------------------------------------
+// A CTA walks the work items w = blockIdx.x, blockIdx.x + gridDim.x, ... (tiles
+// in the grouped order, split-K slices folded in).  The producer streams the
+// k-blocks of consecutive tiles through the stage ring without draining it, and
+// the accumulators are arranged so that a tile's epilogue runs while the MMA
+// issuer works on the next tile: the level-0 chunk buffers acc0[0..1] alternate
+// over the chunk count of all the CTA's tiles, and the higher levels get one
+// buffer per tile parity, rest[0..1].  TMEM columns: acc0[0], acc0[1], rest[0],
+// rest[1], BN each.  The epilogue warps keep private column tables, so no
+// barrier spans warps inside the tile loop and every wait stays bounded.
+struct PBars {
+    uint64_t full[8];
+    uint64_t empty[8];
+    uint64_t acc_full[2];
+    uint64_t acc_empty[2];
+    uint64_t rest_full[2];
+    uint64_t rest_empty[2];
+    uint64_t drain;
+    uint32_t tmem_base;
+    int abort;
+    int never;
+};
+__host__ __device__ constexpr size_t pbars_bytes() { return (sizeof(PBars) + 15) / 16 * 16; }
+__host__ __device__ constexpr int ptmem_cols(int BN) { return 4 * BN <= 128 ? 128 : (4 * BN <= 256 ? 256 : 512); }
+
+template <int S, int BN, int NST, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    split_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                                 int rowsA_pad, int rowsB_pad, const SingleJobs jobs, int nwork, int *gerr) {
+    constexpr int SB = stage_bytes(S, BN);
+    constexpr int A_TILE = BM * BK * 2;
+    constexpr int B_TILE = BN * BK * 2;
+    constexpr uint32_t IDESC = ptx::idesc_bf16_f32(BM, BN);
+    constexpr int NCOLS = ptmem_cols(BN);
+    constexpr bool kEpi32 = S <= 3;
+    static_assert(4 * BN <= 512, "four BN-column accumulators must fit in TMEM");
+
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    PBars *bars = (PBars *)(smem + NST * SB);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < NST; ++st) {
+            ptx::mbar_init(&bars->full[st], 1);
+            ptx::mbar_init(&bars->empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            ptx::mbar_init(&bars->acc_full[b], 1);
+            ptx::mbar_init(&bars->acc_empty[b], 4);
+            ptx::mbar_init(&bars->rest_full[b], 1);
+            ptx::mbar_init(&bars->rest_empty[b], 4);
+        }
+        ptx::mbar_init(&bars->drain, 1);
+        bars->abort = 0;
+        bars->never = 0;
+        ptx::fence_barrier_init();
+        ptx::prefetch_tmap(&tmA);
+        ptx::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(&bars->tmem_base, NCOLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = bars->tmem_base;
+    volatile int *abort = &bars->abort;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0, issued = 0;
+            bool stop = false;
+            for (int w = blockIdx.x; w < nwork && !stop; w += gridDim.x) {
+                const TileJob J = jobs.job_at(w);
+                const int tma_m0 = J.mt * BM, tma_n0 = J.nt * BN;
+                for (int l = 0; l < J.nkb; ++l, ++g) {
+                    const int st = g % NST, round = g / NST;
+                    if (!ptx::mbar_wait(&bars->empty[st], (round & 1) ^ 1, abort, gerr, 1, kWaitNs)) {
+                        stop = true;
+                        break;
+                    }
+                    ptx::mbar_arrive_expect_tx(&bars->full[st], SB);
+                    unsigned char *sa = smem + st * SB;
+                    unsigned char *sb = sa + S * A_TILE;
+                    const int kx = (J.kb0 + l) * BK;
+#pragma unroll
+                    for (int p = 0; p < S; ++p) {
+                        ptx::tma_load_2d(sa + p * A_TILE, &tmA, &bars->full[st], kx, p * rowsA_pad + tma_m0);
+                        ptx::tma_load_2d(sb + p * B_TILE, &tmB, &bars->full[st], kx, p * rowsB_pad + tma_n0);
+                    }
+                    issued = g + 1;
+                }
+            }
+            if (*abort) {  // let every TMA load this thread issued land before the CTA exits
+                for (int l = max(0, issued - NST); l < issued; ++l)
+                    ptx::mbar_wait(&bars->full[l % NST], (l / NST) & 1, &bars->never, gerr, 2, kWaitNs);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const unsigned long long stall = g_stall_mma_ns;
+            bool ok = stall == 0 || ptx::mbar_wait(&bars->drain, 0, abort, gerr, 128, stall);
+            int g = 0, c = 0, n = 0;
+            for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x, ++n) {
+                const TileJob J = jobs.job_at(w);
+                const int j = n & 1;
+                // rest[j] is free once the epilogue of tile n - 2 has read it
+                if (!ptx::mbar_wait(&bars->rest_empty[j], ((n >> 1) & 1) ^ 1, abort, gerr, 4, kWaitNs)) {
+                    ok = false;
+                    break;
+                }
+                ptx::tc_fence_after();
+                const uint32_t rest = tmem + (2 + j) * BN;
+                bool first_rest = true;
+                for (int l = 0; l < J.nkb; ++l, ++g) {
+                    const int st = g % NST, round = g / NST;
+                    const int b = c & 1;
+                    const bool chunk_start = (l % CHUNK_KB) == 0;
+                    if (chunk_start) {
+                        if (!ptx::mbar_wait(&bars->acc_empty[b], ((c >> 1) & 1) ^ 1, abort, gerr, 4, kWaitNs)) {
+                            ok = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                    }
+                    if (!ptx::mbar_wait(&bars->full[st], round & 1, abort, gerr, 8, kWaitNs)) {
+                        ok = false;
+                        break;
+                    }
+                    ptx::tc_fence_after();
+                    const uint32_t sa = ptx::smem_u32(smem + st * SB);
+                    const uint32_t sb = sa + S * A_TILE;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        uint64_t ad[S], bd[S];
+#pragma unroll
+                        for (int p = 0; p < S; ++p) {
+                            ad[p] = ptx::sdesc_k_sw64(sa + p * A_TILE + kk * 32);
+                            bd[p] = ptx::sdesc_k_sw64(sb + p * B_TILE + kk * 32);
+                        }
+                        ptx::mma_bf16(tmem + b * BN, ad[0], bd[0], IDESC, (chunk_start && kk == 0) ? 0u : 1u);
+#pragma unroll
+                        for (int lev = 1; lev < S; ++lev)
+#pragma unroll
+                            for (int p = 0; p <= lev; ++p) {
+                                ptx::mma_bf16(rest, ad[p], bd[lev - p], IDESC, first_rest ? 0u : 1u);
+                                first_rest = false;
+                            }
+                    }
+                    ptx::mma_commit(&bars->empty[st]);
+                    if ((l % CHUNK_KB) == CHUNK_KB - 1 || l == J.nkb - 1) {
+                        ptx::mma_commit(&bars->acc_full[b]);
+                        ++c;
+                    }
+                }
+                if (!ok) break;
+                ptx::mma_commit(&bars->rest_full[j]);
+            }
+            ptx::mma_commit(&bars->drain);
+            ptx::mbar_wait(&bars->drain, 0, &bars->never, gerr, 16, kWaitNs);
+        }
+    } else {
+        // epilogue warps 2..5; TMEM lane quarter = warp % 4; each warp keeps its own
+        // column table (offsets, FP64 and FP32 column scales) behind the barriers
+        const int q = warp & 3;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        unsigned char *tbl = (unsigned char *)bars + pbars_bytes() + (size_t)(warp - 2) * epi_bytes(BN);
+        int64_t *s_coff = (int64_t *)tbl;
+        double *s_sb = (double *)(s_coff + BN);
+        float *s_fsb = (float *)(s_sb + BN);
+        int c = 0, n = 0;
+        for (int w = blockIdx.x; w < nwork; w += gridDim.x, ++n) {
+            const TileJob J = jobs.job_at(w);
+            const int j = n & 1;
+            const int m0 = J.mt * BM, n0 = J.nt * BN, M = J.M, N = J.N, nkb = J.nkb;
+            const OutView C = J.C;
+            __syncwarp();  // the previous tile's table reads are done
+            int ebmin = 1 << 20, ebmax = -(1 << 20);
+            for (int jj = lane; jj < BN; jj += 32) {
+                const int nn = n0 + jj;
+                const double sbn = nn < N ? J.scaleB[nn] : 0.0;
+                s_coff[jj] = nn < N ? dim_off(C.col, (uint32_t)nn) : -1;
+                s_sb[jj] = sbn;
+                s_fsb[jj] = (float)sbn;
+                if (nn < N) {
+                    const int e = exp2_of(sbn);
+                    ebmin = min(ebmin, e);
+                    ebmax = max(ebmax, e);
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ebmin = min(ebmin, __shfl_xor_sync(0xffffffffu, ebmin, off));
+                ebmax = max(ebmax, __shfl_xor_sync(0xffffffffu, ebmax, off));
+            }
+            __syncwarp();
+            int32_t iacc[BN];
+#pragma unroll
+            for (int jj = 0; jj < BN; ++jj) iacc[jj] = 0;
+            const int nch = (nkb + CHUNK_KB - 1) / CHUNK_KB;
+            bool ok = true;
+            for (int ch = 0; ch < nch; ++ch, ++c) {
+                const int b = c & 1;
+                const bool got = ptx::mbar_wait(&bars->acc_full[b], (c >> 1) & 1, abort, gerr, 32, kWaitNs);
+                if (!__all_sync(0xffffffffu, got)) {  // keep the warp converged for tcgen05.ld
+                    ok = false;
+                    break;
+                }
+                ptx::tc_fence_after();
+#pragma unroll
+                for (int gq = 0; gq < BN / 32; ++gq) {
+                    uint32_t r[32];
+                    ptx::tmem_ld32(tmem + lane_off + b * BN + gq * 32, r);
+                    ptx::tmem_ld_wait();
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) iacc[gq * 32 + jj] += __float2int_rn(__uint_as_float(r[jj]));
+                }
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&bars->acc_empty[b]);
+            }
+            if (ok) ok = __all_sync(0xffffffffu, ptx::mbar_wait(&bars->rest_full[j], (n >> 1) & 1, abort, gerr, 64, kWaitNs));
+            if (!ok) break;
+            ptx::tc_fence_after();
+            const int m = m0 + q * 32 + lane;
+            const bool mval = m < M;
+            const double sa = mval ? J.scaleA[m] * 0x1.0p-14 : 0.0;
+            const int64_t crow = mval ? dim_off(C.row, (uint32_t)m) : 0;
+            const bool direct = J.wsz == nullptr;
+            double *wsz = J.wsz;
+            const double alpha = J.alpha, beta = J.beta;
+            const double sa_out = direct ? sa * alpha : sa;
+            const int ea = exp2_of(sa_out);
+            const bool in_range = !mval || sa_out == 0.0 || (ea + ebmin >= kEpi32Lo && ea + ebmax <= kEpi32Hi);
+            const bool epi32 = kEpi32 && __all_sync(0xffffffffu, in_range);
+            const float fsa = (float)sa_out;
+            const uint32_t rest = tmem + (2 + j) * BN;
+#pragma unroll
+            for (int gq = 0; gq < BN / 32; ++gq) {
+                uint32_t r[32];
+                ptx::tmem_ld32(rest + lane_off + gq * 32, r);
+                ptx::tmem_ld_wait();
+                constexpr int kCB = 4;
+#pragma unroll
+                for (int j0 = 0; j0 < 32; j0 += kCB) {
+                    int64_t off[kCB];
+                    double cold[kCB];
+#pragma unroll
+                    for (int u = 0; u < kCB; ++u) {
+                        const int64_t co = s_coff[gq * 32 + j0 + u];
+                        off[u] = (mval && co >= 0) ? crow + co : -1;
+                        cold[u] = (direct && beta != 0.0 && off[u] >= 0) ? C.p[off[u]] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kCB; ++u) {
+                        if (off[u] < 0) continue;
+                        const int nn = n0 + gq * 32 + j0 + u;
+                        const int jj = gq * 32 + j0 + u;
+                        if (kEpi32 && epi32) {
+                            const float f = (__int2float_rn(iacc[jj]) + __uint_as_float(r[j0 + u])) * fsa * s_fsb[jj];
+                            const double val = (double)f;
+                            if (direct)
+                                C.p[off[u]] = beta != 0.0 ? fma(beta, cold[u], val) : val;
+                            else
+                                wsz[(size_t)m * N + nn] = val;
+                            continue;
+                        }
+                        const double val = sa * s_sb[jj] * ((double)iacc[jj] + (double)__uint_as_float(r[j0 + u]));
+                        if (direct) {
+                            double out = alpha * val;
+                            if (beta != 0.0) out = fma(beta, cold[u], out);
+                            C.p[off[u]] = out;
+                        } else {
+                            wsz[(size_t)m * N + nn] = val;
+                        }
+                    }
+                }
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&bars->rest_empty[j]);
         }
     }
 
@@ -728,6 +1027,7 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     splits = (nkb + kbps - 1) / kbps;
     dim3 grid((unsigned)(tiles_m * tiles_n), 1, splits);
     SingleJobs jobs;
+    jobs.splits = splits;
     jobs.M = M;
     jobs.N = N;
     jobs.tiles_m = tiles_m;
@@ -742,6 +1042,75 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     jobs.ws = ws;
     split_gemm_kernel<S, BN, NSTF, MINB, SingleJobs><<<grid, kThreads, smem, st>>>(ta, tb, A.rows_pad, B.rows_pad,
                                                                                  jobs, d_err);
+    CCSD_LAUNCH_CHECK();
+    if (splits > 1) {
+        const size_t total = (size_t)M * N;
+        const int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+        splitk_reduce<<<blocks, 256, 0, st>>>(M, N, splits, alpha, ws, beta, C);
+        CCSD_LAUNCH_CHECK();
+    }
+}
+
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        CCSD_CUDA(cudaGetDevice(&dev));
+        CCSD_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
+// The persistent kernel: as many CTAs as fit (MINB per SM, at most one per work item).
+template <int S, int BN, int NST, int MINB>
+void launch_p(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
+              const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + pbars_bytes() + 4 * epi_bytes(BN) + 1024;
+    // two-per-SM variants request at least 80 KB so that no third CTA (and its TMEM) fits
+    constexpr size_t smem = (MINB > 1 && need < 80 * 1024) ? 80 * 1024 : need;
+    static_assert(MINB * smem <= 227 * 1024 && MINB * ptmem_cols(BN) <= 512, "co-resident CTAs must fit");
+    static bool attr = false;
+    if (!attr) {
+        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_persistent_kernel<S, BN, NST, MINB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    alignas(64) CUtensorMap ta, tb;
+    encode(&ta, A, BM);
+    encode(&tb, B, BN);
+    const int nkb = A.kpad / BK;
+    const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+    const long tiles = (long)tiles_m * tiles_n;
+    const int slots = num_sms() * MINB;
+    // split K when the tiles alone leave CTAs idle, and to keep the int32 level-0 sums bounded
+    int splits = 1;
+    if (tiles < slots) splits = (int)std::min<long>((slots + tiles - 1) / tiles, std::max(1, nkb / 8));
+    splits = std::max(splits, (nkb + kMaxKbPerSplit - 1) / kMaxKbPerSplit);
+    while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
+    if ((nkb + splits - 1) / splits > kMaxKbPerSplit)
+        throw Error(-7, "split GEMM: K too long for the available split-K workspace");
+    int kbps = (nkb + splits - 1) / splits;
+    splits = (nkb + kbps - 1) / kbps;
+    const long nwork = tiles * splits;
+    if (nwork >= (1L << 31)) throw Error(-7, "split GEMM: too many tiles");
+    SingleJobs jobs;
+    jobs.splits = splits;
+    jobs.M = M;
+    jobs.N = N;
+    jobs.tiles_m = tiles_m;
+    jobs.tiles_n = tiles_n;
+    jobs.nkb_total = nkb;
+    jobs.kb_per_split = kbps;
+    jobs.scaleA = A.scale;
+    jobs.scaleB = B.scale;
+    jobs.alpha = alpha;
+    jobs.beta = beta;
+    jobs.C = C;
+    jobs.ws = ws;
+    const int grid = (int)std::min<long>(nwork, slots);
+    split_gemm_persistent_kernel<S, BN, NST, MINB><<<grid, kThreads, smem, st>>>(ta, tb, A.rows_pad, B.rows_pad,
+                                                                               jobs, (int)nwork, d_err);
     CCSD_LAUNCH_CHECK();
     if (splits > 1) {
         const size_t total = (size_t)M * N;
@@ -778,17 +1147,24 @@ void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double
         constexpr int st32 = std::max(2, std::min(3, (100 * 1024) / stage_bytes(S, 32)));
         constexpr int st64 = std::max(2, std::min(3, (100 * 1024) / stage_bytes(S, 64)));
         if (bn == 32)
-            launch_t<S, 32, st32, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+            launch_p<S, 32, st32, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
         else
-            launch_t<S, 64, st64, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+            launch_p<S, 64, st64, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
+        return;
+    }
+    // long K on the widest tile (the pair-form ladder): a tile's fill and epilogue are a
+    // small share of its main loop, and 160 columns (not a persistent width) cut the
+    // passes over A; everything else runs persistent, at most 128 columns wide
+    if (bn == 160 && nkb >= 512) {
+        launch_t<S, 160>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
         return;
     }
     switch (bn) {
-        case 160: launch_t<S, 160>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
-        case 128: launch_t<S, 128>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
-        case 96: launch_t<S, 96>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
-        case 64: launch_t<S, 64>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
-        default: launch_t<S, 32>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        case 160:
+        case 128: launch_p<S, 128, num_stages(S, 128), 1>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        case 96: launch_p<S, 96, num_stages(S, 96), 1>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        case 64: launch_p<S, 64, num_stages(S, 64), 1>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
+        default: launch_p<S, 32, num_stages(S, 32), 1>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
     }
 }
 

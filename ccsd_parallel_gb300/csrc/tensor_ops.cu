@@ -13,7 +13,7 @@ namespace ccsd {
 
 namespace {
 
-constexpr int kReduceBlocks = 4 * 152;
+constexpr int kReduceBlocks = 8 * 152;
 constexpr int kReduceThreads = 256;
 
 inline int grid_for(size_t n, int threads = 256) {
@@ -80,16 +80,46 @@ __global__ void __launch_bounds__(256) permute_axpby_kernel(PermIndex P, int p, 
 
 // R * C < 2^32: 32-bit indices, and (r, c) = divmod(idx, C) as a multiply-high
 // with the constants (cm, cl) of C (the same form as the view offsets)
+// Four elements per thread and iteration (blockDim apart, so loads stay
+// coalesced), their loads issued before any store.
 __global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, double alpha, MatView X, double beta,
                                     OutView Y) {
     const uint32_t total = (uint32_t)R * (uint32_t)C;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
-        const uint32_t r = dim_udiv(idx, cm, cl), c = idx - r * (uint32_t)C;
-        double *y = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
-        double v = alpha == 0.0 ? 0.0 : alpha * X.p[dim_off(X.row, r) + dim_off(X.col, c)];
-        if (beta != 0.0) v = fma(beta, *y, v);
-        *y = v;
+    const uint32_t step = gridDim.x * blockDim.x * 4u;
+    for (uint32_t base = blockIdx.x * blockDim.x * 4u + threadIdx.x; base < total; base += step) {
+        double *yp[4];
+        double xv[4], yv[4];
+        bool in[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t idx = base + u * blockDim.x;
+            in[u] = idx < total && idx >= base;  // idx >= base: no 32-bit wrap
+            const uint32_t r = dim_udiv(in[u] ? idx : 0u, cm, cl), c = (in[u] ? idx : 0u) - r * (uint32_t)C;
+            yp[u] = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
+            xv[u] = (in[u] && alpha != 0.0) ? X.p[dim_off(X.row, r) + dim_off(X.col, c)] : 0.0;
+            yv[u] = (in[u] && beta != 0.0) ? *yp[u] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!in[u]) continue;
+            double v = alpha == 0.0 ? 0.0 : alpha * xv[u];
+            if (beta != 0.0) v = fma(beta, yv[u], v);
+            *yp[u] = v;
+        }
     }
+}
+
+// y = a x1 + b x2 over n contiguous elements, two doubles per load
+__global__ void lincomb2_kernel(size_t n, double a, const double *__restrict__ x1, double b,
+                                const double *__restrict__ x2, double *__restrict__ y) {
+    const size_t n2 = n / 2;
+    const double2 *p1 = reinterpret_cast<const double2 *>(x1), *p2 = reinterpret_cast<const double2 *>(x2);
+    double2 *q = reinterpret_cast<double2 *>(y);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 u = p1[i], w = p2[i];
+        q[i] = make_double2(fma(b, w.x, a * u.x), fma(b, w.y, a * u.y));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) y[n - 1] = fma(b, x2[n - 1], a * x1[n - 1]);
 }
 
 __global__ void tau_kernel(int o, int v, const double *t1, const double *t2, double *tau) {
@@ -355,16 +385,20 @@ __global__ void __launch_bounds__(256) diis_store_kernel(size_t n1, size_t n2, c
     }
 }
 
-// extrapolate: (y1, y2) = sum_q c_q V_q, V_q = (t1 part of length n1, t2 part)
+// extrapolate: (y1, y2) = sum_q c_q V_q, V_q = (t1 part of length n1, t2 part); NV
+// vectors, all loads of an element issued together
+template <int NV>
 __global__ void __launch_bounds__(256) diis_combine_kernel(size_t n1, size_t n2, DiisVecs vecs,
                                                            double *__restrict__ y1, double *__restrict__ y2) {
     const size_t n = n1 + n2;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
+        double x[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = __ldcs(vecs.p[q] + idx);
         double s = 0.0;
 #pragma unroll
-        for (int q = 0; q < kDiisMax; ++q)
-            if (q < vecs.n) s = fma(vecs.c[q], vecs.p[q][idx], s);
+        for (int q = 0; q < NV; ++q) s = fma(vecs.c[q], x[q], s);
         if (idx < n1)
             y1[idx] = s;
         else
@@ -570,7 +604,24 @@ void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const doubl
         d.c[q] = coef[q];
     }
     d.n = n;
-    diis_combine_kernel<<<grid_for(n1 + n2), 256, 0, st>>>(n1, n2, d, y1, y2);
+    const int g = (int)std::min<size_t>((n1 + n2 + 255) / 256, 152 * 8);
+    switch (n) {
+#define CCSD_DIIS_CASE(NV_) \
+    case NV_: diis_combine_kernel<NV_><<<g, 256, 0, st>>>(n1, n2, d, y1, y2); break;
+        CCSD_DIIS_CASE(1) CCSD_DIIS_CASE(2) CCSD_DIIS_CASE(3) CCSD_DIIS_CASE(4) CCSD_DIIS_CASE(5)
+        CCSD_DIIS_CASE(6) CCSD_DIIS_CASE(7) CCSD_DIIS_CASE(8) CCSD_DIIS_CASE(9) CCSD_DIIS_CASE(10)
+        CCSD_DIIS_CASE(11) CCSD_DIIS_CASE(12) CCSD_DIIS_CASE(13) CCSD_DIIS_CASE(14) CCSD_DIIS_CASE(15)
+        CCSD_DIIS_CASE(16)
+#undef CCSD_DIIS_CASE
+    }
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_lincomb2(size_t n, double a, const double *x1, double b, const double *x2, double *y, cudaStream_t st) {
+    if (n == 0) return;
+    if (((uintptr_t)x1 | (uintptr_t)x2 | (uintptr_t)y) & 15)
+        throw Error(-1, "lincomb2: operands must be 16-byte aligned");
+    lincomb2_kernel<<<(int)std::min<size_t>((n / 2 + 255) / 256 + 1, 152 * 16), 256, 0, st>>>(n, a, x1, b, x2, y);
     CCSD_LAUNCH_CHECK();
 }
 
