@@ -55,12 +55,14 @@ def parse():
     ap.add_argument("--fp64-updates", type=int, default=6,
                     help="updates of the FP64 comparison run (0 skips it)")
     ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--compare-split2", type=int, default=1,
+                    help="also time the two-plane split and state its accuracy (split3 runs only)")
     ap.add_argument("--extras", type=int, default=1,
                     help="also measure the Lambda gradient at this workload and the 64-system batched solve")
     ap.add_argument("--method", default="ccsd", choices=["ccsd", "ccsdt-1a"],
                     help="amplitude equations of the timed run (ccsdt-1a: no DIIS, as the reference runs it)")
     ap.add_argument("--sites-out", default="",
-                    help="write the per-contraction-site device profile of the timed run (JSON) here")
+                    help="write the per-contraction-site device profile of the profiled run (JSON) here")
     return ap.parse_args()
 
 
@@ -252,6 +254,18 @@ def measure_extras(cg, fock, df, o, precision):
                            precision=precision, solve_s=t1 - t0, solve_updates=r["iterations"],
                            lambda_grad_s=t2 - t1, lambda_iterations=g["iterations"],
                            lambda_residual=g["residual_norm"])
+    # C2 (o=10, v=90, naux=300): the reference's own CCSD_Memory_optimized::CCSD, compiled unchanged,
+    # takes a median 248.9 s per iteration on one x86-64 core (its own clock, 8 iterations to 1e-10)
+    f2, b2 = cg.make_synthetic(10, 90, 300, 2024)
+    c2 = dict(workload="synthetic o=10 v=90 naux=300 (seed 2024), 7 updates from the MP2 start",
+              reference_memory_optimized_s_per_iteration=248.9,
+              reference_note="CCSD_Memory_optimized::CCSD compiled unchanged, single rank, 1 x86-64 core, median of its "
+                             "own per-iteration clock")
+    for prec in ("fp64", precision):
+        r2 = cg.solve(f2, 10, df=b2, fixed_iterations=7, precision=prec, amplitudes=False)
+        c2[prec + "_update_ms"] = float(np.median(r2["update_ms"][1:]))
+        c2[prec + "_e_corr"] = r2["e_corr"]
+    out["c2"] = c2
     rng = np.random.default_rng(4)
     systems = []
     for k in range(64):
@@ -446,11 +460,25 @@ def main():
         t0 = time.perf_counter()
         diis = WORKLOAD["diis"] if args.method == "ccsd" else 0
         s = cg.Solver(fock, o, df=df, precision=args.precision, fixed_iterations=U,
-                      diis_size=diis, diis_start=2, profile=True, method=args.method)
+                      diis_size=diis, diis_start=2, method=args.method)
         r = s.solve(amplitudes=True)
         t1 = time.perf_counter()
+    # The same solve again with per-site CUDA events (profile mode), for the ladder's
+    # launch times and the launch count.  It issues the kernels directly: an update
+    # replayed from a CUDA graph (the timed solve above, from its second update on)
+    # cannot carry the per-site events.
+    s.set_options(precision=args.precision, fixed_iterations=U, diis_size=diis, diis_start=2,
+                  method=args.method, profile=True)
+    rp = s.solve(amplitudes=False)
     prof = s.profile()
+    # the two-plane form (hi/lo BF16, 3 products) on the same system, for its time and its
+    # accuracy against the FP64 run below; the split3 line above is the headline
+    r2 = None
+    if args.precision == "split3" and args.compare_split2 and args.method == "ccsd":
+        s.set_options(precision="split2", fixed_iterations=U, diis_size=diis, diis_start=2, method=args.method)
+        r2 = s.solve(amplitudes=True)
     s.close()
+    profiled_ms = float(np.asarray(rp["update_ms"])[W:W + K].mean())
     if args.sites_out and rank == 0:
         Path(args.sites_out).write_text(json.dumps(prof, indent=1))
     ms = np.asarray(r["update_ms"])
@@ -470,10 +498,12 @@ def main():
     hw_tflops = lad_exec * nprod / (lad_ms * 1e-3) / 1e12
     traffic, traffic_src = ladder_traffic(o, v)
     flops_upd = r["flops_per_update"]
+    # kernels per update: the profiled solve's count (a graph replays the same kernels)
     launches = prof.get("launches", 0) / max(prof["updates"], 1) * K
 
     # ---- FP64 comparison run (same inputs, same number of updates) --------
     fp64 = {}
+    split2 = None
     nf = min(args.fp64_updates, U)
     if nf > 0:
         with cg.Solver(fock, o, df=df, precision="fp64", fixed_iterations=nf, diis_size=diis,
@@ -482,6 +512,11 @@ def main():
         ms64 = np.asarray(r64["update_ms"])
         f64_s = float(ms64[min(2, nf - 1):].mean()) / 1e3
         de = abs(r["energies"][nf] - r64["energies"][nf])
+        if r2 is not None:
+            s2 = float(np.asarray(r2["update_ms"])[W:W + K].mean()) / 1e3
+            split2 = dict(s_per_iteration=s2, speedup_vs_fp64=f64_s / s2,
+                          abs_dE_corr_vs_fp64=abs(r2["energies"][nf] - r64["energies"][nf]), compared_at_update=nf,
+                          max_abs_dT2_vs_fp64=float(np.abs(r2["t2"] - r64["t2"]).max()) if nf == U else None)
         fp64 = dict(fp64_s_per_iteration=f64_s, speedup_vs_fp64=f64_s / value,
                     abs_dE_corr_vs_fp64=de, compared_at_update=nf,
                     max_abs_dT2_vs_fp64=float(np.abs(r["t2"] - r64["t2"]).max()) if nf == U else None,
@@ -518,8 +553,11 @@ def main():
                       achieved_basis="algorithmic 2 o^2 v^4 per ladder / CUDA-event time of its two launches",
                       hw_tflops=hw_tflops, hw_frac=hw_tflops / peak_t,
                       executed_tflop_per_ladder=lad_exec / 1e12,
-                      peak_source=f"bf16_tflops_sustained of {pk_kind}", ladder_ms=lad_ms),
+                      peak_source=f"bf16_tflops_sustained of {pk_kind}", ladder_ms=lad_ms,
+                      timed_in=f"profiled solve of the same workload right after the timed one "
+                               f"(updates {W}..{U - 1}; {profiled_ms:.2f} ms per update without graphs)"),
         cpu_baseline=cpu,
+        split2=split2,
         e2e=dict(value=e2e_s, unit=UNIT, h2d_bytes_per_step=h2d / U, d2h_bytes_per_step=d2h / U,
                  includes="ccsd_create (H2D of fock + DF factors, block build) + ccsd_solve + T1/T2 read-back"),
         gpu_launches=int(round(launches)),

@@ -155,6 +155,7 @@ SIGNATURES = {
                                     C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_int64,
                                     C.c_void_p]),
     "ccsd_debug_stall_split_mma": (C.c_int, [C.c_uint64]),
+    "ccsd_set_fp64_kernel": (C.c_int, [C.c_int32]),
 }
 
 _lib = None

@@ -18,6 +18,13 @@ struct Error : std::runtime_error {
     Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
+// An allocation that an update asked for while its launches were being captured
+// into a CUDA graph (where cudaMalloc / cudaFree are not allowed): the capture is
+// dropped and the update runs directly, which makes the allocation.
+struct CaptureMiss : Error {
+    explicit CaptureMiss(const std::string &m) : Error(-3, m) {}
+};
+
 #define CCSD_CUDA(call)                                                                    \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
@@ -121,6 +128,9 @@ void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const
 
 // Elementwise/amplitude kernels (all closed-shell spatial, o = nocc, v = nvir).
 void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st);
+// tau as k_tau, and the nblocks block partials of sum_n L[n] tau[n] in the same pass
+void k_tau_dot(int o, int v, const double *t1, const double *t2, const double *L, double *tau, double *partials,
+               int nblocks, cudaStream_t st);
 void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const double *ev, double *t2,
                  cudaStream_t st);
 void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
@@ -132,7 +142,8 @@ void ao_integrals(const ::ccsd_basis &bs, double *S, double *T, double *V, doubl
                   bool device_out, cudaStream_t st);
 // R[i][j][a][b] = R[j][i][b][a] = their mean (o o v v, in place)
 void k_pair_mean(int o, int v, double *R, cudaStream_t st);
-// dinv2 (o o v v: 1 / D_ij^ab, from k_dinv2) may be NULL: then D is formed and divided per element
+// dinv2 (o o v v: 1 / D_ij^ab, from k_dinv2) may be NULL: then D is formed and divided per element.
+// partials NULL (dinv2 given): no partial sums of |t2_new - t2_old|^2, and t2_old is not read
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
                  const double *ev, const double *dinv2, const double *t2_old, double *t2_new,
                  double *partials, int nblocks, cudaStream_t st);
@@ -147,6 +158,13 @@ void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const doubl
                     double *y2, cudaStream_t st);
 // y = a x1 + b x2 over n contiguous elements (16-byte aligned arrays)
 void k_lincomb2(size_t n, double a, const double *x1, double b, const double *x2, double *y, cudaStream_t st);
+// Foo[k][i] += sum_l (2 X[k][l][i][l] - X[k][l][l][i]) for X[k][l][i][j] (o^4)
+void k_foo_from_x(int o, const double *X, double *Foo, cudaStream_t st);
+// S[i][j][a][k] = tmpB[k][i][a][j] + Z[i][j][k][a] + Vk[k][j][a][i] (o^3 v each)
+void k_t1_terms(int o, int v, const double *tmpB, const double *Z, const double *Vk, double *S, cudaStream_t st);
+// out[a][c] += coef sum_k P[k sk + a sa + c sc] for a, c < v, k < o
+void k_diag_acc(int o, int v, double coef, const double *P, int64_t sk, int64_t sa, int64_t sc, double *out,
+                cudaStream_t st);
 // R1[i][a] += sum_k (2 Z[i][k][k][a] - Z[k][i][k][a]) for Z[i][j][k][a] (o o o v)
 void k_r1_from_z(int o, int v, const double *Z, double *R1, cudaStream_t st);
 // out[q] = sum of partials[q * nparts .. q * nparts + nparts) for q < nq

@@ -155,6 +155,7 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
+    release_graphs();
     for (const ProfPending &p : prof_pending_) {
         cudaEventDestroy(p.a);
         cudaEventDestroy(p.b);
@@ -592,18 +593,34 @@ void Engine::residual() {
     cudaStream_t st = st_;
     const double *t1 = t1_.p, *t2 = t2_.p, *tau = tau_.p;
 
-    tau_op(t1, t2, tau_.p);
+    // tau of these amplitudes is already in tau_ when the energy was last taken on them
+    // (every update of a CCSD solve); a recorded residual keeps its own tau step
+    if (!(tau_fresh_ && tape_ == nullptr && opt_.method == CCSD_METHOD_CCSD)) tau_op(t1, t2, tau_.p);
+    tau_fresh_ = false;
     theta_op(t1, t2, th1_.p, th2_.p);
     // the split forms of tau as (ij|cd) (key -1) and of the ring view of t2
     // (key -2) are shared by several contractions of this update, and so are
     // tau read as [i][(l,c,d)] (key -5: Foo, R1_ovvv_tau) and as [a][(k,l,d)]
-    // (key -6: Fvv, R1_ovoo_tau)
+    // (key -6: Fvv, R1_ovoo_tau), and t2 read as [(j,b)][(k,c)] = t2[j][k][b][c]
+    // (key -7: Wvoov_t2, ring1 with symmetric amplitudes)
     if (split_ && opt_.precision != CCSD_PREC_FP64) split_->begin_update();
 
-    // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d]
+    // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d].  With symmetric amplitudes
+    // (DF input, no tape: see r1_from_z below) it is sum_l (2 X[k,l,i,l] - X[k,l,l,i]) of the
+    // o^4 product X[k][l][i][j] = sum_cd (kc|ld) tau[i,j,c,d] that Woooo needs anyway, so X is
+    // formed here (site Woooo_tau) and the o x o x o v^2 contraction is not run.
+    const bool sym_amps = tape_ == nullptr && df_input_;
     copy(Foo_.p, f_oo_off_.p, (size_t)(o2));
-    gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
-         mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, -5, "Foo");
+    if (sym_amps) {
+        Xoooo_.ensure((size_t)o2 * o2);
+        gemm((int)o2, (int)o2, (int)v2, 1.0,
+             mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
+             mv(tau, ix1(v2), ix1(1)), 0.0, ovw(Xoooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
+        k_foo_from_x(io, Xoooo_.p, Foo_.p, st_);
+    } else {
+        gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
+             mv(tau, ix1(ov2), ix1(1)), 1.0, ovw(Foo_.p, ix1(o), ix1(1)), 1, -5, "Foo");
+    }
     // Fvv[a][c] = f_vv' - sum_{kld} Lovov[k,c,l,d] tau[k,l,a,d]
     copy(Fvv_.p, f_vv_off_.p, (size_t)(v2));
     gemm(iv, iv, (int)(o * o * v), -1.0, mv(tau, ix1(v), ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1)),
@@ -623,8 +640,13 @@ void Engine::residual() {
     copy(Lvv_.p, Fvv_.p, (size_t)(v2));
     gemm(iv, iv, io, -1.0, mv(t1, ix1(1), ix1(v)), mv(f_ov_.p, ix1(1), ix1(v)), 1.0,
          ovw(Lvv_.p, ix1(v), ix1(1)), 0, 0, "Lvv_f");
-    gemm((int)v2, 1, (int)ov, 1.0, mv(Lovvv_.p, ix1(1), ix1(v2)), mv(t1, ix1(0), ix1(1)), 1.0,
-         ovw(Lvv_.p, ix1(1), ix1(0)), 0, 0, "Lvv_t1");
+    // With symmetric amplitudes (sym_amps) the Lovvv t1 term is not read from the o v^3 block
+    // here: sum_kd Lovvv[k,d,a,c] t1[k,d] = 2 sum_k X[(k,a,c)][k] - sum_k Y[(k,c,a)][k] with
+    // the products X of site Wvovo_t1v and Y of site Rp_ovvv_t1 below, whose diagonals are
+    // added to Lvv there (Lvv is first read by Rp_Lvv, after both).
+    if (!sym_amps)
+        gemm((int)v2, 1, (int)ov, 1.0, mv(Lovvv_.p, ix1(1), ix1(v2)), mv(t1, ix1(0), ix1(1)), 1.0,
+             ovw(Lvv_.p, ix1(1), ix1(0)), 0, 0, "Lvv_t1");
 
     // ---- T1 numerator ----------------------------------------------------
     copy(R1_.p, f_ov_.p, (size_t)(ov));
@@ -659,7 +681,7 @@ void Engine::residual() {
     // (one perturbed element, as a finite-difference check does), and a recorded
     // residual (gradient, batched solve) follows the contraction's per-element
     // derivative convention, so both keep the contraction.
-    const bool r1_from_z = tape_ == nullptr && df_input_;
+    const bool r1_from_z = sym_amps;
     if (!r1_from_z)
     gemm(io, iv, (int)(o * v2), 1.0, mv(tau, ix1(ov2), ix1(1)),
          mv(Lovvv_.p, ix1(v), ix3((uint32_t)v, (uint32_t)v, v * v2, 1, v2)), 1.0,
@@ -681,10 +703,14 @@ void Engine::residual() {
     gemm((int)(o * o2), io, iv, 1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)o, v * o2, o, 1), ix1(o2)), mv(t1, ix1(v), ix1(1)),
          1.0, ovw(Woooo_.p, ix3((uint32_t)o, (uint32_t)o, o * o2, o2, 1), ix1(o)), 0, 0, "Woooo_t1b");
-    // + sum_cd (kc|ld) tau[i,j,c,d]: M = (k,l), N = (i,j), K = (c,d)
-    gemm((int)o2, (int)o2, (int)v2, 1.0,
-         mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
-         mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
+    // + sum_cd (kc|ld) tau[i,j,c,d]: M = (k,l), N = (i,j), K = (c,d) (already formed as X above
+    // when the amplitudes are symmetric)
+    if (sym_amps)
+        k_lincomb2((size_t)o2 * o2, 1.0, Woooo_.p, 1.0, Xoooo_.p, Woooo_.p, st_);
+    else
+        gemm((int)o2, (int)o2, (int)v2, 1.0,
+             mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
+             mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
 
     // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
     copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
@@ -693,6 +719,8 @@ void Engine::residual() {
     // Y is formed once, into Rp, and Wvoov[i][a][k][c] += Y[(k,c,a)][i] = Rp[k][i][c][a]
     gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
          ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
+    // Lvv[a][c] -= sum_k Y[(k,c,a)][k] = sum_k Rp[k][k][c][a]
+    if (sym_amps) k_diag_acc(o_, v_, -1.0, Rp_.p, (int64_t)(o + 1) * v2, 1, v, Lvv_.p, st_);
     axpby((int)(ov * v), io, 1.0, mv(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 1.0,
           ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)));
     // - sum_l (kc|li) t1[l,a]: M = (i,k,c) (c, contiguous in Wvoov, innermost), N = a, K = l
@@ -706,15 +734,19 @@ void Engine::residual() {
     // - 1/2 sum_ld (lc|kd) t2[i,l,a,d]
     gemm((int)ov, (int)ov, (int)ov, -0.5, mv(t2, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)),
          mv(ovov_.p, ix2((uint32_t)v, v, ov), ix2((uint32_t)v, v * ov, 1)), 1.0,
-         ovw(Wvoov_.p, ix1(ov), ix1(1)), 0, 8, "Wvoov_t2");
+         ovw(Wvoov_.p, ix1(ov), ix1(1)), -7, 8, "Wvoov_t2");
 
     // ---- Wvovo_s[i][a][k][c] = W_akci ------------------------------------
     axpby((int)ov, (int)ov, 1.0, mv(oovv_.p, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)),
                0.0, ovw(Wvovo_.p, ix1(ov), ix1(1)));
-    // + sum_d (kd|ac) t1[i,d]: M = (k,a,c), N = i, K = d
+    // + sum_d (kd|ac) t1[i,d]: M = (k,a,c), N = i, K = d.  Lvv[a][c] += 2 sum_k X[(k,a,c)][k],
+    // the change of sum_k Wvovo[k][a][k][c] across this product
+    const int64_t wv_k = (int64_t)v * (ov + 1);  // Wvovo[k][a][k][c]: k stride, a stride ov
+    if (sym_amps) k_diag_acc(o_, v_, -2.0, Wvovo_.p, wv_k, ov, 1, Lvv_.p, st_);
     gemm((int)(ov * v), io, iv, 1.0,
          mv(ovvv_.p, ix3((uint32_t)v, (uint32_t)v, v * v2, v, 1), ix1(v2)), mv(t1, ix1(v), ix1(1)),
          1.0, ovw(Wvovo_.p, ix3((uint32_t)v, (uint32_t)v, v, ov, 1), ix1(v * ov)), 9, 0, "Wvovo_t1v");
+    if (sym_amps) k_diag_acc(o_, v_, 2.0, Wvovo_.p, wv_k, ov, 1, Lvv_.p, st_);
     // - sum_l (lc|ki) t1[l,a]: M = (i,k,c) (c innermost), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, o, o2), ix1(v * o2)), mv(t1, ix1(1), ix1(v)),
@@ -757,9 +789,15 @@ void Engine::residual() {
     // - sum_k t1[k,a] sum_c (ki|bc) t1[j,c]: Vk[k][i][b][j] = sum_c oovv[k,i,b,c] t1[j,c]
     gemm((int)(o2 * v), io, iv, 1.0, mv(oovv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
          ovw(Vk_.p, ix1(o), ix1(1)), 15, 0, "Rp_oovv_t1");
-    gemm((int)(o * v * o), iv, io, -1.0,
-         mv(Vk_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1), ix1(v)), 0, 0, "Rp_oovv_t1t1");
+    // Unrecorded, the three o^3 v x t1 terms of Rp (this one, tmpB's and Z's below) are summed
+    // into one operand and contracted once (site Rp_t1_o3v), one pass over Rp instead of
+    // three.  This term enters as its transpose Rp^T[i][j][a][b] = Rp[j][i][b][a], which the
+    // update adds anyway (R2 = R + Rp + Rp^T): -sum_k Vk[k][j][a][i] t1[k,b].
+    const bool merge_t1 = tape_ == nullptr;
+    if (!merge_t1)
+        gemm((int)(o * v * o), iv, io, -1.0,
+             mv(Vk_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o * v * o)), mv(t1, ix1(1), ix1(v)),
+             1.0, ovw(Rp_.p, ix3((uint32_t)o, (uint32_t)v, ov2, v2, 1), ix1(v)), 0, 0, "Rp_oovv_t1t1");
     // - sum_k tmpB[k,i,a,j] t1[k,b], tmpB = (ia|jk) + sum_c (kc|ia) t1[j,c]
     axpby((int)(o * ov), io, 1.0,
                mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), 0.0,
@@ -767,16 +805,25 @@ void Engine::residual() {
     gemm((int)(o * ov), io, iv, 1.0,
          mv(ovov_.p, ix3((uint32_t)o, (uint32_t)v, v * o * v, v, 1), ix1(o * v)), mv(t1, ix1(v), ix1(1)),
          1.0, ovw(tmpB_.p, ix1(o), ix1(1)), 16, 0, "Rp_ovov_t1");
-    gemm((int)(o2 * v), iv, io, -1.0,
-         mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
+    if (!merge_t1)
+        gemm((int)(o2 * v), iv, io, -1.0,
+             mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
+             1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
     // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d]
     gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
          mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
          ovw(Z_.p, ix1(ov), ix1(1)), -1, 12, "Rp_Z");
     if (r1_from_z) k_r1_from_z(io, iv, Z_.p, R1_.p, st_);
-    gemm((int)(o2 * v), iv, io, -1.0, mv(Z_.p, ix2((uint32_t)v, ov, 1), ix1(v)), mv(t1, ix1(1), ix1(v)),
-         1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_Z_t1");
+    if (merge_t1) {
+        // S[i][j][a][k] = tmpB[k][i][a][j] + Z[i][j][k][a] + Vk[k][j][a][i]; Rp -= S t1
+        S3_.ensure((size_t)o2 * ov);
+        k_t1_terms(io, iv, tmpB_.p, Z_.p, Vk_.p, S3_.p, st_);
+        gemm((int)(o2 * v), iv, io, -1.0, mv(S3_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+             ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_t1_o3v");
+    } else {
+        gemm((int)(o2 * v), iv, io, -1.0, mv(Z_.p, ix2((uint32_t)v, ov, 1), ix1(v)), mv(t1, ix1(1), ix1(v)),
+             1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_Z_t1");
+    }
     // + sum_c Lvv'[a,c] t2[i,j,c,b]: M = a, N = (i,j,b), K = c
     gemm(iv, (int)(o2 * v), iv, 1.0, mv(Lvv_.p, ix1(v), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, 1), ix1(v)), 1.0, ovw(Rp_.p, ix1(v), ix2((uint32_t)v, v2, 1)), 0, 0, "Rp_Lvv");
@@ -786,10 +833,12 @@ void Engine::residual() {
     gemm(io, (int)ov2, io, -1.0, fik ? mv(Loo_.p, ix1(o), ix1(1)) : mv(Loo_.p, ix1(1), ix1(o)),
          mv(t2, ix1(1), ix1(ov2)), 1.0, ovw(Rp_.p, ix1(ov2), ix1(1)), 0, 0, "Rp_Loo");
     // rings, M = (i,a), N = (j,b), K = (k,c)
-    // + sum_kc Wa[i,a,k,c] t2[k,j,c,b]
+    // + sum_kc Wa[i,a,k,c] t2[k,j,c,b].  With symmetric amplitudes t2[k,j,c,b] = t2[j,k,b,c]:
+    // the view of site Wvoov_t2 (key -7), read along c, whose split is reused here
     gemm((int)ov, (int)ov, (int)ov, 1.0, mv(Wa_.p, ix1(ov), ix1(1)),
-         mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)), 1.0,
-         ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)), 0, 0, "ring1");
+         sym_amps ? mv(t2, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1))
+                  : mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)),
+         1.0, ovw(Rp_.p, ix2((uint32_t)v, ov2, v), ix2((uint32_t)v, v2, 1)), 0, sym_amps ? -7 : 0, "ring1");
     // - sum_kc Wvoov[i,a,k,c] t2[k,j,b,c]
     gemm((int)ov, (int)ov, (int)ov, -1.0, mv(Wvoov_.p, ix1(ov), ix1(1)),
          mv(t2, ix2((uint32_t)v, v2, v), ix2((uint32_t)v, ov2, 1)), 1.0,
@@ -811,9 +860,8 @@ double Engine::reduce_sum(int nparts) {
 // E = sum_ijab [2(ia|jb) - (ib|ja)] tau_ij^ab  (ccsd_memory_optimized.cpp:592-648,
 // without the f_ia t_i^a term, :646)
 double Engine::energy_of(const double *t1, const double *t2) {
-    const size_t nT2 = (size_t)o_ * o_ * v_ * v_;
-    k_tau(o_, v_, t1, t2, tau_.p, st_);
-    k_dot(nT2, Lijab_.p, tau_.p, partials_.p, reduce_blocks(), st_);
+    k_tau_dot(o_, v_, t1, t2, Lijab_.p, tau_.p, partials_.p, reduce_blocks(), st_);
+    tau_fresh_ = t1 == t1_.p && t2 == t2_.p;
     return reduce_sum(reduce_blocks());
 }
 
@@ -860,6 +908,7 @@ void Engine::diis_step(int update_index) {
         diis_b_[(size_t)slot * m + js[q]] = dots[q];
         diis_b_[(size_t)js[q] * m + slot] = dots[q];
     }
+    diis_self_ = diis_b_[(size_t)slot * m + slot];
     if (diis_count_ < 2 || update_index < opt_.diis_start) return;
     // bordered system [B -1; -1 0] [c; lam] = [0; -1], scaled for conditioning
     const int k = diis_count_;
@@ -907,6 +956,83 @@ void Engine::diis_step(int update_index) {
 }
 
 // ---------------------------------------------------------------------------
+// One amplitude update up to the residual norm's partial sums: residual, (T3 terms,)
+// T2 and T1 from the denominators.
+void Engine::update_step() {
+    residual();
+    if (opt_.method != CCSD_METHOD_CCSD) triples_step();  // T3 terms, then T3 from this T2
+    k_update_t2(o_, v_, R_.p, Rp_.p, eo_.p, ev_.p, dinv2_.p, t2_.p, t2n_.p, norm_in_diis_ ? nullptr : partials_.p,
+                reduce_blocks(), st_);
+    k_update_t1(o_, v_, R1_.p, eo_.p, ev_.p, t1_.p, t1n_.p, partials_.p + reduce_blocks(), st_);
+}
+
+// The same through a CUDA graph: captured the first time a parity of the amplitude
+// buffers comes up, replayed afterwards.  Every pointer the update touches is fixed
+// for a solve except the swapped t1/t2 buffers, hence one graph per parity.  A capture
+// that fails leaves graphs off and runs the update directly.
+void Engine::update_step_graph() {
+    for (UpdateGraph &g : graphs_) {
+        if (g.exec && g.t1 == t1_.p && g.t2 == t2_.p) {
+            CCSD_CUDA(cudaGraphLaunch(g.exec, st_));
+            note_launch((int)g.launches);
+            return;
+        }
+    }
+    UpdateGraph &g = graphs_[graphs_[0].exec ? 1 : 0];
+    if (g.exec) {  // both parities taken by other buffers: start over
+        release_graphs();
+    }
+    const long l0 = launch_count();
+    if (cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        graphs_ok_ = false;
+        update_step();
+        return;
+    }
+    auto drop_capture = [&]() {
+        cudaGraph_t gg = nullptr;
+        cudaStreamEndCapture(st_, &gg);
+        if (gg) cudaGraphDestroy(gg);
+        cudaGetLastError();
+        note_launch(-(int)(launch_count() - l0));  // captured launches that never ran
+    };
+    try {
+        update_step();
+    } catch (const CaptureMiss &) {
+        // an operand buffer had to grow: nothing captured has run, so run the update
+        // directly (it makes the allocation); the next update captures again
+        drop_capture();
+        update_step();
+        return;
+    } catch (...) {
+        drop_capture();
+        graphs_ok_ = false;
+        throw;
+    }
+    cudaGraph_t gg = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st_, &gg);
+    if (e == cudaSuccess && gg) e = cudaGraphInstantiate(&g.exec, gg, 0);
+    if (gg) cudaGraphDestroy(gg);
+    if (e != cudaSuccess || !g.exec) {  // not capturable here: run this and later updates directly
+        cudaGetLastError();
+        g.exec = nullptr;
+        graphs_ok_ = false;
+        update_step();
+        return;
+    }
+    g.t1 = t1_.p;
+    g.t2 = t2_.p;
+    g.launches = launch_count() - l0;
+    CCSD_CUDA(cudaGraphLaunch(g.exec, st_));
+}
+
+void Engine::release_graphs() {
+    for (UpdateGraph &g : graphs_) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = UpdateGraph();
+    }
+}
+
 void Engine::solve(ccsd_result *res) {
     const int o = o_, v = v_;
     const size_t nT1 = (size_t)o * v, nT2 = nT1 * o * v;
@@ -933,6 +1059,7 @@ void Engine::solve(ccsd_result *res) {
         k_mp2_guess(o, v, ovov_.p, eo_.p, ev_.p, t2_.p, st_);
     }
     if (opt_.method != CCSD_METHOD_CCSD) triples_setup();  // T3 = 0
+    tau_fresh_ = false;
     double e_new = energy_of(t1_.p, t2_.p);
     int hist = 0;
     if (res->energy_history && res->history_capacity > 0) res->energy_history[hist] = e_new;
@@ -941,6 +1068,15 @@ void Engine::solve(ccsd_result *res) {
     cudaEvent_t ev0, ev1;
     CCSD_CUDA(cudaEventCreate(&ev0));
     CCSD_CUDA(cudaEventCreate(&ev1));
+    // from the second update on, the residual and amplitude update run as captured graphs
+    // (CCSD on a private or user stream, the legacy default stream cannot be captured;
+    // not while profiling, whose per-site events a graph cannot time)
+    release_graphs();
+    // with DIIS the residual norm is the store's <E, E> (E = T_new - T_old), so the T2 update
+    // neither reads T_old nor sums it
+    norm_in_diis_ = opt_.diis_size > 0 && dinv2_.p != nullptr && opt_.method == CCSD_METHOD_CCSD;
+    const bool use_graphs = graphs_ok_ && opt_.method == CCSD_METHOD_CCSD && st_ != nullptr && tape_ == nullptr &&
+                            !opt_.profile;
     int updates = 0;
     bool converged = false;
     const int cap = opt_.fixed_iterations > 0 ? opt_.fixed_iterations : std::max(opt_.max_iter, 1);
@@ -949,13 +1085,14 @@ void Engine::solve(ccsd_result *res) {
             const double e_old = e_new;
             const long launches0 = launch_count();
             CCSD_CUDA(cudaEventRecord(ev0, st_));
-            residual();
-            if (opt_.method != CCSD_METHOD_CCSD) triples_step();  // T3 terms, then T3 from this T2
-            k_update_t2(o, v, R_.p, Rp_.p, eo_.p, ev_.p, dinv2_.p, t2_.p, t2n_.p, partials_.p, reduce_blocks(), st_);
-            k_update_t1(o, v, R1_.p, eo_.p, ev_.p, t1_.p, t1n_.p, partials_.p + reduce_blocks(), st_);
-            const double rn2 = reduce_sum(reduce_blocks() + 1);
-            last_resid_ = std::sqrt(std::max(rn2, 0.0));
+            if (use_graphs && updates >= 1)
+                update_step_graph();
+            else
+                update_step();
+            // |T_new - T_old|^2: the DIIS store's <E, E> when DIIS runs, else the update's partials
+            const double rn2 = norm_in_diis_ ? 0.0 : reduce_sum(reduce_blocks() + 1);
             diis_step(updates);
+            last_resid_ = std::sqrt(std::max(norm_in_diis_ ? diis_self_ : rn2, 0.0));
             std::swap(t1_, t1n_);
             std::swap(t2_, t2n_);
             e_new = energy_of(t1_.p, t2_.p);
@@ -997,10 +1134,12 @@ void Engine::solve(ccsd_result *res) {
     } catch (...) {
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
+        release_graphs();
         throw;
     }
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
+    release_graphs();
     solved_ = true;
     last_e_ = e_new;
     res->e_corr = e_new;

@@ -92,6 +92,20 @@ class Engine {
         double flops;
         bool split;
     };
+    // One update's residual and amplitude-update kernels as a CUDA graph, one per
+    // parity of the swapped amplitude buffers; replayed instead of re-issuing ~130
+    // launches and their host work.  Kept for one solve; not used while profiling
+    // (the per-site CUDA events cannot be timed from a graph).
+    struct UpdateGraph {
+        cudaGraphExec_t exec = nullptr;
+        const double *t1 = nullptr, *t2 = nullptr;
+        long launches = 0;
+    };
+    UpdateGraph graphs_[2];
+    bool graphs_ok_ = true;
+    void update_step();
+    void update_step_graph();
+    void release_graphs();
     cudaEvent_t prof_event();
     void prof_flush();
     std::map<std::string, ProfSite> prof_;
@@ -155,9 +169,12 @@ class Engine {
     DBuf qtmp_;                                // scratch of the Theta adjoint
     bool solved_ = false;
     double last_e_ = 0.0;
-    double energy_of(const double *t1, const double *t2);  // uses tau_ as scratch
+    double energy_of(const double *t1, const double *t2);  // leaves tau(t1, t2) in tau_
+    bool tau_fresh_ = false;  // tau_ holds tau(t1_, t2_) from energy_of
     double reduce_sum(int nparts);
     void diis_step(int update_index);
+    double diis_self_ = 0.0;     // <E, E> of the vector the last diis_step stored
+    bool norm_in_diis_ = false;  // this solve takes |T_new - T_old| from diis_self_
 
     int o_ = 0, v_ = 0, n_ = 0;
     int nf_ = 0, nt_ = 0;  // frozen core orbitals; orbitals of the input arrays (nf_ + n_)
@@ -182,6 +199,8 @@ class Engine {
     DBuf ws_, partials_, scalars_;
     DBuf dinv2_;          // 1 / D_ij^ab, [i][j][a][b] (the update multiplies by it)
     bool df_input_ = false;  // integrals from DF factors: (pq|rs) = (rs|pq) for any input
+    DBuf Xoooo_;             // sum_cd (kc|ld) tau[i,j,c,d], shared by Foo and Woooo
+    DBuf S3_;                // [i][j][a][k]: the o^3 v operands of Rp's t1 terms, summed
     DBuf diis_partials_;  // DIIS overlaps: block partials per stored vector
     // DIIS storage: vectors (T) and errors (T_new - T_old), each o*v + o^2 v^2
     std::vector<DBuf> diis_t_, diis_e_;

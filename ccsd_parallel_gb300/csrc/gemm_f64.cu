@@ -3,13 +3,20 @@
 // C(m,n) = alpha * sum_k A(m,k) B(n,k) + beta * C(m,n), with A, B and C read
 // and written through 3-level index views (common.h), so a 4-index CCSD
 // contraction runs without a transposed copy.  tcgen05 has no f64 kind, so
-// this path is DFMA on the CUDA cores: a 64x64 block tile, 16-deep K step,
-// 4x4 register micro-tile per thread.  Skinny shapes are split over K into a
-// scratch buffer and summed in a fixed order (deterministic results).
+// this path runs a 64x64 block tile with a 16-deep K step either as DFMA on the
+// CUDA cores (4x4 register micro-tile per thread) or as mma.sync m8n8k4 DMMA on
+// the FP64 tensor pipe (ccsd_set_fp64_kernel).  Skinny shapes are split over K
+// into a scratch buffer and summed in a fixed order (deterministic results).
+#include <atomic>
+
 #include "../../include/ccsd_gb300.h"
 #include "common.h"
 
 namespace ccsd {
+
+// the tiled kernel's inner product: CCSD_FP64_DFMA (CUDA cores) or CCSD_FP64_DMMA
+// (mma.sync m8n8k4 on the FP64 tensor pipe); process-wide, ccsd_set_fp64_kernel
+std::atomic<int> g_fp64_kernel{CCSD_FP64_DFMA};
 
 namespace {
 
@@ -105,6 +112,102 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(int M, int N, int K, int k
             for (int j = 0; j < 4; ++j) {
                 int n = n0 + tx + 16 * j;
                 if (n < N) w[(size_t)m * N + n] = acc[i][j];
+            }
+        }
+    }
+}
+
+// The same tile on the FP64 tensor pipe: mma.sync m8n8k4 (DMMA).  The staging into
+// shared memory is the DFMA kernel's; each of the 8 warps owns a 32 x 16 block of the
+// 64 x 64 tile (4 x 2 fragments of 8 x 8, two accumulators per thread and fragment).
+// Fragment layouts (PTX ISA, mma.m8n8k4 .f64): A row-major, lane holds A[lane/4][lane%4];
+// B column-major, lane holds B[k = lane%4][n = lane/4]; C lane holds C[lane/4][2 (lane%4) + e].
+template <bool A_KC, bool B_KC>
+__global__ void __launch_bounds__(NT) gemm_f64_dmma_kernel(int M, int N, int K, int kchunk, double alpha,
+                                                           MatView A, MatView B, double beta, OutView C,
+                                                           double *ws) {
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(K, kbeg + kchunk);
+
+    int64_t a_row[4], b_row[4];
+    bool a_ok[4], b_ok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        int ra = A_KC ? (tid / 16 + 16 * q) : (tid % 64);
+        int rb = B_KC ? (tid / 16 + 16 * q) : (tid % 64);
+        a_ok[q] = (m0 + ra) < M;
+        b_ok[q] = (n0 + rb) < N;
+        a_row[q] = a_ok[q] ? dim_off(A.row, m0 + ra) : 0;
+        b_row[q] = b_ok[q] ? dim_off(B.row, n0 + rb) : 0;
+    }
+
+    double acc[4][2][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+    const int fr = lane >> 2, fk = lane & 3;
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int ka = A_KC ? (tid % 16) : (tid / 64 + 4 * q);
+            int ra = A_KC ? (tid / 16 + 16 * q) : (tid % 64);
+            int kk = k0 + ka;
+            double va = 0.0;
+            if (a_ok[q] && kk < kend) va = A.p[a_row[q] + dim_off(A.col, kk)];
+            As[ka][ra] = va;
+            int kb = B_KC ? (tid % 16) : (tid / 64 + 4 * q);
+            int rb = B_KC ? (tid / 16 + 16 * q) : (tid % 64);
+            int kk2 = k0 + kb;
+            double vb = 0.0;
+            if (b_ok[q] && kk2 < kend) vb = B.p[b_row[q] + dim_off(B.col, kk2)];
+            Bs[kb][rb] = vb;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < BK; ks += 4) {
+            double a[4], b[2];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[ks + fk][wm + 8 * i + fr];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) b[j] = Bs[ks + fk][wn + 8 * j + fr];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                    asm volatile(
+                        "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+                        : "+d"(acc[i][j][0]), "+d"(acc[i][j][1])
+                        : "d"(a[i]), "d"(b[j]));
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = m0 + wm + 8 * i + fr;
+        if (m >= M) continue;
+        const int64_t ro = gridDim.z == 1 ? dim_off(C.row, m) : 0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int n = n0 + wn + 8 * j + 2 * fk + e;
+                if (n >= N) continue;
+                if (gridDim.z == 1) {
+                    double *c = C.p + ro + dim_off(C.col, n);
+                    double v = alpha * acc[i][j][e];
+                    if (beta != 0.0) v = fma(beta, *c, v);
+                    *c = v;
+                } else {
+                    ws[(size_t)blockIdx.z * M * N + (size_t)m * N + n] = acc[i][j][e];
+                }
             }
         }
     }
@@ -514,7 +617,16 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
     dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
     bool akc = A.col.s2 == 1;
     bool bkc = B.col.s2 == 1;
-    if (akc && bkc)
+    if (g_fp64_kernel.load(std::memory_order_relaxed) == CCSD_FP64_DMMA) {
+        if (akc && bkc)
+            gemm_f64_dmma_kernel<true, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+        else if (akc)
+            gemm_f64_dmma_kernel<true, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+        else if (bkc)
+            gemm_f64_dmma_kernel<false, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+        else
+            gemm_f64_dmma_kernel<false, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
+    } else if (akc && bkc)
         gemm_f64_kernel<true, true><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
     else if (akc)
         gemm_f64_kernel<true, false><<<grid, NT, 0, st>>>(M, N, K, kchunk, alpha, A, B, beta, C, ws);
@@ -532,3 +644,8 @@ void gemm_f64(int M, int N, int K, double alpha, const MatView &A, const MatView
 }
 
 }  // namespace ccsd
+
+extern "C" int ccsd_set_fp64_kernel(int32_t kind) {
+    if (kind != CCSD_FP64_DFMA && kind != CCSD_FP64_DMMA) return CCSD_ERR_INVALID_ARG;
+    return ccsd::g_fp64_kernel.exchange(kind);
+}

@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "common.h"
+#include "fp64_ops.cuh"
 #include "ladder_sym.cuh"
 
 namespace ccsd {
@@ -91,8 +92,10 @@ __global__ void __launch_bounds__(256) tau_sym_tiled_kernel(int o, int v, const 
             if (c < v && d < v && d <= c) {
                 const double x1 = tij[(size_t)c * v + d], x2 = s2[tx][q];
                 const double x3 = s3[tx][q], x4 = tji[(size_t)c * v + d];
-                tp[rowp + (int64_t)c * (c + 1) / 2 + d] = 0.25 * ((x1 + x2) + (x3 + x4));
-                if (i > j && c > d) tm[rowm + (int64_t)c * (c - 1) / 2 + d] = 0.25 * ((x1 - x2) + (x3 - x4));
+                // four FP64 additions; the quarter is taken on the exponent field
+                const double u = x1 + x3, w = x2 + x4;
+                tp[rowp + (int64_t)c * (c + 1) / 2 + d] = mul_pow2(u + w, -2);
+                if (i > j && c > d) tm[rowm + (int64_t)c * (c - 1) / 2 + d] = mul_pow2(u - w, -2);
             }
         }
         __syncthreads();

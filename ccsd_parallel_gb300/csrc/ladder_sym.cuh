@@ -35,8 +35,9 @@ __device__ __forceinline__ void tau_sym_elem(int o, int v, const double *__restr
     const double x2 = tau[i * ov2 + j * v2 + (int64_t)d * v + c];
     const double x3 = tau[j * ov2 + i * v2 + (int64_t)d * v + c];
     const double x4 = tau[j * ov2 + i * v2 + (int64_t)c * v + d];
-    tp[idx] = 0.25 * ((x1 + x2) + (x3 + x4));
-    if (i > j && c > d) tm[stri(i, j) * Tmv + stri(c, d)] = 0.25 * ((x1 - x2) + (x3 - x4));
+    const double u = x1 + x3, w = x2 + x4;  // the tiled kernel's order of additions
+    tp[idx] = 0.25 * (u + w);
+    if (i > j && c > d) tm[stri(i, j) * Tmv + stri(c, d)] = 0.25 * (u - w);
 }
 
 // element idx < o^2 v^2 of R[i][j][a][b] += S+ + sgn sgn S-

@@ -453,8 +453,10 @@ struct PBars {
 __host__ __device__ constexpr size_t pbars_bytes() { return (sizeof(PBars) + 15) / 16 * 16; }
 __host__ __device__ constexpr int ptmem_cols(int BN) { return 4 * BN <= 128 ? 128 : (4 * BN <= 256 ? 256 : 512); }
 
-template <int S, int BN, int NST, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB)
+// EW epilogue warps (warps 2 .. EW+1): warp w covers TMEM lane quarter w % 4 and the
+// column slice (w - 2) / 4 of BN / (EW / 4) columns; KCB C loads are issued together.
+template <int S, int BN, int NST, int MINB, int EW, int KCB>
+__global__ void __launch_bounds__(64 + 32 * EW, MINB)
     split_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                                  int rowsA_pad, int rowsB_pad, const SingleJobs jobs, int nwork, int *gerr) {
     constexpr int SB = stage_bytes(S, BN);
@@ -464,6 +466,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
     constexpr int NCOLS = ptmem_cols(BN);
     constexpr bool kEpi32 = S <= 3;
     static_assert(4 * BN <= 512, "four BN-column accumulators must fit in TMEM");
+    static_assert(EW == 4 || EW == 8, "four or eight epilogue warps");
+    constexpr int BW = BN / (EW / 4);  // columns per epilogue warp
+    static_assert(BW % 32 == 0 && 32 % KCB == 0, "column slices of whole 32-column groups");
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -477,9 +482,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
         }
         for (int b = 0; b < 2; ++b) {
             ptx::mbar_init(&bars->acc_full[b], 1);
-            ptx::mbar_init(&bars->acc_empty[b], 4);
+            ptx::mbar_init(&bars->acc_empty[b], EW);
             ptx::mbar_init(&bars->rest_full[b], 1);
-            ptx::mbar_init(&bars->rest_empty[b], 4);
+            ptx::mbar_init(&bars->rest_empty[b], EW);
         }
         ptx::mbar_init(&bars->drain, 1);
         bars->abort = 0;
@@ -592,23 +597,24 @@ __global__ void __launch_bounds__(kThreads, MINB)
             ptx::mbar_wait(&bars->drain, 0, &bars->never, gerr, 16, kWaitNs);
         }
     } else {
-        // epilogue warps 2..5; TMEM lane quarter = warp % 4; each warp keeps its own
-        // column table (offsets, FP64 and FP32 column scales) behind the barriers
+        // epilogue warps 2 .. EW+1; TMEM lane quarter = warp % 4, column slice (warp - 2) / 4;
+        // each warp keeps its own column table (offsets, FP64 and FP32 column scales)
         const int q = warp & 3;
+        const int c0 = ((warp - 2) >> 2) * BW;  // first column of this warp's slice
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        unsigned char *tbl = (unsigned char *)bars + pbars_bytes() + (size_t)(warp - 2) * epi_bytes(BN);
+        unsigned char *tbl = (unsigned char *)bars + pbars_bytes() + (size_t)(warp - 2) * epi_bytes(BW);
         int64_t *s_coff = (int64_t *)tbl;
-        double *s_sb = (double *)(s_coff + BN);
-        float *s_fsb = (float *)(s_sb + BN);
+        double *s_sb = (double *)(s_coff + BW);
+        float *s_fsb = (float *)(s_sb + BW);
         int c = 0, n = 0;
         for (int w = blockIdx.x; w < nwork; w += gridDim.x, ++n) {
             const TileJob J = jobs.job_at(w);
             const int j = n & 1;
-            const int m0 = J.mt * BM, n0 = J.nt * BN, M = J.M, N = J.N, nkb = J.nkb;
+            const int m0 = J.mt * BM, n0 = J.nt * BN + c0, M = J.M, N = J.N, nkb = J.nkb;
             const OutView C = J.C;
             __syncwarp();  // the previous tile's table reads are done
             int ebmin = 1 << 20, ebmax = -(1 << 20);
-            for (int jj = lane; jj < BN; jj += 32) {
+            for (int jj = lane; jj < BW; jj += 32) {
                 const int nn = n0 + jj;
                 const double sbn = nn < N ? J.scaleB[nn] : 0.0;
                 s_coff[jj] = nn < N ? dim_off(C.col, (uint32_t)nn) : -1;
@@ -626,9 +632,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
                 ebmax = max(ebmax, __shfl_xor_sync(0xffffffffu, ebmax, off));
             }
             __syncwarp();
-            int32_t iacc[BN];
+            int32_t iacc[BW];
 #pragma unroll
-            for (int jj = 0; jj < BN; ++jj) iacc[jj] = 0;
+            for (int jj = 0; jj < BW; ++jj) iacc[jj] = 0;
             const int nch = (nkb + CHUNK_KB - 1) / CHUNK_KB;
             bool ok = true;
             for (int ch = 0; ch < nch; ++ch, ++c) {
@@ -640,9 +646,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
                 }
                 ptx::tc_fence_after();
 #pragma unroll
-                for (int gq = 0; gq < BN / 32; ++gq) {
+                for (int gq = 0; gq < BW / 32; ++gq) {
                     uint32_t r[32];
-                    ptx::tmem_ld32(tmem + lane_off + b * BN + gq * 32, r);
+                    ptx::tmem_ld32(tmem + lane_off + b * BN + c0 + gq * 32, r);
                     ptx::tmem_ld_wait();
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj) iacc[gq * 32 + jj] += __float2int_rn(__uint_as_float(r[jj]));
@@ -666,25 +672,24 @@ __global__ void __launch_bounds__(kThreads, MINB)
             const bool in_range = !mval || sa_out == 0.0 || (ea + ebmin >= kEpi32Lo && ea + ebmax <= kEpi32Hi);
             const bool epi32 = kEpi32 && __all_sync(0xffffffffu, in_range);
             const float fsa = (float)sa_out;
-            const uint32_t rest = tmem + (2 + j) * BN;
+            const uint32_t rest = tmem + (2 + j) * BN + c0;
 #pragma unroll
-            for (int gq = 0; gq < BN / 32; ++gq) {
+            for (int gq = 0; gq < BW / 32; ++gq) {
                 uint32_t r[32];
                 ptx::tmem_ld32(rest + lane_off + gq * 32, r);
                 ptx::tmem_ld_wait();
-                constexpr int kCB = 4;
 #pragma unroll
-                for (int j0 = 0; j0 < 32; j0 += kCB) {
-                    int64_t off[kCB];
-                    double cold[kCB];
+                for (int j0 = 0; j0 < 32; j0 += KCB) {
+                    int64_t off[KCB];
+                    double cold[KCB];
 #pragma unroll
-                    for (int u = 0; u < kCB; ++u) {
+                    for (int u = 0; u < KCB; ++u) {
                         const int64_t co = s_coff[gq * 32 + j0 + u];
                         off[u] = (mval && co >= 0) ? crow + co : -1;
                         cold[u] = (direct && beta != 0.0 && off[u] >= 0) ? C.p[off[u]] : 0.0;
                     }
 #pragma unroll
-                    for (int u = 0; u < kCB; ++u) {
+                    for (int u = 0; u < KCB; ++u) {
                         if (off[u] < 0) continue;
                         const int nn = n0 + gq * 32 + j0 + u;
                         const int jj = gq * 32 + j0 + u;
@@ -809,25 +814,49 @@ __device__ __forceinline__ void load_tile(double (&t)[32][33], int rows, int K, 
 
 // The S plane values of x for a row whose maximum has biased exponent emax
 // (0 for a zero row): Y = round(x 2^(7 - e + 8(S-1))) as an integer, peeled into
-// balanced base-256 digits from the bottom; plane p holds d_p 2^(-8p).
+// balanced base-256 digits from the bottom; plane p holds d_p 2^(-8p).  For S <= 3,
+// |Y| <= 2^23 and the right shift is at least 30, so the digits are peeled in 32-bit
+// integers and turned into floats by the exact 1.5 * 2^23 offset (an integer add and
+// an FP32 subtract per digit); this runs on the integer and FP32 pipes only.
+__device__ __forceinline__ float small_int_to_float(int32_t d) {  // exact for |d| < 2^22
+    return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
 template <int S>
 __device__ __forceinline__ void split_digits(double x, int emax, float (&out)[S]) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int e = (int)((bits >> 52) & 0x7FF);
-    long long Y = 0;
+    const uint32_t hi = (uint32_t)(bits >> 32);
+    const int e = (int)((hi >> 20) & 0x7FF);
     const int rs = emax - e + 54 - 8 * S;  // right shift that puts x on the 2^-(8(S-1)) grid
-    if (emax && e && rs < 63) {
-        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-        Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
-        if (bits >> 63) Y = -Y;
-    }
+    if constexpr (S <= 3) {
+        int32_t Y = 0;
+        if (emax && e && rs < 63) {
+            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+            const int32_t q = (int32_t)((mant + (1ull << (rs - 1))) >> rs);
+            Y = (hi >> 31) ? -q : q;
+        }
 #pragma unroll
-    for (int p = S - 1; p >= 1; --p) {
-        const long long d = ((Y + 128) & 255) - 128;
-        Y = (Y - d) >> 8;
-        out[p] = (float)d * exp2f(-8.0f * p);
+        for (int p = S - 1; p >= 1; --p) {
+            const int32_t d = ((Y + 128) & 255) - 128;
+            Y = (Y - d) >> 8;
+            out[p] = small_int_to_float(d) * __int_as_float((127 - 8 * p) << 23);  // d 2^(-8p)
+        }
+        out[0] = small_int_to_float(Y);
+    } else {
+        long long Y = 0;
+        if (emax && e && rs < 63) {
+            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+            Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
+            if (bits >> 63) Y = -Y;
+        }
+#pragma unroll
+        for (int p = S - 1; p >= 1; --p) {
+            const long long d = ((Y + 128) & 255) - 128;
+            Y = (Y - d) >> 8;
+            out[p] = small_int_to_float((int32_t)d) * __int_as_float((127 - 8 * p) << 23);
+        }
+        out[0] = small_int_to_float((int32_t)Y);
     }
-    out[0] = (float)Y;
 }
 
 // Digits of one 32 x 32 block from row r0 and column k0.  Rows below rows_pad
@@ -848,23 +877,11 @@ __device__ void planes_block(int rows, int rows_pad, int K, int kpad, int64_t pi
         const int emax = r < rows ? (int)((rmax[r] >> 52) & 0x7FF) : 0;  // 0: zero (or denormal) row
         if (k0 == 0 && tx == 0)
             scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;  // 2^(emax-1022)
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(t[a][tx]);
-        const int e = (int)((bits >> 52) & 0x7FF);
-        long long Y = 0;
-        const int rs = emax - e + 54 - 8 * S;  // right shift that puts x on the 2^-(8(S-1)) grid
-        if (emax && e && rs < 63) {
-            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-            Y = (long long)((mant + (1ull << (rs - 1))) >> rs);
-            if (bits >> 63) Y = -Y;
-        }
+        float d[S];
+        split_digits<S>(t[a][tx], emax, d);
         __nv_bfloat16 *dst = planes + (size_t)r * pitch + k;
 #pragma unroll
-        for (int p = S - 1; p >= 1; --p) {
-            const long long d = ((Y + 128) & 255) - 128;
-            Y = (Y - d) >> 8;
-            dst[p * plane] = __float2bfloat16_rn((float)d * exp2f(-8.0f * p));
-        }
-        dst[0] = __float2bfloat16_rn((float)Y);
+        for (int p = 0; p < S; ++p) dst[p * plane] = __float2bfloat16_rn(d[p]);
     }
     __syncthreads();  // t is reused by the next block of a looping caller
 }
@@ -906,6 +923,152 @@ __global__ void __launch_bounds__(256) split_rows_kernel(int rows, int K, int kp
             for (int p = 0; p < S; ++p)
                 *reinterpret_cast<__nv_bfloat162 *>(dst + p * plane + k) = __floats2bfloat162_rn(d0[p], d1[p]);
         }
+    }
+}
+
+// The same for views whose k index runs in contiguous, 16-byte aligned groups of G
+// (2 or 4) doubles: a lane loads a group with G/2 16-byte loads and stores G
+// BF16 digits per plane in one 4- or 8-byte store.  Same digits and scales as
+// split_rows_kernel.
+__device__ __forceinline__ unsigned long long absbits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+template <int G>
+__device__ __forceinline__ void load_group(const double *p, double (&x)[G]) {
+#pragma unroll
+    for (int h = 0; h < G / 2; ++h) {
+        const double2 t = __ldg(reinterpret_cast<const double2 *>(p) + h);
+        x[2 * h] = t.x;
+        x[2 * h + 1] = t.y;
+    }
+}
+
+// the S digit planes of one group of G values, stored at dst + p * plane
+template <int S, int G>
+__device__ __forceinline__ void store_group_digits(const double (&x)[G], int emax, __nv_bfloat16 *dst, size_t plane) {
+    float d[G][S];
+#pragma unroll
+    for (int g = 0; g < G; ++g) split_digits<S>(x[g], emax, d[g]);
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(d[0][p], d[1][p]);
+        if constexpr (G == 4) {
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(d[2][p], d[3][p]);
+            uint2 w;
+            w.x = *reinterpret_cast<const uint32_t *>(&lo);
+            w.y = *reinterpret_cast<const uint32_t *>(&hi);
+            *reinterpret_cast<uint2 *>(dst + p * plane) = w;
+        } else {
+            *reinterpret_cast<__nv_bfloat162 *>(dst + p * plane) = lo;
+        }
+    }
+}
+
+// Short rows (K * 8 bytes within L2 for the whole grid): a warp per row, the second
+// pass re-reads the row from L2; UNR groups per lane in flight in the first.
+template <int S, int G>
+__global__ void __launch_bounds__(256) split_rows_vec_kernel(int rows, int K, int kpad, MatView v,
+                                                             __nv_bfloat16 *__restrict__ planes, size_t plane,
+                                                             double *__restrict__ scale) {
+    constexpr int UNR = G == 4 ? 2 : 4, step = 32 * G;
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)(((size_t)gridDim.x * blockDim.x) >> 5);
+    for (int r = warp; r < rows; r += nwarps) {
+        const double *row = v.p + dim_off(v.row, (uint32_t)r);
+        unsigned long long m = 0;
+        int k = G * lane;
+        for (; k + (UNR - 1) * step < K; k += UNR * step) {
+            double x[UNR][G];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) load_group<G>(row + dim_off(v.col, (uint32_t)(k + u * step)), x[u]);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+#pragma unroll
+                for (int g = 0; g < G; ++g) m = max(m, absbits(x[u][g]));
+        }
+        for (; k < K; k += step) {
+            double x[G];
+            load_group<G>(row + dim_off(v.col, (uint32_t)k), x);
+#pragma unroll
+            for (int g = 0; g < G; ++g) m = max(m, absbits(x[g]));
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, m, off));
+        const int emax = (int)((m >> 52) & 0x7FF);  // 0: zero (or denormal) row
+        if (lane == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
+        __nv_bfloat16 *dst = planes + (size_t)r * kpad;
+        for (k = G * lane; k < kpad; k += step) {
+            double x[G];
+            if (k < K) {
+                load_group<G>(row + dim_off(v.col, (uint32_t)k), x);
+            } else {
+#pragma unroll
+                for (int g = 0; g < G; ++g) x[g] = 0.0;
+            }
+            store_group_digits<S, G>(x, emax, dst + k, plane);
+        }
+    }
+}
+
+// Rows of up to kSmemRowK doubles: a block per row stages the row in shared memory
+// on its one read from HBM (UNR groups per thread in flight), takes the maximum, and
+// writes the digits from shared memory.
+constexpr int kSmemRowK = 8192;
+template <int S, int G>
+__global__ void __launch_bounds__(256) split_rows_smem_kernel(int rows, int K, int kpad, MatView v,
+                                                              __nv_bfloat16 *__restrict__ planes, size_t plane,
+                                                              double *__restrict__ scale) {
+    constexpr int UNR = 4, step = 256 * G;
+    extern __shared__ double2 srow[];  // K doubles
+    __shared__ unsigned long long red[8];
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const double *row = v.p + dim_off(v.row, (uint32_t)r);
+        unsigned long long m = 0;
+        int k = G * tid;
+        for (; k + (UNR - 1) * step < K; k += UNR * step) {
+            double x[UNR][G];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) load_group<G>(row + dim_off(v.col, (uint32_t)(k + u * step)), x[u]);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+#pragma unroll
+                for (int h = 0; h < G / 2; ++h)
+                    srow[(k + u * step) / 2 + h] = make_double2(x[u][2 * h], x[u][2 * h + 1]);
+#pragma unroll
+                for (int g = 0; g < G; ++g) m = max(m, absbits(x[u][g]));
+            }
+        }
+        for (; k < K; k += step) {
+            double x[G];
+            load_group<G>(row + dim_off(v.col, (uint32_t)k), x);
+#pragma unroll
+            for (int h = 0; h < G / 2; ++h) srow[k / 2 + h] = make_double2(x[2 * h], x[2 * h + 1]);
+#pragma unroll
+            for (int g = 0; g < G; ++g) m = max(m, absbits(x[g]));
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, m, off));
+        if (lane == 0) red[tid >> 5] = m;
+        __syncthreads();  // the row and the warp maxima are in shared memory
+#pragma unroll
+        for (int q = 0; q < 8; ++q) m = max(m, red[q]);
+        const int emax = (int)((m >> 52) & 0x7FF);  // 0: zero (or denormal) row
+        if (tid == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
+        __nv_bfloat16 *dst = planes + (size_t)r * kpad;
+        for (k = G * tid; k < kpad; k += step) {
+            double x[G];
+#pragma unroll
+            for (int h = 0; h < G / 2; ++h) {
+                const double2 t = k < K ? srow[k / 2 + h] : make_double2(0.0, 0.0);
+                x[2 * h] = t.x;
+                x[2 * h + 1] = t.y;
+            }
+            store_group_digits<S, G>(x, emax, dst + k, plane);
+        }
+        __syncthreads();  // srow and red are rewritten for the next row
     }
 }
 
@@ -1066,13 +1229,18 @@ int num_sms() {
 template <int S, int BN, int NST, int MINB>
 void launch_p(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
               const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
-    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + pbars_bytes() + 4 * epi_bytes(BN) + 1024;
+    // eight epilogue warps where BN splits into two 32-column slices, else four; 16 C loads in
+    // flight per thread with one CTA per SM, 8 with two (the register budget of two CTAs)
+    constexpr int EW = BN % 64 == 0 ? 8 : 4, KCB = MINB == 1 ? 16 : 8;
+    constexpr int BW = BN / (EW / 4);
+    constexpr int threads = 64 + 32 * EW;
+    constexpr size_t need = (size_t)NST * stage_bytes(S, BN) + pbars_bytes() + EW * epi_bytes(BW) + 1024;
     // two-per-SM variants request at least 80 KB so that no third CTA (and its TMEM) fits
     constexpr size_t smem = (MINB > 1 && need < 80 * 1024) ? 80 * 1024 : need;
     static_assert(MINB * smem <= 227 * 1024 && MINB * ptmem_cols(BN) <= 512, "co-resident CTAs must fit");
     static bool attr = false;
     if (!attr) {
-        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_persistent_kernel<S, BN, NST, MINB>,
+        CCSD_CUDA(cudaFuncSetAttribute(split_gemm_persistent_kernel<S, BN, NST, MINB, EW, KCB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
@@ -1085,7 +1253,22 @@ void launch_p(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     const int slots = num_sms() * MINB;
     // split K when the tiles alone leave CTAs idle, and to keep the int32 level-0 sums bounded
     int splits = 1;
-    if (tiles < slots) splits = (int)std::min<long>((slots + tiles - 1) / tiles, std::max(1, nkb / 8));
+    if (tiles < slots) {
+        splits = (int)std::min<long>((slots + tiles - 1) / tiles, std::max(1, nkb / 8));
+    } else if (tiles < 4L * slots && nkb >= 256) {
+        // long K over a few rounds of tiles: the split count (at most 8) that leaves the
+        // last round fullest, the smaller on a tie
+        double best = 0.0;
+        for (int sp = 1; sp <= 8 && nkb / sp >= 32; ++sp) {
+            if (sp > 1 && (size_t)sp * M * N > ws_elems) break;
+            const long w = tiles * sp, rounds = (w + slots - 1) / slots;
+            const double eff = (double)w / ((double)rounds * slots);
+            if (eff > best + 0.02) {
+                best = eff;
+                splits = sp;
+            }
+        }
+    }
     splits = std::max(splits, (nkb + kMaxKbPerSplit - 1) / kMaxKbPerSplit);
     while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
     if ((nkb + splits - 1) / splits > kMaxKbPerSplit)
@@ -1109,7 +1292,7 @@ void launch_p(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     jobs.C = C;
     jobs.ws = ws;
     const int grid = (int)std::min<long>(nwork, slots);
-    split_gemm_persistent_kernel<S, BN, NST, MINB><<<grid, kThreads, smem, st>>>(ta, tb, A.rows_pad, B.rows_pad,
+    split_gemm_persistent_kernel<S, BN, NST, MINB, EW, KCB><<<grid, threads, smem, st>>>(ta, tb, A.rows_pad, B.rows_pad,
                                                                                jobs, (int)nwork, d_err);
     CCSD_LAUNCH_CHECK();
     if (splits > 1) {
@@ -1152,10 +1335,10 @@ void launch_s(const SplitOperand &A, const SplitOperand &B, int M, int N, double
             launch_p<S, 64, st64, 2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
         return;
     }
-    // long K on the widest tile (the pair-form ladder): a tile's fill and epilogue are a
-    // small share of its main loop, and 160 columns (not a persistent width) cut the
-    // passes over A; everything else runs persistent, at most 128 columns wide
-    if (bn == 160 && nkb >= 512) {
+    // long K on at most two 160-wide column tiles (the pair-form ladder): a tile's fill and
+    // epilogue are a small share of its main loop, and 160 columns (not a persistent width)
+    // cut the passes over A; everything else runs persistent, at most 128 columns wide
+    if (bn == 160 && nkb >= 512 && (N + 159) / 160 <= 2) {
         launch_t<S, 160>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st);
         return;
     }
@@ -1270,6 +1453,61 @@ void grouped_split_gemm_launch(const PackedSplit &A, const PackedSplit &B, int b
 }
 
 // ---------------------------------------------------------------------------
+// Whether k runs through the view in contiguous groups of G doubles that start on
+// 16-byte boundaries: unit stride in k, G dividing K and the innermost extent of
+// the k index, and every other stride (of k and of the row index) even.
+static bool k_groups(const MatView &v, int K, int G) {
+    const auto even = [](int64_t s) { return (s & 1) == 0; };
+    if (v.col.s2 != 1 || K % G != 0 || ((uintptr_t)v.p & 15) != 0) return false;
+    if (v.col.e2 != 0xFFFFFFFFu) {
+        if (v.col.e2 % G != 0 || !even(v.col.s1)) return false;
+        if (v.col.e1 != 0xFFFFFFFFu && !even(v.col.s0)) return false;
+    }
+    if (!even(v.row.s2)) return false;
+    if (v.row.e2 != 0xFFFFFFFFu) {
+        if (!even(v.row.s1)) return false;
+        if (v.row.e1 != 0xFFFFFFFFu && !even(v.row.s0)) return false;
+    }
+    return true;
+}
+
+// One pass over a view of 16-byte groups (k_groups): rows up to kSmemRowK long are
+// staged in shared memory, a block per row; short rows (under 1024, whose re-read
+// stays in L2) take a warp per row.  Returns false for the longer rows, which the
+// two-pass kernels take.
+template <int S, int G>
+static bool launch_split_vec_g(int rows, int K, int kpad, const MatView &v, __nv_bfloat16 *pl, size_t plane,
+                               double *scale, cudaStream_t st) {
+    if (K < 1024) {
+        const int grid = (int)std::min<long long>((rows + 7) / 8, 152LL * 8);
+        split_rows_vec_kernel<S, G><<<grid, 256, 0, st>>>(rows, K, kpad, v, pl, plane, scale);
+        CCSD_LAUNCH_CHECK();
+        return true;
+    }
+    if (K > kSmemRowK) return false;
+    const size_t smem = sizeof(double) * (size_t)K;
+    static unsigned long long attr_set = 0;  // per device (the attribute is per context)
+    int dev = 0;
+    CCSD_CUDA(cudaGetDevice(&dev));
+    if (dev < 64 && !(attr_set >> dev & 1ull)) {
+        CCSD_CUDA(cudaFuncSetAttribute(split_rows_smem_kernel<S, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(double) * kSmemRowK)));
+        attr_set |= 1ull << dev;
+    }
+    const long long per_sm = std::max<long long>(1, std::min<long long>(8, (200LL << 10) / (long long)(smem + 1024)));
+    const int grid = (int)std::min<long long>(rows, 152LL * per_sm);
+    split_rows_smem_kernel<S, G><<<grid, 256, smem, st>>>(rows, K, kpad, v, pl, plane, scale);
+    CCSD_LAUNCH_CHECK();
+    return true;
+}
+
+template <int S>
+static bool launch_split_vec(int G, int rows, int K, int kpad, const MatView &v, __nv_bfloat16 *pl, size_t plane,
+                             double *scale, cudaStream_t st) {
+    return G == 4 ? launch_split_vec_g<S, 4>(rows, K, kpad, v, pl, plane, scale, st)
+                  : launch_split_vec_g<S, 2>(rows, K, kpad, v, pl, plane, scale, st);
+}
+
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st) {
     const int nkt = op.kpad / 32, nrt = op.rows_pad / 32;
     const long long blocks = (long long)nkt * nrt;
@@ -1278,6 +1516,18 @@ void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatVie
     // read along rows when the row index is the contiguous one
     const bool rowc = v.row.s2 == 1 && v.col.s2 != 1;
     __nv_bfloat16 *pl0 = (__nv_bfloat16 *)op.planes;
+    const size_t plane0 = (size_t)op.rows_pad * op.kpad;
+    const int G = rowc ? 0 : (k_groups(v, K, 4) ? 4 : (k_groups(v, K, 2) ? 2 : 0));
+    if (G) {  // one HBM pass, 16-byte loads
+        bool done = false;
+        switch (op.nslices) {
+            case 2: done = launch_split_vec<2>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
+            case 3: done = launch_split_vec<3>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
+            case 4: done = launch_split_vec<4>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
+            default: throw Error(-1, "nslices must be 2, 3 or 4");
+        }
+        if (done) return;
+    }
     if (!rowc && K <= 32768 && rows >= 8 * 152) {  // one pass, a warp per row
         const size_t plane = (size_t)op.rows_pad * op.kpad;
         const int grid = (int)std::min<long long>((rows + 7) / 8, 152LL * 8);
@@ -1318,9 +1568,12 @@ void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatVie
 }
 
 void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
-                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
+                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st, int levels) {
     if (A.kpad != B.kpad || A.nslices != B.nslices) throw Error(-1, "split operands disagree");
-    switch (A.nslices) {
+    // a kernel for S planes reads plane p of an operand at plane row p * rows_pad, so it
+    // runs on the first S planes of operands that hold more
+    const int S = levels >= 2 && levels < A.nslices ? levels : A.nslices;
+    switch (S) {
         case 2: launch_s<2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
         case 3: launch_s<3>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
         case 4: launch_s<4>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
@@ -1349,7 +1602,7 @@ SplitEngine::SplitEngine(int nslices, cudaStream_t st) : nslices_(nslices), st_(
                             std::to_string(major) + std::to_string(minor));
     CCSD_CUDA(cudaMalloc(&d_err_, sizeof(int)));
     CCSD_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), st_));
-    ws_elems_ = 8u << 20;
+    ws_elems_ = 32u << 20;  // split-K partials (256 MB)
     CCSD_CUDA(cudaMalloc(&ws_, ws_elems_ * sizeof(double)));
 }
 
@@ -1388,18 +1641,30 @@ void SplitEngine::ensure(SplitOperand &op, int rows, int K) {
     const int kpad = (K + BK - 1) / BK * BK;
     const size_t need = (size_t)nslices_ * rows_pad * kpad * 2;
     if (!op.planes || need > op.bytes || (size_t)rows_pad > op.scale_cap) {
+        // grow both to the largest seen, so that a scratch operand shared by a tall
+        // thin and a square contraction settles after one update instead of being
+        // re-allocated (a device synchronisation) on every one
+        const size_t bytes = need > op.bytes ? need : op.bytes;
+        const size_t cap = (size_t)rows_pad > op.scale_cap ? (size_t)rows_pad : op.scale_cap;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st_, &cs) != cudaSuccess) {
+            cudaGetLastError();
+            cs = cudaStreamCaptureStatusActive;  // the legacy stream while another one captures
+        }
+        if (cs != cudaStreamCaptureStatusNone)
+            throw CaptureMiss("split planes: " + std::to_string(bytes) + " bytes wanted during graph capture");
         free_op(op);
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, need);
+        cudaError_t e = cudaMalloc(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            throw Error(-3, "split planes: cudaMalloc of " + std::to_string(need) + " bytes failed");
+            throw Error(-3, "split planes: cudaMalloc of " + std::to_string(bytes) + " bytes failed");
         }
         op.planes = p;
-        op.bytes = need;
-        CCSD_CUDA(cudaMalloc(&op.scale, sizeof(double) * rows_pad));
-        CCSD_CUDA(cudaMalloc(&op.rmax, sizeof(unsigned long long) * rows_pad));
-        op.scale_cap = rows_pad;
+        op.bytes = bytes;
+        CCSD_CUDA(cudaMalloc(&op.scale, sizeof(double) * cap));
+        CCSD_CUDA(cudaMalloc(&op.rmax, sizeof(unsigned long long) * cap));
+        op.scale_cap = cap;
     }
     op.rows = rows;
     op.rows_pad = rows_pad;
@@ -1449,12 +1714,12 @@ void SplitEngine::gemm(int M, int N, int K, double alpha, const MatView &A, cons
     }
     SplitOperand *a = operand(cache_a, M, K, A, 0);
     SplitOperand *b = operand(cache_b, N, K, B, 1);
-    split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
+    split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_, levels_);
 }
 
 void SplitEngine::run(const SplitOperand &a, const SplitOperand &b, int M, int N, double alpha, double beta,
                       const OutView &C) {
-    split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
+    split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_, levels_);
 }
 
 void SplitEngine::clear_error() { CCSD_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), st_)); }

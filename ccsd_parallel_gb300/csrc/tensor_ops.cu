@@ -8,6 +8,7 @@
 #include <atomic>
 
 #include "common.h"
+#include "fp64_ops.cuh"
 
 namespace ccsd {
 
@@ -29,9 +30,8 @@ __global__ void axpby_view_kernel(int R, int C, double alpha, MatView X, double 
          idx += (size_t)gridDim.x * blockDim.x) {
         uint32_t r = (uint32_t)(idx / C), c = (uint32_t)(idx % C);
         double *y = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
-        double v = alpha == 0.0 ? 0.0 : alpha * X.p[dim_off(X.row, r) + dim_off(X.col, c)];
-        if (beta != 0.0) v = fma(beta, *y, v);
-        *y = v;
+        const double x = alpha == 0.0 ? 0.0 : X.p[dim_off(X.row, r) + dim_off(X.col, c)];
+        *y = axpby_el(alpha, x, beta, beta == 0.0 ? 0.0 : *y);
     }
 }
 
@@ -71,9 +71,7 @@ __global__ void __launch_bounds__(256) permute_axpby_kernel(PermIndex P, int p, 
         const uint32_t iq = iq0 + tx, ip = ip0 + ty + j;
         if (ip < P.ext[p] && iq < P.ext[q]) {
             double *y = Y + yb + (int64_t)ip * P.ys[p] + (int64_t)iq * P.ys[q];
-            double v = alpha == 0.0 ? 0.0 : alpha * t[tx][ty + j];
-            if (beta != 0.0) v = fma(beta, *y, v);
-            *y = v;
+            *y = axpby_el(alpha, t[tx][ty + j], beta, beta == 0.0 ? 0.0 : *y);
         }
     }
 }
@@ -100,12 +98,8 @@ __global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, doub
             yv[u] = (in[u] && beta != 0.0) ? *yp[u] : 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (!in[u]) continue;
-            double v = alpha == 0.0 ? 0.0 : alpha * xv[u];
-            if (beta != 0.0) v = fma(beta, yv[u], v);
-            *yp[u] = v;
-        }
+        for (int u = 0; u < 4; ++u)
+            if (in[u]) *yp[u] = axpby_el(alpha, xv[u], beta, yv[u]);
     }
 }
 
@@ -153,8 +147,9 @@ __global__ void theta_kernel(int o, int v, const double *t1, const double *t2, d
         double tad = t2[i * ov2 + l * v2 + (size_t)a * v + d];
         double tda = t2[i * ov2 + l * v2 + (size_t)d * v + a];
         double tt = t1[i * v + d] * t1[l * v + a];
-        th1[idx] = tad - 0.5 * tda - tt;
-        th2[idx] = 0.5 * tda + tt;
+        const double h = fma(0.5, tda, tt);
+        th1[idx] = tad - h;
+        th2[idx] = h;
     }
 }
 
@@ -265,6 +260,8 @@ __global__ void dinv2_kernel(int o, int v, const double *eo, const double *ev, d
 
 // t2_new = (R + Rp + Rp^T) * dinv with Rp^T[i][j][a][b] = Rp[j][i][b][a]; per-block
 // partial sums of |t2_new - t2_old|^2 (a fixed tile order per block: deterministic)
+// NORM = false: no partial sums (the caller takes the norm elsewhere) and t2o is not read
+template <bool NORM>
 __global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, const double *__restrict__ R,
                                                               const double *__restrict__ Rp,
                                                               const double *__restrict__ dinv,
@@ -290,15 +287,19 @@ __global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, cons
             if (a < v && b < v) {
                 const size_t idx = base + (size_t)a * v + b;
                 const double tn = (R[idx] + Rp[idx] + s[tx][q]) * dinv[idx];
-                const double d = tn - t2o[idx];
-                acc = fma(d, d, acc);
+                if (NORM) {
+                    const double d = tn - t2o[idx];
+                    acc = fma(d, d, acc);
+                }
                 t2n[idx] = tn;
             }
         }
         __syncthreads();
     }
-    const double sum = block_sum(acc);
-    if (threadIdx.x == 0) partials[blockIdx.x] = sum;
+    if (NORM) {
+        const double sum = block_sum(acc);
+        if (threadIdx.x == 0) partials[blockIdx.x] = sum;
+    }
 }
 
 // th1[i,a,l,d] = t2[i,l,a,d] - t2[i,l,d,a]/2 - t1[i,d] t1[l,a]; th2[i,a,l,d] = t2[i,l,d,a]/2 + t1[i,d] t1[l,a]
@@ -327,8 +328,9 @@ __global__ void __launch_bounds__(256) theta_tiled_kernel(int o, int v, const do
                 const double tda = s[tx][q];
                 const double tt = t1[i * v + d] * t1[l * v + a];
                 const size_t out = (((size_t)i * v + a) * o + l) * v + d;
-                th1[out] = tad - 0.5 * tda - tt;
-                th2[out] = 0.5 * tda + tt;
+                const double h = fma(0.5, tda, tt);  // th1 + th2 = t2[i,l,a,d]: three FP64 operations
+                th1[out] = tad - h;
+                th2[out] = h;
             }
         }
         __syncthreads();
@@ -421,6 +423,52 @@ __global__ void r1_from_z_kernel(int o, int v, const double *__restrict__ Z, dou
     }
 }
 
+// out[a][c] += coef sum_k P[k sk + a sa + c sc] over a v x v output (a diagonal of a
+// larger product, summed over its repeated index k)
+__global__ void diag_acc_kernel(int o, int v, double coef, const double *__restrict__ P, int64_t sk, int64_t sa,
+                                int64_t sc, double *__restrict__ out) {
+    const int n = v * v;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int a = idx / v, c = idx % v;
+        const double *q = P + a * sa + c * sc;
+        double s = 0.0;
+        for (int k = 0; k < o; ++k) s += q[k * sk];
+        out[idx] += coef * s;
+    }
+}
+
+// S[i][j][a][k] = tmpB[k][i][a][j] + Z[i][j][k][a] + Vk[k][j][a][i] (all o^3 v); a thread
+// per (i, j, a, k), k fastest (the writes run along memory; the operands are 33 MB at o = 24, v = 300)
+__global__ void t1_terms_kernel(int o, int v, const double *__restrict__ tmpB, const double *__restrict__ Z,
+                                const double *__restrict__ Vk, double *__restrict__ S) {
+    const size_t n = (size_t)o * o * v * o;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % o);
+        size_t r = idx / o;
+        const int a = (int)(r % v);
+        r /= v;
+        const int j = (int)(r % o), i = (int)(r / o);
+        const double t = tmpB[(((size_t)k * o + i) * v + a) * o + j];
+        const double z = Z[(((size_t)i * o + j) * o + k) * v + a];
+        const double w = Vk[(((size_t)k * o + j) * v + a) * o + i];
+        S[idx] = (t + z) + w;
+    }
+}
+
+// Foo[k][i] += sum_l (2 X[k][l][i][l] - X[k][l][l][i])
+__global__ void foo_from_x_kernel(int o, const double *__restrict__ X, double *__restrict__ Foo) {
+    const int n = o * o;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int k = idx / o, i = idx % o;
+        double s = 0.0;
+        for (int l = 0; l < o; ++l) {
+            const size_t kl = ((size_t)k * o + l) * o;
+            s += 2.0 * X[(kl + i) * o + l] - X[(kl + l) * o + i];
+        }
+        Foo[idx] += s;
+    }
+}
+
 // sums of `nq` groups of `nparts` partials: out[q] = sum_b partials[q * nparts + b]
 __global__ void multi_sum_kernel(int nq, int nparts, const double *partials, double *out) {
     for (int q = 0; q < nq; ++q) {
@@ -444,6 +492,27 @@ __global__ void update_t1_kernel(int o, int v, const double *R1, const double *e
     }
     double s = block_sum(acc);
     if (threadIdx.x == 0) partials[0] = s;
+}
+
+// tau = t2 + t1[i][a] t1[j][b] (as tau_rows_kernel) and the block partials of
+// sum L tau in the same pass: a block takes rows (i, j, a) blockIdx.x, + gridDim.x, ...
+__global__ void tau_dot_rows_kernel(int o, int v, const double *__restrict__ t1, const double *__restrict__ t2,
+                                    const double *__restrict__ L, double *__restrict__ tau, double *partials) {
+    const int rows = o * o * v;
+    double acc = 0.0;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int a = r % v, ij = r / v, j = ij % o, i = ij / o;
+        const double ta = t1[i * v + a];
+        const double *t1j = t1 + (size_t)j * v;
+        const size_t base = (size_t)r * v;
+        for (int b = threadIdx.x; b < v; b += blockDim.x) {
+            const double x = fma(ta, t1j[b], t2[base + b]);
+            tau[base + b] = x;
+            acc = fma(L[base + b], x, acc);
+        }
+    }
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
 __global__ void dot_kernel(size_t n, const double *x, const double *y, double *partials) {
@@ -569,6 +638,17 @@ void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaSt
     CCSD_LAUNCH_CHECK();
 }
 
+void k_tau_dot(int o, int v, const double *t1, const double *t2, const double *L, double *tau, double *partials,
+               int nblocks, cudaStream_t st) {
+    if ((size_t)o * o * v * v >= ((size_t)1 << 31)) {
+        k_tau(o, v, t1, t2, tau, st);
+        k_dot((size_t)o * o * v * v, L, tau, partials, nblocks, st);
+        return;
+    }
+    tau_dot_rows_kernel<<<nblocks, v <= 128 ? 128 : 320, 0, st>>>(o, v, t1, t2, L, tau, partials);
+    CCSD_LAUNCH_CHECK();
+}
+
 void k_theta(int o, int v, const double *t1, const double *t2, double *th1, double *th2,
              cudaStream_t st) {
     if ((size_t)o * o * v * v >= ((size_t)1 << 31)) {
@@ -625,6 +705,22 @@ void k_lincomb2(size_t n, double a, const double *x1, double b, const double *x2
     CCSD_LAUNCH_CHECK();
 }
 
+void k_foo_from_x(int o, const double *X, double *Foo, cudaStream_t st) {
+    foo_from_x_kernel<<<(o * o + 255) / 256, 256, 0, st>>>(o, X, Foo);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_diag_acc(int o, int v, double coef, const double *P, int64_t sk, int64_t sa, int64_t sc, double *out,
+                cudaStream_t st) {
+    diag_acc_kernel<<<(v * v + 255) / 256, 256, 0, st>>>(o, v, coef, P, sk, sa, sc, out);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_t1_terms(int o, int v, const double *tmpB, const double *Z, const double *Vk, double *S, cudaStream_t st) {
+    t1_terms_kernel<<<grid_for((size_t)o * o * v * o), 256, 0, st>>>(o, v, tmpB, Z, Vk, S);
+    CCSD_LAUNCH_CHECK();
+}
+
 void k_r1_from_z(int o, int v, const double *Z, double *R1, cudaStream_t st) {
     r1_from_z_kernel<<<(o * v + 255) / 256, 256, 0, st>>>(o, v, Z, R1);
     CCSD_LAUNCH_CHECK();
@@ -644,9 +740,14 @@ void k_mp2_guess(int o, int v, const double *ovov, const double *eo, const doubl
 void k_update_t2(int o, int v, const double *R, const double *Rp, const double *eo,
                  const double *ev, const double *dinv2, const double *t2_old, double *t2_new,
                  double *partials, int nblocks, cudaStream_t st) {
-    if (dinv2 && (size_t)o * o * v * v < ((size_t)1 << 31))
-        update_t2_tiled_kernel<<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
-    else
+    if (dinv2 && (size_t)o * o * v * v < ((size_t)1 << 31)) {
+        if (partials)
+            update_t2_tiled_kernel<true><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
+        else
+            update_t2_tiled_kernel<false><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
+    } else if (!partials) {
+        throw Error(-1, "k_update_t2: the norm-free form needs the 1/D table");
+    } else
         update_t2_kernel<<<nblocks, kReduceThreads, 0, st>>>(o, v, R, Rp, eo, ev, t2_old, t2_new, partials);
     CCSD_LAUNCH_CHECK();
 }

@@ -25,12 +25,15 @@ def main():
     ap.add_argument("--K", type=int, default=7200)
     ap.add_argument("--precision", type=int, default=3, help="0 = FP64, 2/3/4 = split BF16 planes")
     ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--fp64-kernel", choices=("dfma", "dmma"), default="dfma",
+                    help="inner product of the FP64 tiled kernel (precision 0)")
     a = ap.parse_args()
     g = torch.Generator(device="cuda").manual_seed(0)
     A = torch.randn(a.M, a.K, dtype=torch.float64, device="cuda", generator=g)
     B = torch.randn(a.N, a.K, dtype=torch.float64, device="cuda", generator=g)
     Cm = torch.zeros(a.M, a.N, dtype=torch.float64, device="cuda")
     lib = _abi.lib()
+    lib.ccsd_set_fp64_kernel(1 if a.fp64_kernel == "dmma" else 0)
     for r in range(a.repeat):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()

@@ -454,6 +454,17 @@ int ccsd_gemm_noalloc(int32_t precision, int32_t M, int32_t N, int32_t K, double
  * a later ccsd_solve on the same handle starts with a clean error word. */
 int ccsd_debug_stall_split_mma(uint64_t stall_ns);
 
+/* Inner product of the plain-FP64 tiled contraction kernel, process-wide (a
+ * tuning switch with no reference counterpart; the reference's FP64 products are
+ * Armadillo element loops, e.g. accu(integ3_2D % tau3), ccsd_memory_optimized.cpp:2093).
+ *   CCSD_FP64_DFMA  fused multiply-adds on the CUDA cores (default)
+ *   CCSD_FP64_DMMA  mma.sync m8n8k4 on the FP64 tensor pipe
+ * Both sum each output's K products in a different order, so results agree to
+ * rounding, not bit for bit.  Returns the previous kind, or CCSD_ERR_INVALID_ARG. */
+#define CCSD_FP64_DFMA 0
+#define CCSD_FP64_DMMA 1
+int ccsd_set_fp64_kernel(int32_t kind);
+
 /* Seeded synthetic closed-shell system (host only, no GPU needed): diagonal
  * fock (n x n) with occupied U[-2,-0.3] / virtual U[0.1,3] energies, and
  * DF factors B[Q][p][q] = 0.05 z / sqrt(naux), z ~ N(0,1), symmetric in p,q.

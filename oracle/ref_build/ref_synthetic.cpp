@@ -12,6 +12,7 @@
 //
 //   usage: ref_synthetic <input.bin> <log10 tolerance> [mo|ccsd1|ccsdt-<n>]
 //     mo         CCSD_Memory_optimized::CCSD (the reference's "CCSD" method)
+//     mo-print   the same with its own per-iteration output ("Energi: ... Time/iter: ...")
 //     ccsd1      CCSDT::Calc_Energy(toler, -1), the dense spin-orbital CCSD ("CCSD1")
 //     ccsdt-<n>  CCSDT::Calc_Energy(toler, n): 1 = CCSDT-1a, 2 = CCSDT-1b, 3 = CCSDT-2,
 //                4 = CCSDT-3, 5 = CCSDT-4, 6 = CCSDT (initializer.cpp:98-128)
@@ -99,7 +100,9 @@ int main(int argc, char **argv) {
         std::printf("iter %d ecorr %.17e etotal %.17e\n", cc.iter, e, e);
     } else {
         CCSD_Memory_optimized cc(1, Z, R, "synthetic", 2 * g_nocc, 0, 1, &hf, false);
-        const double e = cc.CCSD(toler, false);
+        // "mo-print": the class prints its own per-iteration time (clock(), ccsd_memory_optimized.cpp:515-548)
+        const bool print = argc > 3 && std::strcmp(argv[3], "mo-print") == 0;
+        const double e = cc.CCSD(toler, print);
         std::printf("iter %d ecorr %.17e etotal %.17e\n", cc.iter, cc.E_new, e);
         if (argc > 4) {  // dump the final amplitudes in the class's compact layout
             FILE *o = std::fopen(argv[4], "wb");

@@ -64,6 +64,31 @@ def test_fp64_kernel(M, N, K):
     assert ((out - ref).abs() <= 1e-13 * scale + 1e-300).all()
 
 
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_fp64_dmma_kernel(M, N, K):
+    """The tiled FP64 kernel with its inner product on the FP64 tensor pipe
+    (mma.sync m8n8k4, ccsd_set_fp64_kernel) holds the same 1e-13 bound."""
+    g = torch.Generator(device="cuda").manual_seed(M * 5 + N * 11 + K)
+    A = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(N, K, dtype=torch.float64, device="cuda", generator=g)
+    C0 = torch.randn(M, N, dtype=torch.float64, device="cuda", generator=g)
+    prev = _abi.lib().ccsd_set_fp64_kernel(1)
+    try:
+        out = run_gemm("fp64", A, B, C0, alpha=0.7, beta=-1.3)
+    finally:
+        _abi.lib().ccsd_set_fp64_kernel(prev)
+    ref = 0.7 * (A @ B.T) - 1.3 * C0
+    scale = 0.7 * (A.abs() @ B.abs().T) + 1.3 * C0.abs()
+    assert ((out - ref).abs() <= 1e-13 * scale + 1e-300).all()
+
+
+def test_fp64_kernel_switch_rejects_unknown_kind():
+    lib = _abi.lib()
+    assert lib.ccsd_set_fp64_kernel(7) == _abi.CCSD_ERR_INVALID_ARG
+    prev = lib.ccsd_set_fp64_kernel(1)
+    assert lib.ccsd_set_fp64_kernel(prev) == 1
+
+
 def test_fp64_kernel_beyond_grid_y():
     """N over 65535 column tiles (the CCSDT X3 term's V^3 O columns at nocc=6,
     nvir=40 are 6.1M) runs with the long side in the grid's x dimension."""
@@ -118,3 +143,26 @@ def test_split_level0_is_exact_for_integer_operands():
     out = run_gemm("split2", A, B)
     ref = A @ B.T
     assert torch.equal(out, ref)
+
+
+def test_fp64_solve_with_dmma_matches_dfma():
+    """A whole FP64 CCSD solve (every view orientation of the tiled kernel) with
+    the DMMA inner product: same iteration count and E_corr within 1e-12 of the
+    DFMA solve, T2 within 1e-11."""
+    import ccsd_parallel_gb300 as cg
+    o, v, q = 6, 40, 120
+    fock, b = cg.make_synthetic(o, v, q, 11)
+    out = []
+    lib = _abi.lib()
+    for kind in (0, 1):
+        prev = lib.ccsd_set_fp64_kernel(kind)
+        try:
+            with cg.Solver(fock, o, df=b, precision="fp64", energy_tol=1e-12) as s:
+                out.append(s.solve())
+        finally:
+            lib.ccsd_set_fp64_kernel(prev)
+    a, d = out
+    assert a["converged"] and d["converged"]
+    assert a["iterations"] == d["iterations"]
+    assert abs(a["e_corr"] - d["e_corr"]) < 1e-12
+    assert np.abs(a["t2"] - d["t2"]).max() < 1e-11
