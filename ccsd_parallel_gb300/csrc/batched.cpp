@@ -105,6 +105,8 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         CCSD_CUDA(cudaMallocHost(&h_e_, sizeof(double) * n));
         CCSD_CUDA(cudaMallocHost(&h_n2_, sizeof(double) * n));
         CCSD_CUDA(cudaMallocHost(&h_active_, sizeof(int) * n));
+        CCSD_CUDA(cudaMalloc(&diis_dots_dev_, sizeof(double) * kDiisSlots * n));
+        CCSD_CUDA(cudaMallocHost(&h_diis_dots_, sizeof(double) * kDiisSlots * n));
         CCSD_CUDA(cudaMalloc(&d_err_, sizeof(int)));
         CCSD_CUDA(cudaMemset(d_err_, 0, sizeof(int)));
         record();
@@ -140,6 +142,9 @@ void Batch::release() {
     if (h_e_) cudaFreeHost(h_e_);
     if (h_n2_) cudaFreeHost(h_n2_);
     if (h_active_) cudaFreeHost(h_active_);
+    if (diis_dots_dev_) cudaFree(diis_dots_dev_);
+    if (h_diis_dots_) cudaFreeHost(h_diis_dots_);
+    diis_dots_dev_ = h_diis_dots_ = nullptr;
     desc_ = nullptr;
     active_ = nullptr;
     partials_ = e_dev_ = n2_dev_ = ws_ = h_e_ = h_n2_ = nullptr;
@@ -625,9 +630,17 @@ void Batch::solve(ccsd_result *res) {
             CCSD_CUDA(cudaMemcpyAsync(active_, h_active_, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
             CCSD_CUDA(cudaEventRecord(ev0, st_));
             CCSD_CUDA(cudaGraphLaunch(g_update_, st_));
-            if (opt_.diis_size > 0)
+            if (opt_.diis_size > 0) {
+                // every active system's DIIS store and overlaps, then one read-back and one
+                // synchronisation for all of them, then the host solves and extrapolations
                 for (int s = 0; s < n; ++s)
-                    if (h_active_[s]) eng_[s]->diis_step(updates[s]);
+                    if (h_active_[s]) eng_[s]->diis_store_async(diis_dots_dev_ + (size_t)s * kDiisSlots);
+                CCSD_CUDA(cudaMemcpyAsync(h_diis_dots_, diis_dots_dev_, sizeof(double) * kDiisSlots * n,
+                                          cudaMemcpyDeviceToHost, st_));
+                CCSD_CUDA(cudaStreamSynchronize(st_));
+                for (int s = 0; s < n; ++s)
+                    if (h_active_[s]) eng_[s]->diis_finish(updates[s], h_diis_dots_ + (size_t)s * kDiisSlots);
+            }
             CCSD_CUDA(cudaGraphLaunch(g_energy_, st_));
             CCSD_CUDA(cudaEventRecord(ev1, st_));
             CCSD_CUDA(cudaMemcpyAsync(h_e_, e_dev_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));

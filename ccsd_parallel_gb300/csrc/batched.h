@@ -84,6 +84,8 @@ class Batch {
     double *ws_ = nullptr;
     size_t ws_elems_ = 0;
     double *h_e_ = nullptr, *h_n2_ = nullptr;  // pinned host
+    static constexpr int kDiisSlots = 16;       // DIIS overlaps per system (the largest diis_size)
+    double *diis_dots_dev_ = nullptr, *h_diis_dots_ = nullptr;
     int *h_active_ = nullptr;
     cudaGraphExec_t g_update_ = nullptr, g_energy_ = nullptr;
     int launches_per_update_ = 0;

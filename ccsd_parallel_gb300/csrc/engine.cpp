@@ -661,15 +661,23 @@ void Engine::residual() {
     // - sum_k Foo'[k,i] t1[k,a]
     gemm(io, iv, io, -1.0, mv(Foo_.p, ix1(1), ix1(o)), mv(t1, ix1(1), ix1(v)), 1.0,
          ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_Foo");
-    // + sum_kc Fov[k,c] (2 t2[k,i,c,a] - t2[i,k,c,a])
-    gemm((int)ov, 1, (int)ov, 2.0, mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)),
-         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2a");
-    gemm((int)ov, 1, (int)ov, -1.0, mv(t2, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)),
-         mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2b");
-    // + sum_kc Fov[k,c] t1[i,c] t1[k,a]
+    // + sum_kc Fov[k,c] (2 t2[k,i,c,a] - t2[i,k,c,a]).  With symmetric amplitudes
+    // (t2[i,k,c,a] = t2[k,i,a,c]) this is 2 sum_kc Fov[k,c] th1[k,c,i,a] + 2 sum_kc Fov[k,c] t1[k,a] t1[i,c]:
+    // one pass over th1 instead of two over t2, the second part joining the next term
+    const bool fov_th1 = sym_amps;
+    if (fov_th1) {
+        gemm((int)ov, 1, (int)ov, 2.0, mv(th1_.p, ix1(1), ix1(ov)), mv(Fov_.p, ix1(0), ix1(1)), 1.0,
+             ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_th1");
+    } else {
+        gemm((int)ov, 1, (int)ov, 2.0, mv(t2, ix2((uint32_t)v, v2, 1), ix2((uint32_t)v, ov2, v)),
+             mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2a");
+        gemm((int)ov, 1, (int)ov, -1.0, mv(t2, ix2((uint32_t)v, ov2, 1), ix2((uint32_t)v, v2, v)),
+             mv(Fov_.p, ix1(0), ix1(1)), 1.0, ovw(R1_.p, ix1(1), ix1(0)), 0, 0, "R1_Fov_t2b");
+    }
+    // + sum_kc Fov[k,c] t1[i,c] t1[k,a] (three times that with fov_th1)
     gemm(io, io, iv, 1.0, mv(t1, ix1(v), ix1(1)), mv(Fov_.p, ix1(v), ix1(1)), 0.0,
          ovw(tmpo2_.p, ix1(o), ix1(1)), 0, 0, "R1_Fovt1");
-    gemm(io, iv, io, 1.0, mv(tmpo2_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
+    gemm(io, iv, io, fov_th1 ? 3.0 : 1.0, mv(tmpo2_.p, ix1(o), ix1(1)), mv(t1, ix1(1), ix1(v)), 1.0,
          ovw(R1_.p, ix1(v), ix1(1)), 0, 0, "R1_Fovt1t1");
     // + sum_kc LT1[i,a,k,c] t1[k,c]
     gemm((int)ov, 1, (int)ov, 1.0, mv(LT1_.p, ix1(ov), ix1(1)), mv(t1, ix1(0), ix1(1)), 1.0,
@@ -869,9 +877,11 @@ double Engine::energy_of(const double *t1, const double *t2) {
 // No counterpart in the reference CCSD; the reference's SCF DIIS
 // (hartree_fock_solver.cpp:1252-1311) builds B_ij = <e_i, e_j> and solves the
 // bordered system the same way.  A singular system keeps the plain step.
-void Engine::diis_step(int update_index) {
+// DIIS, first half (no host synchronisation): T_new and E = T_new - T_old go to the
+// next slot, and the overlaps <E, E_j> with every stored slot j (slot order, E itself
+// included) are launched into dots_dev.  Returns their count.
+int Engine::diis_store_async(double *dots_dev) {
     const int m = opt_.diis_size;
-    if (m <= 0) return;
     const size_t nT1 = (size_t)o_ * v_, nT2 = nT1 * o_ * v_, len = nT1 + nT2;
     if ((int)diis_t_.size() != m) {
         diis_t_.clear();
@@ -886,27 +896,40 @@ void Engine::diis_step(int update_index) {
     }
     const int slot = diis_next_;
     DBuf &T = diis_t_[slot], &E = diis_e_[slot];
+    diis_slot_ = slot;
     diis_next_ = (diis_next_ + 1) % m;
     diis_count_ = std::min(diis_count_ + 1, m);
     // one pass: T = x_new, E = x_new - x_old and <E, E_j> for every stored slot j (E itself as NULL)
-    std::vector<int> js;
     std::vector<const double *> others;
-    for (int j = 0; j < diis_count_; ++j) {
-        js.push_back(j);
-        others.push_back(j == slot ? nullptr : diis_e_[j].p);
-    }
+    for (int j = 0; j < diis_count_; ++j) others.push_back(j == slot ? nullptr : diis_e_[j].p);
     const int nb = reduce_blocks();
     diis_partials_.ensure((size_t)m * nb);
-    if (scalars_.n < (size_t)m) scalars_.alloc(std::max<size_t>(m, 8));
     k_diis_store(nT1, nT2, t1n_.p, t2n_.p, t1_.p, t2_.p, T.p, E.p, others.data(), (int)others.size(),
                  diis_partials_.p, nb, st_);
-    k_multi_sum((int)others.size(), nb, diis_partials_.p, scalars_.p, st_);
-    std::vector<double> dots(others.size());
-    CCSD_CUDA(cudaMemcpyAsync(dots.data(), scalars_.p, sizeof(double) * dots.size(), cudaMemcpyDeviceToHost, st_));
+    k_multi_sum((int)others.size(), nb, diis_partials_.p, dots_dev, st_);
+    return (int)others.size();
+}
+
+void Engine::diis_step(int update_index) {
+    const int m = opt_.diis_size;
+    if (m <= 0) return;
+    if (scalars_.n < (size_t)m) scalars_.alloc(std::max<size_t>(m, 8));
+    const int nd = diis_store_async(scalars_.p);
+    std::vector<double> dots(nd);
+    CCSD_CUDA(cudaMemcpyAsync(dots.data(), scalars_.p, sizeof(double) * nd, cudaMemcpyDeviceToHost, st_));
     CCSD_CUDA(cudaStreamSynchronize(st_));
-    for (size_t q = 0; q < js.size(); ++q) {
-        diis_b_[(size_t)slot * m + js[q]] = dots[q];
-        diis_b_[(size_t)js[q] * m + slot] = dots[q];
+    diis_finish(update_index, dots.data());
+}
+
+// DIIS, second half, with the overlaps of diis_store_async on the host: the B matrix,
+// the bordered solve and the extrapolation into (t1n, t2n).
+void Engine::diis_finish(int update_index, const double *dots) {
+    const int m = opt_.diis_size;
+    const size_t nT1 = (size_t)o_ * v_, nT2 = nT1 * o_ * v_;
+    const int slot = diis_slot_;
+    for (int j = 0; j < diis_count_; ++j) {
+        diis_b_[(size_t)slot * m + j] = dots[j];
+        diis_b_[(size_t)j * m + slot] = dots[j];
     }
     diis_self_ = diis_b_[(size_t)slot * m + slot];
     if (diis_count_ < 2 || update_index < opt_.diis_start) return;

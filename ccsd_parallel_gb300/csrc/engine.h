@@ -173,6 +173,9 @@ class Engine {
     bool tau_fresh_ = false;  // tau_ holds tau(t1_, t2_) from energy_of
     double reduce_sum(int nparts);
     void diis_step(int update_index);
+    int diis_store_async(double *dots_dev);                    // DIIS store + overlaps, no sync
+    void diis_finish(int update_index, const double *dots);    // B matrix, solve, extrapolation
+    int diis_slot_ = 0;                                         // the slot the last store used
     double diis_self_ = 0.0;     // <E, E> of the vector the last diis_step stored
     bool norm_in_diis_ = false;  // this solve takes |T_new - T_old| from diis_self_
 

@@ -499,11 +499,14 @@ bool skinny_shape(int M, int N, int K) {
     return lo <= kSkinnyMaxN && hi >= 64 && K >= 256;
 }
 
+// K ranges for the tiled kernel: enough blocks for two per SM.  One SM's FP64 pipe
+// does about 8 GFLOP/s, so a 64 x 64 tile over K = 300 alone takes 80 us; ranges go
+// down to one 16-deep K step when there are few tiles.
 int choose_splits(int M, int N, int K) {
     long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
     if (tiles >= kTargetBlocks) return 1;
     long want = (kTargetBlocks + tiles - 1) / tiles;
-    long maxk = (K + 63) / 64;
+    long maxk = (K + BK - 1) / BK;
     long s = want < maxk ? want : maxk;
     if (s > 64) s = 64;
     return s < 1 ? 1 : (int)s;

@@ -62,40 +62,43 @@ __device__ __forceinline__ void untri32(int P, int &p, int &q) {
 // of (c, d).  tau[i][j] and tau[j][i] are read at tile (C, D) along d directly and at tile
 // (D, C) along c into shared memory, so every element is read once and the pair rows are
 // written along d.  Pair and tile indices are decoded per tile.
+// I: int32_t when every offset of tau and the pair arrays is below 2^31 (64-bit integer
+// arithmetic issues on the FP64 pipe on this part), else int64_t
+template <typename I>
 __global__ void __launch_bounds__(256) tau_sym_tiled_kernel(int o, int v, const double *__restrict__ tau,
                                                             double *__restrict__ tp, double *__restrict__ tm) {
     __shared__ double s2[32][33], s3[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int nt = (v + 31) / 32, ntt = nt * (nt + 1) / 2, To = o * (o + 1) / 2;
-    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2;
-    const size_t v2 = (size_t)v * v;
+    const I Tv = (I)v * (v + 1) / 2, Tmv = (I)v * (v - 1) / 2;
+    const I v2 = (I)v * v;
     const int nblk = To * ntt;
     for (int t = blockIdx.x; t < nblk; t += gridDim.x) {
-        const int I = t / ntt;
+        const int I_ = t / ntt;
         int i, j, C, D;
-        untri32(I, i, j);
+        untri32(I_, i, j);
         untri32(t % ntt, C, D);
-        const double *tij = tau + ((size_t)i * o + j) * v2;
-        const double *tji = tau + ((size_t)j * o + i) * v2;
+        const double *tij = tau + ((I)i * o + j) * v2;
+        const double *tji = tau + ((I)j * o + i) * v2;
         for (int q = ty; q < 32; q += 8) {  // s2[d][c] = tau[i][j][d][c], s3[d][c] = tau[j][i][d][c]
             const int d = D * 32 + q, c = C * 32 + tx;
             const bool in = d < v && c < v;
-            s2[q][tx] = in ? tij[(size_t)d * v + c] : 0.0;
-            s3[q][tx] = in ? tji[(size_t)d * v + c] : 0.0;
+            s2[q][tx] = in ? tij[(I)d * v + c] : 0.0;
+            s3[q][tx] = in ? tji[(I)d * v + c] : 0.0;
         }
         __syncthreads();
         const int d = D * 32 + tx;
-        const int64_t rowp = (int64_t)I * Tv;
-        const int64_t rowm = i > j ? ((int64_t)i * (i - 1) / 2 + j) * Tmv : 0;
+        const I rowp = (I)I_ * Tv;
+        const I rowm = i > j ? ((I)i * (i - 1) / 2 + j) * Tmv : 0;
         for (int q = ty; q < 32; q += 8) {
             const int c = C * 32 + q;
             if (c < v && d < v && d <= c) {
-                const double x1 = tij[(size_t)c * v + d], x2 = s2[tx][q];
-                const double x3 = s3[tx][q], x4 = tji[(size_t)c * v + d];
+                const double x1 = tij[(I)c * v + d], x2 = s2[tx][q];
+                const double x3 = s3[tx][q], x4 = tji[(I)c * v + d];
                 // four FP64 additions; the quarter is taken on the exponent field
                 const double u = x1 + x3, w = x2 + x4;
-                tp[rowp + (int64_t)c * (c + 1) / 2 + d] = mul_pow2(u + w, -2);
-                if (i > j && c > d) tm[rowm + (int64_t)c * (c - 1) / 2 + d] = mul_pow2(u - w, -2);
+                tp[rowp + (I)c * (c + 1) / 2 + d] = mul_pow2(u + w, -2);
+                if (i > j && c > d) tm[rowm + (I)c * (c - 1) / 2 + d] = mul_pow2(u - w, -2);
             }
         }
         __syncthreads();
@@ -104,14 +107,15 @@ __global__ void __launch_bounds__(256) tau_sym_tiled_kernel(int o, int v, const 
 
 // The unpack by tiles of (a, b) for each (i, j): where a >= b the pair rows are read along
 // b directly; where a < b (tiles A <= B) they are read along a into shared memory.
+template <typename I>
 __global__ void __launch_bounds__(256) ladder_unpack_tiled_kernel(int o, int v, const double *__restrict__ sp,
                                                                   const double *__restrict__ sm,
                                                                   double *__restrict__ R) {
     __shared__ double s_p[32][33], s_m[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int nt = (v + 31) / 32, ntiles = o * o * nt * nt;
-    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2;
-    const size_t v2 = (size_t)v * v;
+    const I Tv = (I)v * (v + 1) / 2, Tmv = (I)v * (v - 1) / 2;
+    const I v2 = (I)v * v;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int r = t;
         const int B = r % nt;
@@ -121,31 +125,31 @@ __global__ void __launch_bounds__(256) ladder_unpack_tiled_kernel(int o, int v, 
         const int j = r % o, i = r / o;
         const int i1 = max(i, j), j1 = min(i, j);
         const int sij = i > j ? 1 : (i < j ? -1 : 0);
-        const int64_t rowp = ((int64_t)i1 * (i1 + 1) / 2 + j1) * Tv;
-        const int64_t rowm = sij ? ((int64_t)i1 * (i1 - 1) / 2 + j1) * Tmv : 0;
+        const I rowp = ((I)i1 * (i1 + 1) / 2 + j1) * Tv;
+        const I rowm = sij ? ((I)i1 * (i1 - 1) / 2 + j1) * Tmv : 0;
         if (A <= B) {  // elements a < b: S at pair (b, a), read along a
             for (int q = ty; q < 32; q += 8) {
                 const int b = B * 32 + q, a = A * 32 + tx;
                 const bool in = b < v && a < v && b >= a;
-                s_p[q][tx] = in ? sp[rowp + (int64_t)b * (b + 1) / 2 + a] : 0.0;
-                s_m[q][tx] = (in && sij && b > a) ? sm[rowm + (int64_t)b * (b - 1) / 2 + a] : 0.0;
+                s_p[q][tx] = in ? sp[rowp + (I)b * (b + 1) / 2 + a] : 0.0;
+                s_m[q][tx] = (in && sij && b > a) ? sm[rowm + (I)b * (b - 1) / 2 + a] : 0.0;
             }
         }
         __syncthreads();
         const int b = B * 32 + tx;
-        double *Rij = R + ((size_t)i * o + j) * v2;
+        double *Rij = R + ((I)i * o + j) * v2;
         for (int q = ty; q < 32; q += 8) {
             const int a = A * 32 + q;
             if (a >= v || b >= v) continue;
             double s;
             if (a >= b) {
-                s = sp[rowp + (int64_t)a * (a + 1) / 2 + b];
-                if (sij && a > b) s += sij * sm[rowm + (int64_t)a * (a - 1) / 2 + b];
+                s = sp[rowp + (I)a * (a + 1) / 2 + b];
+                if (sij && a > b) s += sij * sm[rowm + (I)a * (a - 1) / 2 + b];
             } else {
                 s = s_p[tx][q];
                 if (sij) s += -sij * s_m[tx][q];
             }
-            Rij[(size_t)a * v + b] += s;
+            Rij[(I)a * v + b] += s;
         }
         __syncthreads();
     }
@@ -296,10 +300,20 @@ __global__ void w_sym_adj_kernel(int v, const double *__restrict__ wpb, const do
 
 }  // namespace
 
+// every offset of an o^2 v^2 array and of the tau+ pair array below 2^31
+static bool small_offsets(int o, int v) {
+    const int64_t n2 = (int64_t)o * o * v * v, np = (int64_t)o * (o + 1) / 2 * ((int64_t)v * (v + 1) / 2);
+    return n2 < (1LL << 31) && np < (1LL << 31);
+}
+
 void k_tau_sym(int o, int v, const double *tau, double *tp, double *tm, cudaStream_t st) {
     const int64_t nt = (v + 31) / 32, blocks = (int64_t)o * (o + 1) / 2 * (nt * (nt + 1) / 2);
     if (blocks < (1LL << 30) && (int64_t)o * (o + 1) / 2 < (1 << 24)) {
-        tau_sym_tiled_kernel<<<(int)std::min<int64_t>(blocks, 152 * 8), 256, 0, st>>>(o, v, tau, tp, tm);
+        const int grid = (int)std::min<int64_t>(blocks, 152 * 8);
+        if (small_offsets(o, v))
+            tau_sym_tiled_kernel<int32_t><<<grid, 256, 0, st>>>(o, v, tau, tp, tm);
+        else
+            tau_sym_tiled_kernel<int64_t><<<grid, 256, 0, st>>>(o, v, tau, tp, tm);
     } else {
         const size_t n = (size_t)o * (o + 1) / 2 * ((size_t)v * (v + 1) / 2);
         tau_sym_kernel<<<blocks_for(n), 256, 0, st>>>(o, v, tau, tp, tm);
@@ -314,8 +328,10 @@ void k_tau_sym_adj(int o, int v, const double *tpb, const double *tmb, double *t
 
 void k_ladder_unpack(int o, int v, const double *sp, const double *sm, double *R, cudaStream_t st) {
     const int64_t nt = (v + 31) / 32, tiles = (int64_t)o * o * nt * nt;
-    if (tiles < (1LL << 30))
-        ladder_unpack_tiled_kernel<<<(int)std::min<int64_t>(tiles, 152 * 8), 256, 0, st>>>(o, v, sp, sm, R);
+    if (tiles < (1LL << 30) && small_offsets(o, v))
+        ladder_unpack_tiled_kernel<int32_t><<<(int)std::min<int64_t>(tiles, 152 * 8), 256, 0, st>>>(o, v, sp, sm, R);
+    else if (tiles < (1LL << 30))
+        ladder_unpack_tiled_kernel<int64_t><<<(int)std::min<int64_t>(tiles, 152 * 8), 256, 0, st>>>(o, v, sp, sm, R);
     else
         ladder_unpack_kernel<<<blocks_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, sp, sm, R);
     CCSD_LAUNCH_CHECK();

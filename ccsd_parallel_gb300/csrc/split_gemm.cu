@@ -101,6 +101,7 @@ struct TileJob {
     OutView C;
     double *wsz;  // split-K: partial-sum slab [M][N], else null (write C)
     bool run;
+    bool c32;     // every column offset of C below 2^31 (the epilogue's offsets in 32 bits)
 };
 
 // One contraction over the whole grid (grouped rasterisation, split-K over z).
@@ -110,6 +111,7 @@ struct SingleJobs {
     double alpha, beta;
     OutView C;
     double *ws;
+    bool c32 = false;
     __device__ TileJob job() const { return at(blockIdx.x, blockIdx.z); }
     // Work item w of the persistent kernel: split-K slice z = w / tiles, tile w % tiles.
     __device__ TileJob job_at(int w) const {
@@ -135,6 +137,7 @@ struct SingleJobs {
         J.scaleB = scaleB;
         J.alpha = alpha;
         J.beta = beta;
+        J.c32 = c32;
         J.C = C;
         J.wsz = splits == 1 ? nullptr : ws + (size_t)z * M * N;
         J.run = true;
@@ -211,6 +214,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
     const double *__restrict__ scaleB = J.scaleB;
     const double alpha = J.alpha, beta = J.beta;
     const OutView C = J.C;
+    const bool rdc = J.wsz == nullptr && beta != 0.0;  // reads C (one FP64 comparison)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -389,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
                     for (int j = 0; j < kCB; ++j) {
                         const int64_t co = s_coff[g * 32 + j0 + j];
                         off[j] = (mval && co >= 0) ? crow + co : -1;
-                        cold[j] = (direct && beta != 0.0 && off[j] >= 0) ? C.p[off[j]] : 0.0;
+                        cold[j] = (rdc && off[j] >= 0) ? C.p[off[j]] : 0.0;
                     }
 #pragma unroll
                     for (int j = 0; j < kCB; ++j) {
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
                                             s_fsb[jj];
                             const double val = (double)f;
                             if (direct)
-                                C.p[off[j]] = beta != 0.0 ? fma(beta, cold[j], val) : val;
+                                C.p[off[j]] = rdc ? fma(beta, cold[j], val) : val;
                             else
                                 wsz[(size_t)m * N + n] = val;
                             continue;
@@ -409,7 +413,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
                         const double val = sa * s_sb[jj] * ((double)iacc[jj] + (double)__uint_as_float(r[j0 + j]));
                         if (direct) {
                             double out = alpha * val;
-                            if (beta != 0.0) out = fma(beta, cold[j], out);
+                            if (rdc) out = fma(beta, cold[j], out);
                             C.p[off[j]] = out;
                         } else {
                             wsz[(size_t)m * N + n] = val;
@@ -617,7 +621,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, MINB)
             for (int jj = lane; jj < BW; jj += 32) {
                 const int nn = n0 + jj;
                 const double sbn = nn < N ? J.scaleB[nn] : 0.0;
-                s_coff[jj] = nn < N ? dim_off(C.col, (uint32_t)nn) : -1;
+                const int64_t co = nn < N ? dim_off(C.col, (uint32_t)nn) : -1;
+                if (J.c32)
+                    reinterpret_cast<int32_t *>(s_coff)[jj] = (int32_t)co;
+                else
+                    s_coff[jj] = co;
                 s_sb[jj] = sbn;
                 s_fsb[jj] = (float)sbn;
                 if (nn < N) {
@@ -667,52 +675,66 @@ __global__ void __launch_bounds__(64 + 32 * EW, MINB)
             const bool direct = J.wsz == nullptr;
             double *wsz = J.wsz;
             const double alpha = J.alpha, beta = J.beta;
+            const bool rdc = direct && beta != 0.0;  // reads C (one FP64 comparison per tile)
             const double sa_out = direct ? sa * alpha : sa;
             const int ea = exp2_of(sa_out);
             const bool in_range = !mval || sa_out == 0.0 || (ea + ebmin >= kEpi32Lo && ea + ebmax <= kEpi32Hi);
             const bool epi32 = kEpi32 && __all_sync(0xffffffffu, in_range);
             const float fsa = (float)sa_out;
             const uint32_t rest = tmem + (2 + j) * BN + c0;
+            double *cb = C.p + crow;  // this lane's row of C; columns at cb + offset
+            // the element loop over 32- or 64-bit column offsets (64-bit integer arithmetic
+            // issues on the FP64 pipe on this part, which the epilogue's FMA also needs)
+            auto drain = [&](auto zero) {
+                using OffT = decltype(zero);
+                const OffT *coff = reinterpret_cast<const OffT *>(s_coff);
 #pragma unroll
-            for (int gq = 0; gq < BW / 32; ++gq) {
-                uint32_t r[32];
-                ptx::tmem_ld32(rest + lane_off + gq * 32, r);
-                ptx::tmem_ld_wait();
+                for (int gq = 0; gq < BW / 32; ++gq) {
+                    uint32_t r[32];
+                    ptx::tmem_ld32(rest + lane_off + gq * 32, r);
+                    ptx::tmem_ld_wait();
 #pragma unroll
-                for (int j0 = 0; j0 < 32; j0 += KCB) {
-                    int64_t off[KCB];
-                    double cold[KCB];
+                    for (int j0 = 0; j0 < 32; j0 += KCB) {
+                        OffT off[KCB];
+                        double cold[KCB];
 #pragma unroll
-                    for (int u = 0; u < KCB; ++u) {
-                        const int64_t co = s_coff[gq * 32 + j0 + u];
-                        off[u] = (mval && co >= 0) ? crow + co : -1;
-                        cold[u] = (direct && beta != 0.0 && off[u] >= 0) ? C.p[off[u]] : 0.0;
-                    }
-#pragma unroll
-                    for (int u = 0; u < KCB; ++u) {
-                        if (off[u] < 0) continue;
-                        const int nn = n0 + gq * 32 + j0 + u;
-                        const int jj = gq * 32 + j0 + u;
-                        if (kEpi32 && epi32) {
-                            const float f = (__int2float_rn(iacc[jj]) + __uint_as_float(r[j0 + u])) * fsa * s_fsb[jj];
-                            const double val = (double)f;
-                            if (direct)
-                                C.p[off[u]] = beta != 0.0 ? fma(beta, cold[u], val) : val;
-                            else
-                                wsz[(size_t)m * N + nn] = val;
-                            continue;
+                        for (int u = 0; u < KCB; ++u) {
+                            const OffT co = coff[gq * 32 + j0 + u];
+                            off[u] = mval ? co : (OffT)-1;
+                            cold[u] = (rdc && off[u] >= 0) ? cb[off[u]] : 0.0;
                         }
-                        const double val = sa * s_sb[jj] * ((double)iacc[jj] + (double)__uint_as_float(r[j0 + u]));
-                        if (direct) {
-                            double out = alpha * val;
-                            if (beta != 0.0) out = fma(beta, cold[u], out);
-                            C.p[off[u]] = out;
-                        } else {
-                            wsz[(size_t)m * N + nn] = val;
+#pragma unroll
+                        for (int u = 0; u < KCB; ++u) {
+                            if (off[u] < 0) continue;
+                            const int nn = n0 + gq * 32 + j0 + u;
+                            const int jj = gq * 32 + j0 + u;
+                            if (kEpi32 && epi32) {
+                                const float f =
+                                    (__int2float_rn(iacc[jj]) + __uint_as_float(r[j0 + u])) * fsa * s_fsb[jj];
+                                const double val = (double)f;
+                                if (direct)
+                                    cb[off[u]] = rdc ? fma(beta, cold[u], val) : val;
+                                else
+                                    wsz[(size_t)m * N + nn] = val;
+                                continue;
+                            }
+                            const double val =
+                                sa * s_sb[jj] * ((double)iacc[jj] + (double)__uint_as_float(r[j0 + u]));
+                            if (direct) {
+                                double out = alpha * val;
+                                if (rdc) out = fma(beta, cold[u], out);
+                                cb[off[u]] = out;
+                            } else {
+                                wsz[(size_t)m * N + nn] = val;
+                            }
                         }
                     }
                 }
-            }
+            };
+            if (J.c32)
+                drain(int32_t(0));
+            else
+                drain(int64_t(0));
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&bars->rest_empty[j]);
@@ -822,18 +844,37 @@ __device__ __forceinline__ float small_int_to_float(int32_t d) {  // exact for |
     return __int_as_float(0x4B400000 + d) - 12582912.0f;
 }
 
+// A digit value d 2^(-8p) (|d| <= 128) has at most 8 significant bits, so its float
+// encoding ends in 16 zero bits and the BF16 encoding is the top half: taken with
+// integer byte moves instead of the conversion instruction (which issues on the
+// FP64 pipe on this part).
+__device__ __forceinline__ uint32_t bf16x2_of_digits(float lo, float hi) {
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+__device__ __forceinline__ __nv_bfloat16 bf16_of_digit(float f) {
+    return __ushort_as_bfloat16((unsigned short)(__float_as_uint(f) >> 16));
+}
+
 template <int S>
 __device__ __forceinline__ void split_digits(double x, int emax, float (&out)[S]) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const uint32_t hi = (uint32_t)(bits >> 32);
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
     const int e = (int)((hi >> 20) & 0x7FF);
     const int rs = emax - e + 54 - 8 * S;  // right shift that puts x on the 2^-(8(S-1)) grid
     if constexpr (S <= 3) {
+        // q = (mant + 2^(rs-1)) >> rs on the two 32-bit words of mant = mh 2^32 + lo
+        // (rs >= 30; 64-bit integer arithmetic issues on the FP64 pipe here)
         int32_t Y = 0;
         if (emax && e && rs < 63) {
-            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-            const int32_t q = (int32_t)((mant + (1ull << (rs - 1))) >> rs);
-            Y = (hi >> 31) ? -q : q;
+            const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;
+            uint32_t q;
+            if (rs >= 33) {  // the rounding bit lies in the high word; lo cannot carry past it
+                q = (mh + (1u << (rs - 33))) >> (rs - 32);
+            } else {
+                const uint32_t l2 = lo + (1u << (rs - 1));
+                const uint32_t h2 = mh + (l2 < lo ? 1u : 0u);
+                q = rs == 32 ? h2 : __funnelshift_r(l2, h2, rs);
+            }
+            Y = (hi >> 31) ? -(int32_t)q : (int32_t)q;
         }
 #pragma unroll
         for (int p = S - 1; p >= 1; --p) {
@@ -843,6 +884,7 @@ __device__ __forceinline__ void split_digits(double x, int emax, float (&out)[S]
         }
         out[0] = small_int_to_float(Y);
     } else {
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
         long long Y = 0;
         if (emax && e && rs < 63) {
             const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
@@ -881,7 +923,7 @@ __device__ void planes_block(int rows, int rows_pad, int K, int kpad, int64_t pi
         split_digits<S>(t[a][tx], emax, d);
         __nv_bfloat16 *dst = planes + (size_t)r * pitch + k;
 #pragma unroll
-        for (int p = 0; p < S; ++p) dst[p * plane] = __float2bfloat16_rn(d[p]);
+        for (int p = 0; p < S; ++p) dst[p * plane] = bf16_of_digit(d[p]);
     }
     __syncthreads();  // t is reused by the next block of a looping caller
 }
@@ -921,7 +963,7 @@ __global__ void __launch_bounds__(256) split_rows_kernel(int rows, int K, int kp
             split_digits<S>(k + 1 < K ? v.p[ro + dim_off(v.col, (uint32_t)(k + 1))] : 0.0, emax, d1);
 #pragma unroll
             for (int p = 0; p < S; ++p)
-                *reinterpret_cast<__nv_bfloat162 *>(dst + p * plane + k) = __floats2bfloat162_rn(d0[p], d1[p]);
+                *reinterpret_cast<uint32_t *>(dst + p * plane + k) = bf16x2_of_digits(d0[p], d1[p]);
         }
     }
 }
@@ -930,8 +972,8 @@ __global__ void __launch_bounds__(256) split_rows_kernel(int rows, int K, int kp
 // (2 or 4) doubles: a lane loads a group with G/2 16-byte loads and stores G
 // BF16 digits per plane in one 4- or 8-byte store.  Same digits and scales as
 // split_rows_kernel.
-__device__ __forceinline__ unsigned long long absbits(double x) {
-    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+__device__ __forceinline__ uint32_t abshi(double x) {  // high word of |x|: orders |x| by exponent
+    return (uint32_t)__double2hiint(x) & 0x7FFFFFFFu;
 }
 
 template <int G>
@@ -952,15 +994,11 @@ __device__ __forceinline__ void store_group_digits(const double (&x)[G], int ema
     for (int g = 0; g < G; ++g) split_digits<S>(x[g], emax, d[g]);
 #pragma unroll
     for (int p = 0; p < S; ++p) {
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(d[0][p], d[1][p]);
+        const uint32_t lo = bf16x2_of_digits(d[0][p], d[1][p]);
         if constexpr (G == 4) {
-            const __nv_bfloat162 hi = __floats2bfloat162_rn(d[2][p], d[3][p]);
-            uint2 w;
-            w.x = *reinterpret_cast<const uint32_t *>(&lo);
-            w.y = *reinterpret_cast<const uint32_t *>(&hi);
-            *reinterpret_cast<uint2 *>(dst + p * plane) = w;
+            *reinterpret_cast<uint2 *>(dst + p * plane) = make_uint2(lo, bf16x2_of_digits(d[2][p], d[3][p]));
         } else {
-            *reinterpret_cast<__nv_bfloat162 *>(dst + p * plane) = lo;
+            *reinterpret_cast<uint32_t *>(dst + p * plane) = lo;
         }
     }
 }
@@ -977,7 +1015,7 @@ __global__ void __launch_bounds__(256) split_rows_vec_kernel(int rows, int K, in
     const int nwarps = (int)(((size_t)gridDim.x * blockDim.x) >> 5);
     for (int r = warp; r < rows; r += nwarps) {
         const double *row = v.p + dim_off(v.row, (uint32_t)r);
-        unsigned long long m = 0;
+        uint32_t m = 0;  // maximum of the high words of |x|: the row's exponent
         int k = G * lane;
         for (; k + (UNR - 1) * step < K; k += UNR * step) {
             double x[UNR][G];
@@ -986,17 +1024,17 @@ __global__ void __launch_bounds__(256) split_rows_vec_kernel(int rows, int K, in
 #pragma unroll
             for (int u = 0; u < UNR; ++u)
 #pragma unroll
-                for (int g = 0; g < G; ++g) m = max(m, absbits(x[u][g]));
+                for (int g = 0; g < G; ++g) m = max(m, abshi(x[u][g]));
         }
         for (; k < K; k += step) {
             double x[G];
             load_group<G>(row + dim_off(v.col, (uint32_t)k), x);
 #pragma unroll
-            for (int g = 0; g < G; ++g) m = max(m, absbits(x[g]));
+            for (int g = 0; g < G; ++g) m = max(m, abshi(x[g]));
         }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, m, off));
-        const int emax = (int)((m >> 52) & 0x7FF);  // 0: zero (or denormal) row
+        for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+        const int emax = (int)((m >> 20) & 0x7FF);  // 0: zero (or denormal) row
         if (lane == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
         __nv_bfloat16 *dst = planes + (size_t)r * kpad;
         for (k = G * lane; k < kpad; k += step) {
@@ -1022,11 +1060,11 @@ __global__ void __launch_bounds__(256) split_rows_smem_kernel(int rows, int K, i
                                                               double *__restrict__ scale) {
     constexpr int UNR = 4, step = 256 * G;
     extern __shared__ double2 srow[];  // K doubles
-    __shared__ unsigned long long red[8];
+    __shared__ uint32_t red[8];
     const int tid = threadIdx.x, lane = tid & 31;
     for (int r = blockIdx.x; r < rows; r += gridDim.x) {
         const double *row = v.p + dim_off(v.row, (uint32_t)r);
-        unsigned long long m = 0;
+        uint32_t m = 0;  // maximum of the high words of |x|
         int k = G * tid;
         for (; k + (UNR - 1) * step < K; k += UNR * step) {
             double x[UNR][G];
@@ -1038,7 +1076,7 @@ __global__ void __launch_bounds__(256) split_rows_smem_kernel(int rows, int K, i
                 for (int h = 0; h < G / 2; ++h)
                     srow[(k + u * step) / 2 + h] = make_double2(x[u][2 * h], x[u][2 * h + 1]);
 #pragma unroll
-                for (int g = 0; g < G; ++g) m = max(m, absbits(x[u][g]));
+                for (int g = 0; g < G; ++g) m = max(m, abshi(x[u][g]));
             }
         }
         for (; k < K; k += step) {
@@ -1047,15 +1085,15 @@ __global__ void __launch_bounds__(256) split_rows_smem_kernel(int rows, int K, i
 #pragma unroll
             for (int h = 0; h < G / 2; ++h) srow[k / 2 + h] = make_double2(x[2 * h], x[2 * h + 1]);
 #pragma unroll
-            for (int g = 0; g < G; ++g) m = max(m, absbits(x[g]));
+            for (int g = 0; g < G; ++g) m = max(m, abshi(x[g]));
         }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, m, off));
+        for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
         if (lane == 0) red[tid >> 5] = m;
         __syncthreads();  // the row and the warp maxima are in shared memory
 #pragma unroll
         for (int q = 0; q < 8; ++q) m = max(m, red[q]);
-        const int emax = (int)((m >> 52) & 0x7FF);  // 0: zero (or denormal) row
+        const int emax = (int)((m >> 20) & 0x7FF);  // 0: zero (or denormal) row
         if (tid == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
         __nv_bfloat16 *dst = planes + (size_t)r * kpad;
         for (k = G * tid; k < kpad; k += step) {
@@ -1165,6 +1203,25 @@ void set_smem_attr() {
                                        (int)kernel_smem<S, BN, NSTF, MINB>()));
         attr = true;
     }
+}
+
+// Whether every column offset dim_off(C.col, n), n < N, lies in [0, 2^31): the strides
+// are non-negative and the largest offset, at the last index of each level, fits.
+bool col_offsets_32(const OutView &C, int N) {
+    const Dim &d = C.col;
+    if (N <= 0) return true;
+    if (d.s0 < 0 || d.s1 < 0 || d.s2 < 0) return false;
+    int64_t e2 = d.e2 == 0xFFFFFFFFu ? N : std::min<int64_t>(d.e2, N);
+    int64_t q = d.e2 == 0xFFFFFFFFu ? 1 : ((int64_t)N + d.e2 - 1) / d.e2;  // extent of the upper levels
+    int64_t mx = (e2 - 1) * d.s2;
+    if (d.e2 != 0xFFFFFFFFu) {
+        if (d.e1 == 0xFFFFFFFFu) {
+            mx += (q - 1) * d.s1;
+        } else {
+            mx += (std::min<int64_t>(d.e1, q) - 1) * d.s1 + ((q + d.e1 - 1) / d.e1 - 1) * d.s0;
+        }
+    }
+    return mx < (1LL << 31);
 }
 
 template <int S, int BN, int NSTF = 0, int MINB = 1>
@@ -1278,6 +1335,7 @@ void launch_p(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     const long nwork = tiles * splits;
     if (nwork >= (1L << 31)) throw Error(-7, "split GEMM: too many tiles");
     SingleJobs jobs;
+    jobs.c32 = col_offsets_32(C, N);
     jobs.splits = splits;
     jobs.M = M;
     jobs.N = N;

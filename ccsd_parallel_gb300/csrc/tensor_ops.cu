@@ -25,13 +25,15 @@ inline int grid_for(size_t n, int threads = 256) {
 }
 
 __global__ void axpby_view_kernel(int R, int C, double alpha, MatView X, double beta, OutView Y) {
+    const int mode = axpby_mode(alpha, beta);
+    const bool rx = axpby_reads_x(mode), ry = axpby_reads_y(mode);
     size_t total = (size_t)R * C;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
          idx += (size_t)gridDim.x * blockDim.x) {
         uint32_t r = (uint32_t)(idx / C), c = (uint32_t)(idx % C);
         double *y = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
-        const double x = alpha == 0.0 ? 0.0 : X.p[dim_off(X.row, r) + dim_off(X.col, c)];
-        *y = axpby_el(alpha, x, beta, beta == 0.0 ? 0.0 : *y);
+        const double x = rx ? X.p[dim_off(X.row, r) + dim_off(X.col, c)] : 0.0;
+        *y = axpby_apply(mode, alpha, x, beta, ry ? *y : 0.0);
     }
 }
 
@@ -44,8 +46,15 @@ struct PermIndex {
     uint32_t ext[4];
     int64_t xs[4], ys[4];
 };
+// the same with 32-bit strides, for views whose offsets all stay below 2^31 (64-bit
+// integer multiplies and adds issue on the FP64 pipe on this part)
+struct PermIndex32 {
+    uint32_t ext[4];
+    int32_t xs[4], ys[4];
+};
 
-__global__ void __launch_bounds__(256) permute_axpby_kernel(PermIndex P, int p, int q, int u, int w, uint32_t tp,
+template <class PI, typename I>
+__global__ void __launch_bounds__(256) permute_axpby_kernel(PI P, int p, int q, int u, int w, uint32_t tp,
                                                             uint32_t tq, double alpha, const double *__restrict__ X,
                                                             double beta, double *__restrict__ Y) {
     __shared__ double t[32][33];
@@ -55,24 +64,32 @@ __global__ void __launch_bounds__(256) permute_axpby_kernel(PermIndex P, int p, 
     const uint32_t iq0 = (b % tq) * 32;
     b /= tq;
     const uint32_t iu = b % P.ext[u], iw = b / P.ext[u];
-    const int64_t xb = (int64_t)iu * P.xs[u] + (int64_t)iw * P.xs[w];
-    const int64_t yb = (int64_t)iu * P.ys[u] + (int64_t)iw * P.ys[w];
+    const I xb = (I)iu * P.xs[u] + (I)iw * P.xs[w];
+    const I yb = (I)iu * P.ys[u] + (I)iw * P.ys[w];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    const int mode = axpby_mode(alpha, beta);
+    const bool ry = axpby_reads_y(mode);
+    // this thread's Y elements are read before the exchange, so that the X and Y loads
+    // are in flight together
+    double yv[4];
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+        const uint32_t iq = iq0 + tx, ip = ip0 + ty + j;
+        yv[j / 8] = (ry && ip < P.ext[p] && iq < P.ext[q]) ? Y[yb + (I)ip * P.ys[p] + (I)iq * P.ys[q]] : 0.0;
+    }
 #pragma unroll
     for (int j = 0; j < 32; j += 8) {
         const uint32_t ip = ip0 + tx, iq = iq0 + ty + j;
         double v = 0.0;
-        if (ip < P.ext[p] && iq < P.ext[q]) v = X[xb + (int64_t)ip * P.xs[p] + (int64_t)iq * P.xs[q]];
+        if (ip < P.ext[p] && iq < P.ext[q]) v = X[xb + (I)ip * P.xs[p] + (I)iq * P.xs[q]];
         t[ty + j][tx] = v;
     }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < 32; j += 8) {
         const uint32_t iq = iq0 + tx, ip = ip0 + ty + j;
-        if (ip < P.ext[p] && iq < P.ext[q]) {
-            double *y = Y + yb + (int64_t)ip * P.ys[p] + (int64_t)iq * P.ys[q];
-            *y = axpby_el(alpha, t[tx][ty + j], beta, beta == 0.0 ? 0.0 : *y);
-        }
+        if (ip < P.ext[p] && iq < P.ext[q])
+            Y[yb + (I)ip * P.ys[p] + (I)iq * P.ys[q]] = axpby_apply(mode, alpha, t[tx][ty + j], beta, yv[j / 8]);
     }
 }
 
@@ -84,6 +101,8 @@ __global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, doub
                                     OutView Y) {
     const uint32_t total = (uint32_t)R * (uint32_t)C;
     const uint32_t step = gridDim.x * blockDim.x * 4u;
+    const int mode = axpby_mode(alpha, beta);
+    const bool rx = axpby_reads_x(mode), ry = axpby_reads_y(mode);
     for (uint32_t base = blockIdx.x * blockDim.x * 4u + threadIdx.x; base < total; base += step) {
         double *yp[4];
         double xv[4], yv[4];
@@ -94,12 +113,12 @@ __global__ void axpby_view32_kernel(int R, int C, uint32_t cm, uint32_t cl, doub
             in[u] = idx < total && idx >= base;  // idx >= base: no 32-bit wrap
             const uint32_t r = dim_udiv(in[u] ? idx : 0u, cm, cl), c = (in[u] ? idx : 0u) - r * (uint32_t)C;
             yp[u] = Y.p + dim_off(Y.row, r) + dim_off(Y.col, c);
-            xv[u] = (in[u] && alpha != 0.0) ? X.p[dim_off(X.row, r) + dim_off(X.col, c)] : 0.0;
-            yv[u] = (in[u] && beta != 0.0) ? *yp[u] : 0.0;
+            xv[u] = (in[u] && rx) ? X.p[dim_off(X.row, r) + dim_off(X.col, c)] : 0.0;
+            yv[u] = (in[u] && ry) ? *yp[u] : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-            if (in[u]) *yp[u] = axpby_el(alpha, xv[u], beta, yv[u]);
+            if (in[u]) *yp[u] = axpby_apply(mode, alpha, xv[u], beta, yv[u]);
     }
 }
 
@@ -261,7 +280,9 @@ __global__ void dinv2_kernel(int o, int v, const double *eo, const double *ev, d
 // t2_new = (R + Rp + Rp^T) * dinv with Rp^T[i][j][a][b] = Rp[j][i][b][a]; per-block
 // partial sums of |t2_new - t2_old|^2 (a fixed tile order per block: deterministic)
 // NORM = false: no partial sums (the caller takes the norm elsewhere) and t2o is not read
-template <bool NORM>
+// I: the index type, int32_t when every offset is below 2^31 (64-bit integer arithmetic
+// issues on the FP64 pipe on this part), else int64_t
+template <bool NORM, typename I>
 __global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, const double *__restrict__ R,
                                                               const double *__restrict__ Rp,
                                                               const double *__restrict__ dinv,
@@ -270,22 +291,22 @@ __global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, cons
     __shared__ double s[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int nt = (v + 31) / 32, ntiles = o * o * nt * nt;
-    const size_t v2 = (size_t)v * v;
+    const I v2 = (I)v * v;
     double acc = 0.0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile4 T = tile_of(t, o, nt);
-        const double *rpt = Rp + ((size_t)T.j * o + T.i) * v2;  // Rp[j][i][b][a], read along a
+        const double *rpt = Rp + ((I)T.j * o + T.i) * v2;  // Rp[j][i][b][a], read along a
         for (int q = ty; q < 32; q += 8) {
             const int b = T.B * 32 + q, a = T.A * 32 + tx;
-            s[q][tx] = (b < v && a < v) ? rpt[(size_t)b * v + a] : 0.0;
+            s[q][tx] = (b < v && a < v) ? rpt[(I)b * v + a] : 0.0;
         }
         __syncthreads();
-        const size_t base = ((size_t)T.i * o + T.j) * v2;
+        const I base = ((I)T.i * o + T.j) * v2;
         const int b = T.B * 32 + tx;
         for (int q = ty; q < 32; q += 8) {
             const int a = T.A * 32 + q;
             if (a < v && b < v) {
-                const size_t idx = base + (size_t)a * v + b;
+                const I idx = base + (I)a * v + b;
                 const double tn = (R[idx] + Rp[idx] + s[tx][q]) * dinv[idx];
                 if (NORM) {
                     const double d = tn - t2o[idx];
@@ -304,30 +325,31 @@ __global__ void __launch_bounds__(256) update_t2_tiled_kernel(int o, int v, cons
 
 // th1[i,a,l,d] = t2[i,l,a,d] - t2[i,l,d,a]/2 - t1[i,d] t1[l,a]; th2[i,a,l,d] = t2[i,l,d,a]/2 + t1[i,d] t1[l,a]
 // (tiles over (a, d) for each (i, l))
+template <typename I>
 __global__ void __launch_bounds__(256) theta_tiled_kernel(int o, int v, const double *__restrict__ t1,
                                                           const double *__restrict__ t2, double *__restrict__ th1,
                                                           double *__restrict__ th2) {
     __shared__ double s[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int nt = (v + 31) / 32, ntiles = o * o * nt * nt;
-    const size_t v2 = (size_t)v * v;
+    const I v2 = (I)v * v;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile4 T = tile_of(t, o, nt);  // (i, l, A, D)
         const int i = T.i, l = T.j;
-        const double *t2il = t2 + ((size_t)i * o + l) * v2;
+        const double *t2il = t2 + ((I)i * o + l) * v2;
         for (int q = ty; q < 32; q += 8) {  // s[d][a] = t2[i,l,d,a]
             const int d = T.B * 32 + q, a = T.A * 32 + tx;
-            s[q][tx] = (d < v && a < v) ? t2il[(size_t)d * v + a] : 0.0;
+            s[q][tx] = (d < v && a < v) ? t2il[(I)d * v + a] : 0.0;
         }
         __syncthreads();
         const int d = T.B * 32 + tx;
         for (int q = ty; q < 32; q += 8) {
             const int a = T.A * 32 + q;
             if (a < v && d < v) {
-                const double tad = t2il[(size_t)a * v + d];
+                const double tad = t2il[(I)a * v + d];
                 const double tda = s[tx][q];
                 const double tt = t1[i * v + d] * t1[l * v + a];
-                const size_t out = (((size_t)i * v + a) * o + l) * v + d;
+                const I out = (((I)i * v + a) * o + l) * v + d;
                 const double h = fma(0.5, tda, tt);  // th1 + th2 = t2[i,l,a,d]: three FP64 operations
                 th1[out] = tad - h;
                 th2[out] = h;
@@ -360,7 +382,10 @@ struct DiisVecs {
     int n;
 };
 
-__global__ void __launch_bounds__(256) diis_store_kernel(size_t n1, size_t n2, const double *__restrict__ x1n,
+// I: the index type (int32_t below 2^31 elements: 64-bit integer arithmetic issues on
+// the FP64 pipe on this part)
+template <typename I>
+__global__ void __launch_bounds__(256) diis_store_kernel(I n1, I n2, const double *__restrict__ x1n,
                                                          const double *__restrict__ x2n,
                                                          const double *__restrict__ x1o,
                                                          const double *__restrict__ x2o, double *__restrict__ Ts,
@@ -369,9 +394,8 @@ __global__ void __launch_bounds__(256) diis_store_kernel(size_t n1, size_t n2, c
     double acc[kDiisMax];
 #pragma unroll
     for (int q = 0; q < kDiisMax; ++q) acc[q] = 0.0;
-    const size_t n = n1 + n2;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
-         idx += (size_t)gridDim.x * blockDim.x) {
+    const I n = n1 + n2;
+    for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < n; idx += (I)gridDim.x * blockDim.x) {
         const double xn = idx < n1 ? x1n[idx] : x2n[idx - n1];
         const double xo = idx < n1 ? x1o[idx] : x2o[idx - n1];
         const double e = xn - xo;
@@ -389,12 +413,11 @@ __global__ void __launch_bounds__(256) diis_store_kernel(size_t n1, size_t n2, c
 
 // extrapolate: (y1, y2) = sum_q c_q V_q, V_q = (t1 part of length n1, t2 part); NV
 // vectors, all loads of an element issued together
-template <int NV>
-__global__ void __launch_bounds__(256) diis_combine_kernel(size_t n1, size_t n2, DiisVecs vecs,
+template <int NV, typename I>
+__global__ void __launch_bounds__(256) diis_combine_kernel(I n1, I n2, DiisVecs vecs,
                                                            double *__restrict__ y1, double *__restrict__ y2) {
-    const size_t n = n1 + n2;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
-         idx += (size_t)gridDim.x * blockDim.x) {
+    const I n = n1 + n2;
+    for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < n; idx += (I)gridDim.x * blockDim.x) {
         double x[NV];
 #pragma unroll
         for (int q = 0; q < NV; ++q) x[q] = __ldcs(vecs.p[q] + idx);
@@ -602,7 +625,26 @@ bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta
     const uint32_t tp = (P.ext[p] + 31) / 32, tq = (P.ext[q] + 31) / 32;
     const uint64_t blocks = (uint64_t)tp * tq * P.ext[rest[0]] * P.ext[rest[1]];
     if (blocks >= (1ull << 31)) return false;
-    permute_axpby_kernel<<<(unsigned)blocks, 256, 0, st>>>(P, p, q, rest[0], rest[1], tp, tq, alpha, X.p, beta, Y.p);
+    int64_t xmax = 0, ymax = 0;  // largest offsets (strides here are non-negative)
+    bool nonneg = true;
+    for (int i = 0; i < 4; ++i) {
+        nonneg = nonneg && P.xs[i] >= 0 && P.ys[i] >= 0;
+        xmax += (int64_t)(P.ext[i] - 1) * P.xs[i];
+        ymax += (int64_t)(P.ext[i] - 1) * P.ys[i];
+    }
+    if (nonneg && xmax < (1LL << 31) && ymax < (1LL << 31)) {
+        PermIndex32 P32;
+        for (int i = 0; i < 4; ++i) {
+            P32.ext[i] = P.ext[i];
+            P32.xs[i] = (int32_t)P.xs[i];
+            P32.ys[i] = (int32_t)P.ys[i];
+        }
+        permute_axpby_kernel<PermIndex32, int32_t><<<(unsigned)blocks, 256, 0, st>>>(P32, p, q, rest[0], rest[1], tp, tq,
+                                                                                     alpha, X.p, beta, Y.p);
+    } else {
+        permute_axpby_kernel<PermIndex, int64_t><<<(unsigned)blocks, 256, 0, st>>>(P, p, q, rest[0], rest[1], tp, tq,
+                                                                                   alpha, X.p, beta, Y.p);
+    }
     CCSD_LAUNCH_CHECK();
     return true;
 }
@@ -654,7 +696,7 @@ void k_theta(int o, int v, const double *t1, const double *t2, double *th1, doub
     if ((size_t)o * o * v * v >= ((size_t)1 << 31)) {
         theta_kernel<<<grid_for((size_t)o * o * v * v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
     } else {
-        theta_tiled_kernel<<<tiles_grid(o, v), 256, 0, st>>>(o, v, t1, t2, th1, th2);
+        theta_tiled_kernel<int32_t><<<tiles_grid(o, v), 256, 0, st>>>(o, v, t1, t2, th1, th2);  // o^2 v^2 < 2^31
     }
     CCSD_LAUNCH_CHECK();
 }
@@ -671,7 +713,12 @@ void k_diis_store(size_t n1, size_t n2, const double *x1n, const double *x2n, co
     DiisVecs d{};
     for (int q = 0; q < nothers; ++q) d.p[q] = others[q];
     d.n = nothers;
-    diis_store_kernel<<<nblocks, 256, 0, st>>>(n1, n2, x1n, x2n, x1o, x2o, Ts, Es, d, partials);
+    if (n1 + n2 + (size_t)nblocks * 256 < ((size_t)1 << 31))
+        diis_store_kernel<int32_t><<<nblocks, 256, 0, st>>>((int32_t)n1, (int32_t)n2, x1n, x2n, x1o, x2o, Ts, Es, d,
+                                                            partials);
+    else
+        diis_store_kernel<int64_t><<<nblocks, 256, 0, st>>>((int64_t)n1, (int64_t)n2, x1n, x2n, x1o, x2o, Ts, Es, d,
+                                                            partials);
     CCSD_LAUNCH_CHECK();
 }
 
@@ -685,9 +732,15 @@ void k_diis_combine(size_t n1, size_t n2, const double *const *vecs, const doubl
     }
     d.n = n;
     const int g = (int)std::min<size_t>((n1 + n2 + 255) / 256, 152 * 8);
+    const bool i32 = n1 + n2 + (size_t)g * 256 < ((size_t)1 << 31);
     switch (n) {
-#define CCSD_DIIS_CASE(NV_) \
-    case NV_: diis_combine_kernel<NV_><<<g, 256, 0, st>>>(n1, n2, d, y1, y2); break;
+#define CCSD_DIIS_CASE(NV_)                                                                                 \
+    case NV_:                                                                                               \
+        if (i32)                                                                                            \
+            diis_combine_kernel<NV_, int32_t><<<g, 256, 0, st>>>((int32_t)n1, (int32_t)n2, d, y1, y2);   \
+        else                                                                                                \
+            diis_combine_kernel<NV_, int64_t><<<g, 256, 0, st>>>((int64_t)n1, (int64_t)n2, d, y1, y2);   \
+        break;
         CCSD_DIIS_CASE(1) CCSD_DIIS_CASE(2) CCSD_DIIS_CASE(3) CCSD_DIIS_CASE(4) CCSD_DIIS_CASE(5)
         CCSD_DIIS_CASE(6) CCSD_DIIS_CASE(7) CCSD_DIIS_CASE(8) CCSD_DIIS_CASE(9) CCSD_DIIS_CASE(10)
         CCSD_DIIS_CASE(11) CCSD_DIIS_CASE(12) CCSD_DIIS_CASE(13) CCSD_DIIS_CASE(14) CCSD_DIIS_CASE(15)
@@ -742,9 +795,9 @@ void k_update_t2(int o, int v, const double *R, const double *Rp, const double *
                  double *partials, int nblocks, cudaStream_t st) {
     if (dinv2 && (size_t)o * o * v * v < ((size_t)1 << 31)) {
         if (partials)
-            update_t2_tiled_kernel<true><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
+            update_t2_tiled_kernel<true, int32_t><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
         else
-            update_t2_tiled_kernel<false><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
+            update_t2_tiled_kernel<false, int32_t><<<nblocks, 256, 0, st>>>(o, v, R, Rp, dinv2, t2_old, t2_new, partials);
     } else if (!partials) {
         throw Error(-1, "k_update_t2: the norm-free form needs the 1/D table");
     } else
