@@ -14,7 +14,7 @@ namespace ccsd {
 // classified once per thread (axpby_mode: the comparisons are FP64 instructions too)
 // and applied per element (axpby_apply).
 enum AxpbyMode { kAxX, kAxAX, kAxXpY, kAxXpBY, kAxGen, kAxY, kAxBY, kAxZero };
-__device__ __forceinline__ int axpby_mode(double alpha, double beta) {
+__host__ __device__ __forceinline__ int axpby_mode(double alpha, double beta) {
     if (beta == 0.0) return alpha == 1.0 ? kAxX : (alpha == 0.0 ? kAxZero : kAxAX);
     if (alpha == 0.0) return beta == 1.0 ? kAxY : kAxBY;
     if (alpha == 1.0) return beta == 1.0 ? kAxXpY : kAxXpBY;

@@ -53,10 +53,13 @@ struct PermIndex32 {
     int32_t xs[4], ys[4];
 };
 
+// mode: axpby_mode(alpha, beta), classified on the host (a block here handles 4 elements
+// per thread, so per-thread FP64 comparisons would cost more than the arithmetic)
 template <class PI, typename I>
 __global__ void __launch_bounds__(256) permute_axpby_kernel(PI P, int p, int q, int u, int w, uint32_t tp,
-                                                            uint32_t tq, double alpha, const double *__restrict__ X,
-                                                            double beta, double *__restrict__ Y) {
+                                                            uint32_t tq, int mode, double alpha,
+                                                            const double *__restrict__ X, double beta,
+                                                            double *__restrict__ Y) {
     __shared__ double t[32][33];
     uint32_t b = blockIdx.x;
     const uint32_t ip0 = (b % tp) * 32;
@@ -67,7 +70,6 @@ __global__ void __launch_bounds__(256) permute_axpby_kernel(PI P, int p, int q, 
     const I xb = (I)iu * P.xs[u] + (I)iw * P.xs[w];
     const I yb = (I)iu * P.ys[u] + (I)iw * P.ys[w];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    const int mode = axpby_mode(alpha, beta);
     const bool ry = axpby_reads_y(mode);
     // this thread's Y elements are read before the exchange, so that the X and Y loads
     // are in flight together
@@ -526,8 +528,8 @@ __global__ void tau_dot_rows_kernel(int o, int v, const double *__restrict__ t1,
     for (int r = blockIdx.x; r < rows; r += gridDim.x) {
         const int a = r % v, ij = r / v, j = ij % o, i = ij / o;
         const double ta = t1[i * v + a];
-        const double *t1j = t1 + (size_t)j * v;
-        const size_t base = (size_t)r * v;
+        const double *t1j = t1 + j * v;
+        const int base = r * v;  // o^2 v^2 < 2^31 (checked by the caller)
         for (int b = threadIdx.x; b < v; b += blockDim.x) {
             const double x = fma(ta, t1j[b], t2[base + b]);
             tau[base + b] = x;
@@ -639,11 +641,11 @@ bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta
             P32.xs[i] = (int32_t)P.xs[i];
             P32.ys[i] = (int32_t)P.ys[i];
         }
-        permute_axpby_kernel<PermIndex32, int32_t><<<(unsigned)blocks, 256, 0, st>>>(P32, p, q, rest[0], rest[1], tp, tq,
-                                                                                     alpha, X.p, beta, Y.p);
+        permute_axpby_kernel<PermIndex32, int32_t><<<(unsigned)blocks, 256, 0, st>>>(
+            P32, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Y.p);
     } else {
-        permute_axpby_kernel<PermIndex, int64_t><<<(unsigned)blocks, 256, 0, st>>>(P, p, q, rest[0], rest[1], tp, tq,
-                                                                                   alpha, X.p, beta, Y.p);
+        permute_axpby_kernel<PermIndex, int64_t><<<(unsigned)blocks, 256, 0, st>>>(
+            P, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Y.p);
     }
     CCSD_LAUNCH_CHECK();
     return true;
