@@ -751,8 +751,8 @@ __global__ void __launch_bounds__(64 + 32 * EW, MINB)
 
 // ---- FP64 -> S BF16 planes ---------------------------------------------------
 // All integer arithmetic (FP64 runs at 1/64 of the FP32 rate on this part):
-// pass 1 takes the row maxima of |x| as IEEE bit patterns (they order like the
-// values for non-negative doubles); pass 2 turns x into the fixed-point
+// pass 1 takes the row maxima of |x| as the high words of their IEEE bit patterns
+// (they order like the values' exponents for non-negative doubles); pass 2 turns x into the fixed-point
 // integer Y = round(x * 2^(7 - ex + 8(S-1))), ex = exponent of the row
 // maximum (|Y| <= 2^(8S-1)), and peels balanced base-256 digits
 // d in [-128, 127] off Y from the bottom; the remaining top digit P0 lies in
@@ -760,52 +760,59 @@ __global__ void __launch_bounds__(64 + 32 * EW, MINB)
 constexpr int kRowmaxKT = 32;  // 32-wide k tiles per row-max block
 
 // Row maxima of one 32-row x (32 kRowmaxKT)-column block, from row r0 and
-// column kbeg, merged into rmax with atomicMax (32 x 8 threads).
+// column kbeg, merged into rmax with atomicMax (32 x 8 threads).  A row maximum
+// is kept as the high word of |x| (sign cleared), which orders |x| by exponent:
+// only the exponent is used, and the comparisons stay 32-bit (64-bit integer
+// arithmetic issues on the FP64 pipe on this part).  Four loads per thread are
+// issued before their maxima are taken.
 template <bool ROWC>
 __device__ void rowmax_block(int rows, int K, const MatView &v, unsigned long long *rmax, int r0, int kbeg) {
     const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-    const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
+    const auto hiabs = [](double x) { return (uint32_t)__double2hiint(x) & 0x7FFFFFFFu; };
     if (ROWC) {
         // thread owns row r0 + tx; the 8 thread rows split the k range
-        __shared__ unsigned long long part[8][32];
+        __shared__ uint32_t part[8][32];
         const int r = r0 + tx;
-        unsigned long long m = 0;
+        uint32_t m = 0;
         if (r < rows) {
-            const int64_t ro = dim_off(v.row, (uint32_t)r);
+            const double *row = v.p + dim_off(v.row, (uint32_t)r);
             const int kend = min(K, kbeg + 32 * kRowmaxKT);
-            for (int k = kbeg + ty; k < kend; k += 8) {
-                const unsigned long long b =
-                    (unsigned long long)__double_as_longlong(v.p[ro + dim_off(v.col, (uint32_t)k)]) & absmask;
-                m = b > m ? b : m;
+            int k = kbeg + ty;
+            for (; k + 24 < kend; k += 32) {
+                const double x0 = row[dim_off(v.col, (uint32_t)k)], x1 = row[dim_off(v.col, (uint32_t)(k + 8))];
+                const double x2 = row[dim_off(v.col, (uint32_t)(k + 16))], x3 = row[dim_off(v.col, (uint32_t)(k + 24))];
+                m = max(max(m, max(hiabs(x0), hiabs(x1))), max(hiabs(x2), hiabs(x3)));
             }
+            for (; k < kend; k += 8) m = max(m, hiabs(row[dim_off(v.col, (uint32_t)k)]));
         }
         part[ty][tx] = m;
         __syncthreads();
         if (ty == 0 && r < rows) {
 #pragma unroll
-            for (int q = 1; q < 8; ++q) m = part[q][tx] > m ? part[q][tx] : m;
-            if (m) atomicMax(rmax + r, m);
+            for (int q = 1; q < 8; ++q) m = max(m, part[q][tx]);
+            if (m) atomicMax(rmax + r, (unsigned long long)m);
         }
     } else {
         // thread row ty owns rows r0 + ty + 8j; lanes run along k
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int r = r0 + ty + 8 * j;
-            unsigned long long m = 0;
+            uint32_t m = 0;
             if (r < rows) {
-                const int64_t ro = dim_off(v.row, (uint32_t)r);
+                const double *row = v.p + dim_off(v.row, (uint32_t)r);
                 const int kend = min(K, kbeg + 32 * kRowmaxKT);
-                for (int k = kbeg + tx; k < kend; k += 32) {
-                    const unsigned long long b =
-                        (unsigned long long)__double_as_longlong(v.p[ro + dim_off(v.col, (uint32_t)k)]) & absmask;
-                    m = b > m ? b : m;
+                int k = kbeg + tx;
+                for (; k + 96 < kend; k += 128) {
+                    const double x0 = row[dim_off(v.col, (uint32_t)k)], x1 = row[dim_off(v.col, (uint32_t)(k + 32))];
+                    const double x2 = row[dim_off(v.col, (uint32_t)(k + 64))],
+                                 x3 = row[dim_off(v.col, (uint32_t)(k + 96))];
+                    m = max(max(m, max(hiabs(x0), hiabs(x1))), max(hiabs(x2), hiabs(x3)));
                 }
+                for (; k < kend; k += 32) m = max(m, hiabs(row[dim_off(v.col, (uint32_t)k)]));
             }
-            for (int off = 16; off > 0; off >>= 1) {
-                const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
-                m = o > m ? o : m;
-            }
-            if (tx == 0 && r < rows && m) atomicMax(rmax + r, m);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+            if (tx == 0 && r < rows && m) atomicMax(rmax + r, (unsigned long long)m);
         }
     }
     __syncthreads();  // the shared row maxima are reused by the next block of a looping caller
@@ -916,7 +923,7 @@ __device__ void planes_block(int rows, int rows_pad, int K, int kpad, int64_t pi
         const int a = ty + 8 * j;
         const int r = r0 + a, k = k0 + tx;
         if (r >= rows_pad || k >= kpad) continue;
-        const int emax = r < rows ? (int)((rmax[r] >> 52) & 0x7FF) : 0;  // 0: zero (or denormal) row
+        const int emax = r < rows ? (int)((rmax[r] >> 20) & 0x7FF) : 0;  // 0: zero (or denormal) row
         if (k0 == 0 && tx == 0)
             scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;  // 2^(emax-1022)
         float d[S];
@@ -1626,12 +1633,9 @@ void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatVie
 }
 
 void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
-                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st, int levels) {
+                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
     if (A.kpad != B.kpad || A.nslices != B.nslices) throw Error(-1, "split operands disagree");
-    // a kernel for S planes reads plane p of an operand at plane row p * rows_pad, so it
-    // runs on the first S planes of operands that hold more
-    const int S = levels >= 2 && levels < A.nslices ? levels : A.nslices;
-    switch (S) {
+    switch (A.nslices) {
         case 2: launch_s<2>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
         case 3: launch_s<3>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
         case 4: launch_s<4>(A, B, M, N, alpha, beta, C, ws, ws_elems, d_err, st); break;
@@ -1772,12 +1776,12 @@ void SplitEngine::gemm(int M, int N, int K, double alpha, const MatView &A, cons
     }
     SplitOperand *a = operand(cache_a, M, K, A, 0);
     SplitOperand *b = operand(cache_b, N, K, B, 1);
-    split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_, levels_);
+    split_gemm_launch(*a, *b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
 }
 
 void SplitEngine::run(const SplitOperand &a, const SplitOperand &b, int M, int N, double alpha, double beta,
                       const OutView &C) {
-    split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_, levels_);
+    split_gemm_launch(a, b, M, N, alpha, beta, C, ws_, ws_elems_, d_err_, st_);
 }
 
 void SplitEngine::clear_error() { CCSD_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), st_)); }

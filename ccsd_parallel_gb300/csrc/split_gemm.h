@@ -51,9 +51,6 @@ class SplitEngine {
     }
     void run(const SplitOperand &a, const SplitOperand &b, int M, int N, double alpha, double beta,
              const OutView &C);
-    // planes per operand that the products use (split_gemm_launch's `levels`; 0 = all)
-    void set_levels(int levels) { levels_ = levels; }
-    int levels() const { return levels_ > 0 && levels_ < nslices_ ? levels_ : nslices_; }
     // The tensor-core tile is 128 rows by at most 128 columns: a product whose
     // row count is short and column count long runs faster transposed.
     static bool prefer_swap(int M, int N) { return M < 128 && N > M; }
@@ -90,7 +87,6 @@ class SplitEngine {
     int *d_err_ = nullptr;
     double *ws_ = nullptr;
     size_t ws_elems_ = 0;
-    int levels_ = 0;
 };
 
 // ---- grouped split contractions (batched solve) -------------------------------
@@ -133,12 +129,8 @@ void grouped_split_gemm_launch(const PackedSplit &A, const PackedSplit &B, int b
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st);
 // C = alpha * A B^T + beta C for split operands with equal kpad and nslices;
 // `ws` (ws_elems doubles) holds split-K partial sums; `d_err` the error word.
-// levels in [2, nslices) runs the product of the operands' first `levels` planes
-// only (the digit expansion cut after that many terms: the accuracy of a
-// levels-plane split, whose balanced digits leave the same bound); 0 = all.
 void split_gemm_launch(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
-                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st,
-                       int levels = 0);
+                       const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st);
 // One contraction with temporary split operands and workspace.
 void split_gemm_oneshot(int nslices, int M, int N, int K, double alpha, const MatView &A, const MatView &B,
                         double beta, const OutView &C, cudaStream_t st);

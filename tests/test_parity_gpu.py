@@ -270,3 +270,19 @@ def test_restart_arguments_are_checked():
     with pytest.raises(cg.CCSDError) as ei:
         cg.solve(fock, 3, df=b, fixed_iterations=1, t1_start=first["t1"])
     assert ei.value.code == -1 and "t2_start" in str(ei.value)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split3"])
+def test_graph_replay_equals_direct_issue(precision):
+    """From its second update on a solve replays each update from a CUDA graph; with
+    profile=1 it issues the same kernels directly.  Both follow the same iteration bit
+    for bit: every per-update energy and the final amplitudes are equal."""
+    fock, b = cg.make_synthetic(6, 48, 150, 31)
+    kw = dict(df=b, precision=precision, fixed_iterations=8, diis_size=6, diis_start=2)
+    with cg.Solver(fock, 6, **kw) as s:
+        rg = s.solve()
+    with cg.Solver(fock, 6, profile=True, **kw) as s:
+        rd = s.solve()
+    assert np.array_equal(rg["energies"], rd["energies"])
+    assert np.array_equal(rg["t2"], rd["t2"]) and np.array_equal(rg["t1"], rd["t1"])
+    assert rg["residual_norm"] == rd["residual_norm"]
