@@ -82,17 +82,6 @@ void jacobi_eigh(int n, Mat a, std::vector<double> &w, Mat &V) {
     V.swap(Vs);
 }
 
-Mat matmul(int n, const Mat &a, const Mat &b, bool ta = false) {
-    Mat c((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i)
-        for (int k = 0; k < n; ++k) {
-            const double x = ta ? a[(size_t)k * n + i] : a[(size_t)i * n + k];
-            if (x == 0.0) continue;
-            for (int j = 0; j < n; ++j) c[(size_t)i * n + j] += x * b[(size_t)k * n + j];
-        }
-    return c;
-}
-
 // solve A x = b (m x m) by Gaussian elimination with partial pivoting
 std::vector<double> solve_small(int m, Mat A, std::vector<double> b) {
     for (int c = 0; c < m; ++c) {
@@ -138,6 +127,7 @@ struct ScfSystem {
     Dev eri, P_d, G_d, ws;
     size_t ws_n = 1;
     cudaStream_t st;
+    mutable Dev mA, mB, mC;  // operands of the n x n products on the device
 
     ScfSystem(const ccsd_basis &bs, cudaStream_t s) : n(bs.nbf), nn((size_t)bs.nbf * bs.nbf), st(s) {
         S.resize(nn);
@@ -149,6 +139,9 @@ struct ScfSystem {
         for (size_t k = 0; k < nn; ++k) h[k] = T[k] + Vn[k];
         P_d.alloc(2 * nn);
         G_d.alloc(nn);
+        mA.alloc(nn);
+        mB.alloc(nn);
+        mC.alloc(nn);
         ws_n = std::max(gemm_f64_ws_elems((int)nn, 1, (int)nn), (size_t)1);
         ws.alloc(ws_n);
         std::vector<double> lam;
@@ -174,25 +167,42 @@ struct ScfSystem {
         CCSD_CUDA(cudaStreamSynchronize(st));
     }
 
+    // op(a) b for n x n host matrices (op(a) = a^T with ta), k columns of op(a) (rows of b) summed,
+    // as an FP64 contraction on the device: a product costs tens of microseconds there against
+    // milliseconds of host loops at n = 150
+    Mat dmm(const Mat &a, const Mat &b, bool ta = false, int k = -1) const {
+        if (k < 0) k = n;
+        CCSD_CUDA(cudaMemcpyAsync(mA.p, a.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+        CCSD_CUDA(cudaMemcpyAsync(mB.p, b.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+        // C(i, j) = sum_l A(i, l) B(j, l) with A(i, l) = op(a)[i][l], B(j, l) = b[l][j]
+        const MatView Av{mA.p, ta ? ix1(1) : ix1(n), ta ? ix1(n) : ix1(1)};
+        const MatView Bv{mB.p, ix1(1), ix1(n)};
+        gemm_f64(n, n, k, 1.0, Av, Bv, 0.0, OutView{mC.p, ix1(n), ix1(1)}, ws.p, ws_n, st);
+        Mat c(nn);
+        CCSD_CUDA(cudaMemcpyAsync(c.data(), mC.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, st));
+        CCSD_CUDA(cudaStreamSynchronize(st));
+        return c;
+    }
+
     // eigenpairs of X^T F X ascending, C = X W with every column at c^T S c = 1 (Normalize).
     // warm: the previous step's W of this spin; X^T F X is rotated into it first, where it
     // is nearly diagonal, so the Jacobi sweeps start close to the answer (then warm = W)
     void orbitals(const Mat &F, std::vector<double> &eps, Mat &C, Mat &warm) const {
-        const Mat Fo = matmul(n, X, matmul(n, F, X), true);
+        const Mat Fo = dmm(X, dmm(F, X), true);
         Mat W;
         if (warm.size() == nn) {
             Mat V;
-            jacobi_eigh(n, matmul(n, warm, matmul(n, Fo, warm), true), eps, V);
-            W = matmul(n, warm, V);
+            jacobi_eigh(n, dmm(warm, dmm(Fo, warm), true), eps, V);
+            W = dmm(warm, V);
         } else {
             jacobi_eigh(n, Fo, eps, W);
         }
         warm = W;
-        C = matmul(n, X, W);
+        C = dmm(X, W);
+        const Mat SC = dmm(S, C);  // c^T S c = sum_i C[i][c] (S C)[i][c]
         for (int c = 0; c < n; ++c) {
             double s = 0.0;
-            for (int i = 0; i < n; ++i)
-                for (int j = 0; j < n; ++j) s += C[(size_t)i * n + c] * S[(size_t)i * n + j] * C[(size_t)j * n + c];
+            for (int i = 0; i < n; ++i) s += C[(size_t)i * n + c] * SC[(size_t)i * n + c];
             const double f = 1.0 / std::sqrt(s);
             for (int i = 0; i < n; ++i) C[(size_t)i * n + c] *= f;
         }
@@ -200,13 +210,11 @@ struct ScfSystem {
 
     // P = w C_occ C_occ^T over the first k columns
     Mat density(const Mat &C, int k, double w) const {
-        Mat P(nn);
+        Mat Ct(nn);  // C^T, so that the product sums over its first k rows
         for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) {
-                double s = 0.0;
-                for (int c = 0; c < k; ++c) s += C[(size_t)i * n + c] * C[(size_t)j * n + c];
-                P[(size_t)i * n + j] = w * s;
-            }
+            for (int c = 0; c < n; ++c) Ct[(size_t)c * n + i] = C[(size_t)i * n + c];
+        Mat P = dmm(C, Ct, false, k);
+        for (double &x : P) x *= w;
         return P;
     }
 };
@@ -237,8 +245,8 @@ void rhf(const ccsd_basis &bs, int nelec, double tol, int max_iter, ccsd_scf_res
         Fprev = F;
         // DIIS (the reference's, with 3 vectors)
         if (step > 0) {
-            Mat e = matmul(n, matmul(n, F, P), S);
-            const Mat SPF = matmul(n, S, matmul(n, P, F));
+            Mat e = sys.dmm(sys.dmm(F, P), S);
+            const Mat SPF = sys.dmm(S, sys.dmm(P, F));
             for (size_t k = 0; k < nn; ++k) e[k] -= SPF[k];
             errs.push_back(e);
             focks.push_back(F);
