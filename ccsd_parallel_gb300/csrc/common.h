@@ -125,6 +125,10 @@ size_t gemm_f64_ws_elems(int M, int N, int K);
 // Y(r,c) = alpha * X(r,c) + beta * Y(r,c) over an R x C grid (views may permute).
 void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
                 cudaStream_t st);
+// Y = alpha X + beta Yin, Yin read at Y's offsets (another array laid out like Y), by the
+// permute form only; returns false (nothing launched) where that form does not apply
+bool axpby_view_from(int R, int C, double alpha, const MatView &X, double beta, const double *Yin,
+                     const OutView &Y, cudaStream_t st);
 
 // Elementwise/amplitude kernels (all closed-shell spatial, o = nocc, v = nvir).
 void k_tau(int o, int v, const double *t1, const double *t2, double *tau, cudaStream_t st);

@@ -721,16 +721,23 @@ void Engine::residual() {
              mv(tau, ix1(v2), ix1(1)), 1.0, ovw(Woooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
 
     // ---- Wvoov_s[i][a][k][c] = W_akic ------------------------------------
-    copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
     // + sum_d (kc|ad) t1[i,d] is the product Y[(p,q,r)][j] = sum_s (pq|rs) t1[j,s] that
     // also opens Rp (Rp[i][j][a][b] = Y[(i,a,b)][j], its first write of the update):
-    // Y is formed once, into Rp, and Wvoov[i][a][k][c] += Y[(k,c,a)][i] = Rp[k][i][c][a]
+    // Y is formed once, into Rp, and Wvoov[i][a][k][c] = ovov[i][a][k][c] + Y[(k,c,a)][i]
+    // (Rp[k][i][c][a]), one pass over both when unrecorded (no copy of ovov first)
+    if (tape_) copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
     gemm((int)(o * v2), io, iv, 1.0, mv(ovvv_.p, ix1(v), ix1(1)), mv(t1, ix1(v), ix1(1)), 0.0,
          ovw(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 6, 0, "Rp_ovvv_t1");
     // Lvv[a][c] -= sum_k Y[(k,c,a)][k] = sum_k Rp[k][k][c][a]
     if (sym_amps) k_diag_acc(o_, v_, -1.0, Rp_.p, (int64_t)(o + 1) * v2, 1, v, Lvv_.p, st_);
-    axpby((int)(ov * v), io, 1.0, mv(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2)), 1.0,
-          ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov)));
+    {
+        const MatView yv = mv(Rp_.p, ix3((uint32_t)v, (uint32_t)v, ov2, v, 1), ix1(v2));
+        const OutView wv = ovw(Wvoov_.p, ix3((uint32_t)v, (uint32_t)v, v, 1, ov), ix1(v * ov));
+        if (tape_ || !axpby_view_from((int)(ov * v), io, 1.0, yv, 1.0, ovov_.p, wv, st_)) {
+            if (!tape_) copy(Wvoov_.p, ovov_.p, (size_t)(ov * ov));
+            axpby((int)(ov * v), io, 1.0, yv, 1.0, wv);
+        }
+    }
     // - sum_l (kc|li) t1[l,a]: M = (i,k,c) (c, contiguous in Wvoov, innermost), N = a, K = l
     gemm((int)(ov * o), iv, io, -1.0,
          mv(ovoo_.p, ix3((uint32_t)o, (uint32_t)v, 1, v * o2, o2), ix1(o)), mv(t1, ix1(1), ix1(v)),

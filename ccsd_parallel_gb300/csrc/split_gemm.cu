@@ -1057,6 +1057,34 @@ __global__ void __launch_bounds__(256) split_rows_vec_kernel(int rows, int K, in
     }
 }
 
+// Pass 2 for long rows in 16-byte groups, after rowmax_kernel: a block takes 256 G
+// consecutive k of one row (one group per thread) and writes their digits; no shared
+// memory and no exchange, so the loads and stores stream.
+template <int S, int G>
+__global__ void __launch_bounds__(256) split_planes_vec_kernel(int rows, int K, int kpad, MatView v,
+                                                               const unsigned long long *__restrict__ rmax,
+                                                               __nv_bfloat16 *__restrict__ planes, size_t plane,
+                                                               double *__restrict__ scale) {
+    constexpr int chunk = 256 * G;
+    const int nch = (kpad + chunk - 1) / chunk;
+    const long long units = (long long)rows * nch;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        const int r = (int)(u / nch), c = (int)(u - (long long)r * nch);
+        const int emax = (int)((rmax[r] >> 20) & 0x7FF);  // 0: zero (or denormal) row
+        if (c == 0 && threadIdx.x == 0) scale[r] = emax ? __longlong_as_double((long long)(emax + 1) << 52) : 1.0;
+        const int k = c * chunk + G * threadIdx.x;
+        if (k >= kpad) continue;
+        double x[G];
+        if (k < K) {
+            load_group<G>(v.p + dim_off(v.row, (uint32_t)r) + dim_off(v.col, (uint32_t)k), x);
+        } else {
+#pragma unroll
+            for (int g = 0; g < G; ++g) x[g] = 0.0;
+        }
+        store_group_digits<S, G>(x, emax, planes + (size_t)r * kpad + k, plane);
+    }
+}
+
 // Rows of up to kSmemRowK doubles: a block per row stages the row in shared memory
 // on its one read from HBM (UNR groups per thread in flight), takes the maximum, and
 // writes the digits from shared memory.
@@ -1536,20 +1564,31 @@ static bool k_groups(const MatView &v, int K, int G) {
     return true;
 }
 
-// One pass over a view of 16-byte groups (k_groups): rows up to kSmemRowK long are
-// staged in shared memory, a block per row; short rows (under 1024, whose re-read
-// stays in L2) take a warp per row.  Returns false for the longer rows, which the
-// two-pass kernels take.
+// A view of 16-byte groups (k_groups): rows up to kSmemRowK long are staged in shared
+// memory, a block per row (one HBM read); short rows (under 1024, whose re-read stays
+// in L2) take a warp per row; longer rows take two passes (row maxima, then the digits
+// streamed).  Always returns true.
 template <int S, int G>
 static bool launch_split_vec_g(int rows, int K, int kpad, const MatView &v, __nv_bfloat16 *pl, size_t plane,
-                               double *scale, cudaStream_t st) {
+                               double *scale, unsigned long long *rmax, cudaStream_t st) {
     if (K < 1024) {
         const int grid = (int)std::min<long long>((rows + 7) / 8, 152LL * 8);
         split_rows_vec_kernel<S, G><<<grid, 256, 0, st>>>(rows, K, kpad, v, pl, plane, scale);
         CCSD_LAUNCH_CHECK();
         return true;
     }
-    if (K > kSmemRowK) return false;
+    if (K > kSmemRowK) {  // two passes: row maxima, then the digits streamed in 16-byte groups
+        const int nrt = (rows + 31) / 32;
+        const long long nkg = (kpad + 32 * kRowmaxKT - 1) / (32 * kRowmaxKT);
+        CCSD_CUDA(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * rows, st));
+        rowmax_kernel<false><<<(unsigned)(nrt * nkg), dim3(32, 8), 0, st>>>(rows, K, (int)nkg, v, rmax);
+        CCSD_LAUNCH_CHECK();
+        const long long units = (long long)rows * ((kpad + 256 * G - 1) / (256 * G));
+        const int grid = (int)std::min<long long>(units, 152LL * 8 * 4);
+        split_planes_vec_kernel<S, G><<<grid, 256, 0, st>>>(rows, K, kpad, v, rmax, pl, plane, scale);
+        CCSD_LAUNCH_CHECK();
+        return true;
+    }
     const size_t smem = sizeof(double) * (size_t)K;
     static unsigned long long attr_set = 0;  // per device (the attribute is per context)
     int dev = 0;
@@ -1568,9 +1607,9 @@ static bool launch_split_vec_g(int rows, int K, int kpad, const MatView &v, __nv
 
 template <int S>
 static bool launch_split_vec(int G, int rows, int K, int kpad, const MatView &v, __nv_bfloat16 *pl, size_t plane,
-                             double *scale, cudaStream_t st) {
-    return G == 4 ? launch_split_vec_g<S, 4>(rows, K, kpad, v, pl, plane, scale, st)
-                  : launch_split_vec_g<S, 2>(rows, K, kpad, v, pl, plane, scale, st);
+                             double *scale, unsigned long long *rmax, cudaStream_t st) {
+    return G == 4 ? launch_split_vec_g<S, 4>(rows, K, kpad, v, pl, plane, scale, rmax, st)
+                  : launch_split_vec_g<S, 2>(rows, K, kpad, v, pl, plane, scale, rmax, st);
 }
 
 void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatView &v, cudaStream_t st) {
@@ -1586,9 +1625,9 @@ void split_operand_kernel_launch(SplitOperand &op, int rows, int K, const MatVie
     if (G) {  // one HBM pass, 16-byte loads
         bool done = false;
         switch (op.nslices) {
-            case 2: done = launch_split_vec<2>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
-            case 3: done = launch_split_vec<3>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
-            case 4: done = launch_split_vec<4>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, st); break;
+            case 2: done = launch_split_vec<2>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, op.rmax, st); break;
+            case 3: done = launch_split_vec<3>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, op.rmax, st); break;
+            case 4: done = launch_split_vec<4>(G, rows, K, op.kpad, v, pl0, plane0, op.scale, op.rmax, st); break;
             default: throw Error(-1, "nslices must be 2, 3 or 4");
         }
         if (done) return;

@@ -55,11 +55,12 @@ struct PermIndex32 {
 
 // mode: axpby_mode(alpha, beta), classified on the host (a block here handles 4 elements
 // per thread, so per-thread FP64 comparisons would cost more than the arithmetic)
+// Yin: where the Y operand is read (Y itself, or another array with Y's offsets)
 template <class PI, typename I>
 __global__ void __launch_bounds__(256) permute_axpby_kernel(PI P, int p, int q, int u, int w, uint32_t tp,
                                                             uint32_t tq, int mode, double alpha,
                                                             const double *__restrict__ X, double beta,
-                                                            double *__restrict__ Y) {
+                                                            const double *Yin, double *Y) {
     __shared__ double t[32][33];
     uint32_t b = blockIdx.x;
     const uint32_t ip0 = (b % tp) * 32;
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(256) permute_axpby_kernel(PI P, int p, int q, 
 #pragma unroll
     for (int j = 0; j < 32; j += 8) {
         const uint32_t iq = iq0 + tx, ip = ip0 + ty + j;
-        yv[j / 8] = (ry && ip < P.ext[p] && iq < P.ext[q]) ? Y[yb + (I)ip * P.ys[p] + (I)iq * P.ys[q]] : 0.0;
+        yv[j / 8] = (ry && ip < P.ext[p] && iq < P.ext[q]) ? Yin[yb + (I)ip * P.ys[p] + (I)iq * P.ys[q]] : 0.0;
     }
 #pragma unroll
     for (int j = 0; j < 32; j += 8) {
@@ -600,7 +601,9 @@ bool row_levels(int R, const Dim &d, uint32_t ext[3], int64_t str[3]) {
 
 // The permute form when both views are plain 4-index views with the same row
 // levels and 1-level columns, and their unit-stride indices differ.
-bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y, cudaStream_t st) {
+bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y, cudaStream_t st,
+                       const double *Yin = nullptr) {
+    if (!Yin) Yin = Y.p;
     if (X.col.e2 != 0xFFFFFFFFu || Y.col.e2 != 0xFFFFFFFFu) return false;
     if (X.row.e1 != Y.row.e1 || X.row.e2 != Y.row.e2) return false;
     PermIndex P;
@@ -642,15 +645,21 @@ bool try_permute_axpby(int R, int C, double alpha, const MatView &X, double beta
             P32.ys[i] = (int32_t)P.ys[i];
         }
         permute_axpby_kernel<PermIndex32, int32_t><<<(unsigned)blocks, 256, 0, st>>>(
-            P32, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Y.p);
+            P32, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Yin, Y.p);
     } else {
         permute_axpby_kernel<PermIndex, int64_t><<<(unsigned)blocks, 256, 0, st>>>(
-            P, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Y.p);
+            P, p, q, rest[0], rest[1], tp, tq, axpby_mode(alpha, beta), alpha, X.p, beta, Yin, Y.p);
     }
     CCSD_LAUNCH_CHECK();
     return true;
 }
 }  // namespace
+
+bool axpby_view_from(int R, int C, double alpha, const MatView &X, double beta, const double *Yin,
+                     const OutView &Y, cudaStream_t st) {
+    if (R <= 0 || C <= 0) return true;
+    return try_permute_axpby(R, C, alpha, X, beta, Y, st, Yin);
+}
 
 void axpby_view(int R, int C, double alpha, const MatView &X, double beta, const OutView &Y,
                 cudaStream_t st) {
