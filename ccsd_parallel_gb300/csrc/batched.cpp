@@ -96,7 +96,13 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         eo.stream = st_;
         eo.profile = 0;
         eo.verbose = 0;
-        for (int i = 0; i < n; ++i) eng_.emplace_back(new Engine(*problems[i], eo));
+        for (int i = 0; i < n; ++i) {
+            eng_.emplace_back(new Engine(*problems[i], eo));
+            // the batch replays recorded residuals, which contract ovvv directly:
+            // the V+- packs of the unrecorded pair-form Z are not kept
+            eng_.back()->Vzp_.alloc(0);
+            eng_.back()->Vzm_.alloc(0);
+        }
         const int per = grouped_partials_per_part();
         CCSD_CUDA(cudaMalloc(&active_, sizeof(int) * n));
         CCSD_CUDA(cudaMalloc(&partials_, sizeof(double) * per * n));

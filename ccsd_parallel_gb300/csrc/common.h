@@ -191,6 +191,11 @@ void k_ladder_unpack_adj(int o, int v, const double *Rb, double *spb, double *sm
 // W+[tri(a,b)][tri(c,d)], W-[stri(a,b)][stri(c,d)] from W[a][b][c][d] = (ac|bd)
 void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st);
 void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaStream_t st);
+// V+[(k,a)][tri(c,d)] = (kd|ac) + (kc|ad) (c > d), (kc|ac) (c = d); V-[(k,a)][stri(c,d)] =
+// (kd|ac) - (kc|ad), from ovvv[k][d][a][c] = (kd|ac)
+void k_ovvv_pair_pack(int o, int v, const double *ovvv, double *vp, double *vm, cudaStream_t st);
+// Z[i][j][n] = Zs[tri(i,j)][n] + sgn(i-j) Za[stri(i,j)][n], n < o v (za may be null)
+void k_z_pair_unpack(int o, int v, const double *zs, const double *za, double *Z, cudaStream_t st);
 // CCSDT-1a triples (triples.cu), spin orbitals O = 2o, V = 2v:
 // <PQ||RS> blocks from the spatial ovov/ovoo/ovvv blocks; kind 0: vvvo [b][c][e][k],
 // 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c],

@@ -123,6 +123,8 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     taum_.alloc(Tmo * Tmv);
     Sp_.alloc(To * Tv);
     Sm_.alloc(Tmo * Tmv);
+    Zs_.alloc(To * o * v);
+    Za_.alloc(Tmo * o * v);
     t1_.alloc(nT1);
     t2_.alloc(nT2);
     t1n_.alloc(nT1);
@@ -465,9 +467,16 @@ void Engine::build_derived() {
     axpby((int)(o * o), (int)(v * v), -1.0,
           mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
           ovw(Lijab_.p, ix1(v * v), ix1(1)));
+    const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
+    // V+- of the pair-form Z, for the unrecorded residuals of DF inputs (the others
+    // contract ovvv directly); a recorded build leaves them as they are
+    if (!tape_ && df_input_) {
+        Vzp_.ensure((size_t)(o * v) * Tv);
+        Vzm_.ensure((size_t)(o * v) * Tmv);
+        k_ovvv_pair_pack((int)o, (int)v, ovvv_.p, Vzp_.p, Vzm_.p, st_);
+    }
     // W+ [tri(a,b)][tri(c,d)] and W- [stri(a,b)][stri(c,d)] of the pair-form ladder
     if (grad_lean_vvvv_) return;
-    const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
     Wp_.ensure(Tv * Tv);
     Wm_.ensure(Tmv * Tmv);
     w_sym_op(wv_.p, Wp_.p, Wm_.p);
@@ -824,10 +833,27 @@ void Engine::residual() {
         gemm((int)(o2 * v), iv, io, -1.0,
              mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
              1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
-    // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d]
-    gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
-         mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
-         ovw(Z_.p, ix1(ov), ix1(1)), -1, 12, "Rp_Z");
+    // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d].  With symmetric
+    // amplitudes Z takes the ladder's pair form (ladder_sym.cu): Zs = V+ tau+^T over i >= j,
+    // c >= d and Za = V- tau-^T over strict pairs, half of the plain 2 o^3 v^3, with tau+- and
+    // their splits (keys -3, -4) those of the ladder above; Z = unpack(Zs, Za).  The pair form
+    // is the plain one on tau symmetrised over its partners, so it is kept to DF inputs, whose
+    // (pq|rs) = (rs|pq) keeps the amplitudes symmetric also under a perturbed input (a dense
+    // input perturbed in one element does not, and its gradient is that of the plain form).
+    if (sym_amps && Vzp_.p) {
+        const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
+        gemm((int)ov, (int)To, (int)Tv, 1.0, mv(Vzp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
+             ovw(Zs_.p, ix1(1), ix1(ov)), 17, -3, "Rp_Z_sym");
+        const bool anti = Tmo > 0 && Tmv > 0;
+        if (anti)
+            gemm((int)ov, (int)Tmo, (int)Tmv, 1.0, mv(Vzm_.p, ix1(Tmv), ix1(1)), mv(taum_.p, ix1(Tmv), ix1(1)),
+                 0.0, ovw(Za_.p, ix1(1), ix1(ov)), 18, -4, "Rp_Z_anti");
+        k_z_pair_unpack(io, iv, Zs_.p, anti ? Za_.p : nullptr, Z_.p, st_);
+    } else {
+        gemm((int)o2, (int)ov, (int)v2, 1.0, mv(tau, ix1(v2), ix1(1)),
+             mv(ovvv_.p, ix2((uint32_t)v, v * v2, v), ix2((uint32_t)v, 1, v2)), 0.0,
+             ovw(Z_.p, ix1(ov), ix1(1)), -1, 12, "Rp_Z");
+    }
     if (r1_from_z) k_r1_from_z(io, iv, Z_.p, R1_.p, st_);
     if (merge_t1) {
         // S[i][j][a][k] = tmpB[k][i][a][j] + Z[i][j][k][a] + Vk[k][j][a][i]; Rp -= S t1

@@ -190,10 +190,12 @@ class Engine {
     // integral blocks (chemist): ovov[i][a][j][b], oovv[i][j][a][b], ovoo[i][a][j][k],
     // oooo[i][j][k][l], ovvv[i][a][b][c], Wv[a][b][c][d] = (ac|bd)
     DBuf ovov_, oovv_, ovoo_, oooo_, ovvv_, wv_;
-    // derived: L-combinations; W+ [tri(a,b)][tri(c,d)] and W- [stri][stri] of the ladder
-    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_, Wp_, Wm_;
-    // ladder pair forms per update: tau+-, S+- (S stored [ij pair][ab pair])
-    DBuf taup_, taum_, Sp_, Sm_;
+    // derived: L-combinations; W+ [tri(a,b)][tri(c,d)] and W- [stri][stri] of the ladder;
+    // V+ [(k,a)][tri(c,d)] and V- [(k,a)][stri(c,d)] of the pair-form Z (unrecorded DF builds)
+    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_, Wp_, Wm_, Vzp_, Vzm_;
+    // ladder pair forms per update: tau+-, S+- (S stored [ij pair][ab pair]); Zs, Za of the
+    // pair-form Z, stored [ij pair][(k,a)]
+    DBuf taup_, taum_, Sp_, Sm_, Zs_, Za_;
     // amplitudes and intermediates
     DBuf t1_, t2_, t1n_, t2n_, tau_, th1_, th2_;
     DBuf R1_, R_, Rp_;

@@ -298,6 +298,66 @@ __global__ void w_sym_adj_kernel(int v, const double *__restrict__ wpb, const do
     }
 }
 
+// Pair form of Z[i][j][k][a] = sum_cd (kd|ac) tau[i][j][c][d], the o^3 v^3 term of the
+// amplitude equations that goes with the ladder.  With V[(k,a)][c,d] = (kd|ac) and the
+// ladder's tau+- (the halves of tau symmetrised over its partners, above):
+//   Zs[tri(i,j)][(k,a)]  = sum_{c>=d} V+[(k,a)][tri(c,d)]  tau+[tri(i,j)][tri(c,d)]
+//   Za[stri(i,j)][(k,a)] = sum_{c>d}  V-[(k,a)][stri(c,d)] tau-[stri(i,j)][stri(c,d)]
+//   Z[i][j] = Zs + Za,  Z[j][i] = Zs - Za  (i > j),  Z[i][i] = Zs
+// with V+ = V[c,d] + V[d,c] (c > d), V[c,c] (c = d), and V- = V[c,d] - V[d,c]: the
+// plain form on the symmetrised tau, half of its 2 o^3 v^3 operations.
+//
+// V+- from ovvv[k][d][a][c] = (kd|ac), built once.  For one row (k,a) the v x v matrix
+// Y[d][c] = ovvv[k][d][a][c] has row stride v^2; a block takes one row and one 32 x 32
+// tile (C, D), C >= D, reads tile (D, C) along c into shared memory (the transposed
+// reads Y[d][c]) and tile (C, D) along d directly (Y[c][d]), and writes rows of
+// consecutive d.  Every Y element is read once.
+__global__ void __launch_bounds__(256) ovvv_pair_pack_kernel(int o, int v, const double *__restrict__ ovvv,
+                                                             double *__restrict__ vp, double *__restrict__ vm) {
+    __shared__ double s[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int nt = (v + 31) / 32;
+    const int64_t ntt = (int64_t)nt * (nt + 1) / 2, rows = (int64_t)o * v;
+    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2, v2 = (int64_t)v * v;
+    for (int64_t t = blockIdx.x; t < rows * ntt; t += gridDim.x) {
+        const int64_t r = t / ntt;
+        int C, D;
+        untri(t % ntt, C, D);
+        const int k = (int)(r / v), a = (int)(r % v);
+        const double *Y = ovvv + (int64_t)k * v * v2 + (int64_t)a * v;
+        for (int q = ty; q < 32; q += 8) {  // s[q][tx] = Y[d = D*32 + q][c = C*32 + tx]
+            const int d = D * 32 + q, c = C * 32 + tx;
+            s[q][tx] = (d < v && c < v) ? Y[(int64_t)d * v2 + c] : 0.0;
+        }
+        __syncthreads();
+        const int d = D * 32 + tx;
+        for (int q = ty; q < 32; q += 8) {
+            const int c = C * 32 + q;
+            if (c < v && d <= c) {
+                const double x = s[tx][q], y = Y[(int64_t)c * v2 + d];  // Y[d][c], Y[c][d]
+                vp[r * Tv + (int64_t)c * (c + 1) / 2 + d] = c > d ? x + y : x;
+                if (c > d) vm[r * Tmv + (int64_t)c * (c - 1) / 2 + d] = x - y;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Z[i][j][n] = Zs[tri][n] + sgn(i - j) Za[stri][n] for n < o v (za may be null when there
+// are no strict pairs on one side).  Blocks along y take rows (i, j), whose offsets are formed
+// once per row; the offsets within a row (n < 2^31) are 32-bit.
+__global__ void __launch_bounds__(256) z_pair_unpack_kernel(int o, int n, const double *__restrict__ zs,
+                                                            const double *__restrict__ za, double *__restrict__ Z) {
+    for (int row = blockIdx.y; row < o * o; row += gridDim.y) {
+        const int i = row / o, j = row % o, i1 = max(i, j), j1 = min(i, j);
+        const double *ps = zs + ((int64_t)i1 * (i1 + 1) / 2 + j1) * n;
+        const double *pa = (za && i != j) ? za + ((int64_t)i1 * (i1 - 1) / 2 + j1) * n : nullptr;
+        double *z = Z + (int64_t)row * n;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+            z[c] = pa ? (i > j ? ps[c] + pa[c] : ps[c] - pa[c]) : ps[c];
+    }
+}
+
 }  // namespace
 
 // every offset of an o^2 v^2 array and of the tau+ pair array below 2^31
@@ -356,6 +416,21 @@ void k_w_sym(int v, const double *W, double *wp, double *wm, cudaStream_t st) {
 
 void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaStream_t st) {
     w_sym_adj_kernel<<<blocks_for((size_t)v * v * v * v), 256, 0, st>>>(v, wpb, wmb, Wb);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_ovvv_pair_pack(int o, int v, const double *ovvv, double *vp, double *vm, cudaStream_t st) {
+    const int64_t nt = (v + 31) / 32, blocks = (int64_t)o * v * (nt * (nt + 1) / 2);
+    if (blocks == 0) return;
+    ovvv_pair_pack_kernel<<<(int)std::min<int64_t>(blocks, 152 * 8), 256, 0, st>>>(o, v, ovvv, vp, vm);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_z_pair_unpack(int o, int v, const double *zs, const double *za, double *Z, cudaStream_t st) {
+    const int n = o * v;
+    if (n == 0) return;
+    const dim3 grid((unsigned)std::min(4, (n + 255) / 256), (unsigned)std::min(o * o, 65535));
+    z_pair_unpack_kernel<<<grid, 256, 0, st>>>(o, n, zs, za, Z);
     CCSD_LAUNCH_CHECK();
 }
 
