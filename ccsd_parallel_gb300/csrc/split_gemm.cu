@@ -1259,6 +1259,8 @@ bool col_offsets_32(const OutView &C, int N) {
     return mx < (1LL << 31);
 }
 
+int num_sms();
+
 template <int S, int BN, int NSTF = 0, int MINB = 1>
 void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double alpha, double beta,
               const OutView &C, double *ws, size_t ws_elems, int *d_err, cudaStream_t st) {
@@ -1271,9 +1273,27 @@ void launch_t(const SplitOperand &A, const SplitOperand &B, int M, int N, double
     const int nkb = A.kpad / BK;
     const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
     const long tiles = (long)tiles_m * tiles_n;
-    // split K for parallelism (few tiles) and to keep the int32 level-0 sums bounded
+    // split K for parallelism when the tiles are fewer than the CTA slots (SMs x MINB), and to
+    // keep the int32 level-0 sums bounded.  From the fewest splits that fill every slot up to
+    // twice that, the count with the fewest waves per unit of work is taken (the smallest of
+    // equals): 114 tiles on 152 slots take 4 splits, three full waves, rather than 2, whose
+    // second wave is half empty.
     int splits = 1;
-    if (tiles < 148) splits = (int)std::min<long>((148 + tiles - 1) / tiles, std::max(1, nkb / 8));
+    const long slots = (long)num_sms() * MINB;
+    if (tiles < slots) {
+        const long kcap = std::max(1, nkb / 8);
+        const long s0 = std::min<long>((slots + tiles - 1) / tiles, kcap);
+        long best_s = s0;
+        double best = (double)((tiles * s0 + slots - 1) / slots) / (double)s0;
+        for (long s = s0 + 1; s <= std::min<long>(2 * s0, kcap); ++s) {
+            const double c = (double)((tiles * s + slots - 1) / slots) / (double)s;
+            if (c < best - 1e-12) {
+                best = c;
+                best_s = s;
+            }
+        }
+        splits = (int)best_s;
+    }
     splits = std::max(splits, (nkb + kMaxKbPerSplit - 1) / kMaxKbPerSplit);
     while (splits > 1 && (size_t)splits * M * N > ws_elems) --splits;
     if ((nkb + splits - 1) / splits > kMaxKbPerSplit)
