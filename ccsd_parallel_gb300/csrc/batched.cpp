@@ -99,9 +99,11 @@ Batch::Batch(const ccsd_problem *const *problems, int n, const ccsd_options &opt
         for (int i = 0; i < n; ++i) {
             eng_.emplace_back(new Engine(*problems[i], eo));
             // the batch replays recorded residuals, which contract ovvv directly:
-            // the V+- packs of the unrecorded pair-form Z are not kept
+            // the V+- and U+- packs of the unrecorded pair forms are not kept
             eng_.back()->Vzp_.alloc(0);
             eng_.back()->Vzm_.alloc(0);
+            eng_.back()->Uxp_.alloc(0);
+            eng_.back()->Uxm_.alloc(0);
         }
         const int per = grouped_partials_per_part();
         CCSD_CUDA(cudaMalloc(&active_, sizeof(int) * n));

@@ -196,6 +196,14 @@ void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaSt
 void k_ovvv_pair_pack(int o, int v, const double *ovvv, double *vp, double *vm, cudaStream_t st);
 // Z[i][j][n] = Zs[tri(i,j)][n] + sgn(i-j) Za[stri(i,j)][n], n < o v (za may be null)
 void k_z_pair_unpack(int o, int v, const double *zs, const double *za, double *Z, cudaStream_t st);
+// U+[(k,l)][tri(c,d)] = (kc|ld) + (kd|lc) (c > d), (kc|lc) (c = d); U-[(k,l)][stri(c,d)] =
+// (kc|ld) - (kd|lc), from ovov[k][c][l][d] = (kc|ld)
+void k_ovov_pair_pack(int o, int v, const double *ovov, double *up, double *um, cudaStream_t st);
+// X[r][i][j] = Xs[r][tri(i,j)] + sgn(i-j) Xa[r][stri(i,j)], r < o^2 (xa may be null)
+void k_x_pair_unpack(int o, const double *xs, const double *xa, double *X, cudaStream_t st);
+// W+[tri(i,j)][tri(k,l)] = W[kl,ij] + W[lk,ij] (k > l), W[kk,ij]; W-[stri(i,j)][stri(k,l)] =
+// W[kl,ij] - W[lk,ij], from W[k][l][i][j]
+void k_oooo_pair_pack(int o, const double *W, double *wp, double *wm, cudaStream_t st);
 // CCSDT-1a triples (triples.cu), spin orbitals O = 2o, V = 2v:
 // <PQ||RS> blocks from the spatial ovov/ovoo/ovvv blocks; kind 0: vvvo [b][c][e][k],
 // 1: ovoo [m][c][j][k], 2: oovv [j][k][b][c], 3: vovv [b][k][c][d], 4: ooov [k][m][j][c],

@@ -125,6 +125,10 @@ Engine::Engine(const ccsd_problem &prob, const ccsd_options &opts) {
     Sm_.alloc(Tmo * Tmv);
     Zs_.alloc(To * o * v);
     Za_.alloc(Tmo * o * v);
+    Xs_.alloc(o * o * To);
+    Xa_.alloc(o * o * Tmo);
+    Whp_.alloc(To * To);
+    Whm_.alloc(Tmo * Tmo);
     t1_.alloc(nT1);
     t2_.alloc(nT2);
     t1n_.alloc(nT1);
@@ -468,12 +472,15 @@ void Engine::build_derived() {
           mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, 1, o * v)), 1.0,
           ovw(Lijab_.p, ix1(v * v), ix1(1)));
     const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
-    // V+- of the pair-form Z, for the unrecorded residuals of DF inputs (the others
-    // contract ovvv directly); a recorded build leaves them as they are
+    // V+- and U+- of the pair-form Z and X, for the unrecorded residuals of DF inputs (the
+    // others contract ovvv and ovov directly); a recorded build leaves them as they are
     if (!tape_ && df_input_) {
         Vzp_.ensure((size_t)(o * v) * Tv);
         Vzm_.ensure((size_t)(o * v) * Tmv);
         k_ovvv_pair_pack((int)o, (int)v, ovvv_.p, Vzp_.p, Vzm_.p, st_);
+        Uxp_.ensure((size_t)(o * o) * Tv);
+        Uxm_.ensure((size_t)(o * o) * Tmv);
+        k_ovov_pair_pack((int)o, (int)v, ovov_.p, Uxp_.p, Uxm_.p, st_);
     }
     // W+ [tri(a,b)][tri(c,d)] and W- [stri(a,b)][stri(c,d)] of the pair-form ladder
     if (grad_lean_vvvv_) return;
@@ -619,12 +626,32 @@ void Engine::residual() {
     // o^4 product X[k][l][i][j] = sum_cd (kc|ld) tau[i,j,c,d] that Woooo needs anyway, so X is
     // formed here (site Woooo_tau) and the o x o x o v^2 contraction is not run.
     const bool sym_amps = tape_ == nullptr && df_input_;
+    // With symmetric amplitudes the contractions over a (c,d) or (k,l) pair of tau (X here,
+    // the two ladders and Z below) run in pair form on the ladder's tau+- (ladder_sym.cu),
+    // formed once here, and their splits (keys -3, -4) are shared.  The pair forms are the
+    // plain ones on tau symmetrised over its partners, so they are kept to DF inputs, whose
+    // (pq|rs) = (rs|pq) keeps the amplitudes symmetric also under a perturbed input (a dense
+    // input perturbed in one element does not, and its gradient is that of the plain forms).
+    const bool pairs = sym_amps && Vzp_.p && Uxp_.p;
+    const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
+    const bool anti = Tmo > 0 && Tmv > 0;
+    if (pairs) tau_sym_op(tau, taup_.p, taum_.p);
     copy(Foo_.p, f_oo_off_.p, (size_t)(o2));
     if (sym_amps) {
         Xoooo_.ensure((size_t)o2 * o2);
-        gemm((int)o2, (int)o2, (int)v2, 1.0,
-             mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
-             mv(tau, ix1(v2), ix1(1)), 0.0, ovw(Xoooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
+        if (pairs) {
+            // Xs = U+ tau+^T, Xa = U- tau-^T, X = unpack(Xs, Xa): half of the plain 2 o^4 v^2
+            gemm((int)o2, (int)To, (int)Tv, 1.0, mv(Uxp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
+                 ovw(Xs_.p, ix1(To), ix1(1)), 19, -3, "Woooo_tau_sym");
+            if (anti)
+                gemm((int)o2, (int)Tmo, (int)Tmv, 1.0, mv(Uxm_.p, ix1(Tmv), ix1(1)), mv(taum_.p, ix1(Tmv), ix1(1)),
+                     0.0, ovw(Xa_.p, ix1(Tmo), ix1(1)), 20, -4, "Woooo_tau_anti");
+            k_x_pair_unpack(io, Xs_.p, anti ? Xa_.p : nullptr, Xoooo_.p, st_);
+        } else {
+            gemm((int)o2, (int)o2, (int)v2, 1.0,
+                 mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)),
+                 mv(tau, ix1(v2), ix1(1)), 0.0, ovw(Xoooo_.p, ix1(o2), ix1(1)), 5, -1, "Woooo_tau");
+        }
         k_foo_from_x(io, Xoooo_.p, Foo_.p, st_);
     } else {
         gemm(io, io, (int)(o * v2), 1.0, mv(Lovov_.p, ix1(v * o * v), ix3((uint32_t)v, (uint32_t)v, v, o * v, 1)),
@@ -792,19 +819,30 @@ void Engine::residual() {
     axpby((int)o2, (int)v2, 1.0,
                mv(ovov_.p, ix2((uint32_t)o, v * o * v, v), ix2((uint32_t)v, o * v, 1)), 0.0,
                ovw(R_.p, ix1(v2), ix1(1)));
-    // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b]
-    gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
-         1.0, ovw(R_.p, ix1(v2), ix1(1)), 0, 0, "hh_ladder");
+    // + sum_kl Woooo[k,l,i,j] tau[k,l,a,b] (in the ladder's halves below with the pair forms)
+    if (!pairs)
+        gemm((int)o2, (int)v2, (int)o2, 1.0, mv(Woooo_.p, ix1(1), ix1(o2)), mv(tau, ix1(1), ix1(v2)),
+             1.0, ovw(R_.p, ix1(v2), ix1(1)), 0, 0, "hh_ladder");
     // + sum_cd (ac|bd) tau[i,j,c,d]: the v^4 particle-particle ladder in pair form
     // (ladder_sym.cu): S+ = W+ tau+^T over (a>=b, i>=j, c>=d), S- = W- tau-^T over strict
     // pairs, a quarter of the plain 2 o^2 v^4; R += unpack(S+, S-).  S is stored [ij][ab].
     {
-        const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
-        tau_sym_op(tau, taup_.p, taum_.p);
+        if (!pairs) tau_sym_op(tau, taup_.p, taum_.p);
         gemm((int)Tv, (int)To, (int)Tv, 1.0, mv(Wp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
              ovw(Sp_.p, ix1(1), ix1(Tv)), 10, -3, "pp_ladder_sym");
         gemm((int)Tmv, (int)Tmo, (int)Tmv, 1.0, mv(Wm_.p, ix1(Tmv), ix1(1)), mv(taum_.p, ix1(Tmv), ix1(1)), 0.0,
              ovw(Sm_.p, ix1(1), ix1(Tmv)), 11, -4, "pp_ladder_anti");
+        if (pairs) {
+            // the hh ladder in the same halves: S+ += W+ tau+ and S- += W- tau- over (k,l)
+            // pairs, with W+- the (k,l) packs of Woooo[.,ij] and tau+- read as [ab pair][kl
+            // pair] (keys -8, -9): a quarter of the plain 2 o^4 v^2, and no pass of its own over R
+            k_oooo_pair_pack(io, Woooo_.p, Whp_.p, Whm_.p, st_);
+            gemm((int)To, (int)Tv, (int)To, 1.0, mv(Whp_.p, ix1(To), ix1(1)), mv(taup_.p, ix1(1), ix1(Tv)), 1.0,
+                 ovw(Sp_.p, ix1(Tv), ix1(1)), 0, -8, "hh_ladder_sym");
+            if (anti)
+                gemm((int)Tmo, (int)Tmv, (int)Tmo, 1.0, mv(Whm_.p, ix1(Tmo), ix1(1)), mv(taum_.p, ix1(1), ix1(Tmv)),
+                     1.0, ovw(Sm_.p, ix1(Tmv), ix1(1)), 0, -9, "hh_ladder_anti");
+        }
         unpack_op(Sp_.p, Sm_.p, R_.p);
     }
 
@@ -833,18 +871,12 @@ void Engine::residual() {
         gemm((int)(o2 * v), iv, io, -1.0,
              mv(tmpB_.p, ix3((uint32_t)o, (uint32_t)v, v * o, 1, o), ix1(o2 * v)), mv(t1, ix1(1), ix1(v)),
              1.0, ovw(Rp_.p, ix1(v), ix1(1)), 0, 0, "Rp_tmpB_t1");
-    // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d].  With symmetric
-    // amplitudes Z takes the ladder's pair form (ladder_sym.cu): Zs = V+ tau+^T over i >= j,
-    // c >= d and Za = V- tau-^T over strict pairs, half of the plain 2 o^3 v^3, with tau+- and
-    // their splits (keys -3, -4) those of the ladder above; Z = unpack(Zs, Za).  The pair form
-    // is the plain one on tau symmetrised over its partners, so it is kept to DF inputs, whose
-    // (pq|rs) = (rs|pq) keeps the amplitudes symmetric also under a perturbed input (a dense
-    // input perturbed in one element does not, and its gradient is that of the plain form).
-    if (sym_amps && Vzp_.p) {
-        const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
+    // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d].  In pair form
+    // (see the top of this function): Zs = V+ tau+^T over i >= j, c >= d and Za = V- tau-^T
+    // over strict pairs, half of the plain 2 o^3 v^3; Z = unpack(Zs, Za).
+    if (pairs) {
         gemm((int)ov, (int)To, (int)Tv, 1.0, mv(Vzp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
              ovw(Zs_.p, ix1(1), ix1(ov)), 17, -3, "Rp_Z_sym");
-        const bool anti = Tmo > 0 && Tmv > 0;
         if (anti)
             gemm((int)ov, (int)Tmo, (int)Tmv, 1.0, mv(Vzm_.p, ix1(Tmv), ix1(1)), mv(taum_.p, ix1(Tmv), ix1(1)),
                  0.0, ovw(Za_.p, ix1(1), ix1(ov)), 18, -4, "Rp_Z_anti");

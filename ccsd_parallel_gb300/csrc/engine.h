@@ -191,11 +191,13 @@ class Engine {
     // oooo[i][j][k][l], ovvv[i][a][b][c], Wv[a][b][c][d] = (ac|bd)
     DBuf ovov_, oovv_, ovoo_, oooo_, ovvv_, wv_;
     // derived: L-combinations; W+ [tri(a,b)][tri(c,d)] and W- [stri][stri] of the ladder;
-    // V+ [(k,a)][tri(c,d)] and V- [(k,a)][stri(c,d)] of the pair-form Z (unrecorded DF builds)
-    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_, Wp_, Wm_, Vzp_, Vzm_;
+    // V+ [(k,a)][tri(c,d)] and V- [(k,a)][stri(c,d)] of the pair-form Z, U+ [(k,l)][tri(c,d)]
+    // and U- [(k,l)][stri(c,d)] of the pair-form X (unrecorded DF builds)
+    DBuf Lovov_, Lovoo_, Lovvv_, LT1_, Lijab_, Wp_, Wm_, Vzp_, Vzm_, Uxp_, Uxm_;
     // ladder pair forms per update: tau+-, S+- (S stored [ij pair][ab pair]); Zs, Za of the
-    // pair-form Z, stored [ij pair][(k,a)]
-    DBuf taup_, taum_, Sp_, Sm_, Zs_, Za_;
+    // pair-form Z, stored [ij pair][(k,a)]; Xs, Xa of the pair-form X, stored [(k,l)][ij pair];
+    // W+- [ij pair][kl pair] of the pair-form hh ladder
+    DBuf taup_, taum_, Sp_, Sm_, Zs_, Za_, Xs_, Xa_, Whp_, Whm_;
     // amplitudes and intermediates
     DBuf t1_, t2_, t1n_, t2n_, tau_, th1_, th2_;
     DBuf R1_, R_, Rp_;

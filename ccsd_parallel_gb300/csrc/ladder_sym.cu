@@ -298,48 +298,92 @@ __global__ void w_sym_adj_kernel(int v, const double *__restrict__ wpb, const do
     }
 }
 
-// Pair form of Z[i][j][k][a] = sum_cd (kd|ac) tau[i][j][c][d], the o^3 v^3 term of the
-// amplitude equations that goes with the ladder.  With V[(k,a)][c,d] = (kd|ac) and the
+// The same pair form for the other contractions over a (c,d) or (k,l) pair of tau, with the
 // ladder's tau+- (the halves of tau symmetrised over its partners, above):
-//   Zs[tri(i,j)][(k,a)]  = sum_{c>=d} V+[(k,a)][tri(c,d)]  tau+[tri(i,j)][tri(c,d)]
-//   Za[stri(i,j)][(k,a)] = sum_{c>d}  V-[(k,a)][stri(c,d)] tau-[stri(i,j)][stri(c,d)]
-//   Z[i][j] = Zs + Za,  Z[j][i] = Zs - Za  (i > j),  Z[i][i] = Zs
-// with V+ = V[c,d] + V[d,c] (c > d), V[c,c] (c = d), and V- = V[c,d] - V[d,c]: the
-// plain form on the symmetrised tau, half of its 2 o^3 v^3 operations.
+// - Z[i][j][k][a] = sum_cd (kd|ac) tau[ij,cd] (o^3 v^3) and X[k][l][i][j] = sum_cd (kc|ld)
+//   tau[ij,cd] (o^4 v^2).  With V[r][c,d] the integral row r = (k,a) or (k,l):
+//     Ps[tri(i,j)][r]  = sum_{c>=d} V+[r][tri(c,d)]  tau+[tri(i,j)][tri(c,d)]
+//     Pa[stri(i,j)][r] = sum_{c>d}  V-[r][stri(c,d)] tau-[stri(i,j)][stri(c,d)]
+//     P[i][j] = Ps + Pa,  P[j][i] = Ps - Pa  (i > j),  P[i][i] = Ps
+//   with V+ = V[c,d] + V[d,c] (c > d), V[c,c] (c = d), V- = V[c,d] - V[d,c]: the plain
+//   form on the symmetrised tau, half of its operations.
+// - the hh ladder S[ij,ab] = sum_kl W[kl,ij] tau[kl,ab] adds to the pp ladder's halves:
+//     S+[tri(i,j)][tri(a,b)]   += sum_{k>=l} W+[tri(i,j)][tri(k,l)]   tau+[tri(k,l)][tri(a,b)]
+//     S-[stri(i,j)][stri(a,b)] += sum_{k>l}  W-[stri(i,j)][stri(k,l)] tau-[stri(k,l)][stri(a,b)]
+//   with W+- the (k,l) packs of W[.,ij] as above (tau+- of symmetric amplitudes are also
+//   the (k,l)-symmetric and -antisymmetric halves of tau[kl,ab]), a quarter of 2 o^4 v^2.
 //
-// V+- from ovvv[k][d][a][c] = (kd|ac), built once.  For one row (k,a) the v x v matrix
-// Y[d][c] = ovvv[k][d][a][c] has row stride v^2; a block takes one row and one 32 x 32
-// tile (C, D), C >= D, reads tile (D, C) along c into shared memory (the transposed
-// reads Y[d][c]) and tile (C, D) along d directly (Y[c][d]), and writes rows of
-// consecutive d.  Every Y element is read once.
-__global__ void __launch_bounds__(256) ovvv_pair_pack_kernel(int o, int v, const double *__restrict__ ovvv,
-                                                             double *__restrict__ vp, double *__restrict__ vm) {
+// Row packs of V[r][c,d] for r < rows: V+[r][tri(c,d)] = V[c,d] + V[d,c] (c > d), V[c,c]
+// (c = d); V-[r][stri(c,d)] = V[c,d] - V[d,c].  Row r = (r1, r2), r2 < n2, starts at
+// r1 s1 + r2 s2 of a matrix Y[p][q] = base[p sp + q]; V[c,d] = Y[d][c] when yt is set
+// (ovvv[k][d][a][c] = (kd|ac) for Z), else Y[c][d] (ovov[k][c][l][d] = (kc|ld) for X).
+// Built once.  A block takes one row and one 32 x 32 tile (C, D), C >= D, reads tile
+// (D, C) along q into shared memory (the transposed reads Y[d][c]) and tile (C, D) along
+// d directly (Y[c][d]), and writes rows of consecutive d.  Every Y element is read once.
+__global__ void __launch_bounds__(256) row_pair_pack_kernel(int64_t rows, int n2, int64_t s1, int64_t s2, int64_t sp,
+                                                            int v, int yt, const double *__restrict__ base,
+                                                            double *__restrict__ vp, double *__restrict__ vm) {
     __shared__ double s[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int nt = (v + 31) / 32;
-    const int64_t ntt = (int64_t)nt * (nt + 1) / 2, rows = (int64_t)o * v;
-    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2, v2 = (int64_t)v * v;
+    const int64_t ntt = (int64_t)nt * (nt + 1) / 2;
+    const int64_t Tv = (int64_t)v * (v + 1) / 2, Tmv = (int64_t)v * (v - 1) / 2;
     for (int64_t t = blockIdx.x; t < rows * ntt; t += gridDim.x) {
         const int64_t r = t / ntt;
         int C, D;
         untri(t % ntt, C, D);
-        const int k = (int)(r / v), a = (int)(r % v);
-        const double *Y = ovvv + (int64_t)k * v * v2 + (int64_t)a * v;
+        const double *Y = base + (r / n2) * s1 + (r % n2) * s2;
         for (int q = ty; q < 32; q += 8) {  // s[q][tx] = Y[d = D*32 + q][c = C*32 + tx]
             const int d = D * 32 + q, c = C * 32 + tx;
-            s[q][tx] = (d < v && c < v) ? Y[(int64_t)d * v2 + c] : 0.0;
+            s[q][tx] = (d < v && c < v) ? Y[(int64_t)d * sp + c] : 0.0;
         }
         __syncthreads();
         const int d = D * 32 + tx;
         for (int q = ty; q < 32; q += 8) {
             const int c = C * 32 + q;
             if (c < v && d <= c) {
-                const double x = s[tx][q], y = Y[(int64_t)c * v2 + d];  // Y[d][c], Y[c][d]
+                const double ydc = s[tx][q], ycd = Y[(int64_t)c * sp + d];
+                const double x = yt ? ydc : ycd, y = yt ? ycd : ydc;  // V[c,d], V[d,c]
                 vp[r * Tv + (int64_t)c * (c + 1) / 2 + d] = c > d ? x + y : x;
                 if (c > d) vm[r * Tmv + (int64_t)c * (c - 1) / 2 + d] = x - y;
             }
         }
         __syncthreads();
+    }
+}
+
+// X[r][i][j] = Xs[r][tri(i,j)] + sgn(i - j) Xa[r][stri(i,j)] for r < o^2 (the pair index
+// inner: the pair-form X of the o^4 product); xa may be null (no strict pairs)
+__global__ void __launch_bounds__(256) x_pair_unpack_kernel(int o, const double *__restrict__ xs,
+                                                            const double *__restrict__ xa, double *__restrict__ X) {
+    const int64_t To = (int64_t)o * (o + 1) / 2, Tmo = (int64_t)o * (o - 1) / 2, n = (int64_t)o * o * o * o;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e % o), i = (int)((e / o) % o);
+        const int64_t r = e / ((int64_t)o * o);
+        const int i1 = max(i, j), j1 = min(i, j);
+        double x = xs[r * To + (int64_t)i1 * (i1 + 1) / 2 + j1];
+        if (xa && i != j) {
+            const double a = xa[r * Tmo + (int64_t)i1 * (i1 - 1) / 2 + j1];
+            x = i > j ? x + a : x - a;
+        }
+        X[e] = x;
+    }
+}
+
+// Pair packs of the hh-ladder intermediate W[k][l][i][j] over (k, l) for the rows i >= j:
+// wp[tri(i,j)][tri(k,l)] = W[kl,ij] + W[lk,ij] (k > l), W[kk,ij]; wm[stri(i,j)][stri(k,l)] =
+// W[kl,ij] - W[lk,ij] (i > j, k > l).  One thread per wp element.
+__global__ void __launch_bounds__(256) oooo_pair_pack_kernel(int o, const double *__restrict__ W,
+                                                             double *__restrict__ wp, double *__restrict__ wm) {
+    const int64_t To = (int64_t)o * (o + 1) / 2, Tmo = (int64_t)o * (o - 1) / 2, o2 = (int64_t)o * o;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < To * To; e += (int64_t)gridDim.x * blockDim.x) {
+        int i, j, k, l;
+        untri(e / To, i, j);
+        untri(e % To, k, l);
+        const double x = W[((int64_t)k * o + l) * o2 + (int64_t)i * o + j];
+        const double y = W[((int64_t)l * o + k) * o2 + (int64_t)i * o + j];
+        wp[e] = k > l ? x + y : x;
+        if (i > j && k > l) wm[stri(i, j) * Tmo + stri(k, l)] = x - y;
     }
 }
 
@@ -419,10 +463,38 @@ void k_w_sym_adj(int v, const double *wpb, const double *wmb, double *Wb, cudaSt
     CCSD_LAUNCH_CHECK();
 }
 
-void k_ovvv_pair_pack(int o, int v, const double *ovvv, double *vp, double *vm, cudaStream_t st) {
-    const int64_t nt = (v + 31) / 32, blocks = (int64_t)o * v * (nt * (nt + 1) / 2);
+static void row_pair_pack(int64_t rows, int n2, int64_t s1, int64_t s2, int64_t sp, int v, int yt,
+                          const double *base, double *vp, double *vm, cudaStream_t st) {
+    const int64_t nt = (v + 31) / 32, blocks = rows * (nt * (nt + 1) / 2);
     if (blocks == 0) return;
-    ovvv_pair_pack_kernel<<<(int)std::min<int64_t>(blocks, 152 * 8), 256, 0, st>>>(o, v, ovvv, vp, vm);
+    row_pair_pack_kernel<<<(int)std::min<int64_t>(blocks, 152 * 8), 256, 0, st>>>(rows, n2, s1, s2, sp, v, yt, base,
+                                                                                 vp, vm);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_ovvv_pair_pack(int o, int v, const double *ovvv, double *vp, double *vm, cudaStream_t st) {
+    // row (k, a) of Y[d][c] = ovvv[k][d][a][c]: k v^3 + a v, Y row stride v^2; V[c,d] = Y[d][c]
+    const int64_t v2 = (int64_t)v * v;
+    row_pair_pack((int64_t)o * v, v, v * v2, v, v2, v, 1, ovvv, vp, vm, st);
+}
+
+void k_ovov_pair_pack(int o, int v, const double *ovov, double *up, double *um, cudaStream_t st) {
+    // row (k, l) of Y[c][d] = ovov[k][c][l][d]: k v o v + l v, Y row stride o v; U[c,d] = Y[c][d]
+    const int64_t ov = (int64_t)o * v;
+    row_pair_pack((int64_t)o * o, o, v * ov, v, ov, v, 0, ovov, up, um, st);
+}
+
+void k_x_pair_unpack(int o, const double *xs, const double *xa, double *X, cudaStream_t st) {
+    const int64_t n = (int64_t)o * o * o * o;
+    if (n == 0) return;
+    x_pair_unpack_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 8), 256, 0, st>>>(o, xs, xa, X);
+    CCSD_LAUNCH_CHECK();
+}
+
+void k_oooo_pair_pack(int o, const double *W, double *wp, double *wm, cudaStream_t st) {
+    const int64_t To = (int64_t)o * (o + 1) / 2;
+    if (To == 0) return;
+    oooo_pair_pack_kernel<<<(int)std::min<int64_t>((To * To + 255) / 256, 152 * 8), 256, 0, st>>>(o, W, wp, wm);
     CCSD_LAUNCH_CHECK();
 }
 
