@@ -473,11 +473,25 @@ void Engine::build_derived() {
           ovw(Lijab_.p, ix1(v * v), ix1(1)));
     const size_t Tv = (size_t)(v * (v + 1) / 2), Tmv = (size_t)(v * (v - 1) / 2);
     // V+- and U+- of the pair-form Z and X, for the unrecorded residuals of DF inputs (the
-    // others contract ovvv and ovov directly); a recorded build leaves them as they are
+    // others contract ovvv and ovov directly); a recorded build leaves them as they are.
+    // V+- hold about as much as ovvv, and their split planes up to as much again, so they are
+    // built only when the device keeps room for them next to what is still to come (W+- and
+    // their planes, the per-update tensors and DIIS vectors, 2 GiB spare); a system near the
+    // device's capacity contracts ovvv directly for Z, as before.
     if (!tape_ && df_input_) {
-        Vzp_.ensure((size_t)(o * v) * Tv);
-        Vzm_.ensure((size_t)(o * v) * Tmv);
-        k_ovvv_pair_pack((int)o, (int)v, ovvv_.p, Vzp_.p, Vzm_.p, st_);
+        const double vbytes = 8.0 * (double)(o * v) * (double)(Tv + Tmv);
+        const double need = 2.0 * vbytes + 16.0 * ((double)Tv * Tv + (double)Tmv * Tmv) +
+                            192.0 * (double)(o * o) * (double)(v * v) + 2.0 * (1 << 30);
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && (double)free_b > need) {
+            Vzp_.ensure((size_t)(o * v) * Tv);
+            Vzm_.ensure((size_t)(o * v) * Tmv);
+            k_ovvv_pair_pack((int)o, (int)v, ovvv_.p, Vzp_.p, Vzm_.p, st_);
+        } else {
+            cudaGetLastError();
+            Vzp_.alloc(0);
+            Vzm_.alloc(0);
+        }
         Uxp_.ensure((size_t)(o * o) * Tv);
         Uxm_.ensure((size_t)(o * o) * Tmv);
         k_ovov_pair_pack((int)o, (int)v, ovov_.p, Uxp_.p, Uxm_.p, st_);
@@ -632,7 +646,7 @@ void Engine::residual() {
     // plain ones on tau symmetrised over its partners, so they are kept to DF inputs, whose
     // (pq|rs) = (rs|pq) keeps the amplitudes symmetric also under a perturbed input (a dense
     // input perturbed in one element does not, and its gradient is that of the plain forms).
-    const bool pairs = sym_amps && Vzp_.p && Uxp_.p;
+    const bool pairs = sym_amps && Uxp_.p, zpairs = pairs && Vzp_.p;
     const int64_t To = o * (o + 1) / 2, Tmo = o * (o - 1) / 2, Tv = v * (v + 1) / 2, Tmv = v * (v - 1) / 2;
     const bool anti = Tmo > 0 && Tmv > 0;
     if (pairs) tau_sym_op(tau, taup_.p, taum_.p);
@@ -874,7 +888,7 @@ void Engine::residual() {
     // - sum_k Z[i,j,k,a] t1[k,b], Z[i][j][k][a] = sum_cd (kd|ac) tau[i,j,c,d].  In pair form
     // (see the top of this function): Zs = V+ tau+^T over i >= j, c >= d and Za = V- tau-^T
     // over strict pairs, half of the plain 2 o^3 v^3; Z = unpack(Zs, Za).
-    if (pairs) {
+    if (zpairs) {
         gemm((int)ov, (int)To, (int)Tv, 1.0, mv(Vzp_.p, ix1(Tv), ix1(1)), mv(taup_.p, ix1(Tv), ix1(1)), 0.0,
              ovw(Zs_.p, ix1(1), ix1(ov)), 17, -3, "Rp_Z_sym");
         if (anti)
