@@ -638,7 +638,8 @@ void Engine::residual() {
     // Foo[k][i] = f_oo' + sum_{lcd} Lovov[k,c,l,d] tau[i,l,c,d].  With symmetric amplitudes
     // (DF input, no tape: see r1_from_z below) it is sum_l (2 X[k,l,i,l] - X[k,l,l,i]) of the
     // o^4 product X[k][l][i][j] = sum_cd (kc|ld) tau[i,j,c,d] that Woooo needs anyway, so X is
-    // formed here (site Woooo_tau) and the o x o x o v^2 contraction is not run.
+    // formed here (site Woooo_tau, in pair form Woooo_tau_sym/_anti) and the o x o x o v^2
+    // contraction is not run.
     const bool sym_amps = tape_ == nullptr && df_input_;
     // With symmetric amplitudes the contractions over a (c,d) or (k,l) pair of tau (X here,
     // the two ladders and Z below) run in pair form on the ladder's tau+- (ladder_sym.cu),
