@@ -13,11 +13,14 @@ host's BLAS:
 * every step is one whole update -- residual, denominators, DIIS extrapolation
   and energy -- with no term sampled or skipped;
 * every o^3 v^3 and o^2 v^4 term is a matrix product on numpy's BLAS, all host
-  threads; the particle-particle ladder runs in the same pair form as the GPU
-  engine (S+ = tau+ W+^T over c >= d, S- = tau- W-^T over c > d: a quarter of
-  2 o^2 v^4), on W+/W- built once from the DF factors;
-* the integral blocks and W+/W- are built once, outside the timed steps, as the
-  GPU engine builds them in ccsd_create.
+  threads; the contractions over a (c,d) or (k,l) pair of tau run in the same
+  pair forms as the GPU engine with DF inputs, on tau+/tau- formed once per
+  update: the particle-particle ladder (S+ = tau+ W+^T over c >= d, S- =
+  tau- W-^T over c > d: a quarter of 2 o^2 v^4) with the hh ladder added to its
+  halves, Z[i][j][k][a] = sum_cd (kd|ac) tau[ijcd] and X[k][l][i][j] =
+  sum_cd (kc|ld) tau[ijcd] (half of their plain products);
+* the integral blocks, W+/W- and the V+/V- and U+/U- packs of Z and X are built
+  once, outside the timed steps, as the GPU engine builds them in ccsd_create.
 
 ``residual`` equals ``RHFCCSD.residual`` to rounding (tests/test_oracle.py).
 """
@@ -121,10 +124,31 @@ class FullUpdate:
             return tri, stri, sgn
         self._otri_map, self._ostr_map, self._osgn = maps(o)
         self._vtri_map, self._vstr_map, self._vsgn = maps(v)
+        # V+-[(k,a), cd pair] of Z (V[c,d] = (kd|ac)) and U+-[(k,l), cd pair] of X (U[c,d] = (kc|ld))
+        self.Vzp, self.Vzm = self._row_packs(self.ovvvZ.reshape(o * v, v, v))
+        self.Uxp, self.Uxm = self._row_packs(self.ovovT.reshape(o * o, v, v))
 
-    def ladder(self, tau):
-        """sum_cd (ac|bd) tau[i,j,c,d] through the pair forms."""
-        o, v = self.o, self.v
+    @staticmethod
+    def _row_packs(M, chunk: int = 256):
+        """P+[r, tri(c,d)] = M[r,c,d] + M[r,d,c] (c > d), M[r,c,c] (c = d); P-[r, stri(c,d)] =
+        M[r,c,d] - M[r,d,c]; rows a chunk at a time."""
+        n, v = M.shape[0], M.shape[1]
+        tc, td = np.tril_indices(v)
+        sc, sd = np.tril_indices(v, -1)
+        diag = tc == td
+        P = np.empty((n, tc.size))
+        Q = np.empty((n, sc.size))
+        for r0 in range(0, n, chunk):
+            m = M[r0:r0 + chunk]
+            mt = m.transpose(0, 2, 1)
+            p = (m + mt)[:, tc, td]
+            p[:, diag] *= 0.5
+            P[r0:r0 + chunk] = p
+            Q[r0:r0 + chunk] = (m - mt)[:, sc, sd]
+        return P, Q
+
+    def _tau_pairs(self, tau):
+        """tau+[ij pair, cd pair], tau-[strict ij pair, strict cd pair] over the four partners."""
         tsw = tau.transpose(0, 1, 3, 2)
         tji = tau.transpose(1, 0, 3, 2)
         oi, oj = self._otri
@@ -134,10 +158,29 @@ class FullUpdate:
         c_, d_ = tji[oi, oj], tji.transpose(0, 1, 3, 2)[oi, oj]  # tau[jidc], tau[jicd]
         taup = (0.25 * (a + b + c_ + d_))[:, tc, td]
         taum = (0.25 * (a - b + c_ - d_))[self._ostr_in_tri][:, sc, sd]   # strict pairs i > j
-        Sp = taup @ self.Wp.T                              # [ij pair, ab pair]
+        return taup, taum
+
+    def _unpack_pairs(self, Ps, Pa):
+        """P[(i,j), r] = Ps[tri(i,j), r] + sgn(i-j) Pa[stri(i,j), r]."""
+        P = Ps[self._otri_map.ravel()]
+        if Pa.size:
+            P += self._osgn.ravel()[:, None] * Pa[self._ostr_map.ravel()]
+        return P
+
+    def ladder(self, taup, taum, Woooo):
+        """sum_cd (ac|bd) tau[i,j,c,d] + sum_kl Woooo[k,l,i,j] tau[k,l,a,b] through the pair forms:
+        the hh ladder adds W+ tau+ and W- tau- (W+- the (k,l) packs of Woooo[., ., i, j]) to the
+        halves S+- before their one unpack."""
+        o, v = self.o, self.v
+        oi, oj = self._otri
+        si, sj = self._ostr
+        Wt = Woooo.transpose(2, 3, 0, 1)                   # [i, j, k, l]
+        Whp = self._row_packs(np.ascontiguousarray(Wt[oi, oj]))[0]
+        Sp = taup @ self.Wp.T + Whp @ taup                 # [ij pair, ab pair]
         R = Sp[:, self._vtri_map.ravel()].reshape(-1, v, v)[self._otri_map.ravel()].reshape(o, o, v, v)
-        if taum.size and sc.size:
-            Sm = taum @ self.Wm.T
+        if taum.size and self._vstr[0].size:
+            Whm = self._row_packs(np.ascontiguousarray(Wt[si, sj]))[1]
+            Sm = taum @ self.Wm.T + Whm @ taum
             U = (Sm[:, self._vstr_map.ravel()].reshape(-1, v, v) * self._vsgn)[self._ostr_map.ravel()]
             R += U.reshape(o, o, v, v) * self._osgn[:, :, None, None]
         return R
@@ -149,7 +192,6 @@ class FullUpdate:
         ovov, oovv, ovoo, oooo, ovvv = self.ovov, self.oovv, self.ovoo, self.oooo, self.ovvv
         fov = self.f_ov
         tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
-        tau_r = tau.reshape(o * o, v * v)
         # t2 as [(i,a),(l,d)]: t2[i,l,a,d] and t2[i,l,d,a]
         t2_iald = np.ascontiguousarray(t2.transpose(0, 2, 1, 3)).reshape(ov, ov)
         t2_ilda = np.ascontiguousarray(t2.transpose(0, 3, 1, 2)).reshape(ov, ov)
@@ -180,9 +222,11 @@ class FullUpdate:
         R1 -= (np.ascontiguousarray(tau.transpose(0, 1, 3, 2)).reshape(o * o * v, v).T @ self.LovooK).T
 
         # ---- intermediates ---------------------------------------------------
+        taup, taum = self._tau_pairs(tau)
+        X = self._unpack_pairs(taup @ self.Uxp.T, taum @ self.Uxm.T)               # [(i,j), (k,l)]
         Woooo = (oooo.transpose(0, 2, 1, 3) + np.einsum("lcki,jc->klij", ovoo, t1, optimize=True)
                  + np.einsum("kclj,ic->klij", ovoo, t1, optimize=True)
-                 + (self.ovovT.reshape(o * o, v * v) @ tau_r.T).reshape(o, o, o, o))
+                 + X.T.reshape(o, o, o, o))
         # Wvoov and Wvovo stored as [(i,a), (k,c)] (W_akic, W_akci)
         t1t1 = (t1[:, None, None, :] * t1.T[None, :, :, None]).reshape(ov, ov)      # t1[i,d] t1[l,a]
         th1 = t2_iald - 0.5 * t2_ilda - t1t1
@@ -205,7 +249,7 @@ class FullUpdate:
         Rp -= (t1.T @ Vk.reshape(o, -1)).reshape(v, o, v, o).transpose(1, 3, 0, 2)
         tmpB = (np.einsum("kcia,jc->akij", ovov, t1, optimize=True) + ovoo.transpose(1, 3, 0, 2))   # [a,k,i,j]
         Rp -= np.einsum("akij,kb->ijab", tmpB, t1, optimize=True)
-        Z = tau_r @ self.ovvvZ.T                                                    # [(i,j), (k,a)]
+        Z = self._unpack_pairs(taup @ self.Vzp.T, taum @ self.Vzm.T)               # [(i,j), (k,a)]
         Rp -= (Z.reshape(o * o, o, v).transpose(0, 2, 1).reshape(o * o * v, o) @ t1).reshape(o, o, v, v)
         Rp += np.matmul(Lvv_p, t2)
         Rp -= (Loo_p.T @ t2.reshape(o, -1)).reshape(o, o, v, v)
@@ -214,8 +258,7 @@ class FullUpdate:
         ring -= Wvoov @ t2_ilda                                                     # t2_ilda = t2[k,j,b,c]
         Rp += ring.reshape(o, v, o, v).transpose(0, 2, 1, 3)
         Rp -= (Wvovo @ t2_ilda).reshape(o, v, o, v).transpose(0, 2, 3, 1)
-        R2 = self.ovovT + (Woooo.reshape(o * o, o * o).T @ tau_r).reshape(o, o, v, v)
-        R2 += self.ladder(tau)
+        R2 = self.ovovT + self.ladder(taup, taum, Woooo)
         R2 += Rp
         R2 += Rp.transpose(1, 0, 3, 2)
         return R1, R2

@@ -99,9 +99,10 @@ def test_literal_sigma_diverges_normalised_converges():
 
 @pytest.mark.parametrize("o,v,q,seed", [(3, 8, 20, 1), (4, 11, 30, 8), (1, 5, 10, 3), (2, 1, 6, 4), (1, 1, 4, 2)])
 def test_cpu_update_equals_the_oracle_map(o, v, q, seed):
-    """The timed CPU implementation (oracle.cpu_update: BLAS layouts, pair-form
-    ladder on W+/W- from the DF factors) computes the closed-shell map of
-    RHFCCSD.residual, at arbitrary amplitudes, to rounding."""
+    """The timed CPU implementation (oracle.cpu_update: BLAS layouts, the pair
+    forms of both ladders, Z and X on packs built from the DF factors) computes
+    the closed-shell map of RHFCCSD.residual, at symmetric amplitudes, to
+    rounding."""
     from oracle.ccsd_rhf import RHFCCSD
     from oracle.cpu_update import FullUpdate
     fock = np.diag(syn.orbital_energies(o, v, seed))
