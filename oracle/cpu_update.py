@@ -73,9 +73,8 @@ class FullUpdate:
         self.ovooA = np.ascontiguousarray(self.ovoo.transpose(0, 1, 3, 2)).reshape(o * v * o, o)  # [(k,c,i), l]
         self.ovooB = np.ascontiguousarray(self.ovoo.transpose(1, 2, 3, 0)).reshape(v * o * o, o)  # [(c,k,i), l]
         ovvv = self.ovvv
-        # [(k,c,d), a] = 2 (kd|ac) - (kc|ad); [(k,a), (c,d)] = (kd|ac)
+        # [(k,c,d), a] = 2 (kd|ac) - (kc|ad)
         self.LovvvR = (2.0 * ovvv.transpose(0, 3, 1, 2) - ovvv.transpose(0, 1, 3, 2)).reshape(o * v * v, v)
-        self.ovvvZ = np.ascontiguousarray(ovvv.transpose(0, 2, 3, 1)).reshape(o * v, v * v)
         self._build_pairs(bvv)
         self.diis_size, self.diis_start = diis_size, diis_start
         self.t1 = np.zeros((o, v))
@@ -125,7 +124,11 @@ class FullUpdate:
         self._otri_map, self._ostr_map, self._osgn = maps(o)
         self._vtri_map, self._vstr_map, self._vsgn = maps(v)
         # V+-[(k,a), cd pair] of Z (V[c,d] = (kd|ac)) and U+-[(k,l), cd pair] of X (U[c,d] = (kc|ld))
-        self.Vzp, self.Vzm = self._row_packs(self.ovvvZ.reshape(o * v, v, v))
+        # (V[(k,a)][c][d] = (kd|ac) = ovvv[k][d][a][c], packed k at a time from views of ovvv)
+        self.Vzp = np.empty((o * v, v * (v + 1) // 2))
+        self.Vzm = np.empty((o * v, v * (v - 1) // 2))
+        for k in range(o):
+            self.Vzp[k * v:(k + 1) * v], self.Vzm[k * v:(k + 1) * v] = self._row_packs(self.ovvv[k].transpose(1, 2, 0))
         self.Uxp, self.Uxm = self._row_packs(self.ovovT.reshape(o * o, v, v))
 
     @staticmethod
